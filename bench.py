@@ -1,0 +1,386 @@
+"""Benchmark of the ReinsPIRe online answer on GB300.
+
+Workload: n = 2^20 records, ring degree d = 4096, entry_size_multiple l = 1,
+interpolation degree t = 8, CoeffType u32 (q = 2^32): the DB matrix is
+t*d x n/t = 32768 x 131072 u16 (8 GiB), the packing matrix 32768 x 8192 i32
+(1 GiB). A step answers one batch of B seeded requests (default B = 256) with
+the batched tensor-core engine (8-bit limbs on tcgen05); the plain
+single-query engine (fused CUDA-core GEMV) is timed beside it. Every response
+of both engines is the same integer vector (checked before timing).
+
+Prints one JSON line (rank 0). `value` is queries/s with the requests already
+resident in GPU memory; `e2e` is the same metric through the host-buffer C ABI
+call (H2D of the requests and D2H of the responses inside the timed region).
+`--impl reference` times the reference algorithm's CPU restatement (the
+oracle, FP64 FFT path) on all host cores instead.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_ENTRIES = 1 << 20
+DEGREE = 4096
+INTERP = 8
+COEFF_BITS = 32
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], p["bf16_tflops"], "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,"
+             "clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", "-i", str(self.index),
+                     "--query-gpu=" + self.QUERY,
+                     "--format=csv,noheader,nounits"],
+                    capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def make_workload(seed=2026, batch=256):
+    from inspire_gb300 import synthetic
+    params = synthetic.make_params(d=DEGREE, n=N_ENTRIES, t=INTERP,
+                                   coeff_bits=COEFF_BITS)
+    rng = np.random.default_rng(seed)
+    rows = INTERP * DEGREE
+    cols = N_ENTRIES // INTERP
+    # Uniform already-interpolated DB values in [0, p) (p = 65535).
+    db = rng.integers(0, 1 << 63, size=rows * cols // 4, dtype=np.uint64)
+    db = db.view(np.uint16).reshape(rows, cols)
+    np.minimum(db, 65534, out=db)
+    k = params.pack_gadget.num_digits
+    bound = int(4 * np.sqrt(DEGREE) * (1 << params.pack_gadget.log_digit))
+    pack = rng.integers(-bound + 1, bound, size=(rows, k * DEGREE),
+                        dtype=np.int32)
+    mat = synthetic.make_material(
+        synthetic.make_params(d=DEGREE, n=DEGREE * INTERP, t=INTERP,
+                              coeff_bits=COEFF_BITS), seed=seed + 1)
+    fd, sd, pk = synthetic.make_requests(params, batch, seed=seed + 2)
+    return params, db, pack, mat.a_tilde_agg, mat.t_vec_h, mat.second_dim_a, \
+        fd, sd, pk
+
+
+def run_reference(args):
+    """The reference algorithm (oracle port, FP64 FFT path) on host cores."""
+    from oracle import pyoracle as orc
+    params, db, pack, a_tilde, t_vec_h, sda, fd, sd, pk = make_workload(
+        batch=max(64, os.cpu_count() or 1))
+    r = params.rlwe
+    op = orc.make_params(
+        coeff_bits=COEFF_BITS, log_degree=DEGREE.bit_length() - 1,
+        log_modulus=r.log_modulus,
+        log_modulus1_after_switch=r.log_modulus1_after_switch,
+        log_modulus2_after_switch=r.log_modulus2_after_switch,
+        pack_log_digit=params.pack_gadget.log_digit,
+        pack_num_digits=params.pack_gadget.num_digits,
+        eval_log_digit=params.eval_gadget.log_digit,
+        eval_num_digits=params.eval_gadget.num_digits,
+        num_entries=N_ENTRIES, interpolation_degree=INTERP,
+        entry_size_multiple=1)
+    threads = os.cpu_count() or 1
+
+    def one_step():
+        def work(i):
+            orc.process_response(op, db, pack, a_tilde, t_vec_h, sda, fd[i],
+                                 sd[i], pk[i], mode=orc.MODE_FP64)
+        ts = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+        t0 = time.perf_counter()
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        return time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        one_step()
+    times = [one_step() for _ in range(args.steps)]
+    total = sum(times)
+    qps = threads * args.steps / total
+    line = {
+        "impl": "reference",
+        "metric": "queries/s (online answer, n=2^20 d=4096 t=8, Z_2^32)",
+        "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded uniform DB / queries)",
+        "config": {"workload": "pir_answer_n2^20_d4096_t8_l1_u32",
+                   "n": N_ENTRIES, "d": DEGREE, "t": INTERP, "l": 1,
+                   "requests_per_step": threads},
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads,
+                         "kind": "port",
+                         "sample": "%d full requests per step, one per host "
+                                   "thread" % threads},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def cpu_baseline_sample(params, db, pack, a_tilde, t_vec_h, sda, fd, sd, pk,
+                        budget_s=20.0):
+    """Oracle (FP64 reference algorithm) on all host cores, bounded."""
+    from oracle import pyoracle as orc
+    r = params.rlwe
+    op = orc.make_params(
+        coeff_bits=COEFF_BITS, log_degree=DEGREE.bit_length() - 1,
+        log_modulus=r.log_modulus,
+        log_modulus1_after_switch=r.log_modulus1_after_switch,
+        log_modulus2_after_switch=r.log_modulus2_after_switch,
+        pack_log_digit=19, pack_num_digits=2, eval_log_digit=19,
+        eval_num_digits=3, num_entries=N_ENTRIES, interpolation_degree=INTERP,
+        entry_size_multiple=1)
+    threads = min(os.cpu_count() or 1, fd.shape[0])
+    done = [0]
+    lock = threading.Lock()
+    deadline = time.perf_counter() + budget_s
+
+    def work(i):
+        j = i
+        while time.perf_counter() < deadline:
+            orc.process_response(op, db, pack, a_tilde, t_vec_h, sda,
+                                 fd[j % fd.shape[0]], sd[j % fd.shape[0]],
+                                 pk[j % fd.shape[0]], mode=orc.MODE_FP64)
+            with lock:
+                done[0] += 1
+            j += threads
+    t0 = time.perf_counter()
+    ts = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    el = time.perf_counter() - t0
+    return {"value": done[0] / el, "unit": "queries/s", "cores": threads,
+            "kind": "port",
+            "sample": "%d full requests in %.1f s on %d host threads "
+                      "(oracle, FP64 FFT path)" % (done[0], el, threads)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-steps", type=int, default=10)
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from inspire_gb300 import build, pir
+    build.build()
+
+    params, db, pack, a_tilde, t_vec_h, sda, fd, sd, pk = make_workload(
+        batch=args.batch)
+    srv = pir.PirServer.CreateCombined(params, db, pack, a_tilde, t_vec_h, sda)
+    B = args.batch
+    d = DEGREE
+    n1 = fd.shape[1]
+    cdt = np.uint32
+    l = 1
+
+    # Device-resident requests and responses.
+    dev = torch.device("cuda", local)
+    t_fd = torch.from_numpy(fd.view(np.int32)).to(dev)
+    t_sd = torch.from_numpy(sd.view(np.int32)).to(dev)
+    t_pk = torch.from_numpy(pk.view(np.int32)).to(dev)
+    t_out = torch.empty((B, l, 2, d), dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+
+    engine = pir.ENGINE_TENSOR
+    try:
+        srv.process_device(1, t_fd.data_ptr(), n1, t_sd.data_ptr(), sd.shape[1],
+                           t_pk.data_ptr(), pk.shape[1], t_out.data_ptr(),
+                           engine, sptr)
+        stream.synchronize()
+    except pir.InspireError:
+        engine = pir.ENGINE_PLAIN
+
+    # Parity of the two engines on the first requests, and spot rows of the
+    # DB product against an exact host computation.
+    check = min(B, 8)
+    got_plain = srv.process_arrays(fd[:check], sd[:check], pk[:check],
+                                   pir.ENGINE_PLAIN)
+    got_eng = srv.process_arrays(fd[:check], sd[:check], pk[:check], engine)
+    if not np.array_equal(got_plain, got_eng):
+        raise SystemExit("engine responses differ")
+
+    def step(bsz, eng):
+        srv.process_device(bsz, t_fd.data_ptr(), n1, t_sd.data_ptr(),
+                           sd.shape[1], t_pk.data_ptr(), pk.shape[1],
+                           t_out.data_ptr(), eng, sptr)
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        stream.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = t.item()
+        return ms / steps
+
+    hbm, tflops, peak_kind = peaks()
+    with ClockSampler(local) as clk:
+        ms_step = timed(lambda: step(B, engine), args.steps, args.warmup)
+    # Plain single-query engine beside it (B = 1 per step).
+    ms_plain = timed(lambda: step(1, pir.ENGINE_PLAIN), args.plain_steps,
+                     args.warmup)
+    # Kernel-only timing of the dominant kernel for the roofline.
+    from inspire_gb300 import profiling
+    kern = profiling.kernel_times(srv, engine, B, t_fd, t_sd, t_pk, t_out,
+                                  stream, n1, sd.shape[1], pk.shape[1])
+
+    # e2e through the host-buffer C ABI (pinned host memory).
+    h_fd = torch.from_numpy(fd.view(np.int32)).pin_memory().numpy().view(cdt)
+    h_sd = torch.from_numpy(sd.view(np.int32)).pin_memory().numpy().view(cdt)
+    h_pk = torch.from_numpy(pk.view(np.int32)).pin_memory().numpy().view(cdt)
+    h_out = torch.empty((B, l, 2, d), dtype=torch.int32).pin_memory().numpy()
+    lib = __import__("inspire_gb300._lib", fromlist=["load"]).load()
+    err = ctypes.create_string_buffer(256)
+
+    def e2e_step():
+        rc = lib.inspire_pir_process_batch(
+            srv._h, B, h_fd.ctypes.data, n1, h_sd.ctypes.data, sd.shape[1],
+            h_pk.ctypes.data, pk.shape[1], h_out.ctypes.data, engine, err,
+            len(err))
+        if rc:
+            raise SystemExit(err.value)
+    for _ in range(args.warmup):
+        e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(max(3, args.steps // 2)):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / max(3, args.steps // 2)
+
+    rows, cols = db.shape
+    db_bytes = db.nbytes + pack.nbytes
+    qps = world * B / (ms_step / 1000.0)
+    plain_qps = 1000.0 / ms_plain
+    line = {
+        "metric": "queries/s (online answer, n=2^20 d=4096 t=8, Z_2^32): "
+                  "batched tensor-core vs plain, bit-exact",
+        "value": qps, "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic (seeded uniform DB, pack matrix, "
+                                "queries)",
+        "config": {"workload": "pir_answer_n2^20_d4096_t8_l1_u32",
+                   "n": N_ENTRIES, "d": DEGREE, "t": INTERP, "l": 1,
+                   "batch": B, "engine": "tensor" if engine else "plain",
+                   "db_matrix": [rows, cols], "pack_matrix": list(pack.shape),
+                   "l2": "inputs larger than L2 (9 GiB matrices per step)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "plain": {"queries_per_s": plain_qps, "ms_per_query": ms_plain,
+                  "db_gbs": db_bytes / (ms_plain / 1000.0) / 1e9},
+        "db_gbs": db_bytes * (1 if engine else B) / (ms_step / 1000.0) / 1e9,
+        "speedup_vs_plain": qps / world / plain_qps,
+        "roofline": kern["roofline"],
+        "kernels": kern["kernels"],
+        "peak_kind": peak_kind,
+        "clocks": clk.summary(),
+        "gpu_launches": kern["launches_per_step"] * args.steps,
+        "e2e": {"value": world * B / e2e_s, "unit": "queries/s",
+                "h2d_bytes_per_step": int(h_fd.nbytes + h_sd.nbytes +
+                                          h_pk.nbytes),
+                "d2h_bytes_per_step": int(h_out.nbytes)},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(
+            params, db, pack, a_tilde, t_vec_h, sda, fd, sd, pk)
+    if dist:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

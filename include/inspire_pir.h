@@ -1,0 +1,202 @@
+/*
+ * inspire_pir.h -- C ABI of the GB300 (sm_103a) ReinsPIRe online answer path.
+ *
+ * Plain C types only (pointers, sizes, ints): no CUDA, torch or C++ types in
+ * any signature, so cgo / JNI / ctypes / N-API bindings can bind it directly.
+ * The library is libinspire_gb300.so (built by inspire_gb300/build.py).
+ *
+ * Every function returns an int status: 0 on success, otherwise the
+ * absl::StatusCode the reference would return (3 INVALID_ARGUMENT,
+ * 9 FAILED_PRECONDITION, 13 INTERNAL, 8 RESOURCE_EXHAUSTED) with the
+ * reference's message text copied into `err` (NUL-terminated, truncated to
+ * err_len). `err` may be NULL.
+ *
+ * Reference interfaces replaced (paths inside google/InsPIRe):
+ *   PirServer<Db,Coeff,Mat>::Create          crypto/pir/server/pir_server.h:45-49
+ *   PirServer<Db,Coeff,Mat>::ProcessResponse crypto/pir/server/pir_server.h:67-68
+ *   PirServer timing getters                  crypto/pir/server/pir_server.h:70-72
+ *   Matrix<T>::Multiply                       crypto/matrix.h:86-88, 167-195
+ *   Polynomial<T>::InnerProductFft            crypto/polynomial.h:195-199
+ *   ExternalProduct                           crypto/external_product.h:29-33
+ *   FinalizeMatrixPack                        crypto/lwes_to_rlwe.h:114-121
+ */
+#ifndef INSPIRE_PIR_H_
+#define INSPIRE_PIR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define INSPIRE_OK 0
+#define INSPIRE_INVALID_ARGUMENT 3
+#define INSPIRE_RESOURCE_EXHAUSTED 8
+#define INSPIRE_FAILED_PRECONDITION 9
+#define INSPIRE_INTERNAL 13
+
+/* Element kinds of a matrix (the reference's DbDataType / MatCoeffType). */
+#define INSPIRE_U8 0
+#define INSPIRE_U16 1
+#define INSPIRE_U32 2
+#define INSPIRE_U64 3
+#define INSPIRE_I16 4
+#define INSPIRE_I32 5
+
+/* Answer engines for the batched entry points. */
+#define INSPIRE_ENGINE_PLAIN 0  /* fused CUDA-core GEMV, HBM-bound        */
+#define INSPIRE_ENGINE_TENSOR 1 /* 8-bit limbs on the tcgen05 tensor cores */
+
+/* PirParams<CoeffType> (crypto/pir/pir_params.h:36-105) together with the
+ * template arguments of PirServer<DbDataType, CoeffType, MatCoeffType>. */
+typedef struct inspire_pir_params {
+  int32_t coeff_bits;   /* 8 * sizeof(CoeffType): 32 or 64           */
+  int32_t db_kind;      /* DbDataType: INSPIRE_U8 or INSPIRE_U16       */
+  int32_t mat_kind;     /* MatCoeffType: INSPIRE_I16, _I32, _U32, _U64 */
+  int32_t log_degree;   /* d = 1 << log_degree                         */
+  int32_t log_modulus;  /* RlweParams::LogModulus()                    */
+  int32_t log_modulus1_after_switch;
+  int32_t log_modulus2_after_switch;
+  int32_t pack_log_digit;
+  int32_t pack_num_digits;
+  int32_t eval_log_digit;
+  int32_t eval_num_digits;
+  int32_t num_entries;
+  int32_t interpolation_degree;
+  int32_t entry_size_multiple;
+  uint64_t plaintext_modulus;
+} inspire_pir_params;
+
+typedef struct inspire_pir_server inspire_pir_server;
+
+/*
+ * PirServer::Create (crypto/pir/server/pir_server.cc:54-124) from host
+ * memory. The material is the server's combined form:
+ *   db           (l*t*d) x db_cols matrix of db_kind, row-major (the
+ *                vertically concatenated DB matrices; a condensed Matrix has
+ *                the same bytes)
+ *   pack         (l*t*d) x pack_cols matrix of mat_kind, row-major (the
+ *                concatenated PreprocessMatrixPackOutput::matrix, shard-major)
+ *   a_tilde_agg  l*t polynomials (shard-major, slice-minor)
+ *   t_vec_h      l*t*pack_num_digits polynomials
+ *   second_dim_a 2*eval_num_digits polynomials (none when t == 1)
+ * Polynomials are d CoeffType words each. Everything is copied to GPU memory
+ * once; the host buffers may be freed after the call.
+ */
+int inspire_pir_server_create(const inspire_pir_params* params,
+                              const void* db, int64_t db_rows, int64_t db_cols,
+                              const void* pack, int64_t pack_rows,
+                              int64_t pack_cols, const void* a_tilde_agg,
+                              int64_t a_tilde_agg_count, const void* t_vec_h,
+                              int64_t t_vec_h_count, const void* second_dim_a,
+                              int64_t second_dim_a_count,
+                              inspire_pir_server** out, char* err,
+                              size_t err_len);
+
+void inspire_pir_server_destroy(inspire_pir_server* server);
+
+/*
+ * PirServer::ProcessResponse (crypto/pir/server/pir_server.cc:154-306) for
+ * one request in host memory. first_dim has first_dim_len CoeffType words,
+ * second_dim second_dim_count polynomials, packing_key packing_key_count
+ * polynomials. response receives l ciphertexts, each a then b (2*l*d
+ * words). Synchronous; updates the timers.
+ */
+int inspire_pir_process_response(inspire_pir_server* server,
+                                 const void* first_dim, int64_t first_dim_len,
+                                 const void* second_dim,
+                                 int64_t second_dim_count,
+                                 const void* packing_key,
+                                 int64_t packing_key_count, void* response,
+                                 char* err, size_t err_len);
+
+/*
+ * ProcessResponse for `batch` requests in host memory, stacked: request q's
+ * first_dim starts at q*first_dim_len words, its second_dim at
+ * q*second_dim_count*d, its packing key at q*packing_key_count*d; responses
+ * are stacked the same way (2*l*d words each). `engine` selects the DB/pack
+ * product (INSPIRE_ENGINE_*); responses are identical for every engine.
+ */
+int inspire_pir_process_batch(inspire_pir_server* server, int32_t batch,
+                              const void* first_dim, int64_t first_dim_len,
+                              const void* second_dim, int64_t second_dim_count,
+                              const void* packing_key,
+                              int64_t packing_key_count, void* responses,
+                              int32_t engine, char* err, size_t err_len);
+
+/*
+ * Device-resident form of inspire_pir_process_batch: all pointers are CUDA
+ * device pointers and the work is enqueued on `stream` (a cudaStream_t, or
+ * NULL for the legacy default stream) without synchronising. first_dim must
+ * hold db_cols words per request (zero-padded past first_dim_len).
+ */
+int inspire_pir_process_batch_device(inspire_pir_server* server,
+                                     int32_t batch, const void* first_dim,
+                                     int64_t first_dim_len,
+                                     const void* second_dim,
+                                     int64_t second_dim_count,
+                                     const void* packing_key,
+                                     int64_t packing_key_count,
+                                     void* responses, int32_t engine,
+                                     void* stream, char* err, size_t err_len);
+
+/*
+ * Stage 1 alone for a device-resident batch: out[q][r] = (DB * q1_q)[r] +
+ * (P * y_g,q)[r] mod 2^w, the b' + b_agg_partial vector that
+ * FinalizeMatrixPack consumes (pir_server.cc:215-254). first_dim holds
+ * db_cols words per request, packing_key 2*pack_num_digits polynomials per
+ * request (its first half is y_vec_g); out holds rows words per request.
+ * Enqueued on `stream` without synchronising.
+ */
+int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,
+                                const void* first_dim, const void* packing_key,
+                                void* out, int32_t engine, void* stream,
+                                char* err, size_t err_len);
+
+/* Server geometry: rows = l*t*d, and the column counts of both matrices. */
+int inspire_pir_server_shape(const inspire_pir_server* server, int64_t* rows,
+                             int64_t* db_cols, int64_t* pack_cols);
+
+/* GetDbMultiplyTime / GetPackingTime / GetPolyEvalTime
+ * (crypto/pir/server/pir_server.h:70-72), accumulated in milliseconds. */
+int inspire_pir_server_timings(const inspire_pir_server* server,
+                               double* db_mult_ms, double* packing_ms,
+                               double* poly_eval_ms);
+
+/* ---- Component entry points (host memory in and out, synchronous) ---- */
+
+/* Matrix<mat_kind>::Multiply<CoeffType> (crypto/matrix.h:167-195):
+ * out[r] = sum_c mat[r][c] * vec[c] mod 2^coeff_bits. */
+int inspire_matrix_multiply(int32_t mat_kind, int32_t coeff_bits,
+                            const void* mat, int64_t rows, int64_t cols,
+                            const void* vec, void* out, char* err,
+                            size_t err_len);
+
+/* Polynomial<T>::InnerProductFft (crypto/polynomial_fft.cc:68-197): the
+ * exact value sum_i u_i * v_i in Z_{2^w}[X]/(X^d+1) for the operands that
+ * its chunk rule (u_bits, v_bits, chunk_bits, u_is_signed) reads. */
+int inspire_inner_product(int32_t coeff_bits, const void* u, const void* v,
+                          int32_t n, int32_t d, int32_t u_bits, int32_t v_bits,
+                          int32_t chunk_bits, int32_t u_is_signed, void* out,
+                          char* err, size_t err_len);
+
+/* ExternalProduct (crypto/external_product.cc:35-114). rgsw holds
+ * u[0..nd) then v[0..nd), each an (a, b) pair of polynomials. */
+int inspire_external_product(const inspire_pir_params* params,
+                             const void* ct_a, const void* ct_b,
+                             const void* rgsw, void* out_a, void* out_b,
+                             char* err, size_t err_len);
+
+/* FinalizeMatrixPack (crypto/lwes_to_rlwe.cc:448-479): the b polynomial of
+ * the packed ciphertext (its a polynomial is a_tilde_agg unchanged). */
+int inspire_finalize_matrix_pack(const inspire_pir_params* params,
+                                 const void* b, const void* b_agg_partial,
+                                 const void* y_vec_h, const void* t_vec_h,
+                                 void* out_b, char* err, size_t err_len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* INSPIRE_PIR_H_ */

@@ -1,0 +1,67 @@
+"""Loads libinspire_gb300.so and declares the C ABI (include/inspire_pir.h).
+
+There is no fallback: if the library is missing, loading fails loudly.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libinspire_gb300.so")
+
+_lib = None
+
+# name -> (argtypes, restype)
+_vp, _i32, _i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+_cp, _sz = ctypes.c_char_p, ctypes.c_size_t
+_dp = ctypes.POINTER(ctypes.c_double)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+SIGNATURES = {
+    "inspire_pir_server_create": (
+        [_vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp,
+         _i64, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_server_destroy": ([_vp], None),
+    "inspire_pir_process_response": (
+        [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_process_batch": (
+        [_vp, _i32, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i32, _cp, _sz],
+        ctypes.c_int),
+    "inspire_pir_process_batch_device": (
+        [_vp, _i32, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i32, _vp, _cp,
+         _sz], ctypes.c_int),
+    "inspire_pir_products_device": (
+        [_vp, _i32, _vp, _vp, _vp, _i32, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_server_shape": ([_vp, _i64p, _i64p, _i64p], ctypes.c_int),
+    "inspire_pir_server_timings": ([_vp, _dp, _dp, _dp], ctypes.c_int),
+    "inspire_matrix_multiply": (
+        [_i32, _i32, _vp, _i64, _i64, _vp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_inner_product": (
+        [_i32, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _cp, _sz],
+        ctypes.c_int),
+    "inspire_external_product": (
+        [_vp, _vp, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_finalize_matrix_pack": (
+        [_vp, _vp, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),
+}
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+def load(path=LIB_PATH):
+    """Returns the loaded library, raising LibraryMissing if not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise LibraryMissing(
+            "%s is not built; run `python -c \"import __graft_entry__ as g; "
+            "g.build()\"` (the CUDA library has no CPU fallback)" % path)
+    lib = ctypes.CDLL(path)
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib

@@ -1,0 +1,25 @@
+// Batched DB/pack product on the tensor cores with exact 8-bit limbs.
+// Declared here, implemented in limb_gemm.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+
+namespace inspire {
+
+class LimbGemm {
+ public:
+  // Prepares the limb planes of the server matrices. Leaves *out empty when
+  // the parameters are outside what the tensor-core engine supports.
+  static void Create(int coeff_bits, int db_kind, const void* db, int64_t rows,
+                     int64_t db_cols, int mat_kind, const void* pack,
+                     int64_t pack_cols, std::unique_ptr<LimbGemm>* out);
+  virtual ~LimbGemm() = default;
+  // out[q][r] = db[r] . q1[q] + pack[r] . yg[q]  (mod 2^w), q < batch.
+  virtual cudaError_t Run(int batch, const void* q1, int64_t q1_stride,
+                          const void* yg, int64_t yg_stride, void* out,
+                          cudaStream_t stream) = 0;
+};
+
+}  // namespace inspire

@@ -1,0 +1,338 @@
+// Kernels of the polynomial stage of the online answer: the negacyclic
+// products of FinalizeMatrixPack and of the EvalPoly external products, all
+// as exact multi-prime NTTs, plus the Rescale epilogue.
+//
+// Reference: FinalizeMatrixPack (crypto/lwes_to_rlwe.cc:448-479),
+// ExternalProduct (crypto/external_product.cc:35-114), EvalPoly and the
+// modulus switch (crypto/pir/server/pir_server.cc:128-150, 283-297),
+// Polynomial::{LowBits,GadgetInv,Rescale} (crypto/polynomial.cc:287-374).
+#pragma once
+#include <cstdint>
+
+#include "arith.cuh"
+#include "ntt.cuh"
+
+namespace inspire {
+
+constexpr int kPolyThreads = 512;
+constexpr int kMaxPer = 16;  // d / kPolyThreads for d <= 8192
+
+template <typename T>
+struct Bits {
+  static constexpr int value = 8 * sizeof(T);
+};
+
+template <typename T>
+__device__ __forceinline__ T low_bits(T x, int amount) {
+  return amount >= Bits<T>::value ? x : (x & ((T{1} << amount) - 1));
+}
+
+template <typename T>
+__device__ __forceinline__ T shr_or_zero(T x, int amount) {
+  return amount >= Bits<T>::value ? T{0} : (x >> amount);
+}
+
+// Polynomial::Rescale: round(c * 2^lnew / 2^lcur) of the full word.
+template <typename T>
+__device__ __forceinline__ T rescale_word(T c, int lcur, int lnew) {
+  if (lnew >= lcur) {
+    const int s = lnew - lcur;
+    return s >= Bits<T>::value ? T{0} : static_cast<T>(c << s);
+  }
+  const int s = lcur - lnew;
+  if (s >= Bits<T>::value) return c >> (Bits<T>::value - 1);
+  return (c >> s) + ((c >> (s - 1)) & T{1});
+}
+
+template <typename T>
+__device__ __forceinline__ uint32_t to_residue(T x, uint32_t p) {
+  if constexpr (sizeof(T) == 4) {
+    return reduce_u32(x, p);
+  } else {
+    return reduce_u64(x, p);
+  }
+}
+
+// Gadget digit `dg` of a LowBits'd coefficient (Polynomial::GadgetInv with
+// the rounding shift when log_modulus > digits * log_digit).
+template <typename T>
+__device__ __forceinline__ T gadget_digit(T c, int log_modulus, int log_digit,
+                                          int num_digits, int dg) {
+  const int to_shift = log_modulus - num_digits * log_digit;
+  T cur = c;
+  if (to_shift > 0) {
+    cur = (c >> to_shift) + ((c >> (to_shift - 1)) & T{1});
+  }
+  const int sh = dg * log_digit;
+  cur = sh >= Bits<T>::value ? T{0} : (cur >> sh);
+  return low_bits(cur, log_digit);
+}
+
+// Forward NTT of CoeffType polynomials (masked to the bits the reference's
+// chunk rule reads). grid.x = npoly * r, grid.y = batch.
+template <typename T>
+__global__ void __launch_bounds__(kPolyThreads)
+ntt_coeffs_kernel(const T* __restrict__ src, int64_t src_qstride,
+                  int64_t src_off, int npoly, T mask, uint32_t* __restrict__ dst,
+                  NttCtx c) {
+  extern __shared__ uint32_t smem[];
+  const int d = 1 << c.logd;
+  const int poly = blockIdx.x / c.r;
+  const int pi = blockIdx.x % c.r;
+  const int q = blockIdx.y;
+  const uint32_t p = c.p[pi];
+  const T* in = src + q * src_qstride + src_off + static_cast<int64_t>(poly) * d;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    smem[j] = to_residue<T>(in[j] & mask, p);
+  }
+  ntt_forward(smem, c, pi);
+  uint32_t* out = dst + ((static_cast<int64_t>(q) * npoly + poly) * c.r + pi) * d;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) out[j] = smem[j];
+}
+
+// Forward NTT of signed 64-bit polynomials (host-prepared operands).
+__global__ void __launch_bounds__(kPolyThreads)
+ntt_signed_kernel(const int64_t* __restrict__ src, int npoly,
+                  uint32_t* __restrict__ dst, NttCtx c) {
+  extern __shared__ uint32_t smem[];
+  const int d = 1 << c.logd;
+  const int poly = blockIdx.x / c.r;
+  const int pi = blockIdx.x % c.r;
+  const int64_t p = c.p[pi];
+  const int64_t* in = src + static_cast<int64_t>(poly) * d;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    int64_t v = in[j] % p;
+    if (v < 0) v += p;
+    smem[j] = static_cast<uint32_t>(v);
+  }
+  ntt_forward(smem, c, pi);
+  uint32_t* out = dst + (static_cast<int64_t>(poly) * c.r + pi) * d;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) out[j] = smem[j];
+}
+
+// sum_i U_i . V_i per prime, inverse NTT, CRT. One block; used by the
+// InnerProductFft component entry point. U: [n][r][d], V: [n][r][d].
+template <typename T>
+__global__ void __launch_bounds__(kPolyThreads)
+inner_product_finish_kernel(const uint32_t* __restrict__ U,
+                            const uint32_t* __restrict__ V, int n,
+                            T* __restrict__ out, NttCtx c) {
+  extern __shared__ uint32_t smem[];  // [r][d]
+  const int d = 1 << c.logd;
+  for (int pi = 0; pi < c.r; ++pi) {
+    const uint32_t p = c.p[pi];
+    uint32_t* a = smem + static_cast<int64_t>(pi) * d;
+    for (int j = threadIdx.x; j < d; j += blockDim.x) {
+      uint32_t s = 0;
+      for (int i = 0; i < n; ++i) {
+        const int64_t off = (static_cast<int64_t>(i) * c.r + pi) * d + j;
+        s = add_mod(s, mont_mul(U[off], V[off], p, c.pinv[pi]), p);
+      }
+      a[j] = s;
+    }
+    ntt_inverse(a, c, pi);
+  }
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    uint32_t x[kMaxPrimes] = {0, 0, 0, 0, 0};
+#pragma unroll
+    for (int pi = 0; pi < kMaxPrimes; ++pi) {
+      if (pi < c.r) {
+        x[pi] = shoup_mul(smem[static_cast<int64_t>(pi) * d + j], c.scale[pi],
+                          c.scale_s[pi], c.p[pi]);
+      }
+    }
+    out[j] = crt_reconstruct<T>(x, c);
+  }
+}
+
+// FinalizeMatrixPack for every (request, shard, slice):
+//   b_agg = LowBits(LowBits(gemv) + sum_j t_h[j] (*) y_h[j], log_q)
+// gemv already holds b' + b_agg_partial (optionally split in two vectors).
+// grid.x = l * t slices, grid.y = batch. Th: [l*t][k][r][d] (Montgomery-free
+// plain residues), Yh: [batch][k][r][d].
+template <typename T>
+__global__ void __launch_bounds__(kPolyThreads)
+finalize_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ Yh,
+                int k, const T* __restrict__ gemv, const T* __restrict__ gemv2,
+                int64_t gemv_qstride, T* __restrict__ packed_b,
+                int log_q, NttCtx c) {
+  extern __shared__ uint32_t smem[];  // [r][d]
+  const int d = 1 << c.logd;
+  const int s = blockIdx.x;
+  const int q = blockIdx.y;
+  for (int pi = 0; pi < c.r; ++pi) {
+    const uint32_t p = c.p[pi];
+    uint32_t* a = smem + static_cast<int64_t>(pi) * d;
+    for (int j = threadIdx.x; j < d; j += blockDim.x) {
+      uint32_t acc = 0;
+      for (int i = 0; i < k; ++i) {
+        const uint32_t th = Th[((static_cast<int64_t>(s) * k + i) * c.r + pi) * d + j];
+        const uint32_t yh = Yh[((static_cast<int64_t>(q) * k + i) * c.r + pi) * d + j];
+        acc = add_mod(acc, mont_mul(th, yh, p, c.pinv[pi]), p);
+      }
+      a[j] = acc;
+    }
+    ntt_inverse(a, c, pi);
+  }
+  const int64_t base = q * gemv_qstride + static_cast<int64_t>(s) * d;
+  T* outp = packed_b + (static_cast<int64_t>(q) * gridDim.x + s) * d;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    uint32_t x[kMaxPrimes] = {0, 0, 0, 0, 0};
+#pragma unroll
+    for (int pi = 0; pi < kMaxPrimes; ++pi) {
+      if (pi < c.r) {
+        x[pi] = shoup_mul(smem[static_cast<int64_t>(pi) * d + j], c.scale[pi],
+                          c.scale_s[pi], c.p[pi]);
+      }
+    }
+    const T inner = crt_reconstruct<T>(x, c);
+    T g = gemv[base + j];
+    if (gemv2 != nullptr) g += gemv2[base + j];
+    outp[j] = low_bits<T>(static_cast<T>(low_bits<T>(g, log_q) + inner), log_q);
+  }
+}
+
+struct ExtArgs {
+  int log_q;         // LowBits width and GadgetInv log_modulus
+  int log_digit;
+  int num_digits;    // eval gadget digits (ne)
+  uint64_t umask;    // bits of a digit the chunk rule reads
+};
+
+// Reads the Horner state of one coefficient: either the packed ciphertext
+// itself (first step) or CRT(previous product residues) + packed ciphertext.
+template <typename T>
+__device__ __forceinline__ void horner_state(
+    bool first, const uint32_t* __restrict__ resid_in, int64_t resid_base, int d,
+    int j, const T* __restrict__ ca, const T* __restrict__ cb, const NttCtx& c,
+    T& ra, T& rb) {
+  if (first) {
+    ra = ca[j];
+    rb = cb[j];
+    return;
+  }
+  uint32_t xa[kMaxPrimes] = {0, 0, 0, 0, 0};
+  uint32_t xb[kMaxPrimes] = {0, 0, 0, 0, 0};
+#pragma unroll
+  for (int pi = 0; pi < kMaxPrimes; ++pi) {
+    if (pi < c.r) {
+      const int64_t o = resid_base + static_cast<int64_t>(pi) * 2 * d + j;
+      xa[pi] = resid_in[o];
+      xb[pi] = resid_in[o + d];
+    }
+  }
+  ra = crt_reconstruct<T>(xa, c) + (ca != nullptr ? ca[j] : T{0});
+  rb = crt_reconstruct<T>(xb, c) + (cb != nullptr ? cb[j] : T{0});
+}
+
+// One external product per (request, shard) and prime:
+//   digits of LowBits(state) -> NTT -> MAC with the RGSW NTTs -> INTT.
+// Writes scaled residues of (a', b') to resid_out[q][shard][prime][2][d].
+// grid = (r, l, batch). RGSWa: [2ne][r][d] (server), RGSWb:
+// [batch][2ne][r][d] (request). coeff_a/coeff_b select the packed
+// ciphertext added to the previous product (or the initial state).
+template <typename T>
+__global__ void __launch_bounds__(kPolyThreads)
+ext_step_kernel(bool first, const uint32_t* __restrict__ resid_in,
+                uint32_t* __restrict__ resid_out,
+                const T* __restrict__ coeff_a, int64_t coeff_a_shard_stride,
+                const T* __restrict__ coeff_b, int64_t coeff_b_q_stride,
+                int64_t coeff_b_shard_stride,
+                const uint32_t* __restrict__ RGSWa,
+                const uint32_t* __restrict__ RGSWb, ExtArgs e, NttCtx c) {
+  extern __shared__ uint32_t smem[];
+  const int d = 1 << c.logd;
+  const int pi = blockIdx.x;
+  const int shard = blockIdx.y;
+  const int q = blockIdx.z;
+  const int l = gridDim.y;
+  const uint32_t p = c.p[pi];
+  const uint32_t pinv = c.pinv[pi];
+  T* sa = reinterpret_cast<T*>(smem + d);
+  T* sb = sa + d;
+
+  const T* ca = coeff_a + shard * coeff_a_shard_stride;
+  const T* cb = coeff_b + q * coeff_b_q_stride + shard * coeff_b_shard_stride;
+  const int64_t rbase = (static_cast<int64_t>(q) * l + shard) * c.r * 2 * d;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    T ra, rb;
+    horner_state<T>(first, resid_in, rbase, d, j, ca, cb, c, ra, rb);
+    sa[j] = low_bits<T>(ra, e.log_q);
+    sb[j] = low_bits<T>(rb, e.log_q);
+  }
+  uint32_t acc_a[kMaxPer], acc_b[kMaxPer];
+#pragma unroll
+  for (int m = 0; m < kMaxPer; ++m) acc_a[m] = acc_b[m] = 0;
+
+  const int ng = 2 * e.num_digits;
+  for (int g = 0; g < ng; ++g) {
+    const T* src = g < e.num_digits ? sa : sb;
+    const int dg = g < e.num_digits ? g : g - e.num_digits;
+    __syncthreads();
+    for (int j = threadIdx.x; j < d; j += blockDim.x) {
+      const T dig = gadget_digit<T>(src[j], e.log_q, e.log_digit, e.num_digits, dg);
+      smem[j] = to_residue<T>(dig & static_cast<T>(e.umask), p);
+    }
+    ntt_forward(smem, c, pi);
+    const uint32_t* wa = RGSWa + (static_cast<int64_t>(g) * c.r + pi) * d;
+    const uint32_t* wb =
+        RGSWb + ((static_cast<int64_t>(q) * ng + g) * c.r + pi) * d;
+#pragma unroll
+    for (int m = 0; m < kMaxPer; ++m) {
+      const int j = threadIdx.x + m * blockDim.x;
+      if (j < d) {
+        const uint32_t x = smem[j];
+        acc_a[m] = add_mod(acc_a[m], mont_mul(x, __ldg(wa + j), p, pinv), p);
+        acc_b[m] = add_mod(acc_b[m], mont_mul(x, __ldg(wb + j), p, pinv), p);
+      }
+    }
+  }
+  uint32_t* out = resid_out + rbase + static_cast<int64_t>(pi) * 2 * d;
+  for (int half = 0; half < 2; ++half) {
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < kMaxPer; ++m) {
+      const int j = threadIdx.x + m * blockDim.x;
+      if (j < d) smem[j] = half == 0 ? acc_a[m] : acc_b[m];
+    }
+    ntt_inverse(smem, c, pi);
+    for (int j = threadIdx.x; j < d; j += blockDim.x) {
+      out[half * d + j] = shoup_mul(smem[j], c.scale[pi], c.scale_s[pi], p);
+    }
+  }
+}
+
+// Final Horner addition (or the single packed ciphertext when t == 1) and
+// the modulus switch of a to q1 and b to q2. grid = (l, batch).
+// With rescale == false it only reconstructs (component entry point).
+template <typename T>
+__global__ void __launch_bounds__(kPolyThreads)
+finish_kernel(bool from_resid, const uint32_t* __restrict__ resid,
+              const T* __restrict__ coeff_a, int64_t coeff_a_shard_stride,
+              const T* __restrict__ coeff_b, int64_t coeff_b_q_stride,
+              int64_t coeff_b_shard_stride, bool rescale, int log_q, int log_q1,
+              int log_q2, T* __restrict__ out, NttCtx c) {
+  const int d = 1 << c.logd;
+  const int shard = blockIdx.x;
+  const int q = blockIdx.y;
+  const int l = gridDim.x;
+  const T* ca = coeff_a == nullptr ? nullptr : coeff_a + shard * coeff_a_shard_stride;
+  const T* cb = coeff_b == nullptr
+                    ? nullptr
+                    : coeff_b + q * coeff_b_q_stride + shard * coeff_b_shard_stride;
+  const int64_t rbase = (static_cast<int64_t>(q) * l + shard) * c.r * 2 * d;
+  T* oa = out + (static_cast<int64_t>(q) * l + shard) * 2 * d;
+  T* ob = oa + d;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    T ra, rb;
+    horner_state<T>(!from_resid, resid, rbase, d, j, ca, cb, c, ra, rb);
+    if (rescale) {
+      ra = rescale_word<T>(ra, log_q, log_q1);
+      rb = rescale_word<T>(rb, log_q, log_q2);
+    }
+    oa[j] = ra;
+    ob[j] = rb;
+  }
+}
+
+}  // namespace inspire

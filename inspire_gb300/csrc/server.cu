@@ -1,0 +1,1143 @@
+// The PirServer drop-in: server material resident in GPU memory and the
+// C ABI declared in include/inspire_pir.h.
+//
+// Reference: PirServer<Db,Coeff,Mat>::{Create,ProcessResponse,EvalPoly}
+// (crypto/pir/server/pir_server.cc:54-306). The online answer is
+//   1. b' + b_agg_partial = DB * q1 + P * y_g  (fused GEMV or limb GEMM)
+//   2. FinalizeMatrixPack per (shard, slice)   (exact NTT inner products)
+//   3. EvalPoly: t-1 external products per shard (exact NTTs)
+//   4. Rescale a to q1 and b to q2.
+// Every integer result is the exact value the reference's FP64 FFT rounds to
+// whenever that rounding is exact.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/inspire_pir.h"
+#include "arith.cuh"
+#include "internal.h"
+#include "limb_gemm.h"
+#include "ntt.cuh"
+#include "poly_kernels.cuh"
+
+namespace inspire {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Status plumbing.
+// ---------------------------------------------------------------------------
+struct Status {
+  int code = INSPIRE_OK;
+  std::string msg;
+  bool ok() const { return code == INSPIRE_OK; }
+};
+
+Status Err(int code, std::string msg) { return Status{code, std::move(msg)}; }
+
+int Report(const Status& s, char* err, size_t err_len) {
+  if (err != nullptr && err_len > 0) {
+    std::snprintf(err, err_len, "%s", s.ok() ? "" : s.msg.c_str());
+  }
+  return s.code;
+}
+
+Status Cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return Status{};
+  return Err(INSPIRE_INTERNAL,
+             std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define RETURN_IF_ERROR(expr)     \
+  do {                            \
+    Status _s = (expr);           \
+    if (!_s.ok()) return _s;      \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Primes and NTT tables.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kPrimes[kMaxPrimes] = {2147352577u, 2146959361u,
+                                          2146041857u, 2145976321u,
+                                          2144796673u};
+
+uint64_t PowMod(uint64_t b, uint64_t e, uint64_t m) {
+  uint64_t r = 1 % m;
+  b %= m;
+  while (e) {
+    if (e & 1) r = r * b % m;
+    b = b * b % m;
+    e >>= 1;
+  }
+  return r;
+}
+
+uint32_t Generator(uint32_t p) {
+  std::vector<uint64_t> factors;
+  uint64_t n = p - 1;
+  for (uint64_t f = 2; f * f <= n; ++f) {
+    if (n % f == 0) {
+      factors.push_back(f);
+      while (n % f == 0) n /= f;
+    }
+  }
+  if (n > 1) factors.push_back(n);
+  for (uint64_t g = 2;; ++g) {
+    bool ok = true;
+    for (uint64_t f : factors) {
+      if (PowMod(g, (p - 1) / f, p) == 1) {
+        ok = false;
+        break;
+      }
+    }
+    if (ok) return static_cast<uint32_t>(g);
+  }
+}
+
+uint32_t InvMod2_32(uint32_t p) {  // p odd
+  uint32_t x = p;  // correct to 3 bits
+  for (int i = 0; i < 5; ++i) x *= 2 - p * x;
+  return x;
+}
+
+uint32_t Shoup(uint32_t w, uint32_t p) {
+  return static_cast<uint32_t>((static_cast<uint64_t>(w) << 32) / p);
+}
+
+int BitRev(int x, int bits) {
+  int r = 0;
+  for (int b = 0; b < bits; ++b) r = (r << 1) | ((x >> b) & 1);
+  return r;
+}
+
+// Device tables for one ring degree, all primes.
+class NttTables {
+ public:
+  static Status Create(int logd, std::unique_ptr<NttTables>* out) {
+    if (logd < 1 || logd > kLogMaxDegree) {
+      return Err(INSPIRE_INVALID_ARGUMENT, "Invalid log_d.");
+    }
+    std::unique_ptr<NttTables> t(new NttTables());
+    t->logd_ = logd;
+    const int d = 1 << logd;
+    std::vector<uint32_t> host(static_cast<size_t>(kMaxPrimes) * 4 * d);
+    for (int pi = 0; pi < kMaxPrimes; ++pi) {
+      const uint32_t p = kPrimes[pi];
+      const uint64_t psi = PowMod(Generator(p), (p - 1) / (2ull * d), p);
+      const uint64_t psi_inv = PowMod(psi, p - 2, p);
+      if (PowMod(psi, d, p) != p - 1) {
+        return Err(INSPIRE_INTERNAL, "NTT root of unity check failed.");
+      }
+      uint32_t* tab = host.data() + static_cast<size_t>(pi) * 4 * d;
+      for (int i = 0; i < d; ++i) {
+        const int br = BitRev(i, logd);
+        const uint32_t w = static_cast<uint32_t>(PowMod(psi, br, p));
+        const uint32_t iw = static_cast<uint32_t>(PowMod(psi_inv, br, p));
+        tab[i] = w;
+        tab[d + i] = Shoup(w, p);
+        tab[2 * d + i] = iw;
+        tab[3 * d + i] = Shoup(iw, p);
+      }
+    }
+    RETURN_IF_ERROR(Cuda(cudaMalloc(&t->dev_, host.size() * 4), "cudaMalloc"));
+    RETURN_IF_ERROR(Cuda(cudaMemcpy(t->dev_, host.data(), host.size() * 4,
+                                    cudaMemcpyHostToDevice),
+                         "cudaMemcpy"));
+    *out = std::move(t);
+    return Status{};
+  }
+  ~NttTables() {
+    if (dev_) cudaFree(dev_);
+  }
+
+  NttCtx Ctx(int r) const {
+    NttCtx c{};
+    c.logd = logd_;
+    c.r = r;
+    const uint64_t d = 1ull << logd_;
+    for (int i = 0; i < kMaxPrimes; ++i) {
+      const uint32_t p = kPrimes[i];
+      c.p[i] = p;
+      c.pinv[i] = InvMod2_32(p);
+      c.half[i] = (p - 1) / 2;
+      const uint64_t dinv = PowMod(d, p - 2, p);
+      const uint64_t r32 = (1ull << 32) % p;
+      c.scale[i] = static_cast<uint32_t>(dinv * r32 % p);
+      c.scale_s[i] = Shoup(c.scale[i], p);
+      uint64_t prod = 1;
+      for (int j = 0; j < i; ++j) prod *= kPrimes[j];
+      c.pm[i] = prod;
+      for (int j = 0; j < kMaxPrimes; ++j) {
+        const uint64_t inv = PowMod(kPrimes[j] % p, p - 2, p);
+        c.garner[j][i] = j == i ? 0 : static_cast<uint32_t>(inv * r32 % p);
+      }
+    }
+    c.tables = dev_;
+    return c;
+  }
+
+ private:
+  NttTables() = default;
+  int logd_ = 0;
+  uint32_t* dev_ = nullptr;
+};
+
+// Smallest number of primes whose signed CRT range holds |x| < 2^bits.
+Status PrimesFor(double bits, int* r) {
+  for (int n = 1; n <= kMaxPrimes; ++n) {
+    double have = std::log2((kPrimes[n - 1] - 1) / 2.0);
+    for (int j = 0; j < n - 1; ++j) have += std::log2(kPrimes[j]);
+    if (bits < have - 0.01) {
+      *r = std::max(n, 2);
+      return Status{};
+    }
+  }
+  return Err(INSPIRE_INVALID_ARGUMENT,
+             "Negacyclic product exceeds the supported exact range.");
+}
+
+// ---------------------------------------------------------------------------
+// The reference's InnerProductFft chunk rule (polynomial_fft.cc:90-107) and
+// the chunk size its callers pick (lwes_to_rlwe.cc:60-74,
+// external_product.cc:100-102).
+// ---------------------------------------------------------------------------
+struct ChunkRule {
+  int chunk_bits = 0;
+  int u_chunks = 0;
+  int v_chunks = 0;
+};
+
+int ChunkFor(int num_polys, int d) {
+  const int max_allowed =
+      static_cast<int>((53.0 - std::log2(num_polys) - std::log2(d)) / 2.0);
+  return std::min(20, max_allowed);
+}
+
+Status MakeRule(int coeff_bits, int n, int d, int u_bits, int v_bits,
+                int chunk_bits, ChunkRule* rule) {
+  if (u_bits <= 0 || v_bits <= 0 || chunk_bits <= 0 || chunk_bits > 63) {
+    return Err(INSPIRE_INVALID_ARGUMENT, "Invalid bits or chunk_bits.");
+  }
+  if (std::log2(n) + std::log2(d) + 2.0 * chunk_bits > 53.0) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "Potential precision overflow in accumulation.");
+  }
+  const int max_chunks = (coeff_bits + chunk_bits - 1) / chunk_bits;
+  rule->chunk_bits = chunk_bits;
+  rule->u_chunks = std::min((u_bits + chunk_bits - 1) / chunk_bits, max_chunks);
+  rule->v_chunks = std::min((v_bits + chunk_bits - 1) / chunk_bits, max_chunks);
+  return Status{};
+}
+
+uint64_t MaskBits(int bits, int coeff_bits) {
+  const int b = std::min(bits, coeff_bits);
+  return b >= 64 ? ~0ull : ((1ull << b) - 1);
+}
+
+// u rebuilt from its chunks, as the FFT path reads it (with the signed top
+// chunk), as a two's complement 64-bit value.
+int64_t RebuildU(uint64_t x, const ChunkRule& r, int u_bits, bool is_signed) {
+  const uint64_t mask = (1ull << r.chunk_bits) - 1;
+  uint64_t acc = 0;
+  for (int c = 0; c < r.u_chunks; ++c) {
+    const uint64_t chunk = (x >> (r.chunk_bits * c)) & mask;
+    int64_t v = static_cast<int64_t>(chunk);
+    if (is_signed && c == r.u_chunks - 1) {
+      const int bits_in_chunk = u_bits - r.chunk_bits * c;
+      const int shift = 64 - bits_in_chunk;
+      v = static_cast<int64_t>(chunk << shift) >> shift;
+    }
+    acc += static_cast<uint64_t>(v) << (r.chunk_bits * c);
+  }
+  return static_cast<int64_t>(acc);
+}
+
+double BoundBits(int n, int d, double u_bits, double v_bits) {
+  return u_bits + v_bits + std::log2(static_cast<double>(n) * d);
+}
+
+size_t Words(int coeff_bits) { return coeff_bits / 8; }
+
+// ---------------------------------------------------------------------------
+// RAII device buffer.
+// ---------------------------------------------------------------------------
+class DevBuf {
+ public:
+  DevBuf() = default;
+  ~DevBuf() { Free(); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  Status Alloc(size_t bytes) {
+    Free();
+    if (bytes == 0) return Status{};
+    cudaError_t e = cudaMalloc(&ptr_, bytes);
+    if (e != cudaSuccess) {
+      ptr_ = nullptr;
+      return Err(INSPIRE_RESOURCE_EXHAUSTED,
+                 std::string("GPU allocation of ") + std::to_string(bytes) +
+                     " bytes failed: " + cudaGetErrorString(e));
+    }
+    bytes_ = bytes;
+    return Status{};
+  }
+  Status Upload(const void* host, size_t bytes) {
+    RETURN_IF_ERROR(Alloc(bytes));
+    if (bytes == 0) return Status{};
+    return Cuda(cudaMemcpy(ptr_, host, bytes, cudaMemcpyHostToDevice),
+                "cudaMemcpy H2D");
+  }
+  void Free() {
+    if (ptr_) cudaFree(ptr_);
+    ptr_ = nullptr;
+    bytes_ = 0;
+  }
+  template <typename P = void>
+  P* get() const {
+    return static_cast<P*>(ptr_);
+  }
+  size_t bytes() const { return bytes_; }
+
+ private:
+  void* ptr_ = nullptr;
+  size_t bytes_ = 0;
+};
+
+template <typename K>
+Status SetSmem(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return Status{};
+  return Cuda(cudaFuncSetAttribute(kernel,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(bytes)),
+              "cudaFuncSetAttribute");
+}
+
+}  // namespace
+}  // namespace inspire
+
+// ---------------------------------------------------------------------------
+// The server object.
+// ---------------------------------------------------------------------------
+struct inspire_pir_server {
+  inspire_pir_params prm{};
+  int d = 0, t = 0, l = 0, k = 0, ne = 0;
+  int64_t rows = 0, db_cols = 0, pack_cols = 0;
+  int interpolated_rows = 0;
+  inspire::Status deferred;  // error the reference reports per request
+
+  inspire::DevBuf db, pack, a_tilde, th_ntt, rgswa_ntt;
+  std::unique_ptr<inspire::NttTables> tables;
+  inspire::NttCtx ctx_f{}, ctx_e{};
+  uint64_t vmask_f = 0, vmask_e = 0, umask_e = 0;
+  std::unique_ptr<inspire::LimbGemm> limb;
+
+  // Per-batch workspace (grown on demand).
+  int cap = 0;
+  inspire::DevBuf q1, pkey, sdim, gemv, yh, rgswb, packed, resid0, resid1,
+      resp;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::mutex mu;
+  double t_db = 0, t_pack = 0, t_eval = 0;
+
+  ~inspire_pir_server() {
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace inspire {
+namespace {
+
+template <typename T>
+Status RunPolyStage(inspire_pir_server* s, int batch, const T* pkey,
+                    const T* sdim, const T* gemv, T* resp, cudaStream_t st,
+                    bool timed) {
+  const int d = s->d, t = s->t, l = s->l, k = s->k, ne = s->ne;
+  const int log_q = s->prm.log_modulus;
+  // y_h = packing_key[k..2k): forward NTT over the finalize primes.
+  {
+    const NttCtx& c = s->ctx_f;
+    dim3 grid(k * c.r, batch);
+    ntt_coeffs_kernel<T><<<grid, kPolyThreads, d * 4, st>>>(
+        pkey, static_cast<int64_t>(2 * k) * d, static_cast<int64_t>(k) * d, k,
+        static_cast<T>(s->vmask_f), s->yh.get<uint32_t>(), c);
+    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "ntt(y_h)"));
+  }
+  {
+    const NttCtx& c = s->ctx_f;
+    const size_t smem = static_cast<size_t>(c.r) * d * 4;
+    RETURN_IF_ERROR(SetSmem(finalize_kernel<T>, smem));
+    dim3 grid(l * t, batch);
+    finalize_kernel<T><<<grid, kPolyThreads, smem, st>>>(
+        s->th_ntt.get<uint32_t>(), s->yh.get<uint32_t>(), k, gemv, nullptr,
+        s->rows, s->packed.get<T>(), log_q, c);
+    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "finalize"));
+  }
+  if (timed) cudaEventRecord(s->ev[2], st);
+  const T* a_tilde = s->a_tilde.get<T>();
+  const T* packed = s->packed.get<T>();
+  const int64_t a_stride = static_cast<int64_t>(t) * d;        // per shard
+  const int64_t b_qstride = static_cast<int64_t>(l) * t * d;   // per request
+  uint32_t* resid[2] = {s->resid0.get<uint32_t>(), s->resid1.get<uint32_t>()};
+  if (t > 1) {
+    const NttCtx& c = s->ctx_e;
+    dim3 g1(2 * ne * c.r, batch);
+    ntt_coeffs_kernel<T><<<g1, kPolyThreads, d * 4, st>>>(
+        sdim, static_cast<int64_t>(2 * ne) * d, 0, 2 * ne,
+        static_cast<T>(s->vmask_e), s->rgswb.get<uint32_t>(), c);
+    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "ntt(rgsw)"));
+    ExtArgs e{log_q, s->prm.eval_log_digit, ne, s->umask_e};
+    const size_t smem = static_cast<size_t>(d) * 4 + 2ull * d * sizeof(T);
+    RETURN_IF_ERROR(SetSmem(ext_step_kernel<T>, smem));
+    dim3 grid(c.r, l, batch);
+    for (int i = t - 2; i >= 0; --i) {
+      const bool first = i == t - 2;
+      ext_step_kernel<T><<<grid, kPolyThreads, smem, st>>>(
+          first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
+          a_tilde + static_cast<int64_t>(i + 1) * d, a_stride,
+          packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
+          s->rgswa_ntt.get<uint32_t>(), s->rgswb.get<uint32_t>(), e, c);
+      RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
+    }
+  }
+  {
+    dim3 grid(l, batch);
+    finish_kernel<T><<<grid, kPolyThreads, 0, st>>>(
+        t > 1, resid[0], a_tilde, a_stride, packed, b_qstride, a_stride, true,
+        log_q, s->prm.log_modulus1_after_switch,
+        s->prm.log_modulus2_after_switch, resp, t > 1 ? s->ctx_e : s->ctx_f);
+    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "rescale"));
+  }
+  return Status{};
+}
+
+Status EnsureWorkspace(inspire_pir_server* s, int batch) {
+  if (batch <= s->cap) return Status{};
+  const size_t w = Words(s->prm.coeff_bits);
+  const size_t d = s->d;
+  const size_t B = batch;
+  RETURN_IF_ERROR(s->q1.Alloc(B * s->db_cols * w));
+  RETURN_IF_ERROR(s->pkey.Alloc(B * 2 * s->k * d * w));
+  RETURN_IF_ERROR(s->sdim.Alloc(B * std::max(1, 2 * s->ne) * d * w));
+  RETURN_IF_ERROR(s->gemv.Alloc(B * s->rows * w));
+  RETURN_IF_ERROR(s->yh.Alloc(B * s->k * s->ctx_f.r * d * 4));
+  RETURN_IF_ERROR(s->rgswb.Alloc(B * std::max(1, 2 * s->ne) * s->ctx_e.r * d * 4));
+  RETURN_IF_ERROR(s->packed.Alloc(B * s->l * s->t * d * w));
+  RETURN_IF_ERROR(s->resid0.Alloc(B * s->l * s->ctx_e.r * 2 * d * 4));
+  RETURN_IF_ERROR(s->resid1.Alloc(B * s->l * s->ctx_e.r * 2 * d * 4));
+  RETURN_IF_ERROR(s->resp.Alloc(B * s->l * 2 * d * w));
+  s->cap = batch;
+  return Status{};
+}
+
+// Validation shared by every ProcessResponse flavour
+// (pir_server.cc:160-205 plus the product size checks at :231-254).
+Status ValidateRequest(const inspire_pir_server* s, int64_t first_dim_len,
+                       int64_t second_dim_count, int64_t packing_key_count) {
+  if (packing_key_count != 2 * s->k) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "Packing key must contain 2 * num_digits polynomials.");
+  }
+  if (first_dim_len < s->interpolated_rows || first_dim_len > s->db_cols) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "First dimension query size (" + std::to_string(first_dim_len) +
+                   ") is invalid for DB columns (" +
+                   std::to_string(s->db_cols) + ").");
+  }
+  if (s->t > 1 && second_dim_count != 2 * s->ne) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "second_dimension_query size mismatch. Must be 2 * num_digits.");
+  }
+  if (s->pack_cols != static_cast<int64_t>(s->k) * s->d) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "Vector size must match the number of matrix columns.");
+  }
+  return s->deferred;
+}
+
+// Stage 1: out[q] = DB * q1[q] + P * y_g[q] for the whole batch.
+Status Products(inspire_pir_server* s, int batch, const void* q1,
+                const void* pkey, void* out, int engine, cudaStream_t st) {
+  const int cb = s->prm.coeff_bits;
+  if (engine == INSPIRE_ENGINE_TENSOR) {
+    if (!s->limb) {
+      return Err(INSPIRE_FAILED_PRECONDITION,
+                 "tensor engine unavailable for these parameters");
+    }
+    return Cuda(s->limb->Run(batch, q1, s->db_cols, pkey,
+                             static_cast<int64_t>(2 * s->k) * s->d, out, st),
+                "limb gemm");
+  }
+  if (engine != INSPIRE_ENGINE_PLAIN) {
+    return Err(INSPIRE_INVALID_ARGUMENT, "unknown engine.");
+  }
+  return Cuda(launch_fused_gemv(cb, s->prm.db_kind, s->db.get(), s->db_cols, q1,
+                                s->db_cols, s->prm.mat_kind, s->pack.get(),
+                                s->pack_cols, pkey,
+                                static_cast<int64_t>(2 * s->k) * s->d, out,
+                                s->rows, s->rows, batch, st),
+              "fused gemv");
+}
+
+// The device part of a batch: products, polynomial stage, rescale.
+Status AnswerOnDevice(inspire_pir_server* s, int batch, const void* q1,
+                      const void* pkey, const void* sdim, void* resp,
+                      int engine, cudaStream_t st, bool timed) {
+  const int cb = s->prm.coeff_bits;
+  if (timed) cudaEventRecord(s->ev[0], st);
+  RETURN_IF_ERROR(Products(s, batch, q1, pkey, s->gemv.get(), engine, st));
+  if (timed) cudaEventRecord(s->ev[1], st);
+  if (cb == 32) {
+    RETURN_IF_ERROR(RunPolyStage<uint32_t>(
+        s, batch, static_cast<const uint32_t*>(pkey),
+        static_cast<const uint32_t*>(sdim), s->gemv.get<uint32_t>(),
+        static_cast<uint32_t*>(resp), st, timed));
+  } else {
+    RETURN_IF_ERROR(RunPolyStage<uint64_t>(
+        s, batch, static_cast<const uint64_t*>(pkey),
+        static_cast<const uint64_t*>(sdim), s->gemv.get<uint64_t>(),
+        static_cast<uint64_t*>(resp), st, timed));
+  }
+  if (timed) cudaEventRecord(s->ev[3], st);
+  return Status{};
+}
+
+Status ProcessHostBatch(inspire_pir_server* s, int batch, const void* first_dim,
+                        int64_t first_dim_len, const void* second_dim,
+                        int64_t second_dim_count, const void* packing_key,
+                        int64_t packing_key_count, void* responses,
+                        int engine) {
+  if (batch <= 0) return Err(INSPIRE_INVALID_ARGUMENT, "batch must be positive.");
+  RETURN_IF_ERROR(ValidateRequest(s, first_dim_len, second_dim_count,
+                                  packing_key_count));
+  std::lock_guard<std::mutex> lock(s->mu);
+  RETURN_IF_ERROR(EnsureWorkspace(s, batch));
+  const size_t w = Words(s->prm.coeff_bits);
+  const size_t d = s->d;
+  cudaStream_t st = s->stream;
+  // Zero-padded first dimension (pir_server.cc:221-227).
+  RETURN_IF_ERROR(Cuda(cudaMemcpy2DAsync(s->q1.get(), s->db_cols * w, first_dim,
+                                         first_dim_len * w, first_dim_len * w,
+                                         batch, cudaMemcpyHostToDevice, st),
+                       "copy first_dim"));
+  if (first_dim_len < s->db_cols) {
+    RETURN_IF_ERROR(Cuda(
+        cudaMemset2DAsync(static_cast<char*>(s->q1.get()) + first_dim_len * w,
+                          s->db_cols * w, 0, (s->db_cols - first_dim_len) * w,
+                          batch, st),
+        "pad first_dim"));
+  }
+  RETURN_IF_ERROR(Cuda(cudaMemcpyAsync(s->pkey.get(), packing_key,
+                                       batch * packing_key_count * d * w,
+                                       cudaMemcpyHostToDevice, st),
+                       "copy packing_key"));
+  if (s->t > 1) {
+    RETURN_IF_ERROR(Cuda(cudaMemcpyAsync(s->sdim.get(), second_dim,
+                                         batch * second_dim_count * d * w,
+                                         cudaMemcpyHostToDevice, st),
+                         "copy second_dim"));
+  }
+  RETURN_IF_ERROR(AnswerOnDevice(s, batch, s->q1.get(), s->pkey.get(),
+                                 s->sdim.get(), s->resp.get(), engine, st, true));
+  const size_t out_bytes = static_cast<size_t>(batch) * s->l * 2 * d * w;
+  RETURN_IF_ERROR(Cuda(cudaMemcpyAsync(responses, s->resp.get(), out_bytes,
+                                       cudaMemcpyDeviceToHost, st),
+                       "copy response"));
+  RETURN_IF_ERROR(Cuda(cudaStreamSynchronize(st), "answer"));
+  float ms_db = 0, ms_pack = 0, ms_eval = 0;
+  cudaEventElapsedTime(&ms_db, s->ev[0], s->ev[1]);
+  cudaEventElapsedTime(&ms_pack, s->ev[1], s->ev[2]);
+  cudaEventElapsedTime(&ms_eval, s->ev[2], s->ev[3]);
+  s->t_db += ms_db;
+  s->t_pack += ms_pack;
+  s->t_eval += ms_eval;
+  return Status{};
+}
+
+// Server-constant transforms: t_vec_h (signed digits, the chunk rule's
+// operand) and second_dim_a (the RGSW a polynomials).
+template <typename T>
+Status PrepareConstants(inspire_pir_server* s, const T* t_vec_h,
+                        const T* second_dim_a, const ChunkRule& rule_f,
+                        const ChunkRule& rule_e) {
+  const int d = s->d;
+  const int64_t nth = static_cast<int64_t>(s->l) * s->t * s->k;
+  {
+    std::vector<int64_t> th(nth * d);
+    for (int64_t i = 0; i < nth * d; ++i) {
+      th[i] = RebuildU(static_cast<uint64_t>(t_vec_h[i]), rule_f,
+                       s->prm.pack_log_digit, true);
+    }
+    DevBuf tmp;
+    RETURN_IF_ERROR(tmp.Upload(th.data(), th.size() * 8));
+    RETURN_IF_ERROR(s->th_ntt.Alloc(nth * s->ctx_f.r * d * 4));
+    ntt_signed_kernel<<<static_cast<unsigned>(nth * s->ctx_f.r), kPolyThreads,
+                        d * 4>>>(tmp.get<int64_t>(), static_cast<int>(nth),
+                                 s->th_ntt.get<uint32_t>(), s->ctx_f);
+    RETURN_IF_ERROR(Cuda(cudaDeviceSynchronize(), "t_vec_h transform"));
+  }
+  if (s->t > 1) {
+    const int ng = 2 * s->ne;
+    DevBuf tmp;
+    RETURN_IF_ERROR(tmp.Upload(second_dim_a, static_cast<size_t>(ng) * d * sizeof(T)));
+    RETURN_IF_ERROR(s->rgswa_ntt.Alloc(static_cast<size_t>(ng) * s->ctx_e.r * d * 4));
+    dim3 grid(ng * s->ctx_e.r, 1);
+    ntt_coeffs_kernel<T><<<grid, kPolyThreads, d * 4>>>(
+        tmp.get<T>(), 0, 0, ng, static_cast<T>(s->vmask_e),
+        s->rgswa_ntt.get<uint32_t>(), s->ctx_e);
+    RETURN_IF_ERROR(Cuda(cudaDeviceSynchronize(), "second_dim_a transform"));
+  }
+  (void)rule_e;
+  return Status{};
+}
+
+Status CreateServer(const inspire_pir_params* prm, const void* db,
+                    int64_t db_rows, int64_t db_cols, const void* pack,
+                    int64_t pack_rows, int64_t pack_cols,
+                    const void* a_tilde_agg, int64_t a_count,
+                    const void* t_vec_h, int64_t th_count,
+                    const void* second_dim_a, int64_t sda_count,
+                    std::unique_ptr<inspire_pir_server>* out) {
+  if (prm == nullptr) return Err(INSPIRE_INVALID_ARGUMENT, "params is null.");
+  if (prm->coeff_bits != 32 && prm->coeff_bits != 64) {
+    return Err(INSPIRE_INVALID_ARGUMENT, "coeff_bits must be 32 or 64.");
+  }
+  if (prm->db_kind != INSPIRE_U8 && prm->db_kind != INSPIRE_U16) {
+    return Err(INSPIRE_INVALID_ARGUMENT, "DbDataType must be uint8_t or uint16_t.");
+  }
+  if (prm->mat_kind != INSPIRE_I16 && prm->mat_kind != INSPIRE_I32 &&
+      prm->mat_kind != (prm->coeff_bits == 32 ? INSPIRE_U32 : INSPIRE_U64)) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "MatCoeffType must be int16_t, int32_t or CoeffType.");
+  }
+  if (prm->log_degree < 5 || prm->log_degree > 13) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "ring degree must be between 32 and 8192.");
+  }
+  // PirParams::Create validation (crypto/pir/pir_params.cc:29-68).
+  const int t = prm->interpolation_degree;
+  const int d = 1 << prm->log_degree;
+  if (prm->num_entries <= 0) {
+    return Err(INSPIRE_INVALID_ARGUMENT, "num_entries must be strictly positive.");
+  }
+  if (prm->entry_size_multiple <= 0) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "entry_size_multiple must be strictly positive.");
+  }
+  if (t <= 0 || (t & (t - 1)) != 0) {
+    return Err(INSPIRE_INVALID_ARGUMENT, "interpolation_degree must be a power of two.");
+  }
+  if (prm->num_entries % t != 0) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "interpolation_degree (" + std::to_string(t) +
+                   ") must divide num_entries (" +
+                   std::to_string(prm->num_entries) + ").");
+  }
+  if (t > 2 * d) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "interpolation_degree (" + std::to_string(t) +
+                   ") must be less than or equal to 2 * ring degree (" +
+                   std::to_string(2 * d) + ").");
+  }
+  if (prm->log_modulus <= 0 || prm->log_modulus > prm->coeff_bits) {
+    return Err(INSPIRE_INVALID_ARGUMENT, "log_modulus out of range.");
+  }
+  if (prm->pack_num_digits <= 0 || prm->pack_log_digit <= 0 ||
+      prm->eval_num_digits <= 0 || prm->eval_log_digit <= 0) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "log_digit and num_digits must be positive.");
+  }
+  const int l = prm->entry_size_multiple;
+  // PirServer::Create shape checks (pir_server.cc:58-95).
+  if (db_rows != static_cast<int64_t>(l) * t * d) {
+    return Err(INSPIRE_INVALID_ARGUMENT, "DB matrix must have td rows.");
+  }
+  if (db_cols < prm->num_entries / t) {
+    return Err(INSPIRE_INVALID_ARGUMENT, "DB matrix must have at least N/t columns.");
+  }
+  if (a_count != static_cast<int64_t>(l) * t) {
+    return Err(INSPIRE_INVALID_ARGUMENT, "Preprocessed outputs must be of length t.");
+  }
+  if (th_count != static_cast<int64_t>(l) * t * prm->pack_num_digits) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "t_vec_h must hold pack_num_digits polynomials per slice.");
+  }
+  if (pack_rows != db_rows) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "Packing multiplication resulted in incorrect vector size.");
+  }
+  if (t > 1 && sda_count != 2 * prm->eval_num_digits) {
+    return Err(INSPIRE_INVALID_ARGUMENT,
+               "second_dim_query_a must have length 2 * "
+               "PolyEvalGadgetParams().num_digits.");
+  }
+  int dev = 0;
+  RETURN_IF_ERROR(Cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+
+  std::unique_ptr<inspire_pir_server> s(new inspire_pir_server());
+  s->prm = *prm;
+  s->d = d;
+  s->t = t;
+  s->l = l;
+  s->k = prm->pack_num_digits;
+  s->ne = prm->eval_num_digits;
+  s->rows = db_rows;
+  s->db_cols = db_cols;
+  s->pack_cols = pack_cols;
+  s->interpolated_rows = prm->num_entries / t;
+
+  // Chunk rules of the two inner products and the prime counts that make
+  // the NTT route exact for every operand those rules admit.
+  const int cb = prm->coeff_bits;
+  ChunkRule rf, re;
+  Status sf = MakeRule(cb, s->k, d, prm->pack_log_digit, prm->log_modulus,
+                       ChunkFor(s->k, d), &rf);
+  Status se = MakeRule(cb, 2 * s->ne, d, prm->eval_log_digit, prm->log_modulus,
+                       ChunkFor(2 * s->ne, d), &re);
+  if (!sf.ok()) s->deferred = sf;
+  if (t > 1 && !se.ok() && s->deferred.ok()) s->deferred = se;
+  int r_f = 3, r_e = 3;
+  if (sf.ok()) {
+    s->vmask_f = MaskBits(rf.v_chunks * rf.chunk_bits, cb);
+    RETURN_IF_ERROR(PrimesFor(
+        BoundBits(s->k, d, std::min(rf.u_chunks * rf.chunk_bits, 64),
+                  std::min(rf.v_chunks * rf.chunk_bits, cb)),
+        &r_f));
+  }
+  if (se.ok()) {
+    s->vmask_e = MaskBits(re.v_chunks * re.chunk_bits, cb);
+    s->umask_e = MaskBits(re.u_chunks * re.chunk_bits, cb);
+    RETURN_IF_ERROR(PrimesFor(
+        BoundBits(2 * s->ne, d,
+                  std::min({prm->eval_log_digit, re.u_chunks * re.chunk_bits, cb}),
+                  std::min(re.v_chunks * re.chunk_bits, cb)),
+        &r_e));
+  }
+  RETURN_IF_ERROR(NttTables::Create(prm->log_degree, &s->tables));
+  s->ctx_f = s->tables->Ctx(r_f);
+  s->ctx_e = s->tables->Ctx(r_e);
+
+  const size_t w = Words(cb);
+  RETURN_IF_ERROR(s->db.Upload(db, static_cast<size_t>(db_rows) * db_cols *
+                                       elem_size(prm->db_kind)));
+  RETURN_IF_ERROR(s->pack.Upload(pack, static_cast<size_t>(pack_rows) *
+                                           pack_cols * elem_size(prm->mat_kind)));
+  RETURN_IF_ERROR(s->a_tilde.Upload(a_tilde_agg, static_cast<size_t>(a_count) * d * w));
+  if (sf.ok() && (t == 1 || se.ok())) {
+    if (cb == 32) {
+      RETURN_IF_ERROR(PrepareConstants<uint32_t>(
+          s.get(), static_cast<const uint32_t*>(t_vec_h),
+          static_cast<const uint32_t*>(second_dim_a), rf, re));
+    } else {
+      RETURN_IF_ERROR(PrepareConstants<uint64_t>(
+          s.get(), static_cast<const uint64_t*>(t_vec_h),
+          static_cast<const uint64_t*>(second_dim_a), rf, re));
+    }
+  }
+  RETURN_IF_ERROR(Cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking),
+                       "cudaStreamCreate"));
+  for (auto& e : s->ev) RETURN_IF_ERROR(Cuda(cudaEventCreate(&e), "cudaEventCreate"));
+  // The tensor-core engine when the shapes allow it.
+  LimbGemm::Create(cb, prm->db_kind, s->db.get(), db_rows, db_cols,
+                   prm->mat_kind, s->pack.get(), pack_cols, &s->limb);
+  *out = std::move(s);
+  return Status{};
+}
+
+}  // namespace
+}  // namespace inspire
+
+// ---------------------------------------------------------------------------
+// C ABI.
+// ---------------------------------------------------------------------------
+using inspire::Err;
+using inspire::Report;
+using inspire::Status;
+
+extern "C" {
+
+int inspire_pir_server_create(const inspire_pir_params* params, const void* db,
+                              int64_t db_rows, int64_t db_cols,
+                              const void* pack, int64_t pack_rows,
+                              int64_t pack_cols, const void* a_tilde_agg,
+                              int64_t a_tilde_agg_count, const void* t_vec_h,
+                              int64_t t_vec_h_count, const void* second_dim_a,
+                              int64_t second_dim_a_count,
+                              inspire_pir_server** out, char* err,
+                              size_t err_len) {
+  if (out == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "out is null."), err, err_len);
+  }
+  *out = nullptr;
+  std::unique_ptr<inspire_pir_server> s;
+  Status st = inspire::CreateServer(params, db, db_rows, db_cols, pack,
+                                    pack_rows, pack_cols, a_tilde_agg,
+                                    a_tilde_agg_count, t_vec_h, t_vec_h_count,
+                                    second_dim_a, second_dim_a_count, &s);
+  if (st.ok()) *out = s.release();
+  return Report(st, err, err_len);
+}
+
+void inspire_pir_server_destroy(inspire_pir_server* server) { delete server; }
+
+int inspire_pir_process_response(inspire_pir_server* server,
+                                 const void* first_dim, int64_t first_dim_len,
+                                 const void* second_dim,
+                                 int64_t second_dim_count,
+                                 const void* packing_key,
+                                 int64_t packing_key_count, void* response,
+                                 char* err, size_t err_len) {
+  return inspire_pir_process_batch(server, 1, first_dim, first_dim_len,
+                                   second_dim, second_dim_count, packing_key,
+                                   packing_key_count, response,
+                                   INSPIRE_ENGINE_PLAIN, err, err_len);
+}
+
+int inspire_pir_process_batch(inspire_pir_server* server, int32_t batch,
+                              const void* first_dim, int64_t first_dim_len,
+                              const void* second_dim, int64_t second_dim_count,
+                              const void* packing_key,
+                              int64_t packing_key_count, void* responses,
+                              int32_t engine, char* err, size_t err_len) {
+  if (server == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server is null."), err, err_len);
+  }
+  return Report(inspire::ProcessHostBatch(server, batch, first_dim,
+                                          first_dim_len, second_dim,
+                                          second_dim_count, packing_key,
+                                          packing_key_count, responses, engine),
+                err, err_len);
+}
+
+int inspire_pir_process_batch_device(inspire_pir_server* server,
+                                     int32_t batch, const void* first_dim,
+                                     int64_t first_dim_len,
+                                     const void* second_dim,
+                                     int64_t second_dim_count,
+                                     const void* packing_key,
+                                     int64_t packing_key_count,
+                                     void* responses, int32_t engine,
+                                     void* stream, char* err, size_t err_len) {
+  if (server == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server is null."), err, err_len);
+  }
+  if (batch <= 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "batch must be positive."), err,
+                  err_len);
+  }
+  Status st = inspire::ValidateRequest(server, first_dim_len, second_dim_count,
+                                       packing_key_count);
+  if (!st.ok()) return Report(st, err, err_len);
+  std::lock_guard<std::mutex> lock(server->mu);
+  st = inspire::EnsureWorkspace(server, batch);
+  if (!st.ok()) return Report(st, err, err_len);
+  st = inspire::AnswerOnDevice(server, batch, first_dim, packing_key, second_dim,
+                               responses, engine,
+                               static_cast<cudaStream_t>(stream), false);
+  return Report(st, err, err_len);
+}
+
+int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,
+                                const void* first_dim, const void* packing_key,
+                                void* out, int32_t engine, void* stream,
+                                char* err, size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr || batch <= 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server is null or batch <= 0."),
+                  err, err_len);
+  }
+  std::lock_guard<std::mutex> lock(server->mu);
+  Status st = Products(server, batch, first_dim, packing_key, out, engine,
+                       static_cast<cudaStream_t>(stream));
+  return Report(st, err, err_len);
+}
+
+int inspire_pir_server_shape(const inspire_pir_server* server, int64_t* rows,
+                             int64_t* db_cols, int64_t* pack_cols) {
+  if (server == nullptr) return INSPIRE_INVALID_ARGUMENT;
+  if (rows) *rows = server->rows;
+  if (db_cols) *db_cols = server->db_cols;
+  if (pack_cols) *pack_cols = server->pack_cols;
+  return INSPIRE_OK;
+}
+
+int inspire_pir_server_timings(const inspire_pir_server* server,
+                               double* db_mult_ms, double* packing_ms,
+                               double* poly_eval_ms) {
+  if (server == nullptr) return INSPIRE_INVALID_ARGUMENT;
+  if (db_mult_ms) *db_mult_ms = server->t_db;
+  if (packing_ms) *packing_ms = server->t_pack;
+  if (poly_eval_ms) *poly_eval_ms = server->t_eval;
+  return INSPIRE_OK;
+}
+
+int inspire_matrix_multiply(int32_t mat_kind, int32_t coeff_bits,
+                            const void* mat, int64_t rows, int64_t cols,
+                            const void* vec, void* out, char* err,
+                            size_t err_len) {
+  using namespace inspire;
+  if ((coeff_bits != 32 && coeff_bits != 64) || elem_size(mat_kind) == 0 ||
+      rows < 0 || cols < 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "invalid matrix arguments."),
+                  err, err_len);
+  }
+  const size_t w = coeff_bits / 8;
+  DevBuf dm, dv, dout;
+  Status st = dm.Upload(mat, static_cast<size_t>(rows) * cols * elem_size(mat_kind));
+  if (st.ok()) st = dv.Upload(vec, static_cast<size_t>(cols) * w);
+  if (st.ok()) st = dout.Alloc(static_cast<size_t>(rows) * w);
+  if (st.ok() && rows > 0) {
+    st = Cuda(launch_fused_gemv(coeff_bits, mat_kind, dm.get(), cols, dv.get(), cols,
+                                INSPIRE_I32, nullptr, 0, nullptr, 0, dout.get(), rows,
+                                rows, 1, nullptr),
+              "gemv");
+    if (st.ok()) st = Cuda(cudaDeviceSynchronize(), "gemv");
+    if (st.ok()) {
+      st = Cuda(cudaMemcpy(out, dout.get(), rows * w, cudaMemcpyDeviceToHost),
+                "copy out");
+    }
+  }
+  return Report(st, err, err_len);
+}
+
+int inspire_inner_product(int32_t coeff_bits, const void* u, const void* v,
+                          int32_t n, int32_t d, int32_t u_bits, int32_t v_bits,
+                          int32_t chunk_bits, int32_t u_is_signed, void* out,
+                          char* err, size_t err_len) {
+  using namespace inspire;
+  if (n <= 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT,
+                      "Polynomial vectors cannot be empty."),
+                  err, err_len);
+  }
+  if (coeff_bits != 32 && coeff_bits != 64) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "coeff_bits must be 32 or 64."),
+                  err, err_len);
+  }
+  int logd = 0;
+  while ((1 << logd) < d) ++logd;
+  if (d < 2 || (1 << logd) != d || logd > 13) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT,
+                      "Polynomial lengths or context mismatch."),
+                  err, err_len);
+  }
+  ChunkRule rule;
+  Status st = MakeRule(coeff_bits, n, d, u_bits, v_bits, chunk_bits, &rule);
+  if (!st.ok()) return Report(st, err, err_len);
+  const int ub = std::min(rule.u_chunks * rule.chunk_bits, 64);
+  const int vb = std::min(rule.v_chunks * rule.chunk_bits, coeff_bits);
+  int r = 0;
+  st = PrimesFor(BoundBits(n, d, ub, vb), &r);
+  if (!st.ok()) return Report(st, err, err_len);
+  std::unique_ptr<NttTables> tabs;
+  st = NttTables::Create(logd, &tabs);
+  if (!st.ok()) return Report(st, err, err_len);
+  NttCtx c = tabs->Ctx(r);
+  const size_t total = static_cast<size_t>(n) * d;
+  const size_t w = coeff_bits / 8;
+  DevBuf du, dv, dU, dV, dout;
+  // u as the chunk rule rebuilds it (signed when asked); v masked.
+  std::vector<int64_t> ue(total);
+  for (size_t i = 0; i < total; ++i) {
+    const uint64_t x = coeff_bits == 32
+                           ? static_cast<const uint32_t*>(u)[i]
+                           : static_cast<const uint64_t*>(u)[i];
+    ue[i] = RebuildU(x, rule, u_bits, u_is_signed != 0);
+  }
+  const uint64_t vmask = MaskBits(rule.v_chunks * rule.chunk_bits, coeff_bits);
+  const bool u_fits_signed = u_is_signed != 0 || ub < 64;
+  if (st.ok()) st = dU.Alloc(total * r * 4);
+  if (st.ok()) st = dV.Alloc(total * r * 4);
+  if (st.ok()) st = dv.Upload(v, total * w);
+  if (st.ok()) st = dout.Alloc(d * w);
+  if (st.ok()) {
+    if (u_fits_signed) {
+      st = du.Upload(ue.data(), total * 8);
+      if (st.ok()) {
+        ntt_signed_kernel<<<n * r, kPolyThreads, d * 4>>>(du.get<int64_t>(), n,
+                                                         dU.get<uint32_t>(), c);
+      }
+    } else if (coeff_bits == 64) {
+      st = du.Upload(ue.data(), total * 8);  // full-width unsigned u
+      if (st.ok()) {
+        ntt_coeffs_kernel<uint64_t><<<dim3(n * r, 1), kPolyThreads, d * 4>>>(
+            du.get<uint64_t>(), 0, 0, n, ~0ull, dU.get<uint32_t>(), c);
+      }
+    }
+  }
+  if (st.ok()) {
+    if (coeff_bits == 32) {
+      ntt_coeffs_kernel<uint32_t><<<dim3(n * r, 1), kPolyThreads, d * 4>>>(
+          dv.get<uint32_t>(), 0, 0, n, static_cast<uint32_t>(vmask),
+          dV.get<uint32_t>(), c);
+      st = SetSmem(inner_product_finish_kernel<uint32_t>, static_cast<size_t>(r) * d * 4);
+      if (st.ok())
+        inner_product_finish_kernel<uint32_t><<<1, kPolyThreads, r * d * 4>>>(
+            dU.get<uint32_t>(), dV.get<uint32_t>(), n, dout.get<uint32_t>(), c);
+    } else {
+      ntt_coeffs_kernel<uint64_t><<<dim3(n * r, 1), kPolyThreads, d * 4>>>(
+          dv.get<uint64_t>(), 0, 0, n, vmask, dV.get<uint32_t>(), c);
+      st = SetSmem(inner_product_finish_kernel<uint64_t>, static_cast<size_t>(r) * d * 4);
+      if (st.ok())
+        inner_product_finish_kernel<uint64_t><<<1, kPolyThreads, r * d * 4>>>(
+            dU.get<uint32_t>(), dV.get<uint32_t>(), n, dout.get<uint64_t>(), c);
+    }
+  }
+  if (st.ok()) st = Cuda(cudaDeviceSynchronize(), "inner product");
+  if (st.ok()) {
+    st = Cuda(cudaMemcpy(out, dout.get(), d * w, cudaMemcpyDeviceToHost), "copy out");
+  }
+  return Report(st, err, err_len);
+}
+
+int inspire_external_product(const inspire_pir_params* params,
+                             const void* ct_a, const void* ct_b,
+                             const void* rgsw, void* out_a, void* out_b,
+                             char* err, size_t err_len) {
+  using namespace inspire;
+  // A one-request, one-shard server-less run of the EvalPoly step kernel.
+  if (params == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "params is null."), err, err_len);
+  }
+  const int cb = params->coeff_bits;
+  const int d = 1 << params->log_degree;
+  const int ne = params->eval_num_digits;
+  if (ne <= 0 || params->eval_log_digit <= 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "rgsw_ct sizes must match num_digits."),
+                  err, err_len);
+  }
+  ChunkRule re;
+  Status st = MakeRule(cb, 2 * ne, d, params->eval_log_digit, params->log_modulus,
+                       ChunkFor(2 * ne, d), &re);
+  if (!st.ok()) return Report(st, err, err_len);
+  int r = 0;
+  st = PrimesFor(BoundBits(2 * ne, d,
+                           std::min({params->eval_log_digit,
+                                     re.u_chunks * re.chunk_bits, cb}),
+                           std::min(re.v_chunks * re.chunk_bits, cb)),
+                 &r);
+  if (!st.ok()) return Report(st, err, err_len);
+  std::unique_ptr<NttTables> tabs;
+  st = NttTables::Create(params->log_degree, &tabs);
+  if (!st.ok()) return Report(st, err, err_len);
+  NttCtx c = tabs->Ctx(r);
+  const size_t w = cb / 8;
+  const int ng = 2 * ne;
+  // Split the interleaved (a, b) RGSW layout into a-parts and b-parts.
+  std::vector<unsigned char> ra(static_cast<size_t>(ng) * d * w),
+      rb(static_cast<size_t>(ng) * d * w);
+  const unsigned char* src = static_cast<const unsigned char*>(rgsw);
+  for (int g = 0; g < ng; ++g) {
+    std::memcpy(ra.data() + static_cast<size_t>(g) * d * w,
+                src + static_cast<size_t>(2 * g) * d * w, d * w);
+    std::memcpy(rb.data() + static_cast<size_t>(g) * d * w,
+                src + static_cast<size_t>(2 * g + 1) * d * w, d * w);
+  }
+  DevBuf dra, drb, dA, dB, dca, dcb, dres, dout;
+  st = dra.Upload(ra.data(), ra.size());
+  if (st.ok()) st = drb.Upload(rb.data(), rb.size());
+  if (st.ok()) st = dA.Alloc(static_cast<size_t>(ng) * r * d * 4);
+  if (st.ok()) st = dB.Alloc(static_cast<size_t>(ng) * r * d * 4);
+  if (st.ok()) st = dca.Upload(ct_a, d * w);
+  if (st.ok()) st = dcb.Upload(ct_b, d * w);
+  if (st.ok()) st = dres.Alloc(static_cast<size_t>(r) * 2 * d * 4);
+  if (st.ok()) st = dout.Alloc(2 * d * w);
+  const uint64_t vmask = MaskBits(re.v_chunks * re.chunk_bits, cb);
+  ExtArgs e{params->log_modulus, params->eval_log_digit, ne,
+            MaskBits(re.u_chunks * re.chunk_bits, cb)};
+  auto run = [&](auto tag) -> Status {
+    using T = decltype(tag);
+    ntt_coeffs_kernel<T><<<dim3(ng * r, 1), kPolyThreads, d * 4>>>(
+        dra.get<T>(), 0, 0, ng, static_cast<T>(vmask), dA.get<uint32_t>(), c);
+    ntt_coeffs_kernel<T><<<dim3(ng * r, 1), kPolyThreads, d * 4>>>(
+        drb.get<T>(), 0, 0, ng, static_cast<T>(vmask), dB.get<uint32_t>(), c);
+    const size_t smem = static_cast<size_t>(d) * 4 + 2ull * d * sizeof(T);
+    RETURN_IF_ERROR(SetSmem(ext_step_kernel<T>, smem));
+    ext_step_kernel<T><<<dim3(r, 1, 1), kPolyThreads, smem>>>(
+        true, nullptr, dres.get<uint32_t>(), dca.get<T>(), 0, dcb.get<T>(), 0, 0,
+        dA.get<uint32_t>(), dB.get<uint32_t>(), e, c);
+    finish_kernel<T><<<dim3(1, 1), kPolyThreads>>>(
+        true, dres.get<uint32_t>(), nullptr, 0, nullptr, 0, 0, false, 0, 0, 0,
+        dout.get<T>(), c);
+    return Cuda(cudaDeviceSynchronize(), "external product");
+  };
+  if (st.ok()) st = cb == 32 ? run(uint32_t{}) : run(uint64_t{});
+  if (st.ok()) st = Cuda(cudaMemcpy(out_a, dout.get(), d * w, cudaMemcpyDeviceToHost), "copy");
+  if (st.ok())
+    st = Cuda(cudaMemcpy(out_b, dout.get<char>() + d * w, d * w, cudaMemcpyDeviceToHost),
+              "copy");
+  return Report(st, err, err_len);
+}
+
+int inspire_finalize_matrix_pack(const inspire_pir_params* params,
+                                 const void* b, const void* b_agg_partial,
+                                 const void* y_vec_h, const void* t_vec_h,
+                                 void* out_b, char* err, size_t err_len) {
+  using namespace inspire;
+  if (params == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "params is null."), err, err_len);
+  }
+  const int cb = params->coeff_bits;
+  const int d = 1 << params->log_degree;
+  const int k = params->pack_num_digits;
+  if (k <= 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "InnerProduct: size mismatch or empty"),
+                  err, err_len);
+  }
+  ChunkRule rf;
+  Status st = MakeRule(cb, k, d, params->pack_log_digit, params->log_modulus,
+                       ChunkFor(k, d), &rf);
+  if (!st.ok()) return Report(st, err, err_len);
+  int r = 0;
+  st = PrimesFor(BoundBits(k, d, std::min(rf.u_chunks * rf.chunk_bits, 64),
+                           std::min(rf.v_chunks * rf.chunk_bits, cb)),
+                 &r);
+  if (!st.ok()) return Report(st, err, err_len);
+  std::unique_ptr<NttTables> tabs;
+  st = NttTables::Create(params->log_degree, &tabs);
+  if (!st.ok()) return Report(st, err, err_len);
+  NttCtx c = tabs->Ctx(r);
+  const size_t w = cb / 8;
+  std::vector<int64_t> th(static_cast<size_t>(k) * d);
+  for (size_t i = 0; i < th.size(); ++i) {
+    const uint64_t x = cb == 32 ? static_cast<const uint32_t*>(t_vec_h)[i]
+                                : static_cast<const uint64_t*>(t_vec_h)[i];
+    th[i] = RebuildU(x, rf, params->pack_log_digit, true);
+  }
+  DevBuf dth, dTh, dy, dYh, db1, db2, dout;
+  st = dth.Upload(th.data(), th.size() * 8);
+  if (st.ok()) st = dTh.Alloc(static_cast<size_t>(k) * r * d * 4);
+  if (st.ok()) st = dy.Upload(y_vec_h, static_cast<size_t>(k) * d * w);
+  if (st.ok()) st = dYh.Alloc(static_cast<size_t>(k) * r * d * 4);
+  if (st.ok()) st = db1.Upload(b, d * w);
+  if (st.ok()) st = db2.Upload(b_agg_partial, d * w);
+  if (st.ok()) st = dout.Alloc(d * w);
+  const uint64_t vmask = MaskBits(rf.v_chunks * rf.chunk_bits, cb);
+  auto run = [&](auto tag) -> Status {
+    using T = decltype(tag);
+    ntt_signed_kernel<<<k * r, kPolyThreads, d * 4>>>(dth.get<int64_t>(), k,
+                                                      dTh.get<uint32_t>(), c);
+    ntt_coeffs_kernel<T><<<dim3(k * r, 1), kPolyThreads, d * 4>>>(
+        dy.get<T>(), 0, 0, k, static_cast<T>(vmask), dYh.get<uint32_t>(), c);
+    const size_t smem = static_cast<size_t>(r) * d * 4;
+    RETURN_IF_ERROR(SetSmem(finalize_kernel<T>, smem));
+    finalize_kernel<T><<<dim3(1, 1), kPolyThreads, smem>>>(
+        dTh.get<uint32_t>(), dYh.get<uint32_t>(), k, db1.get<T>(), db2.get<T>(), 0,
+        dout.get<T>(), params->log_modulus, c);
+    return Cuda(cudaDeviceSynchronize(), "finalize");
+  };
+  if (st.ok()) st = cb == 32 ? run(uint32_t{}) : run(uint64_t{});
+  if (st.ok()) st = Cuda(cudaMemcpy(out_b, dout.get(), d * w, cudaMemcpyDeviceToHost), "copy");
+  return Report(st, err, err_len);
+}
+
+}  // extern "C"

@@ -1,0 +1,414 @@
+"""Python mirror of the reference PirServer API over the GB300 C ABI.
+
+Names, argument meaning and error behaviour follow the reference
+(google/InsPIRe):
+  PirParams / RlweParams / GadgetParams   crypto/pir/pir_params.h:36-105,
+                                          crypto/encryption.h:30-98
+  PirRequest / PirResponse                crypto/pir/pir_params.h:196-216
+  PreprocessMatrixPackOutput              crypto/lwes_to_rlwe.h:42-47
+  PirPreprocessedData                     crypto/pir/server/pir_preprocessed_data.h
+  PirServer::Create / ProcessResponse     crypto/pir/server/pir_server.h:45-72
+Errors raise InspireError carrying the absl status code and the reference's
+message. Every call runs the CUDA library; there is no CPU path.
+"""
+import ctypes
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib
+
+INVALID_ARGUMENT = 3
+RESOURCE_EXHAUSTED = 8
+FAILED_PRECONDITION = 9
+INTERNAL = 13
+
+ENGINE_PLAIN = 0
+ENGINE_TENSOR = 1
+
+KINDS = {np.dtype(np.uint8): 0, np.dtype(np.uint16): 1,
+         np.dtype(np.uint32): 2, np.dtype(np.uint64): 3,
+         np.dtype(np.int16): 4, np.dtype(np.int32): 5}
+
+
+class InspireError(RuntimeError):
+    """A non-OK status from the library (absl::Status equivalent)."""
+
+    def __init__(self, code, message):
+        super().__init__("status %d: %s" % (code, message))
+        self.code = code
+        self.message = message
+
+
+def _check(rc, err):
+    if rc != 0:
+        raise InspireError(rc, err.value.decode(errors="replace"))
+
+
+def _errbuf():
+    return ctypes.create_string_buffer(1024)
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else None
+
+
+@dataclass(frozen=True)
+class GadgetParams:
+    log_digit: int
+    num_digits: int
+
+
+@dataclass(frozen=True)
+class RlweParams:
+    """RlweParams<CoeffType>: ring degree, log2 of q, q1, q2 (0 bits = 2^w)."""
+    degree: int
+    log_modulus: int
+    log_modulus1_after_switch: int
+    log_modulus2_after_switch: int
+    variance: int = 0
+    coeff_bits: int = 64
+
+    def Degree(self):
+        return self.degree
+
+    def LogModulus(self):
+        return self.log_modulus
+
+    def LogModulus1AfterSwitch(self):
+        return self.log_modulus1_after_switch
+
+    def LogModulus2AfterSwitch(self):
+        return self.log_modulus2_after_switch
+
+
+@dataclass(frozen=True)
+class PirParams:
+    rlwe: RlweParams
+    plaintext_modulus: int
+    pack_gadget: GadgetParams
+    eval_gadget: GadgetParams
+    num_entries: int
+    interpolation_degree: int
+    entry_size_multiple: int = 1
+
+    def RlweParameters(self):
+        return self.rlwe
+
+    def PlaintextModulus(self):
+        return self.plaintext_modulus
+
+    def PackGadgetParams(self):
+        return self.pack_gadget
+
+    def PolyEvalGadgetParams(self):
+        return self.eval_gadget
+
+    def NumEntries(self):
+        return self.num_entries
+
+    def InterpolationDegree(self):
+        return self.interpolation_degree
+
+    def EntrySizeMultiple(self):
+        return self.entry_size_multiple
+
+    def InterpolatedRows(self):
+        return self.num_entries // self.interpolation_degree
+
+    def NumFirstDimSamples(self):
+        d = self.rlwe.degree
+        return (self.InterpolatedRows() + d - 1) // d
+
+    def PaddedCols(self):
+        return self.NumFirstDimSamples() * self.rlwe.degree
+
+    @property
+    def coeff_dtype(self):
+        return np.uint32 if self.rlwe.coeff_bits == 32 else np.uint64
+
+
+@dataclass
+class PreprocessMatrixPackOutput:
+    a_tilde_agg: np.ndarray          # (d,)
+    matrix: np.ndarray               # (d, k*d) MatCoeffType
+    t_vec_h: np.ndarray              # (k, d)
+
+
+@dataclass
+class PirPreprocessedData:
+    db_matrices: List[np.ndarray]                       # l x (t*d, cols)
+    preprocessed_outputs: List[List[PreprocessMatrixPackOutput]]  # l x t
+    second_dim_a: Optional[np.ndarray] = None           # (2*ne, d)
+
+
+@dataclass
+class PirRequest:
+    first_dimension_query: np.ndarray                  # (n_first,)
+    second_dimension_query: np.ndarray                 # (2*ne, d)
+    packing_key: np.ndarray                            # (2*k, d)
+
+
+@dataclass
+class PirResponse:
+    ciphertexts: np.ndarray                            # (l, 2, d): (a, b)
+
+
+class Params(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int32) for n in (
+        "coeff_bits", "db_kind", "mat_kind", "log_degree", "log_modulus",
+        "log_modulus1_after_switch", "log_modulus2_after_switch",
+        "pack_log_digit", "pack_num_digits", "eval_log_digit",
+        "eval_num_digits", "num_entries", "interpolation_degree",
+        "entry_size_multiple")] + [("plaintext_modulus", ctypes.c_uint64)]
+
+
+def c_params(params: PirParams, db_dtype=np.uint16, mat_dtype=np.int32):
+    r = params.rlwe
+    d = r.degree
+    log_d = d.bit_length() - 1
+    p = Params()
+    p.coeff_bits = r.coeff_bits
+    p.db_kind = KINDS[np.dtype(db_dtype)]
+    p.mat_kind = KINDS[np.dtype(mat_dtype)]
+    p.log_degree = log_d
+    p.log_modulus = r.log_modulus
+    p.log_modulus1_after_switch = r.log_modulus1_after_switch
+    p.log_modulus2_after_switch = r.log_modulus2_after_switch
+    p.pack_log_digit = params.pack_gadget.log_digit
+    p.pack_num_digits = params.pack_gadget.num_digits
+    p.eval_log_digit = params.eval_gadget.log_digit
+    p.eval_num_digits = params.eval_gadget.num_digits
+    p.num_entries = params.num_entries
+    p.interpolation_degree = params.interpolation_degree
+    p.entry_size_multiple = params.entry_size_multiple
+    p.plaintext_modulus = params.plaintext_modulus
+    return p
+
+
+class PirServer:
+    """GPU-resident PirServer<DbDataType, CoeffType, MatCoeffType>."""
+
+    def __init__(self, handle, params, rows, db_cols, pack_cols):
+        self._h = handle
+        self.params = params
+        self.rows = rows
+        self.db_cols = db_cols
+        self.pack_cols = pack_cols
+
+    @staticmethod
+    def Create(params: PirParams, data: PirPreprocessedData):
+        """PirServer::Create (crypto/pir/server/pir_server.cc:54-124)."""
+        t = params.interpolation_degree
+        l = params.entry_size_multiple
+        if len(data.db_matrices) != l:
+            raise InspireError(INVALID_ARGUMENT, "db_matrices size mismatch.")
+        if len(data.preprocessed_outputs) != l:
+            raise InspireError(INVALID_ARGUMENT,
+                               "preprocessed_outputs size mismatch.")
+        for outs in data.preprocessed_outputs:
+            if len(outs) != t:
+                raise InspireError(INVALID_ARGUMENT,
+                                   "Preprocessed outputs must be of length t.")
+        db_cols = data.db_matrices[0].shape[1]
+        for m in data.db_matrices:
+            if m.shape[1] != db_cols:
+                raise InspireError(
+                    INVALID_ARGUMENT,
+                    "All DB matrices must have the same number of columns.")
+        # VerticalConcatenate (crypto/matrix.cc:162-206).
+        db = np.ascontiguousarray(np.concatenate(data.db_matrices, axis=0))
+        pack = np.ascontiguousarray(np.concatenate(
+            [o.matrix for outs in data.preprocessed_outputs for o in outs],
+            axis=0))
+        cdt = params.coeff_dtype
+        a_tilde = np.ascontiguousarray(np.stack(
+            [o.a_tilde_agg for outs in data.preprocessed_outputs for o in outs]
+        ).astype(cdt, copy=False))
+        t_vec_h = np.ascontiguousarray(np.concatenate(
+            [np.asarray(o.t_vec_h) for outs in data.preprocessed_outputs
+             for o in outs]).astype(cdt, copy=False))
+        return PirServer.CreateCombined(params, db, pack, a_tilde, t_vec_h,
+                                        data.second_dim_a)
+
+    @staticmethod
+    def CreateCombined(params, db, pack, a_tilde_agg, t_vec_h, second_dim_a):
+        """Create from the already-combined matrices (the server's own
+        layout after VerticalConcatenate)."""
+        lib = _lib.load()
+        cdt = params.coeff_dtype
+        d = params.rlwe.degree
+        db = np.ascontiguousarray(db)
+        pack = np.ascontiguousarray(pack)
+        a_tilde_agg = np.ascontiguousarray(a_tilde_agg, dtype=cdt).reshape(-1, d)
+        t_vec_h = np.ascontiguousarray(t_vec_h, dtype=cdt).reshape(-1, d)
+        if second_dim_a is None:
+            second_dim_a = np.zeros((0, d), dtype=cdt)
+        second_dim_a = np.ascontiguousarray(second_dim_a, dtype=cdt).reshape(-1, d)
+        prm = c_params(params, db.dtype, pack.dtype)
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        rc = lib.inspire_pir_server_create(
+            ctypes.byref(prm), _ptr(db), db.shape[0], db.shape[1], _ptr(pack),
+            pack.shape[0], pack.shape[1], _ptr(a_tilde_agg),
+            a_tilde_agg.shape[0], _ptr(t_vec_h), t_vec_h.shape[0],
+            _ptr(second_dim_a), second_dim_a.shape[0], ctypes.byref(h), err,
+            len(err))
+        _check(rc, err)
+        return PirServer(h, params, db.shape[0], db.shape[1], pack.shape[1])
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            _lib.load().inspire_pir_server_destroy(h)
+            self._h = None
+
+    def ProcessResponse(self, request: PirRequest) -> PirResponse:
+        """PirServer::ProcessResponse (pir_server.cc:154-306)."""
+        return self.ProcessBatch([request])[0]
+
+    def ProcessBatch(self, requests, engine=ENGINE_PLAIN):
+        """Answers several requests of equal shape in one pass."""
+        cdt = self.params.coeff_dtype
+        d = self.params.rlwe.degree
+        fd = np.ascontiguousarray(np.stack(
+            [np.asarray(r.first_dimension_query, dtype=cdt) for r in requests]))
+        sd = np.ascontiguousarray(np.stack(
+            [np.asarray(r.second_dimension_query, dtype=cdt).reshape(-1, d)
+             for r in requests]))
+        pk = np.ascontiguousarray(np.stack(
+            [np.asarray(r.packing_key, dtype=cdt).reshape(-1, d)
+             for r in requests]))
+        out = self.process_arrays(fd, sd, pk, engine)
+        return [PirResponse(ciphertexts=o) for o in out]
+
+    def process_arrays(self, first_dim, second_dim, packing_key,
+                       engine=ENGINE_PLAIN):
+        """Stacked host arrays: (B, n1), (B, 2ne, d), (B, 2k, d) ->
+        responses (B, l, 2, d)."""
+        lib = _lib.load()
+        cdt = self.params.coeff_dtype
+        d = self.params.rlwe.degree
+        l = self.params.entry_size_multiple
+        first_dim = np.ascontiguousarray(first_dim, dtype=cdt)
+        second_dim = np.ascontiguousarray(second_dim, dtype=cdt)
+        packing_key = np.ascontiguousarray(packing_key, dtype=cdt)
+        b = first_dim.shape[0]
+        out = np.empty((b, l, 2, d), dtype=cdt)
+        err = _errbuf()
+        rc = lib.inspire_pir_process_batch(
+            self._h, b, _ptr(first_dim), first_dim.shape[1], _ptr(second_dim),
+            second_dim.shape[1] if second_dim.ndim == 3 else 0,
+            _ptr(packing_key), packing_key.shape[1], _ptr(out), engine, err,
+            len(err))
+        _check(rc, err)
+        return out
+
+    def process_device(self, batch, first_dim_ptr, first_dim_len,
+                       second_dim_ptr, second_dim_count, packing_key_ptr,
+                       packing_key_count, responses_ptr, engine=ENGINE_PLAIN,
+                       stream=0):
+        """Device-resident batch: raw CUDA device pointers, async on stream."""
+        lib = _lib.load()
+        err = _errbuf()
+        rc = lib.inspire_pir_process_batch_device(
+            self._h, batch, ctypes.c_void_p(first_dim_ptr), first_dim_len,
+            ctypes.c_void_p(second_dim_ptr), second_dim_count,
+            ctypes.c_void_p(packing_key_ptr), packing_key_count,
+            ctypes.c_void_p(responses_ptr), engine, ctypes.c_void_p(stream),
+            err, len(err))
+        _check(rc, err)
+
+    def _timings(self):
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _lib.load().inspire_pir_server_timings(self._h, ctypes.byref(a),
+                                               ctypes.byref(b), ctypes.byref(c))
+        return a.value, b.value, c.value
+
+    def GetDbMultiplyTime(self):
+        """Accumulated DB product time in milliseconds."""
+        return self._timings()[0]
+
+    def GetPackingTime(self):
+        return self._timings()[1]
+
+    def GetPolyEvalTime(self):
+        return self._timings()[2]
+
+
+# ---------------------------------------------------------------------------
+# Component entry points (reference functions one by one).
+# ---------------------------------------------------------------------------
+def matrix_multiply(mat, vec, coeff_bits):
+    """Matrix<T>::Multiply<CoeffType> (crypto/matrix.h:167-195)."""
+    lib = _lib.load()
+    mat = np.ascontiguousarray(mat)
+    cdt = np.uint32 if coeff_bits == 32 else np.uint64
+    vec = np.ascontiguousarray(vec, dtype=cdt)
+    if vec.shape[0] != mat.shape[1]:
+        raise InspireError(INVALID_ARGUMENT,
+                           "Vector size must match the number of matrix "
+                           "columns.")
+    out = np.zeros(mat.shape[0], dtype=cdt)
+    err = _errbuf()
+    rc = lib.inspire_matrix_multiply(KINDS[mat.dtype], coeff_bits, _ptr(mat),
+                                     mat.shape[0], mat.shape[1], _ptr(vec),
+                                     _ptr(out), err, len(err))
+    _check(rc, err)
+    return out
+
+
+def inner_product(u, v, coeff_bits, u_bits=None, v_bits=None, chunk_bits=20,
+                  u_signed=False):
+    """Polynomial<T>::InnerProductFft (crypto/polynomial_fft.cc:68-197)."""
+    lib = _lib.load()
+    cdt = np.uint32 if coeff_bits == 32 else np.uint64
+    u = np.ascontiguousarray(u, dtype=cdt)
+    v = np.ascontiguousarray(v, dtype=cdt)
+    if u.ndim == 1:
+        u, v = u[None], v[None]
+    n, d = u.shape
+    out = np.zeros(d, dtype=cdt)
+    err = _errbuf()
+    rc = lib.inspire_inner_product(coeff_bits, _ptr(u), _ptr(v), n, d,
+                                   u_bits or coeff_bits, v_bits or coeff_bits,
+                                   chunk_bits, int(u_signed), _ptr(out), err,
+                                   len(err))
+    _check(rc, err)
+    return out
+
+
+def external_product(params: PirParams, ct_a, ct_b, rgsw):
+    """ExternalProduct (crypto/external_product.cc:35-114)."""
+    lib = _lib.load()
+    cdt = params.coeff_dtype
+    prm = c_params(params)
+    ct_a = np.ascontiguousarray(ct_a, dtype=cdt)
+    ct_b = np.ascontiguousarray(ct_b, dtype=cdt)
+    rgsw = np.ascontiguousarray(rgsw, dtype=cdt)
+    oa = np.zeros_like(ct_a)
+    ob = np.zeros_like(ct_b)
+    err = _errbuf()
+    rc = lib.inspire_external_product(ctypes.byref(prm), _ptr(ct_a),
+                                      _ptr(ct_b), _ptr(rgsw), _ptr(oa),
+                                      _ptr(ob), err, len(err))
+    _check(rc, err)
+    return oa, ob
+
+
+def finalize_matrix_pack(params: PirParams, b, b_agg_partial, y_vec_h,
+                         t_vec_h):
+    """FinalizeMatrixPack (crypto/lwes_to_rlwe.cc:448-479): the b part."""
+    lib = _lib.load()
+    cdt = params.coeff_dtype
+    prm = c_params(params)
+    arrs = [np.ascontiguousarray(x, dtype=cdt)
+            for x in (b, b_agg_partial, y_vec_h, t_vec_h)]
+    out = np.zeros(params.rlwe.degree, dtype=cdt)
+    err = _errbuf()
+    rc = lib.inspire_finalize_matrix_pack(ctypes.byref(prm),
+                                          *[_ptr(a) for a in arrs], _ptr(out),
+                                          err, len(err))
+    _check(rc, err)
+    return out

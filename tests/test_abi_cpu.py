@@ -1,0 +1,63 @@
+"""CPU-side checks of the C ABI library: it loads without a GPU and exports
+every function that include/*.h declares."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+from inspire_gb300 import _lib, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for m in re.finditer(r"\b(inspire_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "inspire_pir_server_create" in names
+    assert "inspire_pir_process_response" in names
+    assert len(names) >= 10
+
+
+def test_library_exports_every_declared_function(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_signatures_cover_header(lib):
+    # Every declared function has a ctypes signature in the Python mirror.
+    for name in declared_functions():
+        assert name in _lib.SIGNATURES, name
+
+
+def test_null_server_is_rejected_without_gpu(lib):
+    err = ctypes.create_string_buffer(256)
+    rc = lib.inspire_pir_process_batch(None, 1, None, 0, None, 0, None, 0,
+                                       None, 0, err, len(err))
+    assert rc == 3
+    assert b"server is null" in err.value
+
+
+def test_inner_product_rejects_empty_without_gpu(lib):
+    err = ctypes.create_string_buffer(256)
+    rc = lib.inspire_inner_product(32, None, None, 0, 32, 32, 32, 20, 0, None,
+                                   err, len(err))
+    assert rc == 3
+    assert b"cannot be empty" in err.value

@@ -100,17 +100,14 @@ def make_workload(seed=2026, batch=256):
     from inspire_gb300 import synthetic
     params = synthetic.make_params(d=DEGREE, n=N_ENTRIES, t=INTERP,
                                    coeff_bits=COEFF_BITS)
-    rng = np.random.default_rng(seed)
     rows = INTERP * DEGREE
     cols = N_ENTRIES // INTERP
     # Uniform already-interpolated DB values in [0, p) (p = 65535).
-    db = rng.integers(0, 1 << 63, size=rows * cols // 4, dtype=np.uint64)
-    db = db.view(np.uint16).reshape(rows, cols)
-    np.minimum(db, 65534, out=db)
+    db = synthetic.parallel_integers((rows, cols), 0, 65535, np.uint16, seed)
     k = params.pack_gadget.num_digits
     bound = int(4 * np.sqrt(DEGREE) * (1 << params.pack_gadget.log_digit))
-    pack = rng.integers(-bound + 1, bound, size=(rows, k * DEGREE),
-                        dtype=np.int32)
+    pack = synthetic.parallel_integers((rows, k * DEGREE), -bound + 1, bound,
+                                       np.int32, seed + 7)
     mat = synthetic.make_material(
         synthetic.make_params(d=DEGREE, n=DEGREE * INTERP, t=INTERP,
                               coeff_bits=COEFF_BITS), seed=seed + 1)

@@ -1,10 +1,578 @@
+// Batched DB x queries product over Z_{2^32} on the 5th-generation tensor
+// cores (tcgen05 + TMEM + TMA), exact.
+//
+// Reference: the per-request GEMVs Matrix<uint16_t>::Multiply and
+// Matrix<int32_t>::Multiply (crypto/matrix.cc:261-374) called by
+// PirServer::ProcessResponse (crypto/pir/server/pir_server.cc:215-248). A
+// batch of B requests turns the two GEMVs into one GEMM:
+//   out[q][r] = sum_c DB[r][c] * q1[q][c] + sum_j P[r][j] * y_g[q][j]  mod 2^32
+//
+// Exactness with fp16 operands and fp32 accumulators. Every matrix entry is
+// split into unsigned bytes (the u16 DB into x0 + 2^8 x1, the pack matrix as
+// its u32 two's complement into p0..p3) and every query word into four bytes
+// y0..y3; bytes are exact fp16 values. Only byte pairs whose weight 2^(8s),
+// s = i + j, is below 2^32 matter. The accumulator of a CTA holds four
+// blocks of 64 fp32 columns, block s collecting every pair of weight 2^(8s):
+//   MMA(X0, [Y0 Y1 Y2 Y3]) -> blocks 0..3,  MMA(X1, [Y0 Y1 Y2]) -> blocks 1..3
+// so each accumulator element receives at most two byte products per K
+// index. A unit of K = 64 therefore sums at most 64 * 2 * 255^2 = 8,323,200
+// < 2^23: every partial sum is an exact fp32 integer, and the epilogue decodes
+// it exactly as bits(v + 2^23) - 0x4B000000 before adding it, shifted by 8s,
+// into a u32 register accumulator. The pack matrix runs as two units per K
+// block (p0,p1 like the DB; then p2 -> blocks 2..3 and p3 -> block 3).
+//
+// Kernel structure (one CTA per 128 DB rows x 64 requests, 8 warps):
+//   warp 0  TMA producer: 3-stage ring of 64 KB (two 128x64 A tiles and a
+//           256x64 B tile of query bytes, 128-byte swizzled)
+//   warp 1  MMA issuer: one thread issues tcgen05.mma (M=128, N=256/192/...,
+//           K=16) into one of two TMEM accumulator buffers (2 x 256 columns)
+//   warp 2  TMEM allocator
+//   warps 4-7 epilogue: tcgen05.ld the finished buffer, decode, accumulate
+// Every mbarrier wait is bounded; on a timeout the kernel raises an error
+// flag, drains its own copies with bounded waits, frees TMEM and returns.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <mutex>
+
+#include "internal.h"
 #include "limb_gemm.h"
 
 namespace inspire {
+namespace {
 
-void LimbGemm::Create(int, int, const void*, int64_t, int64_t, int, const void*,
-                      int64_t, std::unique_ptr<LimbGemm>* out) {
+constexpr int kTileM = 128;        // DB rows per CTA
+constexpr int kTileQ = 64;         // requests per CTA
+constexpr int kTileK = 64;         // K per unit (fp16: 128 bytes per row)
+constexpr int kStages = 3;
+constexpr int kATileBytes = kTileM * kTileK * 2;        // 16 KB
+constexpr int kBTileBytes = 4 * kTileQ * kTileK * 2;    // 32 KB
+constexpr int kStageBytes = 2 * kATileBytes + kBTileBytes;  // 64 KB
+constexpr int kThreads = 256;
+constexpr int kTmemCols = 512;     // two 256-column accumulators
+constexpr uint32_t kSpinLimit = 1u << 25;
+constexpr size_t kSmemBytes = kStages * kStageBytes + 1024 + 256;
+
+// ------------------------------------------------------------------ PTX --
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                   smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false on timeout or when another role has raised the flag.
+// With err == nullptr (draining after an error) it only bounds the wait.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          int* err) {
+  for (uint32_t i = 0;; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 255u) == 255u) {
+      if (err != nullptr && *reinterpret_cast<volatile int*>(err) != 0) {
+        return false;
+      }
+      if (i > kSpinLimit) {
+        if (err != nullptr) atomicExch(err, 1);
+        return false;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(const CUtensorMap* map,
+                                            uint64_t* bar, void* dst, int x,
+                                            int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::"
+      "bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_addr(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t cols) {
+  asm volatile(
+      "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+          smem_addr(dst)),
+      "r"(cols)
+      : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::
+                   : "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t cols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr),
+               "r"(cols)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a_desc,
+                                        uint64_t b_desc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 "
+      "[%0];" ::"r"(smem_addr(bar))
+      : "memory");
+}
+
+#define INSPIRE_R32(i) "=r"(v[i])
+__device__ __forceinline__ void tmem_ld_x32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, "
+      "%30, %31}, [%32];"
+      : INSPIRE_R32(0), INSPIRE_R32(1), INSPIRE_R32(2), INSPIRE_R32(3),
+        INSPIRE_R32(4), INSPIRE_R32(5), INSPIRE_R32(6), INSPIRE_R32(7),
+        INSPIRE_R32(8), INSPIRE_R32(9), INSPIRE_R32(10), INSPIRE_R32(11),
+        INSPIRE_R32(12), INSPIRE_R32(13), INSPIRE_R32(14), INSPIRE_R32(15),
+        INSPIRE_R32(16), INSPIRE_R32(17), INSPIRE_R32(18), INSPIRE_R32(19),
+        INSPIRE_R32(20), INSPIRE_R32(21), INSPIRE_R32(22), INSPIRE_R32(23),
+        INSPIRE_R32(24), INSPIRE_R32(25), INSPIRE_R32(26), INSPIRE_R32(27),
+        INSPIRE_R32(28), INSPIRE_R32(29), INSPIRE_R32(30), INSPIRE_R32(31)
+      : "r"(taddr));
+}
+#undef INSPIRE_R32
+
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO), descriptor version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((addr >> 4) & 0x3FFF);
+  d |= static_cast<uint64_t>(1) << 16;                 // LBO (unused: swizzled)
+  d |= static_cast<uint64_t>(1024 >> 4) << 32;         // SBO
+  d |= static_cast<uint64_t>(1) << 46;                 // version
+  d |= static_cast<uint64_t>(2) << 61;                 // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor of kind::f16: fp16 A/B, fp32 D, both K-major.
+__host__ __device__ constexpr uint32_t instr_desc(int n, int m) {
+  return (1u << 4) | (static_cast<uint32_t>(n >> 3) << 17) |
+         (static_cast<uint32_t>(m >> 4) << 24);
+}
+
+struct LimbArgs {
+  int rows;          // R (multiple of 128)
+  int n_db_units;    // DB columns / 64
+  int n_pk_blocks;   // pack columns / 64
+  int qcap;          // request rows per limb plane in the query maps
+  int batch;         // valid requests
+  int64_t out_stride;
+  uint32_t corr;     // decoded-offset correction, mod 2^32
+};
+
+__global__ void __launch_bounds__(kThreads, 1)
+limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
+                 const __grid_constant__ CUtensorMap tm_pk,
+                 const __grid_constant__ CUtensorMap tm_q,
+                 const __grid_constant__ CUtensorMap tm_y, LimbArgs a,
+                 uint32_t* __restrict__ out, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
+  uint64_t* empty = full + kStages;
+  uint64_t* acc_full = empty + kStages;
+  uint64_t* acc_empty = acc_full + 2;
+  uint64_t* mma_done = acc_empty + 2;
+  uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nqt = (a.batch + kTileQ - 1) / kTileQ;
+  const int row0 = (blockIdx.x / nqt) * kTileM;
+  const int q0 = (blockIdx.x % nqt) * kTileQ;
+  const int n_units = a.n_db_units + 2 * a.n_pk_blocks;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 4);
+    }
+    mbar_init(mma_done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 2) tmem_alloc(tmem_base_slot, kTmemCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_base_slot;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------------------------------------------- TMA producer --
+    int last_unit[kStages] = {-1, -1, -1};
+    for (int u = 0; u < n_units; ++u) {
+      const int s = u % kStages;
+      if (!mbar_wait(&empty[s], ((u / kStages) & 1) ^ 1, err)) break;
+      unsigned char* st = smem + s * kStageBytes;
+      int kind, kb;
+      if (u < a.n_db_units) {
+        kind = 0;
+        kb = u;
+      } else {
+        kind = 1 + ((u - a.n_db_units) & 1);
+        kb = (u - a.n_db_units) >> 1;
+      }
+      const int x = kb * kTileK;
+      const int nb = kind == 2 ? 2 : 4;  // query-byte planes this unit reads
+      mbar_expect_tx(&full[s], 2 * kATileBytes + nb * (kBTileBytes / 4));
+      if (kind == 0) {
+        tma_load_2d(&tm_db, &full[s], st, x, row0);
+        tma_load_2d(&tm_db, &full[s], st + kATileBytes, x, a.rows + row0);
+      } else {
+        const int plane = kind == 1 ? 0 : 2;
+        tma_load_2d(&tm_pk, &full[s], st, x, plane * a.rows + row0);
+        tma_load_2d(&tm_pk, &full[s], st + kATileBytes, x,
+                    (plane + 1) * a.rows + row0);
+      }
+      const CUtensorMap* bm = kind == 0 ? &tm_q : &tm_y;
+      for (int j = 0; j < nb; ++j) {
+        tma_load_2d(bm, &full[s], st + 2 * kATileBytes + j * (kBTileBytes / 4),
+                    x, j * a.qcap + q0);
+      }
+      last_unit[s] = u;
+    }
+    // Drain: every copy this thread issued has landed before the CTA exits.
+    for (int s = 0; s < kStages; ++s) {
+      if (last_unit[s] >= 0) {
+        mbar_wait(&full[s], (last_unit[s] / kStages) & 1, nullptr);
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ------------------------------------------------------ MMA issuer --
+    constexpr uint32_t id256 = instr_desc(256, kTileM);
+    constexpr uint32_t id192 = instr_desc(192, kTileM);
+    constexpr uint32_t id128 = instr_desc(128, kTileM);
+    constexpr uint32_t id64 = instr_desc(64, kTileM);
+    for (int u = 0; u < n_units; ++u) {
+      const int s = u % kStages;
+      const int b = u & 1;
+      if (!mbar_wait(&acc_empty[b], ((u >> 1) & 1) ^ 1, err)) break;
+      if (!mbar_wait(&full[s], (u / kStages) & 1, err)) break;
+      tc_fence_after();
+      const int kind = u < a.n_db_units ? 0 : 1 + ((u - a.n_db_units) & 1);
+      const uint32_t st = smem_addr(smem + s * kStageBytes);
+      const uint32_t d = tmem + b * 256;
+      for (int kk = 0; kk < kTileK / 16; ++kk) {
+        const uint64_t da0 = smem_desc(st + kk * 32);
+        const uint64_t da1 = smem_desc(st + kATileBytes + kk * 32);
+        const uint64_t dbq = smem_desc(st + 2 * kATileBytes + kk * 32);
+        if (kind != 2) {
+          mma_f16(d, da0, dbq, id256, kk > 0);          // x0 * [y0..y3]
+          mma_f16(d + 64, da1, dbq, id192, 1);          // x1 * [y0..y2]
+        } else {
+          mma_f16(d + 128, da0, dbq, id128, kk > 0);    // p2 * [y0 y1]
+          mma_f16(d + 192, da1, dbq, id64, 1);          // p3 * [y0]
+        }
+      }
+      mma_commit(&empty[s]);
+      mma_commit(&acc_full[b]);
+    }
+    mma_commit(mma_done);
+    mbar_wait(mma_done, 0, nullptr);
+  } else if (warp >= 4) {
+    // -------------------------------------------------------- epilogue --
+    const int ew = warp - 4;  // TMEM lanes 32*ew .. 32*ew+31
+    uint32_t acc[kTileQ];
+#pragma unroll
+    for (int i = 0; i < kTileQ; ++i) acc[i] = 0;
+    bool ok = true;
+    for (int u = 0; u < n_units && ok; ++u) {
+      const int b = u & 1;
+      if (!mbar_wait(&acc_full[b], (u >> 1) & 1, err)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const int kind = u < a.n_db_units ? 0 : 1 + ((u - a.n_db_units) & 1);
+      const uint32_t base = tmem + (static_cast<uint32_t>(ew * 32) << 16) + b * 256;
+#pragma unroll
+      for (int sblk = 0; sblk < 4; ++sblk) {
+        if (kind == 2 && sblk < 2) continue;
+        uint32_t v0[32], v1[32];
+        tmem_ld_x32(base + sblk * 64, v0);
+        tmem_ld_x32(base + sblk * 64 + 32, v1);
+        tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          acc[i] += __float_as_uint(__uint_as_float(v0[i]) + 8388608.0f)
+                    << (8 * sblk);
+          acc[32 + i] += __float_as_uint(__uint_as_float(v1[i]) + 8388608.0f)
+                         << (8 * sblk);
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[b]);
+    }
+    if (ok && *reinterpret_cast<volatile int*>(err) == 0) {
+      const int row = row0 + ew * 32 + lane;
+#pragma unroll
+      for (int i = 0; i < kTileQ; ++i) {
+        const int q = q0 + i;
+        if (q < a.batch) out[q * a.out_stride + row] = acc[i] - a.corr;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 2) tmem_dealloc(tmem, kTmemCols);
+}
+
+// Byte planes of a u16 matrix: [2][rows][cols_pad] fp16, zero past cols.
+__global__ void split_u16_kernel(const uint16_t* __restrict__ src,
+                                 int64_t rows, int64_t cols,
+                                 int64_t cols_pad, __half* __restrict__ dst) {
+  const int64_t total = rows * cols_pad;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       i < total; i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = i / cols_pad, c = i % cols_pad;
+    const uint32_t x = c < cols ? src[r * cols + c] : 0u;
+    dst[i] = __uint2half_rn(x & 255u);
+    dst[total + i] = __uint2half_rn(x >> 8);
+  }
+}
+
+// Byte planes of the u32 two's complement of a matrix of `kind`: plane j
+// holds rows_pad x cols_pad fp16 (zero outside rows x cols) and starts at
+// row j * plane_rows.
+__global__ void split_u32_kernel(const void* __restrict__ src, int kind,
+                                 int64_t rows, int64_t cols, int64_t stride,
+                                 int64_t rows_pad, int64_t plane_rows,
+                                 int64_t cols_pad, __half* __restrict__ dst) {
+  const int64_t total = rows_pad * cols_pad;
+  const int64_t plane = plane_rows * cols_pad;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       i < total; i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = i / cols_pad, c = i % cols_pad;
+    uint32_t x = 0;
+    if (r < rows && c < cols) {
+      const int64_t o = r * stride + c;
+      switch (kind) {
+        case kI16: x = static_cast<uint32_t>(static_cast<int32_t>(
+                       static_cast<const int16_t*>(src)[o])); break;
+        case kI32: x = static_cast<uint32_t>(static_cast<const int32_t*>(src)[o]); break;
+        default: x = static_cast<const uint32_t*>(src)[o]; break;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      dst[j * plane + i] = __uint2half_rn((x >> (8 * j)) & 255u);
+    }
+  }
+}
+
+// ------------------------------------------------------------ host side --
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                         cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess) {
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+  });
+  return fn;
+}
+
+// 2-D fp16 tensor [rows][cols], box box_rows x 64, 128-byte swizzle.
+bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols,
+              uint32_t box_rows) {
+  auto fn = encode_fn();
+  if (fn == nullptr) return false;
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {cols * 2};
+  cuuint32_t box[2] = {static_cast<cuuint32_t>(kTileK), box_rows};
+  cuuint32_t elem[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base),
+                  dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+class LimbGemmImpl : public LimbGemm {
+ public:
+  ~LimbGemmImpl() override {
+    for (void* p : {db_planes_, pk_planes_, q_planes_, y_planes_})
+      if (p) cudaFree(p);
+    if (err_) cudaFree(err_);
+  }
+
+  bool Init(const void* db, int64_t rows, int64_t db_cols, int mat_kind,
+            const void* pack, int64_t pack_cols) {
+    rows_ = rows;
+    db_cols_ = db_cols;
+    pk_cols_ = pack_cols;
+    cpad_ = round_up(db_cols, kTileK);
+    kpad_ = round_up(pack_cols, kTileK);
+    if (cudaMalloc(&err_, sizeof(int)) != cudaSuccess) return false;
+    if (cudaMemset(err_, 0, sizeof(int)) != cudaSuccess) return false;
+    if (cudaMalloc(&db_planes_, 2ull * rows * cpad_ * 2) != cudaSuccess) return false;
+    if (cudaMalloc(&pk_planes_, 4ull * rows * kpad_ * 2) != cudaSuccess) return false;
+    split_u16_kernel<<<152 * 16, 256>>>(static_cast<const uint16_t*>(db), rows,
+                                        db_cols, cpad_, db_planes_);
+    split_u32_kernel<<<152 * 16, 256>>>(pack, mat_kind, rows, pack_cols, pack_cols,
+                                        rows, rows, kpad_, pk_planes_);
+    if (cudaDeviceSynchronize() != cudaSuccess) return false;
+    if (!make_map(&tm_db_, db_planes_, 2ull * rows, cpad_, kTileM)) return false;
+    if (!make_map(&tm_pk_, pk_planes_, 4ull * rows, kpad_, kTileM)) return false;
+    if (cudaFuncSetAttribute(limb_gemm_kernel,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kSmemBytes)) != cudaSuccess)
+      return false;
+    return true;
+  }
+
+  cudaError_t EnsureQueries(int batch) {
+    const int64_t need = round_up(batch, kTileQ);
+    if (need <= qcap_) return cudaSuccess;
+    if (q_planes_) cudaFree(q_planes_);
+    if (y_planes_) cudaFree(y_planes_);
+    q_planes_ = y_planes_ = nullptr;
+    qcap_ = 0;
+    cudaError_t e = cudaMalloc(&q_planes_, 4ull * need * cpad_ * 2);
+    if (e != cudaSuccess) return e;
+    e = cudaMalloc(&y_planes_, 4ull * need * kpad_ * 2);
+    if (e != cudaSuccess) return e;
+    if (!make_map(&tm_q_, q_planes_, 4ull * need, cpad_, kTileQ) ||
+        !make_map(&tm_y_, y_planes_, 4ull * need, kpad_, kTileQ)) {
+      return cudaErrorInvalidValue;
+    }
+    qcap_ = need;
+    return cudaSuccess;
+  }
+
+  cudaError_t Run(int batch, const void* q1, int64_t q1_stride, const void* yg,
+                  int64_t yg_stride, void* out, cudaStream_t st) override {
+    if (batch <= 0) return cudaSuccess;
+    cudaError_t e = EnsureQueries(batch);
+    if (e != cudaSuccess) return e;
+    const int64_t bpad = round_up(batch, kTileQ);
+    // Byte planes of the requests, qcap_ rows apart; rows batch..bpad are 0.
+    split_u32_kernel<<<152 * 8, 256, 0, st>>>(q1, kU32, batch, db_cols_, q1_stride,
+                                              bpad, qcap_, cpad_, q_planes_);
+    split_u32_kernel<<<152 * 8, 256, 0, st>>>(yg, kU32, batch, pk_cols_, yg_stride,
+                                              bpad, qcap_, kpad_, y_planes_);
+    LimbArgs a;
+    a.rows = static_cast<int>(rows_);
+    a.n_db_units = static_cast<int>(cpad_ / kTileK);
+    a.n_pk_blocks = static_cast<int>(kpad_ / kTileK);
+    a.qcap = static_cast<int>(qcap_);
+    a.batch = batch;
+    a.out_stride = rows_;
+    // Blocks 0 and 1 decode once per DB unit and per low pack unit, blocks 2
+    // and 3 also once per high pack unit.
+    const uint32_t n01 = static_cast<uint32_t>(a.n_db_units + a.n_pk_blocks);
+    const uint32_t n23 = n01 + static_cast<uint32_t>(a.n_pk_blocks);
+    const uint32_t m = 0x4B000000u;
+    a.corr = n01 * m + n01 * (m << 8) + n23 * (m << 16) + n23 * (m << 24);
+    const int nqt = static_cast<int>(bpad / kTileQ);
+    const unsigned grid = static_cast<unsigned>((rows_ / kTileM) * nqt);
+    limb_gemm_kernel<<<grid, kThreads, kSmemBytes, st>>>(
+        tm_db_, tm_pk_, tm_q_, tm_y_, a, static_cast<uint32_t*>(out), err_);
+    return cudaGetLastError();
+  }
+
+  int CheckError() override {
+    int h = 0;
+    if (cudaMemcpy(&h, err_, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return -1;
+    if (h != 0) cudaMemset(err_, 0, sizeof(int));
+    return h;
+  }
+
+ private:
+  int64_t rows_ = 0, db_cols_ = 0, pk_cols_ = 0, cpad_ = 0, kpad_ = 0;
+  int64_t qcap_ = 0;
+  __half *db_planes_ = nullptr, *pk_planes_ = nullptr;
+  __half *q_planes_ = nullptr, *y_planes_ = nullptr;
+  int* err_ = nullptr;
+  CUtensorMap tm_db_{}, tm_pk_{}, tm_q_{}, tm_y_{};
+};
+
+}  // namespace
+
+void LimbGemm::Create(int coeff_bits, int db_kind, const void* db, int64_t rows,
+                      int64_t db_cols, int mat_kind, const void* pack,
+                      int64_t pack_cols, std::unique_ptr<LimbGemm>* out) {
   out->reset();
+  // Z_{2^32} with a u16 DB: the configuration the byte-limb plan covers.
+  if (coeff_bits != 32 || db_kind != kU16) return;
+  if (mat_kind != kI16 && mat_kind != kI32 && mat_kind != kU32) return;
+  if (rows % kTileM != 0 || db_cols <= 0 || pack_cols <= 0) return;
+  int dev = 0, major = 0, minor = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  if (major != 10) return;
+  std::unique_ptr<LimbGemmImpl> impl(new LimbGemmImpl());
+  if (!impl->Init(db, rows, db_cols, mat_kind, pack, pack_cols)) {
+    cudaGetLastError();
+    return;
+  }
+  *out = std::move(impl);
 }
 
 }  // namespace inspire

@@ -20,6 +20,9 @@ class LimbGemm {
   virtual cudaError_t Run(int batch, const void* q1, int64_t q1_stride,
                           const void* yg, int64_t yg_stride, void* out,
                           cudaStream_t stream) = 0;
+  // Returns (and clears) the kernel's error flag: non-zero when a pipeline
+  // wait timed out in a previous launch. Synchronous.
+  virtual int CheckError() = 0;
 };
 
 }  // namespace inspire

@@ -553,6 +553,9 @@ Status ProcessHostBatch(inspire_pir_server* s, int batch, const void* first_dim,
                                        cudaMemcpyDeviceToHost, st),
                        "copy response"));
   RETURN_IF_ERROR(Cuda(cudaStreamSynchronize(st), "answer"));
+  if (engine == INSPIRE_ENGINE_TENSOR && s->limb && s->limb->CheckError() != 0) {
+    return Err(INSPIRE_INTERNAL, "tensor engine pipeline timed out");
+  }
   float ms_db = 0, ms_pack = 0, ms_eval = 0;
   cudaEventElapsedTime(&ms_db, s->ev[0], s->ev[1]);
   cudaEventElapsedTime(&ms_pack, s->ev[1], s->ev[2]);

@@ -15,6 +15,31 @@ import numpy as np
 from .pir import (GadgetParams, PirParams, PirRequest, RlweParams)
 
 
+def parallel_integers(shape, low, high, dtype, seed, threads=None):
+    """Uniform integers in [low, high) filled by several threads (the numpy
+    generators release the GIL), one independent stream per slice."""
+    import os
+    import threading
+    out = np.empty(int(np.prod(shape)), dtype=dtype)
+    threads = threads or min(32, os.cpu_count() or 1)
+    seqs = np.random.SeedSequence(seed).spawn(threads)
+    n = out.shape[0]
+    step = (n + threads - 1) // threads
+
+    def fill(i):
+        lo, hi = i * step, min(n, (i + 1) * step)
+        if lo < hi:
+            g = np.random.default_rng(seqs[i])
+            out[lo:hi] = g.integers(low, high, size=hi - lo, dtype=dtype)
+
+    ts = [threading.Thread(target=fill, args=(i,)) for i in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    return out.reshape(shape)
+
+
 def make_params(d, n, t, l=1, coeff_bits=32, log_q=None, log_p=16,
                 plaintext_modulus=65535, pack=(19, 2), evalg=(19, 3),
                 log_q1=None, log_q2=None):

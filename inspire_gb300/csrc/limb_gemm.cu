@@ -55,7 +55,7 @@ constexpr int kBTileBytes = 4 * kTileQ * kTileK * 2;    // 32 KB
 constexpr int kStageBytes = 2 * kATileBytes + kBTileBytes;  // 64 KB
 constexpr int kThreads = 256;
 constexpr int kTmemCols = 512;     // two 256-column accumulators
-constexpr uint32_t kSpinLimit = 1u << 25;
+constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr size_t kSmemBytes = kStages * kStageBytes + 1024 + 256;
 
 // ------------------------------------------------------------------ PTX --
@@ -334,7 +334,8 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     bool ok = true;
     for (int u = 0; u < n_units && ok; ++u) {
       const int b = u & 1;
-      if (!mbar_wait(&acc_full[b], (u >> 1) & 1, err)) {
+      // Warp-uniform outcome: the TMEM loads below are .sync.aligned.
+      if (!__all_sync(0xffffffffu, mbar_wait(&acc_full[b], (u >> 1) & 1, err))) {
         ok = false;
         break;
       }

@@ -195,6 +195,28 @@ int inspire_finalize_matrix_pack(const inspire_pir_params* params,
                                  const void* y_vec_h, const void* t_vec_h,
                                  void* out_b, char* err, size_t err_len);
 
+/*
+ * InnerProductFft that allocates no GPU memory, for callers that cannot call
+ * cudaMalloc (a host runtime that owns the device memory budget, a request
+ * path that must not block on allocation). No counterpart in the reference:
+ * it computes exactly what inspire_inner_product computes, but u, v and out
+ * are device pointers owned by the caller (n*d, n*d and d CoeffType words),
+ * the work is enqueued on `stream` (a cudaStream_t, or NULL) without
+ * synchronising, and the NTT scratch is a fixed 1.6 MB __device__ array
+ * inside the library. Limits: n <= 8 polynomials, d <= 4096; larger sizes are
+ * rejected with INVALID_ARGUMENT. The first call on each device looks up that
+ * array's device address (cudaGetSymbolAddress), so make the first call on a
+ * device before capturing any stream. All calls share the array: calls whose
+ * GPU work overlaps (different streams or threads) race and must be
+ * serialised by the caller.
+ */
+int inspire_inner_product_noalloc(int32_t coeff_bits, const void* u,
+                                  const void* v, int32_t n, int32_t d,
+                                  int32_t u_bits, int32_t v_bits,
+                                  int32_t chunk_bits, int32_t u_is_signed,
+                                  void* out, void* stream, char* err,
+                                  size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

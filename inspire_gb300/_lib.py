@@ -40,6 +40,9 @@ SIGNATURES = {
         ctypes.c_int),
     "inspire_external_product": (
         [_vp, _vp, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_inner_product_noalloc": (
+        [_i32, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp, _cp,
+         _sz], ctypes.c_int),
     "inspire_finalize_matrix_pack": (
         [_vp, _vp, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),
 }

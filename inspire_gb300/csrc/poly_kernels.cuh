@@ -91,7 +91,8 @@ ntt_coeffs_kernel(const T* __restrict__ src, int64_t src_qstride,
 }
 
 // Forward NTT of signed 64-bit polynomials (host-prepared operands).
-__global__ void __launch_bounds__(kPolyThreads)
+// Internal linkage: the header is shared by several translation units.
+static __global__ void __launch_bounds__(kPolyThreads)
 ntt_signed_kernel(const int64_t* __restrict__ src, int npoly,
                   uint32_t* __restrict__ dst, NttCtx c) {
   extern __shared__ uint32_t smem[];

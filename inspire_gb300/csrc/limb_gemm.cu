@@ -21,15 +21,26 @@
 // into a u32 register accumulator. The pack matrix runs as two units per K
 // block (p0,p1 like the DB; then p2 -> blocks 2..3 and p3 -> block 3).
 //
-// Kernel structure (one CTA per 128 DB rows x 64 requests, 8 warps):
-//   warp 0  TMA producer: 3-stage ring of 64 KB (two 128x64 A tiles and a
-//           256x64 B tile of query bytes, 128-byte swizzled)
-//   warp 1  MMA issuer: one thread issues tcgen05.mma (M=128, N=256/192/...,
-//           K=16) into one of two TMEM accumulator buffers (2 x 256 columns)
-//   warp 2  TMEM allocator
-//   warps 4-7 epilogue: tcgen05.ld the finished buffer, decode, accumulate
-// Every mbarrier wait is bounded; on a timeout the kernel raises an error
-// flag, drains its own copies with bounded waits, frees TMEM and returns.
+// Kernel structure. Moving operand tiles from L2 into shared memory, not the
+// tensor pipe, limits this GEMM (a K=64 unit of one 128-row block moves
+// 64 KB of fp16 limbs for 3.7 M MACs), so each CTA covers two 128-row blocks
+// that share one 64-request tile, which raises the MACs per byte moved by
+// a third. 12 warps:
+//   warp 0     TMA producer: 4-stage ring of 48 KB (per stage, K = 32: four
+//              128x32 A tiles and a 4 x 64x32 tile of request bytes,
+//              64-byte swizzled); two stages make one exact K=64 unit
+//   warp 1     MMA issuer: one thread issues tcgen05.mma (M=128, K=16,
+//              N=256/192 or 128/64) for row block 0 into TMEM columns
+//              0..255, commits, then row block 1 into columns 256..511, so
+//              one epilogue group drains a block while the other is filled
+//   warp 2     TMEM allocator (512 columns)
+//   warps 4-7  epilogue for row block 0, warps 8-11 for row block 1:
+//              tcgen05.ld, decode, accumulate
+// The K range can be split over several CTAs (split-K) to balance the grid
+// over the SMs; split partial sums are added with 32-bit atomics, which are
+// exact mod 2^32. Every mbarrier wait is bounded; on a timeout the kernel
+// raises an error flag, drains its own copies with bounded waits, frees TMEM
+// and returns.
 #include <cuda.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -46,15 +57,18 @@
 namespace inspire {
 namespace {
 
-constexpr int kTileM = 128;        // DB rows per CTA
+constexpr int kBlockRows = 128;    // rows per MMA (M)
+constexpr int kRowBlocks = 2;      // row blocks per CTA sharing a request tile
+constexpr int kTileRows = kBlockRows * kRowBlocks;
 constexpr int kTileQ = 64;         // requests per CTA
-constexpr int kTileK = 64;         // K per unit (fp16: 128 bytes per row)
-constexpr int kStages = 3;
-constexpr int kATileBytes = kTileM * kTileK * 2;        // 16 KB
-constexpr int kBTileBytes = 4 * kTileQ * kTileK * 2;    // 32 KB
-constexpr int kStageBytes = 2 * kATileBytes + kBTileBytes;  // 64 KB
-constexpr int kThreads = 256;
-constexpr int kTmemCols = 512;     // two 256-column accumulators
+constexpr int kStageK = 32;        // K per pipeline stage (64-byte rows)
+constexpr int kUnitK = 64;         // K per exact accumulation unit
+constexpr int kStages = 4;
+constexpr int kATileBytes = kBlockRows * kStageK * 2;      // 8 KB
+constexpr int kBLimbBytes = kTileQ * kStageK * 2;          // 4 KB
+constexpr int kStageBytes = kRowBlocks * 2 * kATileBytes + 4 * kBLimbBytes;  // 48 KB
+constexpr int kThreads = 384;
+constexpr int kTmemCols = 512;     // one 256-column accumulator per row block
 constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr size_t kSmemBytes = kStages * kStageBytes + 1024 + 256;
 
@@ -184,15 +198,15 @@ __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart (SBO), descriptor version 1.
+// Shared-memory matrix descriptor: K-major, 64-byte swizzle (rows of 64
+// bytes, 8-row groups 512 bytes apart = SBO), descriptor version 1.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   uint64_t d = 0;
   d |= static_cast<uint64_t>((addr >> 4) & 0x3FFF);
   d |= static_cast<uint64_t>(1) << 16;                 // LBO (unused: swizzled)
-  d |= static_cast<uint64_t>(1024 >> 4) << 32;         // SBO
+  d |= static_cast<uint64_t>(512 >> 4) << 32;          // SBO
   d |= static_cast<uint64_t>(1) << 46;                 // version
-  d |= static_cast<uint64_t>(2) << 61;                 // SWIZZLE_128B
+  d |= static_cast<uint64_t>(4) << 61;                 // SWIZZLE_64B
   return d;
 }
 
@@ -203,14 +217,44 @@ __host__ __device__ constexpr uint32_t instr_desc(int n, int m) {
 }
 
 struct LimbArgs {
-  int rows;          // R (multiple of 128)
+  int rows;          // R (multiple of 256)
   int n_db_units;    // DB columns / 64
   int n_pk_blocks;   // pack columns / 64
-  int qcap;          // request rows per limb plane in the query maps
+  int qcap;          // request rows per byte plane in the request maps
   int batch;         // valid requests
+  int ksplit;        // CTAs sharing one (row pair, request tile)
   int64_t out_stride;
-  uint32_t corr;     // decoded-offset correction, mod 2^32
 };
+
+__device__ __forceinline__ int unit_kind(int u, int n_db_units) {
+  return u < n_db_units ? 0 : 1 + ((u - n_db_units) & 1);
+}
+
+// The MMAs of one 32-deep stage for one row block into accumulator d.
+__device__ __forceinline__ void issue_block(uint32_t st, int rb, int kind,
+                                            uint32_t d, bool first_stage) {
+  constexpr uint32_t id256 = instr_desc(256, kBlockRows);
+  constexpr uint32_t id192 = instr_desc(192, kBlockRows);
+  constexpr uint32_t id128 = instr_desc(128, kBlockRows);
+  constexpr uint32_t id64 = instr_desc(64, kBlockRows);
+  const uint32_t a0 = st + (rb * 2 + 0) * kATileBytes;
+  const uint32_t a1 = st + (rb * 2 + 1) * kATileBytes;
+  const uint32_t bq = st + kRowBlocks * 2 * kATileBytes;
+#pragma unroll
+  for (int kk = 0; kk < kStageK / 16; ++kk) {
+    const uint32_t acc = (first_stage && kk == 0) ? 0u : 1u;
+    const uint64_t da0 = smem_desc(a0 + kk * 32);
+    const uint64_t da1 = smem_desc(a1 + kk * 32);
+    const uint64_t dbq = smem_desc(bq + kk * 32);
+    if (kind != 2) {
+      mma_f16(d, da0, dbq, id256, acc);          // x0 * [y0..y3] -> blocks 0..3
+      mma_f16(d + 64, da1, dbq, id192, 1);       // x1 * [y0..y2] -> blocks 1..3
+    } else {
+      mma_f16(d + 128, da0, dbq, id128, acc);    // p2 * [y0 y1]  -> blocks 2..3
+      mma_f16(d + 192, da1, dbq, id64, 1);       // p3 * [y0]     -> block 3
+    }
+  }
+}
 
 __global__ void __launch_bounds__(kThreads, 1)
 limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
@@ -224,23 +268,29 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
   uint64_t* empty = full + kStages;
   uint64_t* acc_full = empty + kStages;
-  uint64_t* acc_empty = acc_full + 2;
-  uint64_t* mma_done = acc_empty + 2;
+  uint64_t* acc_empty = acc_full + kRowBlocks;
+  uint64_t* mma_done = acc_empty + kRowBlocks;
   uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const int nqt = (a.batch + kTileQ - 1) / kTileQ;
-  const int row0 = (blockIdx.x / nqt) * kTileM;
-  const int q0 = (blockIdx.x % nqt) * kTileQ;
+  const int qt = blockIdx.x % nqt;
+  const int rest = blockIdx.x / nqt;
+  const int ks = rest % a.ksplit;
+  const int row0 = (rest / a.ksplit) * kTileRows;
+  const int q0 = qt * kTileQ;
   const int n_units = a.n_db_units + 2 * a.n_pk_blocks;
+  const int per = (n_units + a.ksplit - 1) / a.ksplit;
+  const int u0 = ks * per;
+  const int nu = max(0, min(n_units, u0 + per) - u0);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kRowBlocks; ++b) {
       mbar_init(&acc_full[b], 1);
       mbar_init(&acc_empty[b], 4);
     }
@@ -255,93 +305,93 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
 
   if (warp == 0 && lane == 0) {
     // ---------------------------------------------------- TMA producer --
-    int last_unit[kStages] = {-1, -1, -1};
-    for (int u = 0; u < n_units; ++u) {
-      const int s = u % kStages;
-      if (!mbar_wait(&empty[s], ((u / kStages) & 1) ^ 1, err)) break;
-      unsigned char* st = smem + s * kStageBytes;
-      int kind, kb;
-      if (u < a.n_db_units) {
-        kind = 0;
-        kb = u;
-      } else {
-        kind = 1 + ((u - a.n_db_units) & 1);
-        kb = (u - a.n_db_units) >> 1;
-      }
-      const int x = kb * kTileK;
-      const int nb = kind == 2 ? 2 : 4;  // query-byte planes this unit reads
-      mbar_expect_tx(&full[s], 2 * kATileBytes + nb * (kBTileBytes / 4));
-      if (kind == 0) {
-        tma_load_2d(&tm_db, &full[s], st, x, row0);
-        tma_load_2d(&tm_db, &full[s], st + kATileBytes, x, a.rows + row0);
-      } else {
-        const int plane = kind == 1 ? 0 : 2;
-        tma_load_2d(&tm_pk, &full[s], st, x, plane * a.rows + row0);
-        tma_load_2d(&tm_pk, &full[s], st + kATileBytes, x,
-                    (plane + 1) * a.rows + row0);
-      }
+    int last_g[kStages] = {-1, -1, -1, -1};
+    bool ok = true;
+    for (int i = 0; i < nu && ok; ++i) {
+      const int u = u0 + i;
+      const int kind = unit_kind(u, a.n_db_units);
+      const int kb = kind == 0 ? u : (u - a.n_db_units) >> 1;
+      const int nb = kind == 2 ? 2 : 4;  // request-byte planes this unit reads
+      const CUtensorMap* am = kind == 0 ? &tm_db : &tm_pk;
       const CUtensorMap* bm = kind == 0 ? &tm_q : &tm_y;
-      for (int j = 0; j < nb; ++j) {
-        tma_load_2d(bm, &full[s], st + 2 * kATileBytes + j * (kBTileBytes / 4),
-                    x, j * a.qcap + q0);
+      const int plane0 = kind == 2 ? 2 : 0;
+      for (int h = 0; h < kUnitK / kStageK; ++h) {
+        const int g = 2 * i + h;
+        const int s = g % kStages;
+        if (!mbar_wait(&empty[s], ((g / kStages) & 1) ^ 1, err)) {
+          ok = false;
+          break;
+        }
+        unsigned char* st = smem + s * kStageBytes;
+        const int x = kb * kUnitK + h * kStageK;
+        mbar_expect_tx(&full[s], kRowBlocks * 2 * kATileBytes + nb * kBLimbBytes);
+        for (int rb = 0; rb < kRowBlocks; ++rb) {
+          for (int pl = 0; pl < 2; ++pl) {
+            tma_load_2d(am, &full[s], st + (rb * 2 + pl) * kATileBytes, x,
+                        (plane0 + pl) * a.rows + row0 + rb * kBlockRows);
+          }
+        }
+        for (int j = 0; j < nb; ++j) {
+          tma_load_2d(bm, &full[s],
+                      st + kRowBlocks * 2 * kATileBytes + j * kBLimbBytes, x,
+                      j * a.qcap + q0);
+        }
+        last_g[s] = g;
       }
-      last_unit[s] = u;
     }
     // Drain: every copy this thread issued has landed before the CTA exits.
     for (int s = 0; s < kStages; ++s) {
-      if (last_unit[s] >= 0) {
-        mbar_wait(&full[s], (last_unit[s] / kStages) & 1, nullptr);
-      }
+      if (last_g[s] >= 0) mbar_wait(&full[s], (last_g[s] / kStages) & 1, nullptr);
     }
   } else if (warp == 1 && lane == 0) {
     // ------------------------------------------------------ MMA issuer --
-    constexpr uint32_t id256 = instr_desc(256, kTileM);
-    constexpr uint32_t id192 = instr_desc(192, kTileM);
-    constexpr uint32_t id128 = instr_desc(128, kTileM);
-    constexpr uint32_t id64 = instr_desc(64, kTileM);
-    for (int u = 0; u < n_units; ++u) {
-      const int s = u % kStages;
-      const int b = u & 1;
-      if (!mbar_wait(&acc_empty[b], ((u >> 1) & 1) ^ 1, err)) break;
-      if (!mbar_wait(&full[s], (u / kStages) & 1, err)) break;
-      tc_fence_after();
-      const int kind = u < a.n_db_units ? 0 : 1 + ((u - a.n_db_units) & 1);
-      const uint32_t st = smem_addr(smem + s * kStageBytes);
-      const uint32_t d = tmem + b * 256;
-      for (int kk = 0; kk < kTileK / 16; ++kk) {
-        const uint64_t da0 = smem_desc(st + kk * 32);
-        const uint64_t da1 = smem_desc(st + kATileBytes + kk * 32);
-        const uint64_t dbq = smem_desc(st + 2 * kATileBytes + kk * 32);
-        if (kind != 2) {
-          mma_f16(d, da0, dbq, id256, kk > 0);          // x0 * [y0..y3]
-          mma_f16(d + 64, da1, dbq, id192, 1);          // x1 * [y0..y2]
-        } else {
-          mma_f16(d + 128, da0, dbq, id128, kk > 0);    // p2 * [y0 y1]
-          mma_f16(d + 192, da1, dbq, id64, 1);          // p3 * [y0]
+    bool ok = true;
+    for (int i = 0; i < nu && ok; ++i) {
+      const int kind = unit_kind(u0 + i, a.n_db_units);
+      for (int rb = 0; rb < kRowBlocks && ok; ++rb) {
+        if (!mbar_wait(&acc_empty[rb], (i & 1) ^ 1, err)) {
+          ok = false;
+          break;
         }
+        tc_fence_after();
+        const uint32_t d = tmem + rb * 256;
+        for (int h = 0; h < kUnitK / kStageK; ++h) {
+          const int g = 2 * i + h;
+          const int s = g % kStages;
+          if (rb == 0 && !mbar_wait(&full[s], (g / kStages) & 1, err)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          issue_block(smem_addr(smem + s * kStageBytes), rb, kind, d, h == 0);
+          if (rb == kRowBlocks - 1) mma_commit(&empty[s]);
+        }
+        if (ok) mma_commit(&acc_full[rb]);
       }
-      mma_commit(&empty[s]);
-      mma_commit(&acc_full[b]);
     }
     mma_commit(mma_done);
     mbar_wait(mma_done, 0, nullptr);
   } else if (warp >= 4) {
     // -------------------------------------------------------- epilogue --
-    const int ew = warp - 4;  // TMEM lanes 32*ew .. 32*ew+31
+    const int e = (warp - 4) / 4;   // row block
+    const int ew = (warp - 4) % 4;  // TMEM lanes 32*ew .. 32*ew+31
     uint32_t acc[kTileQ];
 #pragma unroll
     for (int i = 0; i < kTileQ; ++i) acc[i] = 0;
     bool ok = true;
-    for (int u = 0; u < n_units && ok; ++u) {
-      const int b = u & 1;
+    uint32_t n01 = 0, n23 = 0;
+    for (int i = 0; i < nu; ++i) {
       // Warp-uniform outcome: the TMEM loads below are .sync.aligned.
-      if (!__all_sync(0xffffffffu, mbar_wait(&acc_full[b], (u >> 1) & 1, err))) {
+      if (!__all_sync(0xffffffffu, mbar_wait(&acc_full[e], i & 1, err))) {
         ok = false;
         break;
       }
       tc_fence_after();
-      const int kind = u < a.n_db_units ? 0 : 1 + ((u - a.n_db_units) & 1);
-      const uint32_t base = tmem + (static_cast<uint32_t>(ew * 32) << 16) + b * 256;
+      const int kind = unit_kind(u0 + i, a.n_db_units);
+      n23 += 1;
+      n01 += kind != 2 ? 1 : 0;
+      const uint32_t base =
+          tmem + (static_cast<uint32_t>(ew * 32) << 16) + e * 256;
 #pragma unroll
       for (int sblk = 0; sblk < 4; ++sblk) {
         if (kind == 2 && sblk < 2) continue;
@@ -350,23 +400,35 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
         tmem_ld_x32(base + sblk * 64 + 32, v1);
         tmem_wait_ld();
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          acc[i] += __float_as_uint(__uint_as_float(v0[i]) + 8388608.0f)
+        for (int j = 0; j < 32; ++j) {
+          acc[j] += __float_as_uint(__uint_as_float(v0[j]) + 8388608.0f)
                     << (8 * sblk);
-          acc[32 + i] += __float_as_uint(__uint_as_float(v1[i]) + 8388608.0f)
+          acc[32 + j] += __float_as_uint(__uint_as_float(v1[j]) + 8388608.0f)
                          << (8 * sblk);
         }
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[b]);
+      if (lane == 0) mbar_arrive(&acc_empty[e]);
     }
     if (ok && *reinterpret_cast<volatile int*>(err) == 0) {
-      const int row = row0 + ew * 32 + lane;
+      // Every decoded value carried 0x4B000000 (the bits of 2^23), shifted
+      // by its block weight: remove them all at once, mod 2^32.
+      const uint32_t m = 0x4B000000u;
+      const uint32_t corr = n01 * m + n01 * (m << 8) + n23 * (m << 16) +
+                            n23 * (m << 24);
+      const int row = row0 + e * kBlockRows + ew * 32 + lane;
 #pragma unroll
-      for (int i = 0; i < kTileQ; ++i) {
-        const int q = q0 + i;
-        if (q < a.batch) out[q * a.out_stride + row] = acc[i] - a.corr;
+      for (int j = 0; j < kTileQ; ++j) {
+        const int q = q0 + j;
+        if (q < a.batch) {
+          uint32_t* o = out + q * a.out_stride + row;
+          if (a.ksplit == 1) {
+            *o = acc[j] - corr;
+          } else {
+            atomicAdd(o, acc[j] - corr);
+          }
+        }
       }
     }
   }
@@ -435,18 +497,18 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 2-D fp16 tensor [rows][cols], box box_rows x 64, 128-byte swizzle.
+// 2-D fp16 tensor [rows][cols], box box_rows x 32, 64-byte swizzle.
 bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols,
               uint32_t box_rows) {
   auto fn = encode_fn();
   if (fn == nullptr) return false;
   cuuint64_t dims[2] = {cols, rows};
   cuuint64_t strides[1] = {cols * 2};
-  cuuint32_t box[2] = {static_cast<cuuint32_t>(kTileK), box_rows};
+  cuuint32_t box[2] = {static_cast<cuuint32_t>(kStageK), box_rows};
   cuuint32_t elem[2] = {1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base),
                   dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
@@ -466,8 +528,8 @@ class LimbGemmImpl : public LimbGemm {
     rows_ = rows;
     db_cols_ = db_cols;
     pk_cols_ = pack_cols;
-    cpad_ = round_up(db_cols, kTileK);
-    kpad_ = round_up(pack_cols, kTileK);
+    cpad_ = round_up(db_cols, kUnitK);
+    kpad_ = round_up(pack_cols, kUnitK);
     if (cudaMalloc(&err_, sizeof(int)) != cudaSuccess) return false;
     if (cudaMemset(err_, 0, sizeof(int)) != cudaSuccess) return false;
     if (cudaMalloc(&db_planes_, 2ull * rows * cpad_ * 2) != cudaSuccess) return false;
@@ -477,8 +539,11 @@ class LimbGemmImpl : public LimbGemm {
     split_u32_kernel<<<152 * 16, 256>>>(pack, mat_kind, rows, pack_cols, pack_cols,
                                         rows, rows, kpad_, pk_planes_);
     if (cudaDeviceSynchronize() != cudaSuccess) return false;
-    if (!make_map(&tm_db_, db_planes_, 2ull * rows, cpad_, kTileM)) return false;
-    if (!make_map(&tm_pk_, pk_planes_, 4ull * rows, kpad_, kTileM)) return false;
+    if (!make_map(&tm_db_, db_planes_, 2ull * rows, cpad_, kBlockRows)) return false;
+    if (!make_map(&tm_pk_, pk_planes_, 4ull * rows, kpad_, kBlockRows)) return false;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev);
     if (cudaFuncSetAttribute(limb_gemm_kernel,
                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(kSmemBytes)) != cudaSuccess)
@@ -518,22 +583,40 @@ class LimbGemmImpl : public LimbGemm {
                                               bpad, qcap_, kpad_, y_planes_);
     LimbArgs a;
     a.rows = static_cast<int>(rows_);
-    a.n_db_units = static_cast<int>(cpad_ / kTileK);
-    a.n_pk_blocks = static_cast<int>(kpad_ / kTileK);
+    a.n_db_units = static_cast<int>(cpad_ / kUnitK);
+    a.n_pk_blocks = static_cast<int>(kpad_ / kUnitK);
     a.qcap = static_cast<int>(qcap_);
     a.batch = batch;
     a.out_stride = rows_;
-    // Blocks 0 and 1 decode once per DB unit and per low pack unit, blocks 2
-    // and 3 also once per high pack unit.
-    const uint32_t n01 = static_cast<uint32_t>(a.n_db_units + a.n_pk_blocks);
-    const uint32_t n23 = n01 + static_cast<uint32_t>(a.n_pk_blocks);
-    const uint32_t m = 0x4B000000u;
-    a.corr = n01 * m + n01 * (m << 8) + n23 * (m << 16) + n23 * (m << 24);
     const int nqt = static_cast<int>(bpad / kTileQ);
-    const unsigned grid = static_cast<unsigned>((rows_ / kTileM) * nqt);
+    const int64_t tiles = (rows_ / kTileRows) * nqt;
+    a.ksplit = ChooseSplit(tiles, a.n_db_units + 2 * a.n_pk_blocks);
+    if (a.ksplit > 1) {
+      e = cudaMemsetAsync(out, 0, static_cast<size_t>(batch) * rows_ * 4, st);
+      if (e != cudaSuccess) return e;
+    }
+    const unsigned grid = static_cast<unsigned>(tiles * a.ksplit);
     limb_gemm_kernel<<<grid, kThreads, kSmemBytes, st>>>(
         tm_db_, tm_pk_, tm_q_, tm_y_, a, static_cast<uint32_t*>(out), err_);
     return cudaGetLastError();
+  }
+
+  // Split-K factor that fills the SMs in whole waves (one CTA per SM).
+  int ChooseSplit(int64_t tiles, int n_units) const {
+    const int sms = sms_ > 0 ? sms_ : 148;
+    int best = 1;
+    double best_eff = 0;
+    for (int k = 1; k <= 8; ++k) {
+      if (n_units / k < 32) break;
+      const int64_t items = tiles * k;
+      const int64_t waves = (items + sms - 1) / sms;
+      const double eff = static_cast<double>(items) / (waves * sms);
+      if (eff > best_eff + 0.02) {
+        best_eff = eff;
+        best = k;
+      }
+    }
+    return best;
   }
 
   int CheckError() override {
@@ -547,6 +630,7 @@ class LimbGemmImpl : public LimbGemm {
  private:
   int64_t rows_ = 0, db_cols_ = 0, pk_cols_ = 0, cpad_ = 0, kpad_ = 0;
   int64_t qcap_ = 0;
+  int sms_ = 0;
   __half *db_planes_ = nullptr, *pk_planes_ = nullptr;
   __half *q_planes_ = nullptr, *y_planes_ = nullptr;
   int* err_ = nullptr;
@@ -562,7 +646,7 @@ void LimbGemm::Create(int coeff_bits, int db_kind, const void* db, int64_t rows,
   // Z_{2^32} with a u16 DB: the configuration the byte-limb plan covers.
   if (coeff_bits != 32 || db_kind != kU16) return;
   if (mat_kind != kI16 && mat_kind != kI32 && mat_kind != kU32) return;
-  if (rows % kTileM != 0 || db_cols <= 0 || pack_cols <= 0) return;
+  if (rows % kTileRows != 0 || db_cols <= 0 || pack_cols <= 0) return;
   int dev = 0, major = 0, minor = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return;
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);

@@ -27,6 +27,10 @@ struct NttCtx {
 };
 
 #ifdef __CUDACC__
+// Forward transform. Two Cooley-Tukey stages at a time: the quad
+// (x0, x1, x2, x3) = a[j], a[j+t/2], a[j+t], a[j+3t/2] takes stage (m, t)
+// with twiddle W[m+i] on (x0,x2),(x1,x3), then stage (2m, t/2) with W[2m+2i]
+// on (x0,x1) and W[2m+2i+1] on (x2,x3). An odd last stage runs radix-2.
 __device__ __forceinline__ void ntt_forward(uint32_t* a, const NttCtx& c,
                                             int pi) {
   const int d = 1 << c.logd;
@@ -34,22 +38,51 @@ __device__ __forceinline__ void ntt_forward(uint32_t* a, const NttCtx& c,
   const uint32_t* tw = c.tables + static_cast<size_t>(pi) * 4 * d;
   const uint32_t* tws = tw + d;
   __syncthreads();
-  for (int lt = c.logd - 1, m = 1; lt >= 0; --lt, m <<= 1) {
+  int lt = c.logd - 1;  // log2 of the current half-size t
+  int m = 1;
+  for (; lt >= 1; lt -= 2, m <<= 2) {
     const int t = 1 << lt;
+    const int lh = lt - 1;  // log2(t/2)
+    for (int b = threadIdx.x; b < d / 4; b += blockDim.x) {
+      const int i = b >> lh;
+      const int j = (i << (lt + 1)) | (b & ((t >> 1) - 1));
+      const uint32_t w1 = __ldg(tw + m + i), w1s = __ldg(tws + m + i);
+      const uint32_t w2 = __ldg(tw + 2 * m + 2 * i), w2s = __ldg(tws + 2 * m + 2 * i);
+      const uint32_t w3 = __ldg(tw + 2 * m + 2 * i + 1),
+                     w3s = __ldg(tws + 2 * m + 2 * i + 1);
+      uint32_t x0 = a[j], x1 = a[j + (t >> 1)], x2 = a[j + t],
+               x3 = a[j + t + (t >> 1)];
+      uint32_t v = shoup_mul(x2, w1, w1s, p);
+      x2 = sub_mod(x0, v, p);
+      x0 = add_mod(x0, v, p);
+      v = shoup_mul(x3, w1, w1s, p);
+      x3 = sub_mod(x1, v, p);
+      x1 = add_mod(x1, v, p);
+      v = shoup_mul(x1, w2, w2s, p);
+      a[j + (t >> 1)] = sub_mod(x0, v, p);
+      a[j] = add_mod(x0, v, p);
+      v = shoup_mul(x3, w3, w3s, p);
+      a[j + t + (t >> 1)] = sub_mod(x2, v, p);
+      a[j + t] = add_mod(x2, v, p);
+    }
+    __syncthreads();
+  }
+  if (lt == 0) {  // one radix-2 stage left (t = 1)
     for (int b = threadIdx.x; b < d / 2; b += blockDim.x) {
-      const int i = b >> lt;
-      const int j = (i << (lt + 1)) | (b & (t - 1));
+      const int j = b << 1;
       const uint32_t u = a[j];
-      const uint32_t v = shoup_mul(a[j + t], __ldg(tw + m + i),
-                                   __ldg(tws + m + i), p);
+      const uint32_t v = shoup_mul(a[j + 1], __ldg(tw + m + b), __ldg(tws + m + b), p);
       a[j] = add_mod(u, v, p);
-      a[j + t] = sub_mod(u, v, p);
+      a[j + 1] = sub_mod(u, v, p);
     }
     __syncthreads();
   }
 }
 
 // Inverse transform without the final 1/d scaling (folded into `scale`).
+// Two Gentleman-Sande stages at a time: stage (h, t) on (x0,x1),(x2,x3) with
+// IW[h+2i], IW[h+2i+1], then stage (h/2, 2t) on (x0,x2),(x1,x3) with
+// IW[h/2+i], for the quad a[j], a[j+t], a[j+2t], a[j+3t].
 __device__ __forceinline__ void ntt_inverse(uint32_t* a, const NttCtx& c,
                                             int pi) {
   const int d = 1 << c.logd;
@@ -57,16 +90,36 @@ __device__ __forceinline__ void ntt_inverse(uint32_t* a, const NttCtx& c,
   const uint32_t* itw = c.tables + static_cast<size_t>(pi) * 4 * d + 2 * d;
   const uint32_t* itws = itw + d;
   __syncthreads();
-  for (int lt = 0, h = d >> 1; h >= 1; ++lt, h >>= 1) {
+  int lt = 0;
+  int h = d >> 1;
+  for (; lt + 1 < c.logd; lt += 2, h >>= 2) {
+    const int t = 1 << lt;
+    for (int b = threadIdx.x; b < d / 4; b += blockDim.x) {
+      const int i = b >> lt;                    // block of size 4t
+      const int j = (i << (lt + 2)) | (b & (t - 1));
+      const uint32_t wa = __ldg(itw + h + 2 * i), was = __ldg(itws + h + 2 * i);
+      const uint32_t wb = __ldg(itw + h + 2 * i + 1),
+                     wbs = __ldg(itws + h + 2 * i + 1);
+      const uint32_t wc = __ldg(itw + (h >> 1) + i), wcs = __ldg(itws + (h >> 1) + i);
+      const uint32_t x0 = a[j], x1 = a[j + t], x2 = a[j + 2 * t], x3 = a[j + 3 * t];
+      const uint32_t y0 = add_mod(x0, x1, p);
+      const uint32_t y1 = shoup_mul(sub_mod(x0, x1, p), wa, was, p);
+      const uint32_t y2 = add_mod(x2, x3, p);
+      const uint32_t y3 = shoup_mul(sub_mod(x2, x3, p), wb, wbs, p);
+      a[j] = add_mod(y0, y2, p);
+      a[j + 2 * t] = shoup_mul(sub_mod(y0, y2, p), wc, wcs, p);
+      a[j + t] = add_mod(y1, y3, p);
+      a[j + 3 * t] = shoup_mul(sub_mod(y1, y3, p), wc, wcs, p);
+    }
+    __syncthreads();
+  }
+  if (lt < c.logd) {  // one radix-2 stage left (h = 1, t = d/2)
     const int t = 1 << lt;
     for (int b = threadIdx.x; b < d / 2; b += blockDim.x) {
-      const int i = b >> lt;
-      const int j = (i << (lt + 1)) | (b & (t - 1));
-      const uint32_t u = a[j];
-      const uint32_t v = a[j + t];
-      a[j] = add_mod(u, v, p);
-      a[j + t] = shoup_mul(sub_mod(u, v, p), __ldg(itw + h + i),
-                           __ldg(itws + h + i), p);
+      const uint32_t u = a[b];
+      const uint32_t v = a[b + t];
+      a[b] = add_mod(u, v, p);
+      a[b + t] = shoup_mul(sub_mod(u, v, p), __ldg(itw + 1), __ldg(itws + 1), p);
     }
     __syncthreads();
   }

@@ -197,8 +197,18 @@ struct ExtArgs {
   int log_q;         // LowBits width and GadgetInv log_modulus
   int log_digit;
   int num_digits;    // eval gadget digits (ne)
+  int live_digits;   // digits that can be non-zero; the rest are identically 0
   uint64_t umask;    // bits of a digit the chunk rule reads
 };
+
+// Gadget digits at or above the coefficient's width are always zero (e.g.
+// digit 2 of a 19 x 3 gadget over 32-bit coefficients): their products are
+// zero and are skipped.
+inline int LiveDigits(int log_q, int log_digit, int num_digits) {
+  if (log_q - num_digits * log_digit > 0) return num_digits;
+  const int live = (log_q + log_digit - 1) / log_digit;
+  return live < num_digits ? live : num_digits;
+}
 
 // Reads the Horner state of one coefficient: either the packed ciphertext
 // itself (first step) or CRT(previous product residues) + packed ciphertext.
@@ -269,6 +279,7 @@ ext_step_kernel(bool first, const uint32_t* __restrict__ resid_in,
   for (int g = 0; g < ng; ++g) {
     const T* src = g < e.num_digits ? sa : sb;
     const int dg = g < e.num_digits ? g : g - e.num_digits;
+    if (dg >= e.live_digits) continue;
     __syncthreads();
     for (int j = threadIdx.x; j < d; j += blockDim.x) {
       const T dig = gadget_digit<T>(src[j], e.log_q, e.log_digit, e.num_digits, dg);

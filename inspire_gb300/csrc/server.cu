@@ -363,11 +363,14 @@ Status RunPolyStage(inspire_pir_server* s, int batch, const T* pkey,
                     bool timed) {
   const int d = s->d, t = s->t, l = s->l, k = s->k, ne = s->ne;
   const int log_q = s->prm.log_modulus;
+  // d/16 coefficients per thread at most (kMaxPer), smaller CTAs otherwise
+  // so that batches fill the SMs without a wave tail.
+  const int nt = d <= 16 * 256 ? 256 : kPolyThreads;
   // y_h = packing_key[k..2k): forward NTT over the finalize primes.
   {
     const NttCtx& c = s->ctx_f;
     dim3 grid(k * c.r, batch);
-    ntt_coeffs_kernel<T><<<grid, kPolyThreads, d * 4, st>>>(
+    ntt_coeffs_kernel<T><<<grid, nt, d * 4, st>>>(
         pkey, static_cast<int64_t>(2 * k) * d, static_cast<int64_t>(k) * d, k,
         static_cast<T>(s->vmask_f), s->yh.get<uint32_t>(), c);
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "ntt(y_h)"));
@@ -377,7 +380,7 @@ Status RunPolyStage(inspire_pir_server* s, int batch, const T* pkey,
     const size_t smem = static_cast<size_t>(c.r) * d * 4;
     RETURN_IF_ERROR(SetSmem(finalize_kernel<T>, smem));
     dim3 grid(l * t, batch);
-    finalize_kernel<T><<<grid, kPolyThreads, smem, st>>>(
+    finalize_kernel<T><<<grid, nt, smem, st>>>(
         s->th_ntt.get<uint32_t>(), s->yh.get<uint32_t>(), k, gemv, nullptr,
         s->rows, s->packed.get<T>(), log_q, c);
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "finalize"));
@@ -391,17 +394,18 @@ Status RunPolyStage(inspire_pir_server* s, int batch, const T* pkey,
   if (t > 1) {
     const NttCtx& c = s->ctx_e;
     dim3 g1(2 * ne * c.r, batch);
-    ntt_coeffs_kernel<T><<<g1, kPolyThreads, d * 4, st>>>(
+    ntt_coeffs_kernel<T><<<g1, nt, d * 4, st>>>(
         sdim, static_cast<int64_t>(2 * ne) * d, 0, 2 * ne,
         static_cast<T>(s->vmask_e), s->rgswb.get<uint32_t>(), c);
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "ntt(rgsw)"));
-    ExtArgs e{log_q, s->prm.eval_log_digit, ne, s->umask_e};
+    ExtArgs e{log_q, s->prm.eval_log_digit, ne,
+              LiveDigits(log_q, s->prm.eval_log_digit, ne), s->umask_e};
     const size_t smem = static_cast<size_t>(d) * 4 + 2ull * d * sizeof(T);
     RETURN_IF_ERROR(SetSmem(ext_step_kernel<T>, smem));
     dim3 grid(c.r, l, batch);
     for (int i = t - 2; i >= 0; --i) {
       const bool first = i == t - 2;
-      ext_step_kernel<T><<<grid, kPolyThreads, smem, st>>>(
+      ext_step_kernel<T><<<grid, nt, smem, st>>>(
           first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
           a_tilde + static_cast<int64_t>(i + 1) * d, a_stride,
           packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
@@ -411,7 +415,7 @@ Status RunPolyStage(inspire_pir_server* s, int batch, const T* pkey,
   }
   {
     dim3 grid(l, batch);
-    finish_kernel<T><<<grid, kPolyThreads, 0, st>>>(
+    finish_kernel<T><<<grid, nt, 0, st>>>(
         t > 1, resid[0], a_tilde, a_stride, packed, b_qstride, a_stride, true,
         log_q, s->prm.log_modulus1_after_switch,
         s->prm.log_modulus2_after_switch, resp, t > 1 ? s->ctx_e : s->ctx_f);
@@ -1056,6 +1060,7 @@ int inspire_external_product(const inspire_pir_params* params,
   if (st.ok()) st = dout.Alloc(2 * d * w);
   const uint64_t vmask = MaskBits(re.v_chunks * re.chunk_bits, cb);
   ExtArgs e{params->log_modulus, params->eval_log_digit, ne,
+            LiveDigits(params->log_modulus, params->eval_log_digit, ne),
             MaskBits(re.u_chunks * re.chunk_bits, cb)};
   auto run = [&](auto tag) -> Status {
     using T = decltype(tag);

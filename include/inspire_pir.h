@@ -154,6 +154,99 @@ int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,
                                 void* out, int32_t engine, void* stream,
                                 char* err, size_t err_len);
 
+/*
+ * The packing step of a device-resident batch, as the packing benchmark's
+ * server loop runs it (crypto/pir/benchmarking/pir_packing_metrics_tool.cc:
+ * 226-283): DB * q1 + P * y_g, then FinalizeMatrixPack
+ * (crypto/lwes_to_rlwe.cc:448-479) of every shard, with no EvalPoly and no
+ * modulus switch. out: batch x (l*t) x 2 x d words, the (a_tilde_agg, b_agg)
+ * pair of each shard. Same validation and error strings as ProcessResponse;
+ * enqueued on `stream` without synchronising.
+ */
+int inspire_pir_pack_batch_device(inspire_pir_server* server, int32_t batch,
+                                  const void* first_dim, int64_t first_dim_len,
+                                  const void* packing_key,
+                                  int64_t packing_key_count, void* out,
+                                  int32_t engine, void* stream, char* err,
+                                  size_t err_len);
+
+/*
+ * ExternalProduct (crypto/external_product.cc:35-114) of `batch` independent
+ * RLWE ciphertexts, each with its own RGSW ciphertext, under the server's
+ * eval gadget (eval_log_digit x eval_num_digits, log_modulus). Device
+ * pointers: ct = batch x 2 x d words (a, b); rgsw = batch x 2*ne x 2 x d
+ * (u[0..ne) then v[0..ne), each an (a, b) pair, the layout
+ * inspire_external_product takes); out = batch x 2 x d. Enqueued on `stream`.
+ */
+int inspire_pir_external_product_device(inspire_pir_server* server,
+                                        int32_t batch, const void* ct,
+                                        const void* rgsw, void* out,
+                                        void* stream, char* err,
+                                        size_t err_len);
+
+/*
+ * CUDA graphs of the device entry points (no reference counterpart: the
+ * reference has no GPU). inspire_graph_begin starts capturing `stream` (a
+ * created stream, not the legacy default one); the device calls made on it
+ * by this thread are recorded, not run; inspire_graph_end instantiates them
+ * and inspire_graph_launch replays them, with the same pointers and batch
+ * sizes, as one launch. Make each call once outside a capture first, with
+ * the same batch sizes: that allocates the workspace and request planes
+ * (allocation inside a capture fails the capture). The recorded calls use
+ * the server's own workspace, so a replay must not overlap any other call
+ * on that server. inspire_pir_server_check reports a tensor-engine pipeline
+ * timeout recorded by earlier launches (call it after synchronising).
+ */
+typedef struct inspire_graph inspire_graph;
+int inspire_graph_begin(void* stream, char* err, size_t err_len);
+int inspire_graph_end(void* stream, inspire_graph** out, char* err,
+                      size_t err_len);
+int inspire_graph_launch(inspire_graph* graph, void* stream, char* err,
+                         size_t err_len);
+void inspire_graph_destroy(inspire_graph* graph);
+int inspire_pir_server_check(inspire_pir_server* server, char* err,
+                             size_t err_len);
+
+/*
+ * Workspaces: the state of one in-flight batch (device buffers, the tensor
+ * engine's request byte planes, a CUDA stream, pinned host staging). Several
+ * workspaces of one server run concurrently on their own streams; this is
+ * what a continuous-batching request loop submits to. A workspace is used
+ * by one thread at a time.
+ */
+typedef struct inspire_pir_workspace inspire_pir_workspace;
+
+/* Device bytes one workspace of max_batch requests holds (HBM admission). */
+int64_t inspire_pir_workspace_bytes(const inspire_pir_server* server,
+                                    int32_t max_batch);
+
+int inspire_pir_workspace_create(inspire_pir_server* server, int32_t max_batch,
+                                 inspire_pir_workspace** out, char* err,
+                                 size_t err_len);
+
+void inspire_pir_workspace_destroy(inspire_pir_workspace* ws);
+
+/* Pinned host staging of a workspace, max_batch requests each: first_dim
+ * holds db_cols words per request (zero past first_dim_len), second_dim
+ * 2*eval_num_digits polynomials, packing_key 2*pack_num_digits polynomials,
+ * responses 2*l polynomials. */
+int inspire_pir_workspace_host_buffers(inspire_pir_workspace* ws,
+                                       void** first_dim, void** second_dim,
+                                       void** packing_key, void** responses);
+
+/* Enqueues ProcessResponse for the first `batch` staged requests (copies in,
+ * answer, copies the responses back to the staging) and returns at once. */
+int inspire_pir_workspace_submit(inspire_pir_workspace* ws, int32_t batch,
+                                 int32_t engine, char* err, size_t err_len);
+
+/* 1 when the last submitted batch has finished, 0 while it runs, < 0 on a
+ * CUDA error. */
+int inspire_pir_workspace_poll(inspire_pir_workspace* ws);
+
+/* Blocks until the last submitted batch has finished; its status. */
+int inspire_pir_workspace_wait(inspire_pir_workspace* ws, char* err,
+                               size_t err_len);
+
 /* Server geometry: rows = l*t*d, and the column counts of both matrices. */
 int inspire_pir_server_shape(const inspire_pir_server* server, int64_t* rows,
                              int64_t* db_cols, int64_t* pack_cols);

@@ -31,6 +31,24 @@ SIGNATURES = {
          _sz], ctypes.c_int),
     "inspire_pir_products_device": (
         [_vp, _i32, _vp, _vp, _vp, _i32, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_pack_batch_device": (
+        [_vp, _i32, _vp, _i64, _vp, _i64, _vp, _i32, _vp, _cp, _sz],
+        ctypes.c_int),
+    "inspire_pir_external_product_device": (
+        [_vp, _i32, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_graph_begin": ([_vp, _cp, _sz], ctypes.c_int),
+    "inspire_graph_end": ([_vp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_graph_launch": ([_vp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_graph_destroy": ([_vp], None),
+    "inspire_pir_server_check": ([_vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_workspace_bytes": ([_vp, _i32], ctypes.c_int64),
+    "inspire_pir_workspace_create": ([_vp, _i32, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_workspace_destroy": ([_vp], None),
+    "inspire_pir_workspace_host_buffers": ([_vp, _vp, _vp, _vp, _vp],
+                                           ctypes.c_int),
+    "inspire_pir_workspace_submit": ([_vp, _i32, _i32, _cp, _sz], ctypes.c_int),
+    "inspire_pir_workspace_poll": ([_vp], ctypes.c_int),
+    "inspire_pir_workspace_wait": ([_vp, _cp, _sz], ctypes.c_int),
     "inspire_pir_server_shape": ([_vp, _i64p, _i64p, _i64p], ctypes.c_int),
     "inspire_pir_server_timings": ([_vp, _dp, _dp, _dp], ctypes.c_int),
     "inspire_matrix_multiply": (

@@ -515,10 +515,22 @@ bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols,
 
 int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
+class LimbScratchImpl : public LimbScratch {
+ public:
+  ~LimbScratchImpl() override {
+    if (q_planes) cudaFree(q_planes);
+    if (y_planes) cudaFree(y_planes);
+  }
+  int64_t qcap = 0;
+  __half* q_planes = nullptr;
+  __half* y_planes = nullptr;
+  CUtensorMap tm_q{}, tm_y{};
+};
+
 class LimbGemmImpl : public LimbGemm {
  public:
   ~LimbGemmImpl() override {
-    for (void* p : {db_planes_, pk_planes_, q_planes_, y_planes_})
+    for (void* p : {db_planes_, pk_planes_})
       if (p) cudaFree(p);
     if (err_) cudaFree(err_);
   }
@@ -551,41 +563,52 @@ class LimbGemmImpl : public LimbGemm {
     return true;
   }
 
-  cudaError_t EnsureQueries(int batch) {
+  std::unique_ptr<LimbScratch> NewScratch() override {
+    return std::unique_ptr<LimbScratch>(new LimbScratchImpl());
+  }
+
+  int64_t ScratchBytes(int batch) const override {
     const int64_t need = round_up(batch, kTileQ);
-    if (need <= qcap_) return cudaSuccess;
-    if (q_planes_) cudaFree(q_planes_);
-    if (y_planes_) cudaFree(y_planes_);
-    q_planes_ = y_planes_ = nullptr;
-    qcap_ = 0;
-    cudaError_t e = cudaMalloc(&q_planes_, 4ull * need * cpad_ * 2);
+    return 4 * need * (cpad_ + kpad_) * 2;
+  }
+
+  cudaError_t EnsureQueries(LimbScratchImpl* sc, int batch) {
+    const int64_t need = round_up(batch, kTileQ);
+    if (need <= sc->qcap) return cudaSuccess;
+    if (sc->q_planes) cudaFree(sc->q_planes);
+    if (sc->y_planes) cudaFree(sc->y_planes);
+    sc->q_planes = sc->y_planes = nullptr;
+    sc->qcap = 0;
+    cudaError_t e = cudaMalloc(&sc->q_planes, 4ull * need * cpad_ * 2);
     if (e != cudaSuccess) return e;
-    e = cudaMalloc(&y_planes_, 4ull * need * kpad_ * 2);
+    e = cudaMalloc(&sc->y_planes, 4ull * need * kpad_ * 2);
     if (e != cudaSuccess) return e;
-    if (!make_map(&tm_q_, q_planes_, 4ull * need, cpad_, kTileQ) ||
-        !make_map(&tm_y_, y_planes_, 4ull * need, kpad_, kTileQ)) {
+    if (!make_map(&sc->tm_q, sc->q_planes, 4ull * need, cpad_, kTileQ) ||
+        !make_map(&sc->tm_y, sc->y_planes, 4ull * need, kpad_, kTileQ)) {
       return cudaErrorInvalidValue;
     }
-    qcap_ = need;
+    sc->qcap = need;
     return cudaSuccess;
   }
 
   cudaError_t Run(int batch, const void* q1, int64_t q1_stride, const void* yg,
-                  int64_t yg_stride, void* out, cudaStream_t st) override {
+                  int64_t yg_stride, void* out, LimbScratch* scratch,
+                  cudaStream_t st) override {
     if (batch <= 0) return cudaSuccess;
-    cudaError_t e = EnsureQueries(batch);
+    LimbScratchImpl* sc = static_cast<LimbScratchImpl*>(scratch);
+    cudaError_t e = EnsureQueries(sc, batch);
     if (e != cudaSuccess) return e;
     const int64_t bpad = round_up(batch, kTileQ);
-    // Byte planes of the requests, qcap_ rows apart; rows batch..bpad are 0.
+    // Byte planes of the requests, qcap rows apart; rows batch..bpad are 0.
     split_u32_kernel<<<152 * 8, 256, 0, st>>>(q1, kU32, batch, db_cols_, q1_stride,
-                                              bpad, qcap_, cpad_, q_planes_);
+                                              bpad, sc->qcap, cpad_, sc->q_planes);
     split_u32_kernel<<<152 * 8, 256, 0, st>>>(yg, kU32, batch, pk_cols_, yg_stride,
-                                              bpad, qcap_, kpad_, y_planes_);
+                                              bpad, sc->qcap, kpad_, sc->y_planes);
     LimbArgs a;
     a.rows = static_cast<int>(rows_);
     a.n_db_units = static_cast<int>(cpad_ / kUnitK);
     a.n_pk_blocks = static_cast<int>(kpad_ / kUnitK);
-    a.qcap = static_cast<int>(qcap_);
+    a.qcap = static_cast<int>(sc->qcap);
     a.batch = batch;
     a.out_stride = rows_;
     const int nqt = static_cast<int>(bpad / kTileQ);
@@ -597,7 +620,7 @@ class LimbGemmImpl : public LimbGemm {
     }
     const unsigned grid = static_cast<unsigned>(tiles * a.ksplit);
     limb_gemm_kernel<<<grid, kThreads, kSmemBytes, st>>>(
-        tm_db_, tm_pk_, tm_q_, tm_y_, a, static_cast<uint32_t*>(out), err_);
+        tm_db_, tm_pk_, sc->tm_q, sc->tm_y, a, static_cast<uint32_t*>(out), err_);
     return cudaGetLastError();
   }
 
@@ -629,12 +652,10 @@ class LimbGemmImpl : public LimbGemm {
 
  private:
   int64_t rows_ = 0, db_cols_ = 0, pk_cols_ = 0, cpad_ = 0, kpad_ = 0;
-  int64_t qcap_ = 0;
   int sms_ = 0;
   __half *db_planes_ = nullptr, *pk_planes_ = nullptr;
-  __half *q_planes_ = nullptr, *y_planes_ = nullptr;
   int* err_ = nullptr;
-  CUtensorMap tm_db_{}, tm_pk_{}, tm_q_{}, tm_y_{};
+  CUtensorMap tm_db_{}, tm_pk_{};
 };
 
 }  // namespace

@@ -8,6 +8,13 @@
 
 namespace inspire {
 
+// Per-batch state of the tensor engine (the request byte planes and their
+// TMA descriptors). One per in-flight batch.
+class LimbScratch {
+ public:
+  virtual ~LimbScratch() = default;
+};
+
 class LimbGemm {
  public:
   // Prepares the limb planes of the server matrices. Leaves *out empty when
@@ -16,10 +23,13 @@ class LimbGemm {
                      int64_t db_cols, int mat_kind, const void* pack,
                      int64_t pack_cols, std::unique_ptr<LimbGemm>* out);
   virtual ~LimbGemm() = default;
+  virtual std::unique_ptr<LimbScratch> NewScratch() = 0;
+  // Device bytes the scratch for `batch` requests holds.
+  virtual int64_t ScratchBytes(int batch) const = 0;
   // out[q][r] = db[r] . q1[q] + pack[r] . yg[q]  (mod 2^w), q < batch.
   virtual cudaError_t Run(int batch, const void* q1, int64_t q1_stride,
                           const void* yg, int64_t yg_stride, void* out,
-                          cudaStream_t stream) = 0;
+                          LimbScratch* scratch, cudaStream_t stream) = 0;
   // Returns (and clears) the kernel's error flag: non-zero when a pipeline
   // wait timed out in a previous launch. Synchronous.
   virtual int CheckError() = 0;

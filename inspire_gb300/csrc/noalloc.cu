@@ -246,7 +246,7 @@ Status Run(const void* u, const void* v, int n, int d, int logd, int u_bits,
   noalloc_ntt_u_kernel<T><<<n * r, kPolyThreads, d * 4, st>>>(
       static_cast<const T*>(u), chunk_bits, u_chunks, u_bits, is_signed, U, c);
   ntt_coeffs_kernel<T><<<dim3(n * r, 1), kPolyThreads, d * 4, st>>>(
-      static_cast<const T*>(v), 0, 0, n, static_cast<T>(vmask), V, c);
+      static_cast<const T*>(v), 0, 0, n, static_cast<T>(vmask), V, d, c);
   inner_product_finish_kernel<T><<<1, kPolyThreads, smem_fin, st>>>(
       U, V, n, static_cast<T*>(out), c);
   e = cudaGetLastError();

@@ -74,14 +74,14 @@ template <typename T>
 __global__ void __launch_bounds__(kPolyThreads)
 ntt_coeffs_kernel(const T* __restrict__ src, int64_t src_qstride,
                   int64_t src_off, int npoly, T mask, uint32_t* __restrict__ dst,
-                  NttCtx c) {
+                  int64_t poly_stride, NttCtx c) {
   extern __shared__ uint32_t smem[];
   const int d = 1 << c.logd;
   const int poly = blockIdx.x / c.r;
   const int pi = blockIdx.x % c.r;
   const int q = blockIdx.y;
   const uint32_t p = c.p[pi];
-  const T* in = src + q * src_qstride + src_off + static_cast<int64_t>(poly) * d;
+  const T* in = src + q * src_qstride + src_off + poly * poly_stride;
   for (int j = threadIdx.x; j < d; j += blockDim.x) {
     smem[j] = to_residue<T>(in[j] & mask, p);
   }
@@ -193,6 +193,23 @@ finalize_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ Yh
   }
 }
 
+// The packed ciphertexts as (a_tilde_agg, b_agg) pairs:
+// out[q][s] = (a[s], b[q][s]). grid = (shards, batch).
+template <typename T>
+__global__ void __launch_bounds__(kPolyThreads)
+pack_out_kernel(const T* __restrict__ a, const T* __restrict__ b, int d,
+                T* __restrict__ out) {
+  const int s = blockIdx.x;
+  const int64_t qs = static_cast<int64_t>(blockIdx.y) * gridDim.x + s;
+  const T* as = a + static_cast<int64_t>(s) * d;
+  const T* bs = b + qs * d;
+  T* o = out + qs * 2 * d;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    o[j] = as[j];
+    o[d + j] = bs[j];
+  }
+}
+
 struct ExtArgs {
   int log_q;         // LowBits width and GadgetInv log_modulus
   int log_digit;
@@ -239,17 +256,18 @@ __device__ __forceinline__ void horner_state(
 // One external product per (request, shard) and prime:
 //   digits of LowBits(state) -> NTT -> MAC with the RGSW NTTs -> INTT.
 // Writes scaled residues of (a', b') to resid_out[q][shard][prime][2][d].
-// grid = (r, l, batch). RGSWa: [2ne][r][d] (server), RGSWb:
-// [batch][2ne][r][d] (request). coeff_a/coeff_b select the packed
+// grid = (r, l, batch). RGSWa: [2ne][r][d] (server; rgswa_qstride = 0) or
+// [batch][2ne][r][d] (rgswa_qstride = 2ne*r*d), RGSWb: [batch][2ne][r][d]. coeff_a/coeff_b select the packed
 // ciphertext added to the previous product (or the initial state).
 template <typename T>
 __global__ void __launch_bounds__(kPolyThreads)
 ext_step_kernel(bool first, const uint32_t* __restrict__ resid_in,
                 uint32_t* __restrict__ resid_out,
-                const T* __restrict__ coeff_a, int64_t coeff_a_shard_stride,
+                const T* __restrict__ coeff_a, int64_t coeff_a_q_stride,
+                int64_t coeff_a_shard_stride,
                 const T* __restrict__ coeff_b, int64_t coeff_b_q_stride,
                 int64_t coeff_b_shard_stride,
-                const uint32_t* __restrict__ RGSWa,
+                const uint32_t* __restrict__ RGSWa, int64_t rgswa_qstride,
                 const uint32_t* __restrict__ RGSWb, ExtArgs e, NttCtx c) {
   extern __shared__ uint32_t smem[];
   const int d = 1 << c.logd;
@@ -262,7 +280,7 @@ ext_step_kernel(bool first, const uint32_t* __restrict__ resid_in,
   T* sa = reinterpret_cast<T*>(smem + d);
   T* sb = sa + d;
 
-  const T* ca = coeff_a + shard * coeff_a_shard_stride;
+  const T* ca = coeff_a + q * coeff_a_q_stride + shard * coeff_a_shard_stride;
   const T* cb = coeff_b + q * coeff_b_q_stride + shard * coeff_b_shard_stride;
   const int64_t rbase = (static_cast<int64_t>(q) * l + shard) * c.r * 2 * d;
   for (int j = threadIdx.x; j < d; j += blockDim.x) {
@@ -286,7 +304,8 @@ ext_step_kernel(bool first, const uint32_t* __restrict__ resid_in,
       smem[j] = to_residue<T>(dig & static_cast<T>(e.umask), p);
     }
     ntt_forward(smem, c, pi);
-    const uint32_t* wa = RGSWa + (static_cast<int64_t>(g) * c.r + pi) * d;
+    const uint32_t* wa =
+        RGSWa + q * rgswa_qstride + (static_cast<int64_t>(g) * c.r + pi) * d;
     const uint32_t* wb =
         RGSWb + ((static_cast<int64_t>(q) * ng + g) * c.r + pi) * d;
 #pragma unroll

@@ -323,14 +323,43 @@ Status SetSmem(K kernel, size_t bytes) {
 }  // namespace inspire
 
 // ---------------------------------------------------------------------------
-// The server object.
+// The server object and its per-batch workspaces.
 // ---------------------------------------------------------------------------
+namespace inspire {
+
+// Everything one in-flight batch needs: device buffers, the tensor engine's
+// request byte planes, a stream, timing events and pinned host staging. A
+// server answers synchronous calls with its own workspace; callers that want
+// several batches in flight (the serving loop) create more.
+struct Workspace {
+  int cap = 0;
+  DevBuf q1, pkey, sdim, gemv, yh, rgswb, packed, resid0, resid1, resp;
+  DevBuf rgswa;  // per-request RGSW a-parts (batched ExternalProduct only)
+  std::unique_ptr<LimbScratch> limb;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t done = nullptr;
+  void* host[4] = {nullptr, nullptr, nullptr, nullptr};  // fd, sd, pk, resp
+  int pending_engine = -1;
+  ~Workspace() {
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    if (done) cudaEventDestroy(done);
+    if (stream) cudaStreamDestroy(stream);
+    for (auto& h : host)
+      if (h) cudaFreeHost(h);
+  }
+};
+
+}  // namespace inspire
+
 struct inspire_pir_server {
   inspire_pir_params prm{};
   int d = 0, t = 0, l = 0, k = 0, ne = 0;
   int64_t rows = 0, db_cols = 0, pack_cols = 0;
   int interpolated_rows = 0;
   inspire::Status deferred;  // error the reference reports per request
+  inspire::Status eval_rule;  // chunk rule of the eval-gadget inner product
 
   inspire::DevBuf db, pack, a_tilde, th_ntt, rgswa_ntt;
   std::unique_ptr<inspire::NttTables> tables;
@@ -338,41 +367,42 @@ struct inspire_pir_server {
   uint64_t vmask_f = 0, vmask_e = 0, umask_e = 0;
   std::unique_ptr<inspire::LimbGemm> limb;
 
-  // Per-batch workspace (grown on demand).
-  int cap = 0;
-  inspire::DevBuf q1, pkey, sdim, gemv, yh, rgswb, packed, resid0, resid1,
-      resp;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  std::mutex mu;
+  std::unique_ptr<inspire::Workspace> ws0;  // for the synchronous calls
+  std::mutex mu;                           // guards ws0 and the timers
   double t_db = 0, t_pack = 0, t_eval = 0;
+};
 
-  ~inspire_pir_server() {
-    for (auto& e : ev)
-      if (e) cudaEventDestroy(e);
-    if (stream) cudaStreamDestroy(stream);
-  }
+struct inspire_graph {
+  cudaGraphExec_t exec = nullptr;
+};
+
+struct inspire_pir_workspace {
+  inspire_pir_server* server = nullptr;
+  inspire::Workspace ws;
 };
 
 namespace inspire {
 namespace {
 
+// d/16 coefficients per thread at most (kMaxPer), smaller CTAs otherwise so
+// that batches fill the SMs without a wave tail.
+inline int PolyThreads(int d) { return d <= 16 * 256 ? 256 : kPolyThreads; }
+
+// FinalizeMatrixPack for every shard of every request of a batch
+// (lwes_to_rlwe.cc:448-479): w->packed[q][shard] = b_agg.
 template <typename T>
-Status RunPolyStage(inspire_pir_server* s, int batch, const T* pkey,
-                    const T* sdim, const T* gemv, T* resp, cudaStream_t st,
-                    bool timed) {
-  const int d = s->d, t = s->t, l = s->l, k = s->k, ne = s->ne;
+Status FinalizeStage(inspire_pir_server* s, Workspace* w, int batch,
+                     const T* pkey, const T* gemv, cudaStream_t st) {
+  const int d = s->d, t = s->t, l = s->l, k = s->k;
   const int log_q = s->prm.log_modulus;
-  // d/16 coefficients per thread at most (kMaxPer), smaller CTAs otherwise
-  // so that batches fill the SMs without a wave tail.
-  const int nt = d <= 16 * 256 ? 256 : kPolyThreads;
+  const int nt = PolyThreads(d);
   // y_h = packing_key[k..2k): forward NTT over the finalize primes.
   {
     const NttCtx& c = s->ctx_f;
     dim3 grid(k * c.r, batch);
     ntt_coeffs_kernel<T><<<grid, nt, d * 4, st>>>(
         pkey, static_cast<int64_t>(2 * k) * d, static_cast<int64_t>(k) * d, k,
-        static_cast<T>(s->vmask_f), s->yh.get<uint32_t>(), c);
+        static_cast<T>(s->vmask_f), w->yh.get<uint32_t>(), d, c);
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "ntt(y_h)"));
   }
   {
@@ -381,22 +411,33 @@ Status RunPolyStage(inspire_pir_server* s, int batch, const T* pkey,
     RETURN_IF_ERROR(SetSmem(finalize_kernel<T>, smem));
     dim3 grid(l * t, batch);
     finalize_kernel<T><<<grid, nt, smem, st>>>(
-        s->th_ntt.get<uint32_t>(), s->yh.get<uint32_t>(), k, gemv, nullptr,
-        s->rows, s->packed.get<T>(), log_q, c);
+        s->th_ntt.get<uint32_t>(), w->yh.get<uint32_t>(), k, gemv, nullptr,
+        s->rows, w->packed.get<T>(), log_q, c);
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "finalize"));
   }
-  if (timed) cudaEventRecord(s->ev[2], st);
+  return Status{};
+}
+
+template <typename T>
+Status RunPolyStage(inspire_pir_server* s, Workspace* w, int batch,
+                    const T* pkey, const T* sdim, const T* gemv, T* resp,
+                    cudaStream_t st, bool timed) {
+  const int d = s->d, t = s->t, l = s->l, ne = s->ne;
+  const int log_q = s->prm.log_modulus;
+  const int nt = PolyThreads(d);
+  RETURN_IF_ERROR(FinalizeStage<T>(s, w, batch, pkey, gemv, st));
+  if (timed) cudaEventRecord(w->ev[2], st);
   const T* a_tilde = s->a_tilde.get<T>();
-  const T* packed = s->packed.get<T>();
+  const T* packed = w->packed.get<T>();
   const int64_t a_stride = static_cast<int64_t>(t) * d;        // per shard
   const int64_t b_qstride = static_cast<int64_t>(l) * t * d;   // per request
-  uint32_t* resid[2] = {s->resid0.get<uint32_t>(), s->resid1.get<uint32_t>()};
+  uint32_t* resid[2] = {w->resid0.get<uint32_t>(), w->resid1.get<uint32_t>()};
   if (t > 1) {
     const NttCtx& c = s->ctx_e;
     dim3 g1(2 * ne * c.r, batch);
     ntt_coeffs_kernel<T><<<g1, nt, d * 4, st>>>(
         sdim, static_cast<int64_t>(2 * ne) * d, 0, 2 * ne,
-        static_cast<T>(s->vmask_e), s->rgswb.get<uint32_t>(), c);
+        static_cast<T>(s->vmask_e), w->rgswb.get<uint32_t>(), d, c);
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "ntt(rgsw)"));
     ExtArgs e{log_q, s->prm.eval_log_digit, ne,
               LiveDigits(log_q, s->prm.eval_log_digit, ne), s->umask_e};
@@ -407,9 +448,9 @@ Status RunPolyStage(inspire_pir_server* s, int batch, const T* pkey,
       const bool first = i == t - 2;
       ext_step_kernel<T><<<grid, nt, smem, st>>>(
           first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
-          a_tilde + static_cast<int64_t>(i + 1) * d, a_stride,
+          a_tilde + static_cast<int64_t>(i + 1) * d, 0, a_stride,
           packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
-          s->rgswa_ntt.get<uint32_t>(), s->rgswb.get<uint32_t>(), e, c);
+          s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
       RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
     }
   }
@@ -424,23 +465,46 @@ Status RunPolyStage(inspire_pir_server* s, int batch, const T* pkey,
   return Status{};
 }
 
-Status EnsureWorkspace(inspire_pir_server* s, int batch) {
-  if (batch <= s->cap) return Status{};
+int64_t WorkspaceBytes(const inspire_pir_server* s, int batch) {
+  const int64_t w = Words(s->prm.coeff_bits);
+  const int64_t d = s->d;
+  const int64_t B = batch;
+  int64_t b = B * s->db_cols * w + B * 2 * s->k * d * w +
+              B * std::max(1, 2 * s->ne) * d * w + B * s->rows * w +
+              B * s->k * s->ctx_f.r * d * 4 +
+              B * std::max(1, 2 * s->ne) * s->ctx_e.r * d * 4 +
+              B * s->l * s->t * d * w + 2 * B * s->l * s->ctx_e.r * 2 * d * 4 +
+              B * s->l * 2 * d * w;
+  if (s->limb) b += s->limb->ScratchBytes(batch);
+  return b;
+}
+
+Status EnsureWorkspace(inspire_pir_server* s, Workspace* ws, int batch) {
+  if (batch <= ws->cap) return Status{};
   const size_t w = Words(s->prm.coeff_bits);
   const size_t d = s->d;
   const size_t B = batch;
-  RETURN_IF_ERROR(s->q1.Alloc(B * s->db_cols * w));
-  RETURN_IF_ERROR(s->pkey.Alloc(B * 2 * s->k * d * w));
-  RETURN_IF_ERROR(s->sdim.Alloc(B * std::max(1, 2 * s->ne) * d * w));
-  RETURN_IF_ERROR(s->gemv.Alloc(B * s->rows * w));
-  RETURN_IF_ERROR(s->yh.Alloc(B * s->k * s->ctx_f.r * d * 4));
-  RETURN_IF_ERROR(s->rgswb.Alloc(B * std::max(1, 2 * s->ne) * s->ctx_e.r * d * 4));
-  RETURN_IF_ERROR(s->packed.Alloc(B * s->l * s->t * d * w));
-  RETURN_IF_ERROR(s->resid0.Alloc(B * s->l * s->ctx_e.r * 2 * d * 4));
-  RETURN_IF_ERROR(s->resid1.Alloc(B * s->l * s->ctx_e.r * 2 * d * 4));
-  RETURN_IF_ERROR(s->resp.Alloc(B * s->l * 2 * d * w));
-  s->cap = batch;
+  RETURN_IF_ERROR(ws->q1.Alloc(B * s->db_cols * w));
+  RETURN_IF_ERROR(ws->pkey.Alloc(B * 2 * s->k * d * w));
+  RETURN_IF_ERROR(ws->sdim.Alloc(B * std::max(1, 2 * s->ne) * d * w));
+  RETURN_IF_ERROR(ws->gemv.Alloc(B * s->rows * w));
+  RETURN_IF_ERROR(ws->yh.Alloc(B * s->k * s->ctx_f.r * d * 4));
+  RETURN_IF_ERROR(ws->rgswb.Alloc(B * std::max(1, 2 * s->ne) * s->ctx_e.r * d * 4));
+  RETURN_IF_ERROR(ws->packed.Alloc(B * s->l * s->t * d * w));
+  RETURN_IF_ERROR(ws->resid0.Alloc(B * s->l * s->ctx_e.r * 2 * d * 4));
+  RETURN_IF_ERROR(ws->resid1.Alloc(B * s->l * s->ctx_e.r * 2 * d * 4));
+  RETURN_IF_ERROR(ws->resp.Alloc(B * s->l * 2 * d * w));
+  if (s->limb && !ws->limb) ws->limb = s->limb->NewScratch();
+  ws->cap = batch;
   return Status{};
+}
+
+Status InitWorkspace(Workspace* ws) {
+  RETURN_IF_ERROR(Cuda(cudaStreamCreateWithFlags(&ws->stream, cudaStreamNonBlocking),
+                       "cudaStreamCreate"));
+  for (auto& e : ws->ev) RETURN_IF_ERROR(Cuda(cudaEventCreate(&e), "cudaEventCreate"));
+  return Cuda(cudaEventCreateWithFlags(&ws->done, cudaEventDisableTiming),
+              "cudaEventCreate");
 }
 
 // Validation shared by every ProcessResponse flavour
@@ -469,16 +533,19 @@ Status ValidateRequest(const inspire_pir_server* s, int64_t first_dim_len,
 }
 
 // Stage 1: out[q] = DB * q1[q] + P * y_g[q] for the whole batch.
-Status Products(inspire_pir_server* s, int batch, const void* q1,
-                const void* pkey, void* out, int engine, cudaStream_t st) {
+Status Products(inspire_pir_server* s, Workspace* ws, int batch,
+                const void* q1, const void* pkey, void* out, int engine,
+                cudaStream_t st) {
   const int cb = s->prm.coeff_bits;
   if (engine == INSPIRE_ENGINE_TENSOR) {
     if (!s->limb) {
       return Err(INSPIRE_FAILED_PRECONDITION,
                  "tensor engine unavailable for these parameters");
     }
+    if (!ws->limb) ws->limb = s->limb->NewScratch();
     return Cuda(s->limb->Run(batch, q1, s->db_cols, pkey,
-                             static_cast<int64_t>(2 * s->k) * s->d, out, st),
+                             static_cast<int64_t>(2 * s->k) * s->d, out,
+                             ws->limb.get(), st),
                 "limb gemm");
   }
   if (engine != INSPIRE_ENGINE_PLAIN) {
@@ -493,26 +560,108 @@ Status Products(inspire_pir_server* s, int batch, const void* q1,
 }
 
 // The device part of a batch: products, polynomial stage, rescale.
-Status AnswerOnDevice(inspire_pir_server* s, int batch, const void* q1,
-                      const void* pkey, const void* sdim, void* resp,
-                      int engine, cudaStream_t st, bool timed) {
+Status AnswerOnDevice(inspire_pir_server* s, Workspace* w, int batch,
+                      const void* q1, const void* pkey, const void* sdim,
+                      void* resp, int engine, cudaStream_t st, bool timed) {
   const int cb = s->prm.coeff_bits;
-  if (timed) cudaEventRecord(s->ev[0], st);
-  RETURN_IF_ERROR(Products(s, batch, q1, pkey, s->gemv.get(), engine, st));
-  if (timed) cudaEventRecord(s->ev[1], st);
+  if (timed) cudaEventRecord(w->ev[0], st);
+  RETURN_IF_ERROR(Products(s, w, batch, q1, pkey, w->gemv.get(), engine, st));
+  if (timed) cudaEventRecord(w->ev[1], st);
   if (cb == 32) {
     RETURN_IF_ERROR(RunPolyStage<uint32_t>(
-        s, batch, static_cast<const uint32_t*>(pkey),
-        static_cast<const uint32_t*>(sdim), s->gemv.get<uint32_t>(),
+        s, w, batch, static_cast<const uint32_t*>(pkey),
+        static_cast<const uint32_t*>(sdim), w->gemv.get<uint32_t>(),
         static_cast<uint32_t*>(resp), st, timed));
   } else {
     RETURN_IF_ERROR(RunPolyStage<uint64_t>(
-        s, batch, static_cast<const uint64_t*>(pkey),
-        static_cast<const uint64_t*>(sdim), s->gemv.get<uint64_t>(),
+        s, w, batch, static_cast<const uint64_t*>(pkey),
+        static_cast<const uint64_t*>(sdim), w->gemv.get<uint64_t>(),
         static_cast<uint64_t*>(resp), st, timed));
   }
-  if (timed) cudaEventRecord(s->ev[3], st);
+  if (timed) cudaEventRecord(w->ev[3], st);
   return Status{};
+}
+
+// Zero-padded first dimension of a device-resident batch
+// (pir_server.cc:221-227): the products read db_cols words per request, so
+// short requests are copied into the workspace and padded there.
+Status DeviceFirstDim(inspire_pir_server* s, Workspace* ws, int batch,
+                      const void** first_dim, int64_t first_dim_len,
+                      cudaStream_t st) {
+  if (first_dim_len >= s->db_cols) return Status{};
+  const size_t w = Words(s->prm.coeff_bits);
+  RETURN_IF_ERROR(Cuda(cudaMemcpy2DAsync(ws->q1.get(), s->db_cols * w, *first_dim,
+                                         first_dim_len * w, first_dim_len * w,
+                                         batch, cudaMemcpyDeviceToDevice, st),
+                       "copy first_dim"));
+  RETURN_IF_ERROR(Cuda(
+      cudaMemset2DAsync(static_cast<char*>(ws->q1.get()) + first_dim_len * w,
+                        s->db_cols * w, 0, (s->db_cols - first_dim_len) * w,
+                        batch, st),
+      "pad first_dim"));
+  *first_dim = ws->q1.get();
+  return Status{};
+}
+
+// The packing tool's server step for a batch: products, then
+// FinalizeMatrixPack of every shard, written as (a_tilde_agg, b_agg) pairs;
+// no EvalPoly, no modulus switch.
+Status PackOnDevice(inspire_pir_server* s, Workspace* w, int batch,
+                    const void* q1, const void* pkey, void* out, int engine,
+                    cudaStream_t st) {
+  RETURN_IF_ERROR(Products(s, w, batch, q1, pkey, w->gemv.get(), engine, st));
+  auto run = [&](auto tag) -> Status {
+    using T = decltype(tag);
+    RETURN_IF_ERROR(FinalizeStage<T>(s, w, batch, static_cast<const T*>(pkey),
+                                     w->gemv.get<T>(), st));
+    pack_out_kernel<T><<<dim3(s->l * s->t, batch), PolyThreads(s->d), 0, st>>>(
+        s->a_tilde.get<T>(), w->packed.get<T>(), s->d, static_cast<T*>(out));
+    return Cuda(cudaGetLastError(), "pack output");
+  };
+  return s->prm.coeff_bits == 32 ? run(uint32_t{}) : run(uint64_t{});
+}
+
+// ExternalProduct (external_product.cc:35-114) of `batch` independent
+// ciphertexts, each with its own RGSW ciphertext, with the server's eval
+// gadget and NTT tables. ct: [batch][2][d] (a, b); rgsw: [batch][2ne][2][d]
+// (u[0..ne) then v[0..ne), each an (a, b) pair); out: [batch][2][d].
+Status ExternalOnDevice(inspire_pir_server* s, Workspace* w, int batch,
+                        const void* ct, const void* rgsw, void* out,
+                        cudaStream_t st) {
+  RETURN_IF_ERROR(s->eval_rule);
+  const int d = s->d, ne = s->ne, ng = 2 * s->ne;
+  const NttCtx& c = s->ctx_e;
+  const size_t need = static_cast<size_t>(batch) * ng * c.r * d * 4;
+  if (w->rgswa.bytes() < need) RETURN_IF_ERROR(w->rgswa.Alloc(need));
+  const int nt = PolyThreads(d);
+  auto run = [&](auto tag) -> Status {
+    using T = decltype(tag);
+    const T* rg = static_cast<const T*>(rgsw);
+    const int64_t qs = static_cast<int64_t>(2 * ng) * d;
+    ntt_coeffs_kernel<T><<<dim3(ng * c.r, batch), nt, d * 4, st>>>(
+        rg, qs, 0, ng, static_cast<T>(s->vmask_e), w->rgswa.get<uint32_t>(),
+        2 * d, c);
+    ntt_coeffs_kernel<T><<<dim3(ng * c.r, batch), nt, d * 4, st>>>(
+        rg, qs, d, ng, static_cast<T>(s->vmask_e), w->rgswb.get<uint32_t>(),
+        2 * d, c);
+    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "ntt(rgsw)"));
+    ExtArgs e{s->prm.log_modulus, s->prm.eval_log_digit, ne,
+              LiveDigits(s->prm.log_modulus, s->prm.eval_log_digit, ne),
+              s->umask_e};
+    const size_t smem = static_cast<size_t>(d) * 4 + 2ull * d * sizeof(T);
+    RETURN_IF_ERROR(SetSmem(ext_step_kernel<T>, smem));
+    const T* cta = static_cast<const T*>(ct);
+    ext_step_kernel<T><<<dim3(c.r, 1, batch), nt, smem, st>>>(
+        true, nullptr, w->resid0.get<uint32_t>(), cta, 2 * d, 0, cta + d, 2 * d,
+        0, w->rgswa.get<uint32_t>(), static_cast<int64_t>(ng) * c.r * d,
+        w->rgswb.get<uint32_t>(), e, c);
+    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
+    finish_kernel<T><<<dim3(1, batch), nt, 0, st>>>(
+        true, w->resid0.get<uint32_t>(), nullptr, 0, nullptr, 0, 0, false, 0, 0,
+        0, static_cast<T*>(out), c);
+    return Cuda(cudaGetLastError(), "external product output");
+  };
+  return s->prm.coeff_bits == 32 ? run(uint32_t{}) : run(uint64_t{});
 }
 
 Status ProcessHostBatch(inspire_pir_server* s, int batch, const void* first_dim,
@@ -524,36 +673,37 @@ Status ProcessHostBatch(inspire_pir_server* s, int batch, const void* first_dim,
   RETURN_IF_ERROR(ValidateRequest(s, first_dim_len, second_dim_count,
                                   packing_key_count));
   std::lock_guard<std::mutex> lock(s->mu);
-  RETURN_IF_ERROR(EnsureWorkspace(s, batch));
+  Workspace* ws = s->ws0.get();
+  RETURN_IF_ERROR(EnsureWorkspace(s, ws, batch));
   const size_t w = Words(s->prm.coeff_bits);
   const size_t d = s->d;
-  cudaStream_t st = s->stream;
+  cudaStream_t st = ws->stream;
   // Zero-padded first dimension (pir_server.cc:221-227).
-  RETURN_IF_ERROR(Cuda(cudaMemcpy2DAsync(s->q1.get(), s->db_cols * w, first_dim,
+  RETURN_IF_ERROR(Cuda(cudaMemcpy2DAsync(ws->q1.get(), s->db_cols * w, first_dim,
                                          first_dim_len * w, first_dim_len * w,
                                          batch, cudaMemcpyHostToDevice, st),
                        "copy first_dim"));
   if (first_dim_len < s->db_cols) {
     RETURN_IF_ERROR(Cuda(
-        cudaMemset2DAsync(static_cast<char*>(s->q1.get()) + first_dim_len * w,
+        cudaMemset2DAsync(static_cast<char*>(ws->q1.get()) + first_dim_len * w,
                           s->db_cols * w, 0, (s->db_cols - first_dim_len) * w,
                           batch, st),
         "pad first_dim"));
   }
-  RETURN_IF_ERROR(Cuda(cudaMemcpyAsync(s->pkey.get(), packing_key,
+  RETURN_IF_ERROR(Cuda(cudaMemcpyAsync(ws->pkey.get(), packing_key,
                                        batch * packing_key_count * d * w,
                                        cudaMemcpyHostToDevice, st),
                        "copy packing_key"));
   if (s->t > 1) {
-    RETURN_IF_ERROR(Cuda(cudaMemcpyAsync(s->sdim.get(), second_dim,
+    RETURN_IF_ERROR(Cuda(cudaMemcpyAsync(ws->sdim.get(), second_dim,
                                          batch * second_dim_count * d * w,
                                          cudaMemcpyHostToDevice, st),
                          "copy second_dim"));
   }
-  RETURN_IF_ERROR(AnswerOnDevice(s, batch, s->q1.get(), s->pkey.get(),
-                                 s->sdim.get(), s->resp.get(), engine, st, true));
+  RETURN_IF_ERROR(AnswerOnDevice(s, ws, batch, ws->q1.get(), ws->pkey.get(),
+                                 ws->sdim.get(), ws->resp.get(), engine, st, true));
   const size_t out_bytes = static_cast<size_t>(batch) * s->l * 2 * d * w;
-  RETURN_IF_ERROR(Cuda(cudaMemcpyAsync(responses, s->resp.get(), out_bytes,
+  RETURN_IF_ERROR(Cuda(cudaMemcpyAsync(responses, ws->resp.get(), out_bytes,
                                        cudaMemcpyDeviceToHost, st),
                        "copy response"));
   RETURN_IF_ERROR(Cuda(cudaStreamSynchronize(st), "answer"));
@@ -561,9 +711,9 @@ Status ProcessHostBatch(inspire_pir_server* s, int batch, const void* first_dim,
     return Err(INSPIRE_INTERNAL, "tensor engine pipeline timed out");
   }
   float ms_db = 0, ms_pack = 0, ms_eval = 0;
-  cudaEventElapsedTime(&ms_db, s->ev[0], s->ev[1]);
-  cudaEventElapsedTime(&ms_pack, s->ev[1], s->ev[2]);
-  cudaEventElapsedTime(&ms_eval, s->ev[2], s->ev[3]);
+  cudaEventElapsedTime(&ms_db, ws->ev[0], ws->ev[1]);
+  cudaEventElapsedTime(&ms_pack, ws->ev[1], ws->ev[2]);
+  cudaEventElapsedTime(&ms_eval, ws->ev[2], ws->ev[3]);
   s->t_db += ms_db;
   s->t_pack += ms_pack;
   s->t_eval += ms_eval;
@@ -600,7 +750,7 @@ Status PrepareConstants(inspire_pir_server* s, const T* t_vec_h,
     dim3 grid(ng * s->ctx_e.r, 1);
     ntt_coeffs_kernel<T><<<grid, kPolyThreads, d * 4>>>(
         tmp.get<T>(), 0, 0, ng, static_cast<T>(s->vmask_e),
-        s->rgswa_ntt.get<uint32_t>(), s->ctx_e);
+        s->rgswa_ntt.get<uint32_t>(), d, s->ctx_e);
     RETURN_IF_ERROR(Cuda(cudaDeviceSynchronize(), "second_dim_a transform"));
   }
   (void)rule_e;
@@ -712,6 +862,7 @@ Status CreateServer(const inspire_pir_params* prm, const void* db,
                        ChunkFor(2 * s->ne, d), &re);
   if (!sf.ok()) s->deferred = sf;
   if (t > 1 && !se.ok() && s->deferred.ok()) s->deferred = se;
+  s->eval_rule = se;
   int r_f = 3, r_e = 3;
   if (sf.ok()) {
     s->vmask_f = MaskBits(rf.v_chunks * rf.chunk_bits, cb);
@@ -750,9 +901,8 @@ Status CreateServer(const inspire_pir_params* prm, const void* db,
           static_cast<const uint64_t*>(second_dim_a), rf, re));
     }
   }
-  RETURN_IF_ERROR(Cuda(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking),
-                       "cudaStreamCreate"));
-  for (auto& e : s->ev) RETURN_IF_ERROR(Cuda(cudaEventCreate(&e), "cudaEventCreate"));
+  s->ws0.reset(new Workspace());
+  RETURN_IF_ERROR(InitWorkspace(s->ws0.get()));
   // The tensor-core engine when the shapes allow it.
   LimbGemm::Create(cb, prm->db_kind, s->db.get(), db_rows, db_cols,
                    prm->mat_kind, s->pack.get(), pack_cols, &s->limb);
@@ -845,12 +995,125 @@ int inspire_pir_process_batch_device(inspire_pir_server* server,
                                        packing_key_count);
   if (!st.ok()) return Report(st, err, err_len);
   std::lock_guard<std::mutex> lock(server->mu);
-  st = inspire::EnsureWorkspace(server, batch);
+  inspire::Workspace* ws = server->ws0.get();
+  st = inspire::EnsureWorkspace(server, ws, batch);
   if (!st.ok()) return Report(st, err, err_len);
-  st = inspire::AnswerOnDevice(server, batch, first_dim, packing_key, second_dim,
-                               responses, engine,
-                               static_cast<cudaStream_t>(stream), false);
+  const cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  st = inspire::DeviceFirstDim(server, ws, batch, &first_dim, first_dim_len, cs);
+  if (st.ok()) {
+    st = inspire::AnswerOnDevice(server, ws, batch, first_dim, packing_key,
+                                 second_dim, responses, engine, cs, false);
+  }
   return Report(st, err, err_len);
+}
+
+int inspire_pir_pack_batch_device(inspire_pir_server* server, int32_t batch,
+                                  const void* first_dim, int64_t first_dim_len,
+                                  const void* packing_key,
+                                  int64_t packing_key_count, void* out,
+                                  int32_t engine, void* stream, char* err,
+                                  size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr || batch <= 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server is null or batch <= 0."),
+                  err, err_len);
+  }
+  Status st = ValidateRequest(server, first_dim_len, 2 * server->ne,
+                              packing_key_count);
+  if (!st.ok()) return Report(st, err, err_len);
+  std::lock_guard<std::mutex> lock(server->mu);
+  Workspace* ws = server->ws0.get();
+  st = EnsureWorkspace(server, ws, batch);
+  const cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  if (st.ok()) st = DeviceFirstDim(server, ws, batch, &first_dim, first_dim_len, cs);
+  if (st.ok()) st = PackOnDevice(server, ws, batch, first_dim, packing_key, out, engine, cs);
+  return Report(st, err, err_len);
+}
+
+int inspire_pir_external_product_device(inspire_pir_server* server,
+                                        int32_t batch, const void* ct,
+                                        const void* rgsw, void* out,
+                                        void* stream, char* err,
+                                        size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr || batch <= 0 || ct == nullptr || rgsw == nullptr ||
+      out == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT,
+                      "server, ct, rgsw and out must be set and batch positive."),
+                  err, err_len);
+  }
+  std::lock_guard<std::mutex> lock(server->mu);
+  Workspace* ws = server->ws0.get();
+  Status st = EnsureWorkspace(server, ws, batch);
+  if (st.ok()) {
+    st = ExternalOnDevice(server, ws, batch, ct, rgsw, out,
+                          static_cast<cudaStream_t>(stream));
+  }
+  return Report(st, err, err_len);
+}
+
+int inspire_graph_begin(void* stream, char* err, size_t err_len) {
+  using namespace inspire;
+  if (stream == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT,
+                      "graph capture needs a created stream, not the legacy "
+                      "default stream."),
+                  err, err_len);
+  }
+  return Report(Cuda(cudaStreamBeginCapture(static_cast<cudaStream_t>(stream),
+                                            cudaStreamCaptureModeThreadLocal),
+                     "cudaStreamBeginCapture"),
+                err, err_len);
+}
+
+int inspire_graph_end(void* stream, inspire_graph** out, char* err,
+                      size_t err_len) {
+  using namespace inspire;
+  if (stream == nullptr || out == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "stream and out must be set."),
+                  err, err_len);
+  }
+  *out = nullptr;
+  cudaGraph_t graph = nullptr;
+  Status st = Cuda(cudaStreamEndCapture(static_cast<cudaStream_t>(stream), &graph),
+                   "cudaStreamEndCapture (a call inside the capture failed or "
+                   "allocated)");
+  cudaGraphExec_t exec = nullptr;
+  if (st.ok()) st = Cuda(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+  if (graph) cudaGraphDestroy(graph);
+  if (!st.ok()) return Report(st, err, err_len);
+  *out = new inspire_graph{exec};
+  return INSPIRE_OK;
+}
+
+int inspire_graph_launch(inspire_graph* graph, void* stream, char* err,
+                         size_t err_len) {
+  using namespace inspire;
+  if (graph == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "graph is null."), err, err_len);
+  }
+  return Report(Cuda(cudaGraphLaunch(graph->exec, static_cast<cudaStream_t>(stream)),
+                     "cudaGraphLaunch"),
+                err, err_len);
+}
+
+void inspire_graph_destroy(inspire_graph* graph) {
+  if (graph == nullptr) return;
+  if (graph->exec) cudaGraphExecDestroy(graph->exec);
+  delete graph;
+}
+
+int inspire_pir_server_check(inspire_pir_server* server, char* err,
+                             size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server is null."), err, err_len);
+  }
+  if (server->limb && server->limb->CheckError() != 0) {
+    return Report(Err(INSPIRE_INTERNAL, "tensor engine pipeline timed out"), err,
+                  err_len);
+  }
+  return INSPIRE_OK;
 }
 
 int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,
@@ -863,8 +1126,124 @@ int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,
                   err, err_len);
   }
   std::lock_guard<std::mutex> lock(server->mu);
-  Status st = Products(server, batch, first_dim, packing_key, out, engine,
-                       static_cast<cudaStream_t>(stream));
+  Status st = Products(server, server->ws0.get(), batch, first_dim, packing_key,
+                       out, engine, static_cast<cudaStream_t>(stream));
+  return Report(st, err, err_len);
+}
+
+int64_t inspire_pir_workspace_bytes(const inspire_pir_server* server,
+                                    int32_t max_batch) {
+  if (server == nullptr || max_batch <= 0) return -1;
+  return inspire::WorkspaceBytes(server, max_batch);
+}
+
+int inspire_pir_workspace_create(inspire_pir_server* server, int32_t max_batch,
+                                 inspire_pir_workspace** out, char* err,
+                                 size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr || out == nullptr || max_batch <= 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT,
+                      "server/out must be set and max_batch positive."),
+                  err, err_len);
+  }
+  *out = nullptr;
+  std::unique_ptr<inspire_pir_workspace> w(new inspire_pir_workspace());
+  w->server = server;
+  Status st = InitWorkspace(&w->ws);
+  if (st.ok()) st = EnsureWorkspace(server, &w->ws, max_batch);
+  const size_t cw = Words(server->prm.coeff_bits);
+  const size_t d = server->d;
+  const size_t sizes[4] = {
+      static_cast<size_t>(max_batch) * server->db_cols * cw,
+      static_cast<size_t>(max_batch) * std::max(1, 2 * server->ne) * d * cw,
+      static_cast<size_t>(max_batch) * 2 * server->k * d * cw,
+      static_cast<size_t>(max_batch) * server->l * 2 * d * cw};
+  for (int i = 0; i < 4 && st.ok(); ++i) {
+    st = Cuda(cudaMallocHost(&w->ws.host[i], sizes[i]), "cudaMallocHost");
+    if (st.ok()) std::memset(w->ws.host[i], 0, sizes[i]);
+  }
+  if (st.ok()) *out = w.release();
+  return Report(st, err, err_len);
+}
+
+void inspire_pir_workspace_destroy(inspire_pir_workspace* ws) {
+  if (ws != nullptr) cudaStreamSynchronize(ws->ws.stream);
+  delete ws;
+}
+
+int inspire_pir_workspace_host_buffers(inspire_pir_workspace* ws,
+                                       void** first_dim, void** second_dim,
+                                       void** packing_key, void** responses) {
+  if (ws == nullptr) return INSPIRE_INVALID_ARGUMENT;
+  if (first_dim) *first_dim = ws->ws.host[0];
+  if (second_dim) *second_dim = ws->ws.host[1];
+  if (packing_key) *packing_key = ws->ws.host[2];
+  if (responses) *responses = ws->ws.host[3];
+  return INSPIRE_OK;
+}
+
+int inspire_pir_workspace_submit(inspire_pir_workspace* ws, int32_t batch,
+                                 int32_t engine, char* err, size_t err_len) {
+  using namespace inspire;
+  if (ws == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "workspace is null."), err, err_len);
+  }
+  inspire_pir_server* s = ws->server;
+  Workspace* w = &ws->ws;
+  if (batch <= 0 || batch > w->cap) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT,
+                      "batch must be between 1 and the workspace capacity."),
+                  err, err_len);
+  }
+  Status st = s->deferred;
+  const size_t cw = Words(s->prm.coeff_bits);
+  const size_t d = s->d;
+  const cudaStream_t sm = w->stream;
+  const size_t nfd = static_cast<size_t>(batch) * s->db_cols * cw;
+  const size_t nsd = static_cast<size_t>(batch) * 2 * s->ne * d * cw;
+  const size_t npk = static_cast<size_t>(batch) * 2 * s->k * d * cw;
+  if (st.ok()) st = Cuda(cudaMemcpyAsync(w->q1.get(), w->host[0], nfd,
+                                         cudaMemcpyHostToDevice, sm), "copy");
+  if (st.ok() && s->t > 1) {
+    st = Cuda(cudaMemcpyAsync(w->sdim.get(), w->host[1], nsd, cudaMemcpyHostToDevice,
+                              sm), "copy");
+  }
+  if (st.ok()) st = Cuda(cudaMemcpyAsync(w->pkey.get(), w->host[2], npk,
+                                         cudaMemcpyHostToDevice, sm), "copy");
+  if (st.ok()) {
+    st = AnswerOnDevice(s, w, batch, w->q1.get(), w->pkey.get(), w->sdim.get(),
+                        w->resp.get(), engine, sm, false);
+  }
+  if (st.ok()) {
+    st = Cuda(cudaMemcpyAsync(w->host[3], w->resp.get(),
+                              static_cast<size_t>(batch) * s->l * 2 * d * cw,
+                              cudaMemcpyDeviceToHost, sm),
+              "copy");
+  }
+  if (st.ok()) st = Cuda(cudaEventRecord(w->done, sm), "cudaEventRecord");
+  if (st.ok()) w->pending_engine = engine;
+  return Report(st, err, err_len);
+}
+
+int inspire_pir_workspace_poll(inspire_pir_workspace* ws) {
+  if (ws == nullptr) return -INSPIRE_INVALID_ARGUMENT;
+  const cudaError_t e = cudaEventQuery(ws->ws.done);
+  if (e == cudaSuccess) return 1;
+  if (e == cudaErrorNotReady) return 0;
+  return -INSPIRE_INTERNAL;
+}
+
+int inspire_pir_workspace_wait(inspire_pir_workspace* ws, char* err,
+                               size_t err_len) {
+  using namespace inspire;
+  if (ws == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "workspace is null."), err, err_len);
+  }
+  Status st = Cuda(cudaEventSynchronize(ws->ws.done), "answer");
+  if (st.ok() && ws->ws.pending_engine == INSPIRE_ENGINE_TENSOR &&
+      ws->server->limb && ws->server->limb->CheckError() != 0) {
+    st = Err(INSPIRE_INTERNAL, "tensor engine pipeline timed out");
+  }
   return Report(st, err, err_len);
 }
 
@@ -977,7 +1356,7 @@ int inspire_inner_product(int32_t coeff_bits, const void* u, const void* v,
       st = du.Upload(ue.data(), total * 8);  // full-width unsigned u
       if (st.ok()) {
         ntt_coeffs_kernel<uint64_t><<<dim3(n * r, 1), kPolyThreads, d * 4>>>(
-            du.get<uint64_t>(), 0, 0, n, ~0ull, dU.get<uint32_t>(), c);
+            du.get<uint64_t>(), 0, 0, n, ~0ull, dU.get<uint32_t>(), d, c);
       }
     }
   }
@@ -985,14 +1364,14 @@ int inspire_inner_product(int32_t coeff_bits, const void* u, const void* v,
     if (coeff_bits == 32) {
       ntt_coeffs_kernel<uint32_t><<<dim3(n * r, 1), kPolyThreads, d * 4>>>(
           dv.get<uint32_t>(), 0, 0, n, static_cast<uint32_t>(vmask),
-          dV.get<uint32_t>(), c);
+          dV.get<uint32_t>(), d, c);
       st = SetSmem(inner_product_finish_kernel<uint32_t>, static_cast<size_t>(r) * d * 4);
       if (st.ok())
         inner_product_finish_kernel<uint32_t><<<1, kPolyThreads, r * d * 4>>>(
             dU.get<uint32_t>(), dV.get<uint32_t>(), n, dout.get<uint32_t>(), c);
     } else {
       ntt_coeffs_kernel<uint64_t><<<dim3(n * r, 1), kPolyThreads, d * 4>>>(
-          dv.get<uint64_t>(), 0, 0, n, vmask, dV.get<uint32_t>(), c);
+          dv.get<uint64_t>(), 0, 0, n, vmask, dV.get<uint32_t>(), d, c);
       st = SetSmem(inner_product_finish_kernel<uint64_t>, static_cast<size_t>(r) * d * 4);
       if (st.ok())
         inner_product_finish_kernel<uint64_t><<<1, kPolyThreads, r * d * 4>>>(
@@ -1065,14 +1444,14 @@ int inspire_external_product(const inspire_pir_params* params,
   auto run = [&](auto tag) -> Status {
     using T = decltype(tag);
     ntt_coeffs_kernel<T><<<dim3(ng * r, 1), kPolyThreads, d * 4>>>(
-        dra.get<T>(), 0, 0, ng, static_cast<T>(vmask), dA.get<uint32_t>(), c);
+        dra.get<T>(), 0, 0, ng, static_cast<T>(vmask), dA.get<uint32_t>(), d, c);
     ntt_coeffs_kernel<T><<<dim3(ng * r, 1), kPolyThreads, d * 4>>>(
-        drb.get<T>(), 0, 0, ng, static_cast<T>(vmask), dB.get<uint32_t>(), c);
+        drb.get<T>(), 0, 0, ng, static_cast<T>(vmask), dB.get<uint32_t>(), d, c);
     const size_t smem = static_cast<size_t>(d) * 4 + 2ull * d * sizeof(T);
     RETURN_IF_ERROR(SetSmem(ext_step_kernel<T>, smem));
     ext_step_kernel<T><<<dim3(r, 1, 1), kPolyThreads, smem>>>(
-        true, nullptr, dres.get<uint32_t>(), dca.get<T>(), 0, dcb.get<T>(), 0, 0,
-        dA.get<uint32_t>(), dB.get<uint32_t>(), e, c);
+        true, nullptr, dres.get<uint32_t>(), dca.get<T>(), 0, 0, dcb.get<T>(), 0, 0,
+        dA.get<uint32_t>(), 0, dB.get<uint32_t>(), e, c);
     finish_kernel<T><<<dim3(1, 1), kPolyThreads>>>(
         true, dres.get<uint32_t>(), nullptr, 0, nullptr, 0, 0, false, 0, 0, 0,
         dout.get<T>(), c);
@@ -1135,7 +1514,7 @@ int inspire_finalize_matrix_pack(const inspire_pir_params* params,
     ntt_signed_kernel<<<k * r, kPolyThreads, d * 4>>>(dth.get<int64_t>(), k,
                                                       dTh.get<uint32_t>(), c);
     ntt_coeffs_kernel<T><<<dim3(k * r, 1), kPolyThreads, d * 4>>>(
-        dy.get<T>(), 0, 0, k, static_cast<T>(vmask), dYh.get<uint32_t>(), c);
+        dy.get<T>(), 0, 0, k, static_cast<T>(vmask), dYh.get<uint32_t>(), d, c);
     const size_t smem = static_cast<size_t>(r) * d * 4;
     RETURN_IF_ERROR(SetSmem(finalize_kernel<T>, smem));
     finalize_kernel<T><<<dim3(1, 1), kPolyThreads, smem>>>(

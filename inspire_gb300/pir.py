@@ -320,6 +320,35 @@ class PirServer:
             err, len(err))
         _check(rc, err)
 
+    def pack_device(self, batch, first_dim_ptr, first_dim_len,
+                    packing_key_ptr, packing_key_count, out_ptr,
+                    engine=ENGINE_PLAIN, stream=0):
+        """Packing step of a device batch (products + FinalizeMatrixPack per
+        shard, no EvalPoly or modulus switch): out is batch x l*t x 2 x d."""
+        err = _errbuf()
+        rc = _lib.load().inspire_pir_pack_batch_device(
+            self._h, batch, ctypes.c_void_p(first_dim_ptr), first_dim_len,
+            ctypes.c_void_p(packing_key_ptr), packing_key_count,
+            ctypes.c_void_p(out_ptr), engine, ctypes.c_void_p(stream), err,
+            len(err))
+        _check(rc, err)
+
+    def external_product_device(self, batch, ct_ptr, rgsw_ptr, out_ptr,
+                                stream=0):
+        """ExternalProduct of `batch` ciphertexts (batch x 2 x d) with their
+        own RGSW ciphertexts (batch x 2ne x 2 x d) under the eval gadget."""
+        err = _errbuf()
+        rc = _lib.load().inspire_pir_external_product_device(
+            self._h, batch, ctypes.c_void_p(ct_ptr), ctypes.c_void_p(rgsw_ptr),
+            ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream), err, len(err))
+        _check(rc, err)
+
+    def check(self):
+        """Raises if a tensor-engine launch recorded a pipeline timeout."""
+        err = _errbuf()
+        _check(_lib.load().inspire_pir_server_check(self._h, err, len(err)),
+               err)
+
     def _timings(self):
         a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
         _lib.load().inspire_pir_server_timings(self._h, ctypes.byref(a),
@@ -335,6 +364,52 @@ class PirServer:
 
     def GetPolyEvalTime(self):
         return self._timings()[2]
+
+
+class Graph:
+    """A CUDA graph of device entry points (inspire_graph_*).
+
+        with Graph(stream) as g:       # records, does not run
+            srv.process_device(..., stream=stream)
+        g.launch(stream)               # replays as one launch
+
+    Make each recorded call once before capturing, with the same batch
+    sizes (that allocates the workspaces); a replay must not overlap other
+    calls on the same server.
+    """
+
+    def __init__(self, stream):
+        self.stream = stream
+        self._g = None
+
+    def __enter__(self):
+        err = _errbuf()
+        _check(_lib.load().inspire_graph_begin(ctypes.c_void_p(self.stream),
+                                               err, len(err)), err)
+        return self
+
+    def __exit__(self, exc_type, exc, tb):
+        err = _errbuf()
+        g = ctypes.c_void_p()
+        rc = _lib.load().inspire_graph_end(ctypes.c_void_p(self.stream),
+                                           ctypes.byref(g), err, len(err))
+        if exc_type is None:
+            _check(rc, err)
+            self._g = g
+        elif g.value:
+            _lib.load().inspire_graph_destroy(g)
+        return False
+
+    def launch(self, stream=None):
+        err = _errbuf()
+        s = self.stream if stream is None else stream
+        _check(_lib.load().inspire_graph_launch(self._g, ctypes.c_void_p(s),
+                                                err, len(err)), err)
+
+    def __del__(self):
+        if getattr(self, "_g", None) is not None and _lib._lib is not None:
+            _lib._lib.inspire_graph_destroy(self._g)
+            self._g = None
 
 
 # ---------------------------------------------------------------------------

@@ -275,6 +275,30 @@ def test_server_short_first_dimension_is_zero_padded():
     _server_case(params, np.uint16, np.int32, seed=91, batch=1, pad_to=96)
 
 
+@pytest.mark.parametrize("engine", [pir.ENGINE_PLAIN, pir.ENGINE_TENSOR])
+def test_device_call_short_first_dimension(engine):
+    # Device-pointer call with n/t < DB columns: the padding is zeroed on the
+    # device, the response equals the host call's.
+    import torch
+    params = synthetic.make_params(d=128, n=2 * 4000, t=2, coeff_bits=32)
+    mat = synthetic.make_material(params, seed=5, pad_to=256)
+    srv = pir.PirServer.CreateCombined(params, mat.db, mat.pack,
+                                       mat.a_tilde_agg, mat.t_vec_h,
+                                       mat.second_dim_a)
+    fd, sd, pk = synthetic.make_requests(params, 5, seed=6)
+    assert fd.shape[1] == 4000 and mat.db.shape[1] == 4096
+    want = srv.process_arrays(fd, sd, pk, pir.ENGINE_PLAIN)
+    dev = torch.device("cuda", 0)
+    t_fd, t_sd, t_pk = (torch.from_numpy(x.view(np.int32)).to(dev)
+                        for x in (fd, sd, pk))
+    out = torch.zeros((5, 1, 2, 128), dtype=torch.int32, device=dev)
+    srv.process_device(5, t_fd.data_ptr(), 4000, t_sd.data_ptr(), sd.shape[1],
+                       t_pk.data_ptr(), pk.shape[1], out.data_ptr(), engine,
+                       torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), want)
+
+
 def test_server_request_validation():
     params = synthetic.make_params(d=64, n=1024, t=2, coeff_bits=32)
     mat = synthetic.make_material(params, seed=3)

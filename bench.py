@@ -213,6 +213,89 @@ def cpu_baseline_sample(params, db, pack, a_tilde, t_vec_h, sda, fd, sd, pk,
                       "(oracle, FP64 FFT path)" % (done[0], el, threads)}
 
 
+def run_pack_workload(args):
+    """The packing micro-workload: 256 instances of packing d = 2048 LWE
+    ciphertexts into one RLWE ciphertext (t = 1: DB and pack products, then
+    FinalizeMatrixPack; pir_packing_metrics_tool.cc:226-283) followed by one
+    ExternalProduct (eval gadget 19 x 3) of each packed ciphertext with its
+    own RGSW ciphertext, replayed as one CUDA graph per step."""
+    import torch
+    from inspire_gb300 import build, pir, synthetic
+    build.build()
+    d, B = 2048, args.batch
+    params = synthetic.make_params(d=d, n=2048, t=1, coeff_bits=COEFF_BITS)
+    mat = synthetic.make_material(params, seed=31)
+    srv = pir.PirServer.CreateCombined(params, mat.db, mat.pack,
+                                       mat.a_tilde_agg, mat.t_vec_h,
+                                       mat.second_dim_a)
+    fd, _, pk = synthetic.make_requests(params, B, seed=32)
+    ne = params.eval_gadget.num_digits
+    rgsw = synthetic.parallel_integers((B, 2 * ne, 2, d), 0, 1 << 32,
+                                       np.uint64, 33).astype(np.uint32)
+    dev = torch.device("cuda", 0)
+    t_fd = torch.from_numpy(fd.view(np.int32)).to(dev)
+    t_pk = torch.from_numpy(pk.view(np.int32)).to(dev)
+    t_rg = torch.from_numpy(rgsw.view(np.int32)).to(dev)
+    packed = torch.zeros((B, 1, 2, d), dtype=torch.int32, device=dev)
+    ext = torch.zeros((B, 2, d), dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    engine = pir.ENGINE_TENSOR
+
+    def step(eng):
+        srv.pack_device(B, t_fd.data_ptr(), fd.shape[1], t_pk.data_ptr(),
+                        pk.shape[1], packed.data_ptr(), eng, sp)
+        srv.external_product_device(B, packed.data_ptr(), t_rg.data_ptr(),
+                                    ext.data_ptr(), sp)
+    try:
+        step(engine)
+    except pir.InspireError:
+        engine = pir.ENGINE_PLAIN
+        step(engine)
+    stream.synchronize()
+    ref = ext.clone()
+    step(pir.ENGINE_PLAIN)
+    stream.synchronize()
+    if not torch.equal(ref, ext):
+        raise SystemExit("engine outputs differ")
+    step(engine)
+    stream.synchronize()
+    with pir.Graph(sp) as g:
+        step(engine)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+    with ClockSampler(0) as clk:
+        ms_graph = timed(lambda: g.launch(sp))
+    ms_eager = timed(lambda: step(engine))
+    srv.check()
+    line = {
+        "metric": "packed RLWE ciphertexts/s (d=2048 LWEs -> 1 RLWE, "
+                  "pack 19x2, + ExternalProduct 19x3), bit-exact",
+        "value": B / (ms_graph / 1000.0), "unit": "instances/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_graph, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded uniform pack matrix, keys, RGSW)",
+        "config": {"workload": "pack_d2048_b%d_graph" % B, "d": d,
+                   "instances": B, "engine": "tensor" if engine else "plain",
+                   "l2": "working set fits L2 (40 MiB of matrices)"},
+        "eager_ms_per_step": ms_eager,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -222,7 +305,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=10)
+    ap.add_argument("--workload", default="answer", choices=["answer", "pack"],
+                    help="answer: the online answer (default); pack: the "
+                         "packing micro-workload")
     args = ap.parse_args()
+    if args.workload == "pack" and args.impl == "ours":
+        run_pack_workload(args)
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

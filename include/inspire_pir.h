@@ -7,7 +7,8 @@
  *
  * Every function returns an int status: 0 on success, otherwise the
  * absl::StatusCode the reference would return (3 INVALID_ARGUMENT,
- * 9 FAILED_PRECONDITION, 13 INTERNAL, 8 RESOURCE_EXHAUSTED) with the
+ * 4 DEADLINE_EXCEEDED, 8 RESOURCE_EXHAUSTED, 9 FAILED_PRECONDITION,
+ * 13 INTERNAL) with the
  * reference's message text copied into `err` (NUL-terminated, truncated to
  * err_len). `err` may be NULL.
  *
@@ -32,6 +33,7 @@ extern "C" {
 
 #define INSPIRE_OK 0
 #define INSPIRE_INVALID_ARGUMENT 3
+#define INSPIRE_DEADLINE_EXCEEDED 4
 #define INSPIRE_RESOURCE_EXHAUSTED 8
 #define INSPIRE_FAILED_PRECONDITION 9
 #define INSPIRE_INTERNAL 13
@@ -128,8 +130,9 @@ int inspire_pir_process_batch(inspire_pir_server* server, int32_t batch,
 /*
  * Device-resident form of inspire_pir_process_batch: all pointers are CUDA
  * device pointers and the work is enqueued on `stream` (a cudaStream_t, or
- * NULL for the legacy default stream) without synchronising. first_dim must
- * hold db_cols words per request (zero-padded past first_dim_len).
+ * NULL for the legacy default stream) without synchronising. first_dim holds
+ * first_dim_len words per request; when that is below db_cols the library
+ * copies the batch into its workspace and zero-pads it there.
  */
 int inspire_pir_process_batch_device(inspire_pir_server* server,
                                      int32_t batch, const void* first_dim,
@@ -246,6 +249,80 @@ int inspire_pir_workspace_poll(inspire_pir_workspace* ws);
 /* Blocks until the last submitted batch has finished; its status. */
 int inspire_pir_workspace_wait(inspire_pir_workspace* ws, char* err,
                                size_t err_len);
+
+/*
+ * Continuous batching (no reference counterpart: the reference answers one
+ * request per ProcessResponse call). One engine serves several servers
+ * ("queues", which may differ in ring degree, interpolation degree and entry
+ * size multiple). Each queue owns a ring of `ring_slots` request slots in
+ * pinned host memory; a scheduler thread batches the submitted slots of a
+ * queue in ring order (up to max_batch per batch) onto the queue's in-flight
+ * workspaces as soon as one is free, so batches of all queues overlap on the
+ * device. Workspaces per queue: hbm_budget / n_servers / the workspace bytes
+ * of max_batch requests, between 1 and max_workspaces. Batches of more than
+ * plain_max_batch requests use the tensor engine when the server has it.
+ * Every response is the one inspire_pir_process_response gives for the same
+ * request.
+ *
+ * A caller: inspire_serving_acquire (a slot: pointers to its first_dim
+ * (db_cols words), second_dim (2*ne*d), packing_key (2*k*d) and response
+ * (l*2*d) areas) -> writes the request -> inspire_serving_submit (with the
+ * first dimension's length; the rest of the slot's first_dim is zeroed;
+ * ProcessResponse's checks and messages) -> inspire_serving_wait -> reads
+ * the response -> inspire_serving_release. A slot is written by its caller
+ * only between acquire and submit. Destroy the engine after the last wait
+ * has returned; requests still queued then are dropped.
+ */
+typedef struct inspire_serving inspire_serving;
+
+typedef struct inspire_serving_stats {
+  int64_t requests;        /* completed since the last reset */
+  int64_t failed;
+  int64_t batches;
+  int64_t tensor_batches;
+  double mean_batch;
+  double p50_ms;           /* submit -> completion, over completed requests */
+  double p99_ms;
+  double max_ms;
+  int32_t max_inflight;    /* batches on the device at once, all queues */
+  int32_t reserved;
+} inspire_serving_stats;
+
+int inspire_serving_create(inspire_pir_server* const* servers,
+                           int32_t n_servers, int32_t max_batch,
+                           int32_t plain_max_batch, int32_t ring_slots,
+                           int64_t hbm_budget, int32_t max_workspaces,
+                           inspire_serving** out, char* err, size_t err_len);
+/* The same scheduler over a host-only loopback device (for tests on machines
+ * without a GPU): queue q has slots of slot_words[4q..4q+3] u32 words
+ * (first_dim, second_dim, packing_key, response); response word k is
+ * first_dim[0] * 7 + q + k, ready delay_us after the batch launches; a
+ * request whose first word is 0xDEAD fails its batch. */
+int inspire_serving_create_loopback(int32_t n_queues, const int64_t* slot_words,
+                                    int32_t workspaces, int32_t delay_us,
+                                    int32_t max_batch, int32_t plain_max_batch,
+                                    int32_t ring_slots, inspire_serving** out,
+                                    char* err, size_t err_len);
+void inspire_serving_destroy(inspire_serving* engine);
+/* Blocks up to timeout_ms for a free slot (RESOURCE_EXHAUSTED after). */
+int inspire_serving_acquire(inspire_serving* engine, int32_t queue,
+                            int32_t timeout_ms, int64_t* ticket,
+                            void** first_dim, void** second_dim,
+                            void** packing_key, void** response, char* err,
+                            size_t err_len);
+int inspire_serving_submit(inspire_serving* engine, int64_t ticket,
+                           int64_t first_dim_len, char* err, size_t err_len);
+/* 0 when the response is in the slot; the request's error status otherwise;
+ * DEADLINE_EXCEEDED if still running after timeout_ms. */
+int inspire_serving_wait(inspire_serving* engine, int64_t ticket,
+                         int32_t timeout_ms, char* err, size_t err_len);
+int inspire_serving_release(inspire_serving* engine, int64_t ticket);
+int inspire_serving_get_stats(inspire_serving* engine,
+                               inspire_serving_stats* out);
+int inspire_serving_reset_stats(inspire_serving* engine);
+int inspire_serving_queue_info(inspire_serving* engine, int32_t queue,
+                               int32_t* workspaces, int64_t* workspace_bytes,
+                               int32_t* ring_slots);
 
 /* Server geometry: rows = l*t*d, and the column counts of both matrices. */
 int inspire_pir_server_shape(const inspire_pir_server* server, int64_t* rows,

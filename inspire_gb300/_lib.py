@@ -41,6 +41,19 @@ SIGNATURES = {
     "inspire_graph_launch": ([_vp, _vp, _cp, _sz], ctypes.c_int),
     "inspire_graph_destroy": ([_vp], None),
     "inspire_pir_server_check": ([_vp, _cp, _sz], ctypes.c_int),
+    "inspire_serving_create": (
+        [_vp, _i32, _i32, _i32, _i32, _i64, _i32, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_serving_create_loopback": (
+        [_i32, _vp, _i32, _i32, _i32, _i32, _i32, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_serving_destroy": ([_vp], None),
+    "inspire_serving_acquire": (
+        [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_serving_submit": ([_vp, _i64, _i64, _cp, _sz], ctypes.c_int),
+    "inspire_serving_wait": ([_vp, _i64, _i32, _cp, _sz], ctypes.c_int),
+    "inspire_serving_release": ([_vp, _i64], ctypes.c_int),
+    "inspire_serving_get_stats": ([_vp, _vp], ctypes.c_int),
+    "inspire_serving_reset_stats": ([_vp], ctypes.c_int),
+    "inspire_serving_queue_info": ([_vp, _i32, _vp, _vp, _vp], ctypes.c_int),
     "inspire_pir_workspace_bytes": ([_vp, _i32], ctypes.c_int64),
     "inspire_pir_workspace_create": ([_vp, _i32, _vp, _cp, _sz], ctypes.c_int),
     "inspire_pir_workspace_destroy": ([_vp], None),

@@ -7,28 +7,33 @@
 // batch of B requests turns the two GEMVs into one GEMM:
 //   out[q][r] = sum_c DB[r][c] * q1[q][c] + sum_j P[r][j] * y_g[q][j]  mod 2^32
 //
-// Exactness with fp16 operands and fp32 accumulators. Every matrix entry is
-// split into unsigned bytes (the u16 DB into x0 + 2^8 x1, the pack matrix as
-// its u32 two's complement into p0..p3) and every query word into four bytes
-// y0..y3; bytes are exact fp16 values. Only byte pairs whose weight 2^(8s),
-// s = i + j, is below 2^32 matter. The accumulator of a CTA holds four
-// blocks of 64 fp32 columns, block s collecting every pair of weight 2^(8s):
+// Exactness with fp16 operands and fp32 accumulators. Every operand is split
+// into balanced base-256 digits, exact fp16 values:
+//   * a query word q (mod 2^32) into y0..y3 in [-128, 127], with
+//     q = y0 + 2^8 y1 + 2^16 y2 + 2^24 y3 mod 2^32 (the top carry drops);
+//   * a pack entry (its u32 two's complement, mod 2^32) into p0..p3 likewise;
+//   * a DB entry x in [0, 2^16) as x - 2^15 = x0 + 2^8 x1 with x0 in
+//     [-128, 127], x1 in [-128, 128]; the offset comes back as
+//     2^15 * sum_c q1[c], one word per request added in the epilogue.
+// Only digit pairs whose weight 2^(8s), s = i + j, is below 2^32 matter. The
+// accumulator of a CTA holds four blocks of 64 fp32 columns, block s
+// collecting every pair of weight 2^(8s):
 //   MMA(X0, [Y0 Y1 Y2 Y3]) -> blocks 0..3,  MMA(X1, [Y0 Y1 Y2]) -> blocks 1..3
-// so each accumulator element receives at most two byte products per K
-// index. A unit of K = 64 therefore sums at most 64 * 2 * 255^2 = 8,323,200
-// < 2^23: every partial sum is an exact fp32 integer, and the epilogue decodes
-// it exactly as bits(v + 2^23) - 0x4B000000 before adding it, shifted by 8s,
-// into a u32 register accumulator. The pack matrix runs as two units per K
-// block (p0,p1 like the DB; then p2 -> blocks 2..3 and p3 -> block 3).
+// so each accumulator element receives at most two digit products per K
+// index, each of magnitude <= 128 * 128 = 2^14. A unit of K = 128 therefore
+// keeps every partial sum v in [-2^22, 2^22]: exact fp32 integers, decoded
+// exactly as bits(v + 1.5 * 2^23) - 0x4B400000 (v + 1.5 * 2^23 lies in
+// [2^23, 2^24], where consecutive integers are consecutive encodings) before
+// being added, shifted by 8s, into a u32 register accumulator. Signed digits
+// halve the decode work per MAC against unsigned bytes, whose K = 64 units
+// already reach 2^23. The pack matrix runs as two units per K block (p0,p1
+// like the DB; then p2 -> blocks 2..3 and p3 -> block 3).
 //
-// Kernel structure. Moving operand tiles from L2 into shared memory, not the
-// tensor pipe, limits this GEMM (a K=64 unit of one 128-row block moves
-// 64 KB of fp16 limbs for 3.7 M MACs), so each CTA covers two 128-row blocks
-// that share one 64-request tile, which raises the MACs per byte moved by
-// a third. 12 warps:
+// Kernel structure. Each CTA covers two 128-row blocks that share one
+// 64-request tile (fewer operand bytes moved from L2 per MAC). 12 warps:
 //   warp 0     TMA producer: 4-stage ring of 48 KB (per stage, K = 32: four
-//              128x32 A tiles and a 4 x 64x32 tile of request bytes,
-//              64-byte swizzled); two stages make one exact K=64 unit
+//              128x32 A tiles and a 4 x 64x32 tile of request digits,
+//              64-byte swizzled); four stages make one exact K=128 unit
 //   warp 1     MMA issuer: one thread issues tcgen05.mma (M=128, K=16,
 //              N=256/192 or 128/64) for row block 0 into TMEM columns
 //              0..255, commits, then row block 1 into columns 256..511, so
@@ -62,7 +67,8 @@ constexpr int kRowBlocks = 2;      // row blocks per CTA sharing a request tile
 constexpr int kTileRows = kBlockRows * kRowBlocks;
 constexpr int kTileQ = 64;         // requests per CTA
 constexpr int kStageK = 32;        // K per pipeline stage (64-byte rows)
-constexpr int kUnitK = 64;         // K per exact accumulation unit
+constexpr int kUnitK = 128;        // K per exact accumulation unit
+constexpr int kStagesPerUnit = kUnitK / kStageK;
 constexpr int kStages = 4;
 constexpr int kATileBytes = kBlockRows * kStageK * 2;      // 8 KB
 constexpr int kBLimbBytes = kTileQ * kStageK * 2;          // 4 KB
@@ -218,8 +224,8 @@ __host__ __device__ constexpr uint32_t instr_desc(int n, int m) {
 
 struct LimbArgs {
   int rows;          // R (multiple of 256)
-  int n_db_units;    // DB columns / 64
-  int n_pk_blocks;   // pack columns / 64
+  int n_db_units;    // DB columns / kUnitK
+  int n_pk_blocks;   // pack columns / kUnitK
   int qcap;          // request rows per byte plane in the request maps
   int batch;         // valid requests
   int ksplit;        // CTAs sharing one (row pair, request tile)
@@ -261,6 +267,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
                  const __grid_constant__ CUtensorMap tm_pk,
                  const __grid_constant__ CUtensorMap tm_q,
                  const __grid_constant__ CUtensorMap tm_y, LimbArgs a,
+                 const uint32_t* __restrict__ qsum,
                  uint32_t* __restrict__ out, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
@@ -315,8 +322,8 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       const CUtensorMap* am = kind == 0 ? &tm_db : &tm_pk;
       const CUtensorMap* bm = kind == 0 ? &tm_q : &tm_y;
       const int plane0 = kind == 2 ? 2 : 0;
-      for (int h = 0; h < kUnitK / kStageK; ++h) {
-        const int g = 2 * i + h;
+      for (int h = 0; h < kStagesPerUnit; ++h) {
+        const int g = kStagesPerUnit * i + h;
         const int s = g % kStages;
         if (!mbar_wait(&empty[s], ((g / kStages) & 1) ^ 1, err)) {
           ok = false;
@@ -355,8 +362,8 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
         }
         tc_fence_after();
         const uint32_t d = tmem + rb * 256;
-        for (int h = 0; h < kUnitK / kStageK; ++h) {
-          const int g = 2 * i + h;
+        for (int h = 0; h < kStagesPerUnit; ++h) {
+          const int g = kStagesPerUnit * i + h;
           const int s = g % kStages;
           if (rb == 0 && !mbar_wait(&full[s], (g / kStages) & 1, err)) {
             ok = false;
@@ -401,9 +408,9 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
         tmem_wait_ld();
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
-          acc[j] += __float_as_uint(__uint_as_float(v0[j]) + 8388608.0f)
+          acc[j] += __float_as_uint(__uint_as_float(v0[j]) + 12582912.0f)
                     << (8 * sblk);
-          acc[32 + j] += __float_as_uint(__uint_as_float(v1[j]) + 8388608.0f)
+          acc[32 + j] += __float_as_uint(__uint_as_float(v1[j]) + 12582912.0f)
                          << (8 * sblk);
         }
       }
@@ -412,9 +419,9 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       if (lane == 0) mbar_arrive(&acc_empty[e]);
     }
     if (ok && *reinterpret_cast<volatile int*>(err) == 0) {
-      // Every decoded value carried 0x4B000000 (the bits of 2^23), shifted
-      // by its block weight: remove them all at once, mod 2^32.
-      const uint32_t m = 0x4B000000u;
+      // Every decoded value carried 0x4B400000 (the bits of 1.5 * 2^23),
+      // shifted by its block weight: remove them all at once, mod 2^32.
+      const uint32_t m = 0x4B400000u;
       const uint32_t corr = n01 * m + n01 * (m << 8) + n23 * (m << 16) +
                             n23 * (m << 24);
       const int row = row0 + e * kBlockRows + ew * 32 + lane;
@@ -423,10 +430,12 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
         const int q = q0 + j;
         if (q < a.batch) {
           uint32_t* o = out + q * a.out_stride + row;
+          // The DB offset 2^15 * sum_c q1[c], once per output word.
+          const uint32_t v = acc[j] - corr + (ks == 0 ? __ldg(qsum + q) << 15 : 0u);
           if (a.ksplit == 1) {
-            *o = acc[j] - corr;
+            *o = v;
           } else {
-            atomicAdd(o, acc[j] - corr);
+            atomicAdd(o, v);
           }
         }
       }
@@ -438,7 +447,9 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   if (warp == 2) tmem_dealloc(tmem, kTmemCols);
 }
 
-// Byte planes of a u16 matrix: [2][rows][cols_pad] fp16, zero past cols.
+// Digit planes of a u16 matrix: x - 2^15 = x0 + 2^8 x1 (x0 in [-128, 127],
+// x1 in [-128, 128]) as [2][rows][cols_pad] fp16; zero past cols (padding
+// columns meet zero query words, so their value does not matter).
 __global__ void split_u16_kernel(const uint16_t* __restrict__ src,
                                  int64_t rows, int64_t cols,
                                  int64_t cols_pad, __half* __restrict__ dst) {
@@ -446,15 +457,37 @@ __global__ void split_u16_kernel(const uint16_t* __restrict__ src,
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
        i < total; i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     const int64_t r = i / cols_pad, c = i % cols_pad;
-    const uint32_t x = c < cols ? src[r * cols + c] : 0u;
-    dst[i] = __uint2half_rn(x & 255u);
-    dst[total + i] = __uint2half_rn(x >> 8);
+    const int v = c < cols ? static_cast<int>(src[r * cols + c]) - 32768 : 0;
+    const int x0 = ((v + 128) & 255) - 128;
+    const int x1 = (v - x0) / 256;
+    dst[i] = __int2half_rn(x0);
+    dst[total + i] = __int2half_rn(x1);
   }
 }
 
-// Byte planes of the u32 two's complement of a matrix of `kind`: plane j
-// holds rows_pad x cols_pad fp16 (zero outside rows x cols) and starts at
-// row j * plane_rows.
+// sum_c q1[q][c] mod 2^32 per request (the DB offset term). One CTA per
+// request; blockDim.x = 256.
+__global__ void row_sum_kernel(const uint32_t* __restrict__ q1, int64_t cols,
+                               int64_t stride, uint32_t* __restrict__ sum) {
+  __shared__ uint32_t part[8];
+  const uint32_t* row = q1 + blockIdx.x * stride;
+  uint32_t s = 0;
+  for (int64_t c = threadIdx.x; c < cols; c += blockDim.x) s += row[c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < 8; ++w) t += part[w];
+    sum[blockIdx.x] = t;
+  }
+}
+
+// Balanced base-256 digit planes (each in [-128, 127], the top carry
+// dropped: mod 2^32) of the u32 two's complement of a matrix of `kind`:
+// plane j holds rows_pad x cols_pad fp16 (zero outside rows x cols) and
+// starts at row j * plane_rows.
 __global__ void split_u32_kernel(const void* __restrict__ src, int kind,
                                  int64_t rows, int64_t cols, int64_t stride,
                                  int64_t rows_pad, int64_t plane_rows,
@@ -474,9 +507,13 @@ __global__ void split_u32_kernel(const void* __restrict__ src, int kind,
         default: x = static_cast<const uint32_t*>(src)[o]; break;
       }
     }
+    int carry = 0;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      dst[j * plane + i] = __uint2half_rn((x >> (8 * j)) & 255u);
+      int b = static_cast<int>((x >> (8 * j)) & 255u) + carry;
+      carry = b >= 128 ? 1 : 0;
+      b -= carry << 8;
+      dst[j * plane + i] = __int2half_rn(b);
     }
   }
 }
@@ -520,10 +557,12 @@ class LimbScratchImpl : public LimbScratch {
   ~LimbScratchImpl() override {
     if (q_planes) cudaFree(q_planes);
     if (y_planes) cudaFree(y_planes);
+    if (qsum) cudaFree(qsum);
   }
   int64_t qcap = 0;
   __half* q_planes = nullptr;
   __half* y_planes = nullptr;
+  uint32_t* qsum = nullptr;  // sum_c q1[q][c] per request
   CUtensorMap tm_q{}, tm_y{};
 };
 
@@ -569,7 +608,11 @@ class LimbGemmImpl : public LimbGemm {
 
   int64_t ScratchBytes(int batch) const override {
     const int64_t need = round_up(batch, kTileQ);
-    return 4 * need * (cpad_ + kpad_) * 2;
+    return 4 * need * (cpad_ + kpad_) * 2 + 4 * need;
+  }
+
+  cudaError_t Reserve(LimbScratch* scratch, int batch) override {
+    return EnsureQueries(static_cast<LimbScratchImpl*>(scratch), batch);
   }
 
   cudaError_t EnsureQueries(LimbScratchImpl* sc, int batch) {
@@ -577,11 +620,15 @@ class LimbGemmImpl : public LimbGemm {
     if (need <= sc->qcap) return cudaSuccess;
     if (sc->q_planes) cudaFree(sc->q_planes);
     if (sc->y_planes) cudaFree(sc->y_planes);
+    if (sc->qsum) cudaFree(sc->qsum);
     sc->q_planes = sc->y_planes = nullptr;
+    sc->qsum = nullptr;
     sc->qcap = 0;
     cudaError_t e = cudaMalloc(&sc->q_planes, 4ull * need * cpad_ * 2);
     if (e != cudaSuccess) return e;
     e = cudaMalloc(&sc->y_planes, 4ull * need * kpad_ * 2);
+    if (e != cudaSuccess) return e;
+    e = cudaMalloc(&sc->qsum, 4ull * need);
     if (e != cudaSuccess) return e;
     if (!make_map(&sc->tm_q, sc->q_planes, 4ull * need, cpad_, kTileQ) ||
         !make_map(&sc->tm_y, sc->y_planes, 4ull * need, kpad_, kTileQ)) {
@@ -604,6 +651,8 @@ class LimbGemmImpl : public LimbGemm {
                                               bpad, sc->qcap, cpad_, sc->q_planes);
     split_u32_kernel<<<152 * 8, 256, 0, st>>>(yg, kU32, batch, pk_cols_, yg_stride,
                                               bpad, sc->qcap, kpad_, sc->y_planes);
+    row_sum_kernel<<<batch, 256, 0, st>>>(static_cast<const uint32_t*>(q1), db_cols_,
+                                         q1_stride, sc->qsum);
     LimbArgs a;
     a.rows = static_cast<int>(rows_);
     a.n_db_units = static_cast<int>(cpad_ / kUnitK);
@@ -620,7 +669,8 @@ class LimbGemmImpl : public LimbGemm {
     }
     const unsigned grid = static_cast<unsigned>(tiles * a.ksplit);
     limb_gemm_kernel<<<grid, kThreads, kSmemBytes, st>>>(
-        tm_db_, tm_pk_, sc->tm_q, sc->tm_y, a, static_cast<uint32_t*>(out), err_);
+        tm_db_, tm_pk_, sc->tm_q, sc->tm_y, a, sc->qsum, static_cast<uint32_t*>(out),
+        err_);
     return cudaGetLastError();
   }
 

@@ -26,6 +26,9 @@ class LimbGemm {
   virtual std::unique_ptr<LimbScratch> NewScratch() = 0;
   // Device bytes the scratch for `batch` requests holds.
   virtual int64_t ScratchBytes(int batch) const = 0;
+  // Allocates the scratch for up to `batch` requests now (Run allocates on
+  // first use otherwise).
+  virtual cudaError_t Reserve(LimbScratch* scratch, int batch) = 0;
   // out[q][r] = db[r] . q1[q] + pack[r] . yg[q]  (mod 2^w), q < batch.
   virtual cudaError_t Run(int batch, const void* q1, int64_t q1_stride,
                           const void* yg, int64_t yg_stride, void* out,

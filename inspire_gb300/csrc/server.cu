@@ -28,6 +28,7 @@
 #include "limb_gemm.h"
 #include "ntt.cuh"
 #include "poly_kernels.cuh"
+#include "server_api.h"
 
 namespace inspire {
 namespace {
@@ -911,6 +912,118 @@ Status CreateServer(const inspire_pir_params* prm, const void* db,
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// Interface for the native serving loop (server_api.h).
+// ---------------------------------------------------------------------------
+ServerGeometry GetGeometry(const inspire_pir_server* s) {
+  ServerGeometry g;
+  g.db_cols = s->db_cols;
+  g.interpolated_rows = s->interpolated_rows;
+  g.d = s->d;
+  g.l = s->l;
+  g.nsd = s->t > 1 ? 2 * s->ne : 0;
+  g.npk = 2 * s->k;
+  g.word_bytes = static_cast<int>(Words(s->prm.coeff_bits));
+  g.tensor = s->limb != nullptr;
+  return g;
+}
+
+int64_t BatchWorkspaceBytes(const inspire_pir_server* s, int max_batch) {
+  return WorkspaceBytes(s, max_batch);
+}
+
+int NewBatchWorkspace(inspire_pir_server* s, int max_batch, Workspace** out,
+                      std::string* err) {
+  *out = nullptr;
+  std::unique_ptr<Workspace> w(new Workspace());
+  Status st = InitWorkspace(w.get());
+  if (st.ok()) st = EnsureWorkspace(s, w.get(), max_batch);
+  if (st.ok() && w->limb) {
+    st = Cuda(s->limb->Reserve(w->limb.get(), max_batch), "tensor engine scratch");
+  }
+  if (!st.ok()) {
+    *err = st.msg;
+    return st.code;
+  }
+  *out = w.release();
+  return INSPIRE_OK;
+}
+
+void DeleteBatchWorkspace(Workspace* w) {
+  if (w == nullptr) return;
+  cudaStreamSynchronize(w->stream);
+  delete w;
+}
+
+int ValidateFirstDim(const inspire_pir_server* s, int64_t first_dim_len,
+                     std::string* err) {
+  Status st = ValidateRequest(s, first_dim_len, 2 * s->ne, 2 * s->k);
+  if (!st.ok()) *err = st.msg;
+  return st.code;
+}
+
+int LaunchBatch(inspire_pir_server* s, Workspace* w, const RequestSegment* segs,
+                int nseg, int engine, std::string* err) {
+  const size_t cw = Words(s->prm.coeff_bits);
+  const size_t d = s->d;
+  const size_t fd = s->db_cols * cw, sd = 2 * s->ne * d * cw,
+               pk = 2 * s->k * d * cw, rs = 2 * s->l * d * cw;
+  const cudaStream_t st = w->stream;
+  int batch = 0;
+  Status status;
+  auto copy = [&](void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+    if (status.ok() && bytes > 0) {
+      status = Cuda(cudaMemcpyAsync(dst, src, bytes, kind, st), "request copy");
+    }
+  };
+  for (int i = 0; i < nseg; ++i) {
+    const size_t n = segs[i].count;
+    copy(w->q1.get<char>() + batch * fd, segs[i].first_dim, n * fd,
+         cudaMemcpyHostToDevice);
+    if (s->t > 1) {
+      copy(w->sdim.get<char>() + batch * sd, segs[i].second_dim, n * sd,
+           cudaMemcpyHostToDevice);
+    }
+    copy(w->pkey.get<char>() + batch * pk, segs[i].packing_key, n * pk,
+         cudaMemcpyHostToDevice);
+    batch += segs[i].count;
+  }
+  if (status.ok() && (batch <= 0 || batch > w->cap)) {
+    status = Err(INSPIRE_INVALID_ARGUMENT, "batch exceeds the workspace capacity.");
+  }
+  if (status.ok()) {
+    status = AnswerOnDevice(s, w, batch, w->q1.get(), w->pkey.get(), w->sdim.get(),
+                            w->resp.get(), engine, st, false);
+  }
+  int off = 0;
+  for (int i = 0; i < nseg; ++i) {
+    copy(segs[i].responses, w->resp.get<char>() + off * rs, segs[i].count * rs,
+         cudaMemcpyDeviceToHost);
+    off += segs[i].count;
+  }
+  if (status.ok()) status = Cuda(cudaEventRecord(w->done, st), "cudaEventRecord");
+  if (!status.ok()) *err = status.msg;
+  return status.code;
+}
+
+int QueryBatch(Workspace* w) {
+  const cudaError_t e = cudaEventQuery(w->done);
+  if (e == cudaSuccess) return 1;
+  if (e == cudaErrorNotReady) return 0;
+  return -1;
+}
+
+int FinishBatch(inspire_pir_server* s, Workspace* w, int engine, std::string* err) {
+  Status st = Cuda(cudaEventSynchronize(w->done), "answer");
+  if (st.ok() && engine == INSPIRE_ENGINE_TENSOR && s->limb &&
+      s->limb->CheckError() != 0) {
+    st = Err(INSPIRE_INTERNAL, "tensor engine pipeline timed out");
+  }
+  if (!st.ok()) *err = st.msg;
+  return st.code;
+}
+
 }  // namespace inspire
 
 // ---------------------------------------------------------------------------

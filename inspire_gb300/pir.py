@@ -20,6 +20,7 @@ import numpy as np
 from . import _lib
 
 INVALID_ARGUMENT = 3
+DEADLINE_EXCEEDED = 4
 RESOURCE_EXHAUSTED = 8
 FAILED_PRECONDITION = 9
 INTERNAL = 13

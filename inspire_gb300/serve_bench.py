@@ -132,8 +132,7 @@ def main(argv=None):
                                hbm_budget=int(args.hbm_budget_gb * (1 << 30)),
                                max_workspaces=3, plain_max_batch=4) as eng:
         for frac in [float(x) for x in args.loads.split(",")]:
-            eng.latencies.clear()
-            eng.batches.clear()
+            eng.reset_stats()
             n, t_sub, t_all, results = run_load(
                 eng, pools, names, weights, frac * peak, args.seconds, rng)
             mismatches = sum(
@@ -146,12 +145,11 @@ def main(argv=None):
                 "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
                 "mean_batch": st["mean_batch"],
                 "max_inflight": st["max_inflight"],
-                "engines": sorted({"tensor" if e else "plain"
-                                   for _, _, e in eng.batches}),
+                "batches": st["batches"],
+                "tensor_batches": st["tensor_batches"],
+                "submit_s": t_sub,
                 "mismatches": mismatches})
-        ws = {nm: {"workspaces": len(db.free) + len(db.inflight),
-                   "workspace_gb": db.workspace_bytes / 1e9}
-              for nm, db in eng.dbs.items()}
+        ws = {nm: eng.queue_info(nm) for nm in names}
     line = {
         "metric": "serving p50/p99 latency and queries/s, open-loop Poisson "
                   "arrivals over two device-resident DBs, bit-exact",

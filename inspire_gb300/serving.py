@@ -1,23 +1,20 @@
-"""Continuous-batching request loop over GPU-resident PIR servers.
+"""Continuous batching over GPU-resident PIR servers (Python facade).
 
-Requests for several databases (servers of different shapes: ring degree,
-interpolation degree, entry size multiple l) arrive on any thread via
-submit(); a scheduler thread groups the pending requests of each database
-into batches and launches them on free workspaces (inspire_pir_workspace_*:
-device buffers + a CUDA stream + pinned staging). A database has several
-workspaces, so a batch is admitted as soon as a workspace frees up, while
-earlier batches are still on the GPU: their work overlaps on the device. The
-number of workspaces is set by an HBM budget (workspace bytes come from the
-library). Small batches run on the plain engine, larger ones on the
-tensor-core engine; both give identical responses.
+The request loop itself is native (inspire_gb300/csrc/serving.cu, the
+inspire_serving_* C ABI): every server is a queue with a ring of request
+slots in pinned host memory, and one scheduler thread batches submitted
+slots onto in-flight workspaces as soon as one frees up, so batches of all
+servers overlap on the GPU. The number of workspaces per server comes from
+an HBM budget; small batches use the plain engine, larger ones the tensor
+engine. Every response is identical to the one PirServer::ProcessResponse
+gives for the same request (crypto/pir/server/pir_server.cc:154-306).
 
-The reference serves one request per ProcessResponse call on one thread
-(crypto/pir/server/pir_server.cc:154-306); the loop keeps that call's
-semantics per request (same response bytes) and adds batching.
+This module adds Futures: submit() copies a request into a slot and returns
+a Future resolving to the (l, 2, d) response; a completion thread waits for
+the tickets and copies the responses out.
 """
 import ctypes
 import threading
-import time
 from collections import deque
 from concurrent.futures import Future
 
@@ -26,145 +23,102 @@ import numpy as np
 from . import _lib, pir
 
 
-class _Workspace:
-    """One in-flight batch slot of a database (wraps inspire_pir_workspace)."""
-
-    def __init__(self, db, max_batch):
-        lib = _lib.load()
-        self.db = db
-        self.max_batch = max_batch
-        h = ctypes.c_void_p()
-        err = ctypes.create_string_buffer(512)
-        rc = lib.inspire_pir_workspace_create(db.server._h, max_batch,
-                                              ctypes.byref(h), err, len(err))
-        if rc:
-            raise pir.InspireError(rc, err.value.decode())
-        self.h = h
-        ptrs = [ctypes.c_void_p() for _ in range(4)]
-        lib.inspire_pir_workspace_host_buffers(h, *[ctypes.byref(p) for p in ptrs])
-        cdt = db.server.params.coeff_dtype
-        d = db.d
-        shapes = [(max_batch, db.server.db_cols), (max_batch, db.nsd, d),
-                  (max_batch, db.npk, d), (max_batch, db.l, 2, d)]
-        self.host = []
-        for p, shp in zip(ptrs, shapes):
-            n = int(np.prod(shp))
-            buf = (ctypes.c_uint8 * (n * np.dtype(cdt).itemsize)).from_address(
-                p.value) if n else None
-            arr = (np.frombuffer(buf, dtype=cdt).reshape(shp) if n
-                   else np.zeros(shp, dtype=cdt))
-            self.host.append(arr)
-        self.items = []
-        self.t_launch = 0.0
-
-    def submit(self, items, engine):
-        lib = _lib.load()
-        fd, sd, pk, _ = self.host
-        for i, it in enumerate(items):
-            n1 = it.first_dim.shape[0]
-            fd[i, :n1] = it.first_dim
-            fd[i, n1:] = 0
-            if self.db.nsd:
-                sd[i] = it.second_dim
-            pk[i] = it.packing_key
-        err = ctypes.create_string_buffer(512)
-        rc = lib.inspire_pir_workspace_submit(self.h, len(items), engine, err,
-                                              len(err))
-        if rc:
-            raise pir.InspireError(rc, err.value.decode())
-        self.items = items
-        self.t_launch = time.perf_counter()
-
-    def done(self):
-        return _lib.load().inspire_pir_workspace_poll(self.h) != 0
-
-    def finish(self):
-        lib = _lib.load()
-        err = ctypes.create_string_buffer(512)
-        rc = lib.inspire_pir_workspace_wait(self.h, err, len(err))
-        items, self.items = self.items, []
-        if rc:
-            return items, pir.InspireError(rc, err.value.decode())
-        resp = self.host[3]
-        return items, [resp[i].copy() for i in range(len(items))]
-
-    def close(self):
-        if self.h:
-            _lib.load().inspire_pir_workspace_destroy(self.h)
-            self.h = None
-
-
-class _Item:
-    __slots__ = ("db", "first_dim", "second_dim", "packing_key", "future",
-                 "t_submit", "t_done")
-
-    def __init__(self, db, fd, sd, pk):
-        self.db = db
-        self.first_dim = fd
-        self.second_dim = sd
-        self.packing_key = pk
-        self.future = Future()
-        self.t_submit = time.perf_counter()
-        self.t_done = None
-
-
-class _Database:
-    def __init__(self, name, server):
+class _Queue:
+    def __init__(self, name, index, d, l, nsd, npk, db_cols, dtype,
+                 min_first_dim):
         self.name = name
-        self.server = server
-        self.workspace_bytes = 0
-        p = server.params
-        self.d = p.rlwe.degree
-        self.l = p.entry_size_multiple
-        self.nsd = (2 * p.eval_gadget.num_digits
-                    if p.interpolation_degree > 1 else 0)
-        self.npk = 2 * p.pack_gadget.num_digits
-        self.pending = deque()
-        self.free = []
-        self.inflight = []
+        self.index = index
+        self.d, self.l, self.nsd, self.npk = d, l, nsd, npk
+        self.db_cols = db_cols
+        self.dtype = np.dtype(dtype)
+        self.min_first_dim = min_first_dim
+        self.views = {}      # slot address -> numpy views of the slot
+
+    def slot_views(self, ptrs):
+        key = ptrs[0]
+        v = self.views.get(key)
+        if v is None:
+            shapes = [(self.db_cols,), (self.nsd, self.d), (self.npk, self.d),
+                      (self.l, 2, self.d)]
+            v = []
+            for p, shp in zip(ptrs, shapes):
+                n = int(np.prod(shp))
+                if n == 0:
+                    v.append(np.zeros(shp, dtype=self.dtype))
+                    continue
+                buf = (ctypes.c_char * (n * self.dtype.itemsize)).from_address(p)
+                v.append(np.frombuffer(buf, dtype=self.dtype).reshape(shp))
+            self.views[key] = v
+        return v
 
 
 class ServingEngine:
     """Continuous batching over one or more PirServer instances.
 
     servers: {name: PirServer}. max_batch: requests per batch. hbm_budget:
-    device bytes the workspaces of all databases may take (split evenly);
-    each database gets between 1 and max_workspaces of them. plain_max_batch:
+    device bytes the workspaces of all servers may take (split evenly);
+    each server gets between 1 and max_workspaces of them. plain_max_batch:
     batches up to this size use the plain engine, larger ones the tensor
-    engine when the server has it.
+    engine when the server has it. ring_slots: request slots per server
+    (default 4 * max_batch).
     """
 
     def __init__(self, servers, max_batch=256, hbm_budget=8 << 30,
-                 max_workspaces=3, plain_max_batch=4, workspace_factory=None,
-                 workspace_bytes=None):
+                 max_workspaces=3, plain_max_batch=4, ring_slots=None,
+                 _loopback=None):
+        self._lib = _lib.load()
         self.max_batch = max_batch
-        self.plain_max_batch = plain_max_batch
-        self.dbs = {n: _Database(n, s) for n, s in servers.items()}
-        factory = workspace_factory or _Workspace
-        if workspace_bytes is None:
-            lib = _lib.load()
-
-            def workspace_bytes(server, b):
-                return lib.inspire_pir_workspace_bytes(server._h, b)
-        share = hbm_budget // max(1, len(self.dbs))
-        for db in self.dbs.values():
-            per = workspace_bytes(db.server, max_batch)
-            # HBM admission: as many in-flight batch slots as the budget holds.
-            n = int(max(1, min(max_workspaces, share // max(per, 1))))
-            db.free = [factory(db, max_batch) for _ in range(n)]
-            db.workspace_bytes = per
+        ring_slots = ring_slots or 4 * max_batch
+        err = pir._errbuf()
+        h = ctypes.c_void_p()
+        self.queues = {}
+        if _loopback is None:
+            names = list(servers)
+            arr = (ctypes.c_void_p * len(names))(*[servers[n]._h.value
+                                                   if isinstance(servers[n]._h, ctypes.c_void_p)
+                                                   else servers[n]._h for n in names])
+            rc = self._lib.inspire_serving_create(
+                arr, len(names), max_batch, plain_max_batch, ring_slots,
+                int(hbm_budget), max_workspaces, ctypes.byref(h), err, len(err))
+            pir._check(rc, err)
+            for i, n in enumerate(names):
+                s = servers[n]
+                p = s.params
+                self.queues[n] = _Queue(
+                    n, i, p.rlwe.degree, p.entry_size_multiple,
+                    2 * p.eval_gadget.num_digits if p.interpolation_degree > 1 else 0,
+                    2 * p.pack_gadget.num_digits, s.db_cols, p.coeff_dtype,
+                    p.InterpolatedRows())
+        else:
+            names, words, workspaces, delay_us = _loopback
+            w = (ctypes.c_int64 * (4 * len(names)))(*[x for q in words for x in q])
+            rc = self._lib.inspire_serving_create_loopback(
+                len(names), w, workspaces, delay_us, max_batch,
+                plain_max_batch, ring_slots, ctypes.byref(h), err, len(err))
+            pir._check(rc, err)
+            for i, (n, q) in enumerate(zip(names, words)):
+                # Loopback slots: flat u32 words (d = 1 polynomial rows).
+                self.queues[n] = _Queue(n, i, 1, q[3] // 2, q[1], q[2], q[0],
+                                        np.uint32, 1)
+        self._h = h
+        self._pending = deque()
         self._cv = threading.Condition()
         self._stop = False
         self._thread = None
-        self.latencies = []
-        self.batches = []          # (db name, batch size, engine)
-        self.max_inflight = 0
-        self._tensor_ok = {n: True for n in self.dbs}
+
+    @classmethod
+    def loopback(cls, queues, workspaces=2, delay_us=200, **kw):
+        """An engine over the host-only loopback device: queues is
+        {name: (first_dim_words, second_dim_words, packing_key_words,
+        response_words)}; see inspire_serving_create_loopback."""
+        names = list(queues)
+        return cls(None, _loopback=(names, [tuple(queues[n]) for n in names],
+                                    workspaces, delay_us), **kw)
 
     # -- public ----------------------------------------------------------
     def start(self):
         self._stop = False
-        self._thread = threading.Thread(target=self._loop, daemon=True)
+        self._thread = threading.Thread(target=self._complete, daemon=True)
         self._thread.start()
         return self
 
@@ -174,9 +128,10 @@ class ServingEngine:
             self._cv.notify_all()
         if self._thread:
             self._thread.join()
-        for db in self.dbs.values():
-            for ws in db.free + [w for w in db.inflight]:
-                ws.close()
+            self._thread = None
+        if self._h:
+            self._lib.inspire_serving_destroy(self._h)
+            self._h = None
 
     def __enter__(self):
         return self.start()
@@ -184,94 +139,84 @@ class ServingEngine:
     def __exit__(self, *exc):
         self.stop()
 
-    def submit(self, db_name, first_dim, second_dim, packing_key):
+    def submit(self, name, first_dim, second_dim, packing_key):
         """Queues one request; returns a Future resolving to (l, 2, d)."""
-        db = self.dbs[db_name]
-        cdt = db.server.params.coeff_dtype
-        it = _Item(db, np.asarray(first_dim, dtype=cdt),
-                   np.asarray(second_dim, dtype=cdt).reshape(db.nsd, db.d),
-                   np.asarray(packing_key, dtype=cdt).reshape(db.npk, db.d))
-        if it.first_dim.shape[0] > db.server.db_cols:
+        q = self.queues[name]
+        fd = np.asarray(first_dim, dtype=q.dtype).reshape(-1)
+        err = pir._errbuf()
+        ticket = ctypes.c_int64()
+        ptrs = [ctypes.c_void_p() for _ in range(4)]
+        if fd.shape[0] > q.db_cols or fd.shape[0] < q.min_first_dim:
             raise pir.InspireError(
                 pir.INVALID_ARGUMENT,
                 "First dimension query size (%d) is invalid for DB columns "
-                "(%d)." % (it.first_dim.shape[0], db.server.db_cols))
+                "(%d)." % (fd.shape[0], q.db_cols))
+        rc = self._lib.inspire_serving_acquire(
+            self._h, q.index, 60000, ctypes.byref(ticket),
+            *[ctypes.byref(p) for p in ptrs], err, len(err))
+        pir._check(rc, err)
+        v = q.slot_views([p.value for p in ptrs])
+        v[0][:fd.shape[0]] = fd
+        if q.nsd:
+            v[1][...] = np.asarray(second_dim, dtype=q.dtype).reshape(q.nsd, q.d)
+        v[2][...] = np.asarray(packing_key, dtype=q.dtype).reshape(q.npk, q.d)
+        fut = Future()
+        rc = self._lib.inspire_serving_submit(self._h, ticket.value,
+                                              fd.shape[0], err, len(err))
+        if rc:
+            self._lib.inspire_serving_release(self._h, ticket.value)
+            pir._check(rc, err)
         with self._cv:
-            db.pending.append(it)
+            self._pending.append((ticket.value, v[3], fut))
             self._cv.notify()
-        return it.future
+        return fut
 
     def stats(self):
-        lat = np.array(self.latencies) if self.latencies else np.zeros(1)
-        return {"requests": len(self.latencies),
-                "p50_ms": float(np.percentile(lat, 50) * 1e3),
-                "p99_ms": float(np.percentile(lat, 99) * 1e3),
-                "batches": len(self.batches),
-                "mean_batch": (float(np.mean([b for _, b, _ in self.batches]))
-                               if self.batches else 0.0),
-                "max_inflight": self.max_inflight}
+        s = _Stats()
+        self._lib.inspire_serving_get_stats(self._h, ctypes.byref(s))
+        return {"requests": s.requests, "failed": s.failed,
+                "batches": s.batches, "tensor_batches": s.tensor_batches,
+                "mean_batch": s.mean_batch, "p50_ms": s.p50_ms,
+                "p99_ms": s.p99_ms, "max_ms": s.max_ms,
+                "max_inflight": s.max_inflight}
 
-    # -- scheduler -------------------------------------------------------
-    def _engine_for(self, db, n):
-        if n > self.plain_max_batch and self._tensor_ok[db.name]:
-            return pir.ENGINE_TENSOR
-        return pir.ENGINE_PLAIN
+    def reset_stats(self):
+        self._lib.inspire_serving_reset_stats(self._h)
 
-    def _loop(self):
+    def queue_info(self, name):
+        ws, b, slots = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
+        self._lib.inspire_serving_queue_info(
+            self._h, self.queues[name].index, ctypes.byref(ws),
+            ctypes.byref(b), ctypes.byref(slots))
+        return {"workspaces": ws.value, "workspace_bytes": b.value,
+                "ring_slots": slots.value}
+
+    # -- completion ------------------------------------------------------
+    def _complete(self):
+        err = pir._errbuf()
         while True:
-            progressed = False
-            # Retire finished batches (their workspaces become free slots).
-            for db in self.dbs.values():
-                still = []
-                for ws in db.inflight:
-                    if ws.done():
-                        items, res = ws.finish()
-                        t = time.perf_counter()
-                        for k, it in enumerate(items):
-                            it.t_done = t
-                            if isinstance(res, Exception):
-                                it.future.set_exception(res)
-                            else:
-                                it.future.set_result(res[k])
-                                self.latencies.append(t - it.t_submit)
-                        db.free.append(ws)
-                        progressed = True
-                    else:
-                        still.append(ws)
-                db.inflight = still
-            # Admit pending requests into free workspaces.
             with self._cv:
-                if self._stop and not any(d.pending or d.inflight
-                                          for d in self.dbs.values()):
+                while not self._pending and not self._stop:
+                    self._cv.wait()
+                if not self._pending:
                     return
-                launch = []
-                for db in self.dbs.values():
-                    while db.pending and db.free:
-                        n = min(len(db.pending), self.max_batch)
-                        items = [db.pending.popleft() for _ in range(n)]
-                        launch.append((db, db.free.pop(), items))
-            for db, ws, items in launch:
-                eng = self._engine_for(db, len(items))
-                try:
-                    ws.submit(items, eng)
-                except pir.InspireError as e:
-                    if eng == pir.ENGINE_TENSOR and e.code == pir.FAILED_PRECONDITION:
-                        self._tensor_ok[db.name] = False
-                        eng = pir.ENGINE_PLAIN
-                        ws.submit(items, eng)
-                    else:
-                        for it in items:
-                            it.future.set_exception(e)
-                        db.free.append(ws)
-                        continue
-                db.inflight.append(ws)
-                self.batches.append((db.name, len(items), eng))
-                progressed = True
-            inflight = sum(len(d.inflight) for d in self.dbs.values())
-            self.max_inflight = max(self.max_inflight, inflight)
-            if not progressed:
-                with self._cv:
-                    if inflight:
-                        self._cv.wait(timeout=0.0002)
-                    elif not self._stop and not any(d.pending for d in self.dbs.values()):
-                        self._cv.wait(timeout=0.05)
+                ticket, resp, fut = self._pending.popleft()
+            while True:
+                rc = self._lib.inspire_serving_wait(self._h, ticket, 1000, err,
+                                                    len(err))
+                if rc != pir.DEADLINE_EXCEEDED:
+                    break
+            if rc == 0:
+                fut.set_result(resp.copy())
+            else:
+                fut.set_exception(pir.InspireError(rc, err.value.decode()))
+            self._lib.inspire_serving_release(self._h, ticket)
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("requests", ctypes.c_int64), ("failed", ctypes.c_int64),
+                ("batches", ctypes.c_int64),
+                ("tensor_batches", ctypes.c_int64),
+                ("mean_batch", ctypes.c_double), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
+                ("max_inflight", ctypes.c_int32), ("reserved", ctypes.c_int32)]

@@ -17,9 +17,9 @@ def built():
     build.build()
 
 
-def _db(d, n, t, l, seed):
+def _db(d, n, t, l, seed, pad_to=1):
     params = synthetic.make_params(d=d, n=n, t=t, l=l, coeff_bits=32)
-    mat = synthetic.make_material(params, seed=seed)
+    mat = synthetic.make_material(params, seed=seed, pad_to=pad_to)
     srv = pir.PirServer.CreateCombined(params, mat.db, mat.pack,
                                        mat.a_tilde_agg, mat.t_vec_h,
                                        mat.second_dim_a)
@@ -39,7 +39,9 @@ def test_mixed_batching_matches_alone():
     # In the mix: two client threads submit interleaved requests for both
     # databases while earlier batches are in flight.
     with serving.ServingEngine({"A": sa, "B": sb}, max_batch=16,
-                               max_workspaces=3, plain_max_batch=2) as eng:
+                               max_workspaces=3, plain_max_batch=2,
+                               hbm_budget=1 << 30) as eng:
+        assert eng.queue_info("A")["workspaces"] == 3
         futs = {"A": [None] * 40, "B": [None] * 40}
 
         def client(name):
@@ -86,11 +88,37 @@ def test_workspaces_overlap_and_tensor_engine_is_used():
                                plain_max_batch=4) as eng:
         futs = [eng.submit("A", fd[i], sd[i], pk[i]) for i in range(96)]
         got = np.stack([f.result(timeout=120) for f in futs])
-        engines = {e for _, _, e in eng.batches}
         stats = eng.stats()
     assert np.array_equal(got, want)
-    assert pir.ENGINE_TENSOR in engines
+    assert stats["tensor_batches"] >= 1
     assert stats["max_inflight"] >= 2
+
+
+def test_short_first_dimension_and_errors_in_the_mix():
+    pa, ma, sa = _db(128, 2 * 4000, 2, 1, seed=8, pad_to=256)
+    assert sa.db_cols == 4096
+    fd, sd, pk = synthetic.make_requests(pa, 6, seed=9)
+    alone = sa.process_arrays(fd, sd, pk)
+    with serving.ServingEngine({"A": sa}, max_batch=4, max_workspaces=2) as eng:
+        futs = [eng.submit("A", fd[i], sd[i], pk[i]) for i in range(6)]
+        with pytest.raises(pir.InspireError, match="First dimension query size"):
+            eng.submit("A", fd[0][:10], sd[0], pk[0])
+        for i, f in enumerate(futs):
+            assert np.array_equal(f.result(timeout=120), alone[i])
+
+
+def test_hbm_budget_limits_workspaces():
+    pa, _, sa = _db(128, 8192, 2, 1, seed=10)
+    lib = pir._lib.load()
+    per = lib.inspire_pir_workspace_bytes(sa._h, 64)
+    with serving.ServingEngine({"A": sa, "B": sa}, max_batch=64,
+                               hbm_budget=2 * per + per // 2,
+                               max_workspaces=4) as eng:
+        assert eng.queue_info("A")["workspaces"] == 1
+        assert eng.queue_info("A")["workspace_bytes"] == per
+    with serving.ServingEngine({"A": sa}, max_batch=64, hbm_budget=10 * per,
+                               max_workspaces=4) as eng:
+        assert eng.queue_info("A")["workspaces"] == 4
 
 
 def test_workspace_bytes_scale_with_batch():

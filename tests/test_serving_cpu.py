@@ -1,137 +1,175 @@
-"""Scheduling logic of the continuous-batching loop, on the CPU.
+"""The native continuous-batching scheduler on the CPU.
 
-A fake workspace stands in for the GPU one: it "answers" a batch with a
-deterministic function of each request and finishes after a delay, so the
-test can check batching, per-database FIFO order, HBM admission (in-flight
-slot counts), result routing and error propagation without a GPU.
+The engine runs over its host-only loopback device (response word k of a
+request is first_dim[0] * 7 + queue + k, ready a set delay after the batch
+launches), so batching, ring order, admission, result routing and error
+propagation are checked without a GPU.
 """
 import threading
-import time
-from types import SimpleNamespace
 
 import numpy as np
 import pytest
 
-from inspire_gb300 import pir, serving, synthetic
+from inspire_gb300 import _lib, pir, serving
+
+QUEUES = {"A": (16, 4, 4, 8), "BB": (32, 0, 8, 4)}
 
 
-class FakeWorkspace:
-    live = 0
-    peak = 0
-    lock = threading.Lock()
-
-    def __init__(self, db, max_batch):
-        self.db = db
-        self.items = []
-        self.t_ready = 0.0
-        self.fail = False
-
-    def submit(self, items, engine):
-        if any(int(it.first_dim[0]) == 999 for it in items):
-            raise pir.InspireError(pir.INVALID_ARGUMENT, "bad request")
-        self.items = items
-        self.engine = engine
-        self.t_ready = time.perf_counter() + 0.01
-        with FakeWorkspace.lock:
-            FakeWorkspace.live += 1
-            FakeWorkspace.peak = max(FakeWorkspace.peak, FakeWorkspace.live)
-
-    def done(self):
-        return time.perf_counter() >= self.t_ready
-
-    def finish(self):
-        with FakeWorkspace.lock:
-            FakeWorkspace.live -= 1
-        items, self.items = self.items, []
-        l, d = self.db.l, self.db.d
-        return items, [np.full((l, 2, d), int(it.first_dim[0]) * 7 + len(self.db.name),
-                               dtype=np.uint32) for it in items]
-
-    def close(self):
-        pass
+@pytest.fixture(scope="module", autouse=True)
+def lib():
+    try:
+        return _lib.load()
+    except _lib.LibraryMissing:
+        pytest.skip("library not built")
 
 
-def fake_server(d=32, t=2, l=1, db_cols=64):
-    params = synthetic.make_params(d=d, n=db_cols * t, t=t, l=l, coeff_bits=32)
-    return SimpleNamespace(params=params, db_cols=db_cols, _h=None)
-
-
-def engine(**kw):
-    servers = {"A": fake_server(l=2), "BB": fake_server(d=64, t=4)}
-    return serving.ServingEngine(servers, workspace_factory=FakeWorkspace,
-                                 workspace_bytes=lambda s, b: 1 << 20, **kw)
-
-
-def _req(db, i):
-    fd = np.array([i] + [0] * 9, dtype=np.uint32)
-    sd = np.zeros((db.nsd, db.d), dtype=np.uint32)
-    pk = np.zeros((db.npk, db.d), dtype=np.uint32)
+def _req(eng, name, i):
+    q = eng.queues[name]
+    fd = np.zeros(q.db_cols, dtype=np.uint32)
+    fd[0] = i
+    sd = np.zeros((q.nsd, q.d), dtype=np.uint32)
+    pk = np.zeros((q.npk, q.d), dtype=np.uint32)
     return fd, sd, pk
 
 
+def _want(eng, name, i):
+    q = eng.queues[name]
+    k = np.arange(q.l * 2 * q.d, dtype=np.uint64)
+    return ((i * 7 + q.index + k) % (1 << 32)).astype(np.uint32).reshape(
+        q.l, 2, q.d)
+
+
 def test_results_route_to_their_requests():
-    FakeWorkspace.peak = 0
-    with engine(max_batch=8, hbm_budget=6 << 20, max_workspaces=3) as eng:
+    with serving.ServingEngine.loopback(QUEUES, workspaces=3, delay_us=300,
+                                        max_batch=8) as eng:
         futs = []
-        for i in range(50):
+        for i in range(200):
             name = "A" if i % 3 else "BB"
-            futs.append((name, i, eng.submit(name, *_req(eng.dbs[name], i))))
+            futs.append((name, i, eng.submit(name, *_req(eng, name, i))))
         for name, i, f in futs:
-            got = f.result(timeout=10)
-            db = eng.dbs[name]
-            assert got.shape == (db.l, 2, db.d)
-            assert int(got[0, 0, 0]) == i * 7 + len(name)
+            assert np.array_equal(f.result(timeout=30), _want(eng, name, i))
         st = eng.stats()
-    assert st["requests"] == 50
-    assert max(b for _, b, _ in eng.batches) <= 8
-
-
-def test_hbm_budget_limits_inflight_slots():
-    # 2 MiB budget split over 2 databases at 1 MiB per workspace: 1 slot each.
-    FakeWorkspace.peak = 0
-    with engine(max_batch=4, hbm_budget=2 << 20, max_workspaces=3) as eng:
-        assert all(len(db.free) == 1 for db in eng.dbs.values())
-        futs = [eng.submit("A", *_req(eng.dbs["A"], i)) for i in range(20)]
-        for f in futs:
-            f.result(timeout=10)
-    assert FakeWorkspace.peak <= 2
+    assert st["requests"] == 200 and st["failed"] == 0
+    assert st["mean_batch"] <= 8
 
 
 def test_requests_queued_while_busy_are_batched():
-    with engine(max_batch=16, hbm_budget=1 << 20, max_workspaces=1) as eng:
-        futs = [eng.submit("A", *_req(eng.dbs["A"], i)) for i in range(40)]
+    with serving.ServingEngine.loopback({"A": (4, 0, 2, 2)}, workspaces=1,
+                                        delay_us=5000, max_batch=16) as eng:
+        futs = [eng.submit("A", *_req(eng, "A", i)) for i in range(64)]
+        for i, f in enumerate(futs):
+            assert np.array_equal(f.result(timeout=30), _want(eng, "A", i))
+        st = eng.stats()
+    assert st["batches"] < 64
+    assert st["mean_batch"] > 1.5
+    assert st["max_inflight"] == 1
+
+
+def test_workspaces_overlap():
+    with serving.ServingEngine.loopback({"A": (4, 0, 2, 2)}, workspaces=3,
+                                        delay_us=20000, max_batch=2) as eng:
+        futs = [eng.submit("A", *_req(eng, "A", i)) for i in range(12)]
         for f in futs:
-            f.result(timeout=10)
-        sizes = [b for n, b, _ in eng.batches if n == "A"]
-    assert sum(sizes) == 40
-    assert max(sizes) > 1
+            f.result(timeout=30)
+        assert eng.stats()["max_inflight"] >= 2
 
 
 def test_small_batches_use_plain_engine_large_tensor():
-    with engine(max_batch=32, hbm_budget=1 << 20, max_workspaces=1,
-                plain_max_batch=2) as eng:
-        f = eng.submit("A", *_req(eng.dbs["A"], 1))
-        f.result(timeout=10)
-        futs = [eng.submit("A", *_req(eng.dbs["A"], i)) for i in range(30)]
+    with serving.ServingEngine.loopback({"A": (4, 0, 2, 2)}, workspaces=1,
+                                        delay_us=3000, max_batch=32,
+                                        plain_max_batch=2) as eng:
+        eng.submit("A", *_req(eng, "A", 1)).result(timeout=30)
+        assert eng.stats()["tensor_batches"] == 0
+        futs = [eng.submit("A", *_req(eng, "A", i)) for i in range(40)]
         for f in futs:
-            f.result(timeout=10)
-    engines = [e for _, b, e in eng.batches]
-    assert engines[0] == pir.ENGINE_PLAIN
-    assert pir.ENGINE_TENSOR in engines
+            f.result(timeout=30)
+        assert eng.stats()["tensor_batches"] >= 1
 
 
 def test_failed_batch_sets_exceptions_and_loop_survives():
-    with engine(max_batch=4, hbm_budget=1 << 20, max_workspaces=1) as eng:
-        bad = eng.submit("A", *_req(eng.dbs["A"], 999))
-        with pytest.raises(pir.InspireError):
-            bad.result(timeout=10)
-        ok = eng.submit("A", *_req(eng.dbs["A"], 5))
-        assert int(ok.result(timeout=10)[0, 0, 0]) == 5 * 7 + 1
+    with serving.ServingEngine.loopback({"A": (4, 0, 2, 2)}, workspaces=1,
+                                        delay_us=100, max_batch=4) as eng:
+        bad = eng.submit("A", *_req(eng, "A", 0xDEAD))
+        with pytest.raises(pir.InspireError, match="rejected"):
+            bad.result(timeout=30)
+        ok = eng.submit("A", *_req(eng, "A", 5))
+        assert np.array_equal(ok.result(timeout=30), _want(eng, "A", 5))
+        assert eng.stats()["failed"] >= 1
 
 
 def test_first_dimension_longer_than_db_is_rejected():
-    with engine() as eng:
-        db = eng.dbs["A"]
-        fd = np.zeros(db.server.db_cols + 1, dtype=np.uint32)
+    with serving.ServingEngine.loopback(QUEUES) as eng:
+        fd, sd, pk = _req(eng, "A", 1)
         with pytest.raises(pir.InspireError, match="First dimension query size"):
-            eng.submit("A", fd, *_req(db, 0)[1:])
+            eng.submit("A", np.zeros(17, np.uint32), sd, pk)
+
+
+def test_short_first_dimension_is_zero_padded():
+    # A slot reused after a full-length request must not leak its old words.
+    with serving.ServingEngine.loopback({"A": (8, 0, 2, 2)}, workspaces=1,
+                                        delay_us=100, max_batch=1,
+                                        ring_slots=1) as eng:
+        fd, sd, pk = _req(eng, "A", 3)
+        fd[:] = 9
+        eng.submit("A", fd, sd, pk).result(timeout=30)
+        eng.submit("A", fd[:2], sd, pk).result(timeout=30)
+        q = eng.queues["A"]
+        slot = next(iter(q.views.values()))
+        assert list(slot[0][2:]) == [0] * 6
+
+
+def test_many_client_threads():
+    with serving.ServingEngine.loopback(QUEUES, workspaces=2, delay_us=200,
+                                        max_batch=16, ring_slots=64) as eng:
+        errors = []
+
+        def client(name, base):
+            try:
+                fs = [(i, eng.submit(name, *_req(eng, name, i)))
+                      for i in range(base, base + 150)]
+                for i, f in fs:
+                    assert np.array_equal(f.result(timeout=60),
+                                          _want(eng, name, i))
+            except Exception as e:  # surfaced below
+                errors.append(e)
+
+        ths = [threading.Thread(target=client, args=(n, b))
+               for n, b in (("A", 0), ("BB", 1000), ("A", 2000), ("BB", 3000))]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        assert not errors, errors
+        assert eng.stats()["requests"] == 600
+
+
+def test_bad_ticket_and_arguments(lib):
+    err = pir._errbuf()
+    import ctypes
+    h = ctypes.c_void_p()
+    words = (ctypes.c_int64 * 4)(4, 0, 2, 2)
+    rc = lib.inspire_serving_create_loopback(1, words, 1, 0, 8, 2, 4,
+                                             ctypes.byref(h), err, len(err))
+    assert rc == pir.INVALID_ARGUMENT       # ring_slots < max_batch
+    rc = lib.inspire_serving_create_loopback(1, words, 1, 0, 8, 2, 8,
+                                             ctypes.byref(h), err, len(err))
+    assert rc == 0
+    try:
+        assert lib.inspire_serving_submit(h, 12345, 1, err, len(err)) == \
+            pir.INVALID_ARGUMENT
+        assert lib.inspire_serving_wait(h, 12345, 1, err, len(err)) == \
+            pir.INVALID_ARGUMENT
+        t = ctypes.c_int64()
+        p = [ctypes.c_void_p() for _ in range(4)]
+        assert lib.inspire_serving_acquire(h, 3, 10, ctypes.byref(t),
+                                           *[ctypes.byref(x) for x in p],
+                                           err, len(err)) == pir.INVALID_ARGUMENT
+        assert lib.inspire_serving_acquire(h, 0, 10, ctypes.byref(t),
+                                           *[ctypes.byref(x) for x in p],
+                                           err, len(err)) == 0
+        # Not submitted yet: waiting is refused, releasing is allowed.
+        assert lib.inspire_serving_wait(h, t.value, 1, err, len(err)) == \
+            pir.FAILED_PRECONDITION
+        assert lib.inspire_serving_release(h, t.value) == 0
+    finally:
+        lib.inspire_serving_destroy(h)

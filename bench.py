@@ -358,6 +358,12 @@ def main():
     except pir.InspireError:
         engine = pir.ENGINE_PLAIN
 
+    # The tensor engine's split-K factor for this batch size, by timing.
+    tuned = None
+    if engine == pir.ENGINE_TENSOR:
+        split, tune_ms = srv.autotune(B)
+        tuned = {"split_k": split, "product_ms": tune_ms}
+
     # Parity of the two engines on the first requests, and spot rows of the
     # DB product against an exact host computation.
     check = min(B, 8)
@@ -444,7 +450,8 @@ def main():
                    "batch": B, "engine": "tensor" if engine else "plain",
                    "db_matrix": [rows, cols], "pack_matrix": list(pack.shape),
                    "l2": "inputs larger than L2 (9 GiB matrices per step)",
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "autotune": tuned},
         "plain": {"queries_per_s": plain_qps, "ms_per_query": ms_plain,
                   "db_gbs": db_bytes / (ms_plain / 1000.0) / 1e9},
         "db_gbs": db_bytes * (1 if engine else B) / (ms_step / 1000.0) / 1e9,

@@ -200,6 +200,16 @@ int inspire_pir_external_product_device(inspire_pir_server* server,
  * on that server. inspire_pir_server_check reports a tensor-engine pipeline
  * timeout recorded by earlier launches (call it after synchronising).
  */
+/*
+ * Autotuner of the tensor engine (no reference counterpart): times the
+ * split-K factors of the batched product for `batch` requests on this
+ * server's matrices and keeps the fastest for later batches of the same
+ * size (rounded up to 64 requests). Reports the factor and the product's
+ * time in ms. Synchronous; FAILED_PRECONDITION without the tensor engine.
+ */
+int inspire_pir_autotune(inspire_pir_server* server, int32_t batch,
+                         int32_t* split, float* ms, char* err, size_t err_len);
+
 typedef struct inspire_graph inspire_graph;
 int inspire_graph_begin(void* stream, char* err, size_t err_len);
 int inspire_graph_end(void* stream, inspire_graph** out, char* err,
@@ -261,6 +271,9 @@ int inspire_pir_workspace_wait(inspire_pir_workspace* ws, char* err,
  * device. Workspaces per queue: hbm_budget / n_servers / the workspace bytes
  * of max_batch requests, between 1 and max_workspaces. Batches of more than
  * plain_max_batch requests use the tensor engine when the server has it.
+ * max_wait_us is the batching window: a queue's partial batch waits until its
+ * oldest request has waited that long (0: launch as soon as a workspace is
+ * free, the lowest latency at light load).
  * Every response is the one inspire_pir_process_response gives for the same
  * request.
  *
@@ -290,9 +303,10 @@ typedef struct inspire_serving_stats {
 
 int inspire_serving_create(inspire_pir_server* const* servers,
                            int32_t n_servers, int32_t max_batch,
-                           int32_t plain_max_batch, int32_t ring_slots,
-                           int64_t hbm_budget, int32_t max_workspaces,
-                           inspire_serving** out, char* err, size_t err_len);
+                           int32_t plain_max_batch, int32_t max_wait_us,
+                           int32_t ring_slots, int64_t hbm_budget,
+                           int32_t max_workspaces, inspire_serving** out,
+                           char* err, size_t err_len);
 /* The same scheduler over a host-only loopback device (for tests on machines
  * without a GPU): queue q has slots of slot_words[4q..4q+3] u32 words
  * (first_dim, second_dim, packing_key, response); response word k is
@@ -301,8 +315,9 @@ int inspire_serving_create(inspire_pir_server* const* servers,
 int inspire_serving_create_loopback(int32_t n_queues, const int64_t* slot_words,
                                     int32_t workspaces, int32_t delay_us,
                                     int32_t max_batch, int32_t plain_max_batch,
-                                    int32_t ring_slots, inspire_serving** out,
-                                    char* err, size_t err_len);
+                                    int32_t max_wait_us, int32_t ring_slots,
+                                    inspire_serving** out, char* err,
+                                    size_t err_len);
 void inspire_serving_destroy(inspire_serving* engine);
 /* Blocks up to timeout_ms for a free slot (RESOURCE_EXHAUSTED after). */
 int inspire_serving_acquire(inspire_serving* engine, int32_t queue,

@@ -36,15 +36,18 @@ SIGNATURES = {
         ctypes.c_int),
     "inspire_pir_external_product_device": (
         [_vp, _i32, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_autotune": ([_vp, _i32, _vp, _vp, _cp, _sz], ctypes.c_int),
     "inspire_graph_begin": ([_vp, _cp, _sz], ctypes.c_int),
     "inspire_graph_end": ([_vp, _vp, _cp, _sz], ctypes.c_int),
     "inspire_graph_launch": ([_vp, _vp, _cp, _sz], ctypes.c_int),
     "inspire_graph_destroy": ([_vp], None),
     "inspire_pir_server_check": ([_vp, _cp, _sz], ctypes.c_int),
     "inspire_serving_create": (
-        [_vp, _i32, _i32, _i32, _i32, _i64, _i32, _vp, _cp, _sz], ctypes.c_int),
+        [_vp, _i32, _i32, _i32, _i32, _i32, _i64, _i32, _vp, _cp, _sz],
+        ctypes.c_int),
     "inspire_serving_create_loopback": (
-        [_i32, _vp, _i32, _i32, _i32, _i32, _i32, _vp, _cp, _sz], ctypes.c_int),
+        [_i32, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _cp, _sz],
+        ctypes.c_int),
     "inspire_serving_destroy": ([_vp], None),
     "inspire_serving_acquire": (
         [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),

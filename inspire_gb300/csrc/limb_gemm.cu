@@ -53,6 +53,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 
@@ -641,6 +642,67 @@ class LimbGemmImpl : public LimbGemm {
   cudaError_t Run(int batch, const void* q1, int64_t q1_stride, const void* yg,
                   int64_t yg_stride, void* out, LimbScratch* scratch,
                   cudaStream_t st) override {
+    return Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, 0);
+  }
+
+  // Times every split-K factor that keeps at least 8 K units per CTA and at
+  // least 80 % of the last wave busy (plus the heuristic choice) on this
+  // batch size and keeps the fastest for later launches of the same padded
+  // batch size. Synchronises `st`.
+  cudaError_t Tune(int batch, const void* q1, int64_t q1_stride, const void* yg,
+                   int64_t yg_stride, void* out, LimbScratch* scratch,
+                   cudaStream_t st, int* chosen, float* best_ms) override {
+    if (batch <= 0) return cudaErrorInvalidValue;
+    const int64_t bpad = round_up(batch, kTileQ);
+    const int64_t tiles = (rows_ / kTileRows) * (bpad / kTileQ);
+    const int n_units = static_cast<int>((cpad_ + 2 * kpad_) / kUnitK);
+    const int sms = sms_ > 0 ? sms_ : 148;
+    const int heuristic = ChooseSplit(tiles, n_units);
+    cudaEvent_t e0, e1;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e != cudaSuccess) return e;
+    e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) {
+      cudaEventDestroy(e0);
+      return e;
+    }
+    int best = heuristic;
+    float best_t = 0;
+    for (int k = 1; k <= 16 && e == cudaSuccess; ++k) {
+      if (n_units / k < 8) break;
+      const int64_t items = tiles * k;
+      const int64_t waves = (items + sms - 1) / sms;
+      const double eff = static_cast<double>(items) / (waves * sms);
+      if (k != heuristic && eff < 0.8) continue;
+      e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, k);
+      if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+      for (int r = 0; r < 2 && e == cudaSuccess; ++r) {
+        e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, k);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e == cudaSuccess && (best_t == 0 || ms < best_t)) {
+        best_t = ms;
+        best = k;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return e;
+    {
+      std::lock_guard<std::mutex> lk(tune_mu_);
+      tuned_[bpad] = best;
+    }
+    if (chosen) *chosen = best;
+    if (best_ms) *best_ms = best_t / 2;
+    return cudaSuccess;
+  }
+
+  cudaError_t Launch(int batch, const void* q1, int64_t q1_stride, const void* yg,
+                     int64_t yg_stride, void* out, LimbScratch* scratch,
+                     cudaStream_t st, int force_split) {
     if (batch <= 0) return cudaSuccess;
     LimbScratchImpl* sc = static_cast<LimbScratchImpl*>(scratch);
     cudaError_t e = EnsureQueries(sc, batch);
@@ -662,7 +724,8 @@ class LimbGemmImpl : public LimbGemm {
     a.out_stride = rows_;
     const int nqt = static_cast<int>(bpad / kTileQ);
     const int64_t tiles = (rows_ / kTileRows) * nqt;
-    a.ksplit = ChooseSplit(tiles, a.n_db_units + 2 * a.n_pk_blocks);
+    a.ksplit = force_split > 0 ? force_split
+                               : Split(bpad, tiles, a.n_db_units + 2 * a.n_pk_blocks);
     if (a.ksplit > 1) {
       e = cudaMemsetAsync(out, 0, static_cast<size_t>(batch) * rows_ * 4, st);
       if (e != cudaSuccess) return e;
@@ -672,6 +735,17 @@ class LimbGemmImpl : public LimbGemm {
         tm_db_, tm_pk_, sc->tm_q, sc->tm_y, a, sc->qsum, static_cast<uint32_t*>(out),
         err_);
     return cudaGetLastError();
+  }
+
+  // The tuned split-K factor for this padded batch size, else the
+  // heuristic one.
+  int Split(int64_t bpad, int64_t tiles, int n_units) {
+    {
+      std::lock_guard<std::mutex> lk(tune_mu_);
+      auto it = tuned_.find(bpad);
+      if (it != tuned_.end()) return it->second;
+    }
+    return ChooseSplit(tiles, n_units);
   }
 
   // Split-K factor that fills the SMs in whole waves (one CTA per SM).
@@ -706,6 +780,8 @@ class LimbGemmImpl : public LimbGemm {
   __half *db_planes_ = nullptr, *pk_planes_ = nullptr;
   int* err_ = nullptr;
   CUtensorMap tm_db_{}, tm_pk_{};
+  std::mutex tune_mu_;
+  std::map<int64_t, int> tuned_;  // padded batch size -> split-K factor
 };
 
 }  // namespace

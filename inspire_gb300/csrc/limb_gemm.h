@@ -33,6 +33,13 @@ class LimbGemm {
   virtual cudaError_t Run(int batch, const void* q1, int64_t q1_stride,
                           const void* yg, int64_t yg_stride, void* out,
                           LimbScratch* scratch, cudaStream_t stream) = 0;
+  // Autotuner: times the split-K factors for this batch size on these
+  // operands, keeps the fastest for later Runs of the same padded batch
+  // size and reports it. Synchronises the stream.
+  virtual cudaError_t Tune(int batch, const void* q1, int64_t q1_stride,
+                           const void* yg, int64_t yg_stride, void* out,
+                           LimbScratch* scratch, cudaStream_t stream,
+                           int* chosen, float* best_ms) = 0;
   // Returns (and clears) the kernel's error flag: non-zero when a pipeline
   // wait timed out in a previous launch. Synchronous.
   virtual int CheckError() = 0;

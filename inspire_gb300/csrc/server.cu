@@ -1216,6 +1216,43 @@ void inspire_graph_destroy(inspire_graph* graph) {
   delete graph;
 }
 
+int inspire_pir_autotune(inspire_pir_server* server, int32_t batch,
+                         int32_t* split, float* ms, char* err, size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr || batch <= 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server is null or batch <= 0."),
+                  err, err_len);
+  }
+  if (!server->limb) {
+    return Report(Err(INSPIRE_FAILED_PRECONDITION,
+                      "tensor engine unavailable for these parameters"),
+                  err, err_len);
+  }
+  std::lock_guard<std::mutex> lock(server->mu);
+  Workspace* ws = server->ws0.get();
+  Status st = EnsureWorkspace(server, ws, batch);
+  if (st.ok() && !ws->limb) ws->limb = server->limb->NewScratch();
+  if (st.ok()) {
+    // The workspace's request buffers are timed as they are: the kernels'
+    // work does not depend on the operand values.
+    st = Cuda(cudaMemsetAsync(ws->q1.get(), 0, ws->q1.bytes(), ws->stream), "memset");
+  }
+  int chosen = 0;
+  float best = 0;
+  if (st.ok()) {
+    st = Cuda(server->limb->Tune(batch, ws->q1.get(), server->db_cols, ws->pkey.get(),
+                                 static_cast<int64_t>(2 * server->k) * server->d,
+                                 ws->gemv.get(), ws->limb.get(), ws->stream, &chosen,
+                                 &best),
+              "autotune");
+  }
+  if (st.ok()) {
+    if (split) *split = chosen;
+    if (ms) *ms = best;
+  }
+  return Report(st, err, err_len);
+}
+
 int inspire_pir_server_check(inspire_pir_server* server, char* err,
                              size_t err_len) {
   using namespace inspire;

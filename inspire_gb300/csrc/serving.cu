@@ -234,8 +234,12 @@ struct Queue {
 
 class Engine {
  public:
-  Engine(std::unique_ptr<Backend> b, int max_batch, int plain_max_batch)
-      : be_(std::move(b)), max_batch_(max_batch), plain_max_(plain_max_batch) {}
+  Engine(std::unique_ptr<Backend> b, int max_batch, int plain_max_batch,
+         int max_wait_us)
+      : be_(std::move(b)),
+        max_batch_(max_batch),
+        plain_max_(plain_max_batch),
+        wait_(std::chrono::microseconds(max_wait_us)) {}
 
   ~Engine() {
     {
@@ -449,9 +453,30 @@ class Engine {
     }
   }
 
+  // A queue's batch is ready when it is full, when the batching window is
+  // off, or when its oldest request has waited the window out.
+  bool Ready(const Ring& r, int n, Clock::time_point now,
+             Clock::time_point* due) const {
+    if (n >= max_batch_ || wait_.count() == 0 || stop_) return true;
+    const Clock::time_point d = r.t_submit[r.next_launch % r.cap] + wait_;
+    if (now >= d) return true;
+    *due = std::min(*due, d);
+    return false;
+  }
+
+  int Queued(const Ring& r) const {
+    int n = 0;
+    while (n < max_batch_ && r.next_launch + n < r.head &&
+           r.state[(r.next_launch + n) % r.cap] == kQueued) {
+      ++n;
+    }
+    return n;
+  }
+
   void Loop() {
     for (;;) {
       bool progressed = false;
+      Clock::time_point due = Clock::time_point::max();
       // Retire finished batches, oldest first per queue.
       for (int q = 0; q < static_cast<int>(q_.size()); ++q) {
         Queue& qq = q_[q];
@@ -486,11 +511,7 @@ class Engine {
             std::lock_guard<std::mutex> lk(mu_);
             Ring& r = qq.ring;
             if (qq.free_ws.empty()) break;
-            int n = 0;
-            while (n < max_batch_ && r.next_launch + n < r.head &&
-                   r.state[(r.next_launch + n) % r.cap] == kQueued) {
-              ++n;
-            }
+            const int n = Queued(r);
             // Slots that failed validation at submit are skipped over.
             if (n == 0) {
               while (r.next_launch < r.head &&
@@ -500,6 +521,7 @@ class Engine {
               }
               break;
             }
+            if (!Ready(r, n, Clock::now(), &due)) break;
             b.first = r.next_launch;
             b.n = n;
             b.ws = qq.free_ws.back();
@@ -547,24 +569,28 @@ class Engine {
       if (!progressed) {
         std::unique_lock<std::mutex> lk(mu_);
         bool busy = false, pending = false;
+        const Clock::time_point now = Clock::now();
         for (const Queue& qq : q_) {
           busy = busy || !qq.inflight.empty();
           const Ring& r = qq.ring;
-          pending = pending || (r.next_launch < r.head &&
-                                r.state[r.next_launch % r.cap] == kQueued &&
-                                !qq.free_ws.empty());
+          const int n = Queued(r);
+          pending = pending || (n > 0 && !qq.free_ws.empty() && Ready(r, n, now, &due));
         }
         if (stop_ && !busy) return;
         if (pending) continue;
-        // Poll the device while batches run; sleep until a submit otherwise.
-        cv_work_.wait_for(lk, busy ? std::chrono::microseconds(50)
-                                   : std::chrono::microseconds(20000));
+        // Poll the device while batches run, wake for the next batching
+        // window to close, sleep until a submit otherwise.
+        Clock::duration wait = busy ? Clock::duration(std::chrono::microseconds(50))
+                                    : Clock::duration(std::chrono::milliseconds(20));
+        if (due != Clock::time_point::max()) wait = std::min(wait, due - now);
+        if (wait > Clock::duration::zero()) cv_work_.wait_for(lk, wait);
       }
     }
   }
 
   std::unique_ptr<Backend> be_;
   int max_batch_, plain_max_;
+  Clock::duration wait_;
   std::vector<Queue> q_;
   std::mutex mu_;
   std::condition_variable cv_work_, cv_done_, cv_space_;
@@ -592,11 +618,12 @@ int Report(int code, const std::string& msg, char* err, size_t err_len) {
 }
 
 int Start(std::unique_ptr<inspire::Backend> be, int32_t max_batch,
-          int32_t plain_max_batch, int32_t ring_slots, inspire_serving** out,
-          char* err, size_t err_len) {
+          int32_t plain_max_batch, int32_t max_wait_us, int32_t ring_slots,
+          inspire_serving** out, char* err, size_t err_len) {
   std::string msg;
   std::unique_ptr<inspire_serving> s(new inspire_serving());
-  s->engine.reset(new inspire::Engine(std::move(be), max_batch, plain_max_batch));
+  s->engine.reset(new inspire::Engine(std::move(be), max_batch, plain_max_batch,
+                                      max_wait_us));
   const int rc = s->engine->Init(ring_slots, &msg);
   if (rc != INSPIRE_OK) return Report(rc, msg, err, err_len);
   *out = s.release();
@@ -609,11 +636,11 @@ extern "C" {
 
 int inspire_serving_create(inspire_pir_server* const* servers, int32_t n_servers,
                            int32_t max_batch, int32_t plain_max_batch,
-                           int32_t ring_slots, int64_t hbm_budget,
-                           int32_t max_workspaces, inspire_serving** out,
-                           char* err, size_t err_len) {
+                           int32_t max_wait_us, int32_t ring_slots,
+                           int64_t hbm_budget, int32_t max_workspaces,
+                           inspire_serving** out, char* err, size_t err_len) {
   if (out == nullptr || servers == nullptr || n_servers <= 0 || max_batch <= 0 ||
-      ring_slots < max_batch || max_workspaces <= 0) {
+      ring_slots < max_batch || max_workspaces <= 0 || max_wait_us < 0) {
     return Report(INSPIRE_INVALID_ARGUMENT,
                   "servers/out must be set, max_batch > 0, ring_slots >= "
                   "max_batch and max_workspaces > 0.",
@@ -624,23 +651,26 @@ int inspire_serving_create(inspire_pir_server* const* servers, int32_t n_servers
   std::unique_ptr<inspire::PirBackend> be(new inspire::PirBackend());
   const int rc = be->Init(servers, n_servers, max_batch, hbm_budget, max_workspaces, &msg);
   if (rc != INSPIRE_OK) return Report(rc, msg, err, err_len);
-  return Start(std::move(be), max_batch, plain_max_batch, ring_slots, out, err, err_len);
+  return Start(std::move(be), max_batch, plain_max_batch, max_wait_us, ring_slots, out,
+               err, err_len);
 }
 
 int inspire_serving_create_loopback(int32_t n_queues, const int64_t* slot_words,
                                     int32_t workspaces, int32_t delay_us,
                                     int32_t max_batch, int32_t plain_max_batch,
-                                    int32_t ring_slots, inspire_serving** out,
-                                    char* err, size_t err_len) {
+                                    int32_t max_wait_us, int32_t ring_slots,
+                                    inspire_serving** out, char* err,
+                                    size_t err_len) {
   if (out == nullptr || slot_words == nullptr || n_queues <= 0 || workspaces <= 0 ||
-      max_batch <= 0 || ring_slots < max_batch || delay_us < 0) {
+      max_batch <= 0 || ring_slots < max_batch || delay_us < 0 || max_wait_us < 0) {
     return Report(INSPIRE_INVALID_ARGUMENT, "invalid loopback configuration.", err,
                   err_len);
   }
   *out = nullptr;
   std::unique_ptr<inspire::Backend> be(
       new inspire::LoopbackBackend(n_queues, slot_words, workspaces, delay_us));
-  return Start(std::move(be), max_batch, plain_max_batch, ring_slots, out, err, err_len);
+  return Start(std::move(be), max_batch, plain_max_batch, max_wait_us, ring_slots, out,
+               err, err_len);
 }
 
 void inspire_serving_destroy(inspire_serving* s) { delete s; }

@@ -344,6 +344,16 @@ class PirServer:
             ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream), err, len(err))
         _check(rc, err)
 
+    def autotune(self, batch):
+        """Tunes the tensor engine's split-K factor for this batch size;
+        returns (factor, product ms)."""
+        err = _errbuf()
+        k, ms = ctypes.c_int32(), ctypes.c_float()
+        _check(_lib.load().inspire_pir_autotune(self._h, batch, ctypes.byref(k),
+                                                ctypes.byref(ms), err, len(err)),
+               err)
+        return k.value, ms.value
+
     def check(self):
         """Raises if a tensor-engine launch recorded a pipeline timeout."""
         err = _errbuf()

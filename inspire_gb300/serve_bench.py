@@ -112,6 +112,7 @@ def main(argv=None):
         if args.small:
             n //= 16
         params, srv = make_server(n, d, t, l, seed=1000 + 10 * i)
+        srv.autotune(args.max_batch)
         fd, sd, pk = synthetic.make_requests(params, args.pool, seed=2000 + i)
         alone = np.stack([srv.process_arrays(fd[j:j + 1], sd[j:j + 1],
                                              pk[j:j + 1])[0]

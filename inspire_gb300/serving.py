@@ -59,13 +59,15 @@ class ServingEngine:
     device bytes the workspaces of all servers may take (split evenly);
     each server gets between 1 and max_workspaces of them. plain_max_batch:
     batches up to this size use the plain engine, larger ones the tensor
-    engine when the server has it. ring_slots: request slots per server
+    engine when the server has it. max_wait_us: batching window (a partial
+    batch waits until its oldest request has waited this long; 0 launches as
+    soon as a workspace is free). ring_slots: request slots per server
     (default 4 * max_batch).
     """
 
     def __init__(self, servers, max_batch=256, hbm_budget=8 << 30,
-                 max_workspaces=3, plain_max_batch=4, ring_slots=None,
-                 _loopback=None):
+                 max_workspaces=3, plain_max_batch=4, max_wait_us=0,
+                 ring_slots=None, _loopback=None):
         self._lib = _lib.load()
         self.max_batch = max_batch
         ring_slots = ring_slots or 4 * max_batch
@@ -74,12 +76,12 @@ class ServingEngine:
         self.queues = {}
         if _loopback is None:
             names = list(servers)
-            arr = (ctypes.c_void_p * len(names))(*[servers[n]._h.value
-                                                   if isinstance(servers[n]._h, ctypes.c_void_p)
-                                                   else servers[n]._h for n in names])
+            arr = (ctypes.c_void_p * len(names))(
+                *[servers[n]._h.value for n in names])
             rc = self._lib.inspire_serving_create(
-                arr, len(names), max_batch, plain_max_batch, ring_slots,
-                int(hbm_budget), max_workspaces, ctypes.byref(h), err, len(err))
+                arr, len(names), max_batch, plain_max_batch, max_wait_us,
+                ring_slots, int(hbm_budget), max_workspaces, ctypes.byref(h),
+                err, len(err))
             pir._check(rc, err)
             for i, n in enumerate(names):
                 s = servers[n]
@@ -94,7 +96,8 @@ class ServingEngine:
             w = (ctypes.c_int64 * (4 * len(names)))(*[x for q in words for x in q])
             rc = self._lib.inspire_serving_create_loopback(
                 len(names), w, workspaces, delay_us, max_batch,
-                plain_max_batch, ring_slots, ctypes.byref(h), err, len(err))
+                plain_max_batch, max_wait_us, ring_slots, ctypes.byref(h), err,
+                len(err))
             pir._check(rc, err)
             for i, (n, q) in enumerate(zip(names, words)):
                 # Loopback slots: flat u32 words (d = 1 polynomial rows).

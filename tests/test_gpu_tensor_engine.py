@@ -172,6 +172,17 @@ def test_tensor_engine_repeated_batches_reuse_buffers():
                               srv.process_arrays(fd, sd, pk, pir.ENGINE_PLAIN))
 
 
+def test_autotuned_split_keeps_responses_identical():
+    params = synthetic.make_params(d=256, n=4 * 16384, t=4, coeff_bits=32)
+    mat = synthetic.make_material(params, seed=21)
+    srv = _server(params, mat)
+    split, ms = srv.autotune(100)
+    assert split >= 1 and ms > 0
+    fd, sd, pk = synthetic.make_requests(params, 100, seed=22, full_range=True)
+    assert np.array_equal(srv.process_arrays(fd, sd, pk, pir.ENGINE_TENSOR),
+                          srv.process_arrays(fd, sd, pk, pir.ENGINE_PLAIN))
+
+
 def test_tensor_engine_unavailable_for_u64():
     params = synthetic.make_params(d=128, n=8192, t=2, coeff_bits=64, log_q=52)
     mat = synthetic.make_material(params, seed=1, pad_to=32)
@@ -179,3 +190,5 @@ def test_tensor_engine_unavailable_for_u64():
     fd, sd, pk = synthetic.make_requests(params, 1)
     with pytest.raises(pir.InspireError, match="tensor engine unavailable"):
         srv.process_arrays(fd, sd, pk, pir.ENGINE_TENSOR)
+    with pytest.raises(pir.InspireError, match="tensor engine unavailable"):
+        srv.autotune(8)

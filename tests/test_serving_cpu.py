@@ -65,6 +65,24 @@ def test_requests_queued_while_busy_are_batched():
     assert st["max_inflight"] == 1
 
 
+def test_batching_window_groups_light_traffic():
+    # Requests trickle in one by one with a free workspace each time: with
+    # no window every request is its own batch, with a window they group.
+    import time
+    for window, expect_grouped in ((0, False), (30000, True)):
+        with serving.ServingEngine.loopback({"A": (4, 0, 2, 2)}, workspaces=4,
+                                            delay_us=50, max_batch=64,
+                                            max_wait_us=window) as eng:
+            futs = []
+            for i in range(20):
+                futs.append(eng.submit("A", *_req(eng, "A", i)))
+                time.sleep(0.001)
+            for i, f in enumerate(futs):
+                assert np.array_equal(f.result(timeout=30), _want(eng, "A", i))
+            st = eng.stats()
+        assert (st["mean_batch"] > 2) == expect_grouped, (window, st)
+
+
 def test_workspaces_overlap():
     with serving.ServingEngine.loopback({"A": (4, 0, 2, 2)}, workspaces=3,
                                         delay_us=20000, max_batch=2) as eng:
@@ -148,10 +166,10 @@ def test_bad_ticket_and_arguments(lib):
     import ctypes
     h = ctypes.c_void_p()
     words = (ctypes.c_int64 * 4)(4, 0, 2, 2)
-    rc = lib.inspire_serving_create_loopback(1, words, 1, 0, 8, 2, 4,
+    rc = lib.inspire_serving_create_loopback(1, words, 1, 0, 8, 2, 0, 4,
                                              ctypes.byref(h), err, len(err))
     assert rc == pir.INVALID_ARGUMENT       # ring_slots < max_batch
-    rc = lib.inspire_serving_create_loopback(1, words, 1, 0, 8, 2, 8,
+    rc = lib.inspire_serving_create_loopback(1, words, 1, 0, 8, 2, 0, 8,
                                              ctypes.byref(h), err, len(err))
     assert rc == 0
     try:

@@ -125,6 +125,158 @@ __device__ __forceinline__ void ntt_inverse(uint32_t* a, const NttCtx& c,
   }
 }
 
+// The same transforms with ITERS quads per thread per double stage known at
+// compile time (blockDim.x * 4 * ITERS == d): every quad's operands and
+// twiddles are loaded before any butterfly, so the loads of a stage overlap
+// instead of one quad's latency following another's. ITERS == 0 falls back
+// to the loops above (any d and block size).
+template <int ITERS>
+__device__ __forceinline__ void ntt_forward_t(uint32_t* a, const NttCtx& c,
+                                              int pi) {
+  if constexpr (ITERS == 0) {
+    ntt_forward(a, c, pi);
+  } else {
+    const uint32_t p = c.p[pi];
+    const int d = 1 << c.logd;
+    const uint32_t* tw = c.tables + static_cast<size_t>(pi) * 4 * d;
+    const uint32_t* tws = tw + d;
+    __syncthreads();
+    int lt = c.logd - 1;
+    int m = 1;
+    for (; lt >= 1; lt -= 2, m <<= 2) {
+      const int t = 1 << lt;
+      const int lh = lt - 1;
+      uint32_t x[ITERS][4], w[ITERS][6];
+      int jj[ITERS];
+#pragma unroll
+      for (int it = 0; it < ITERS; ++it) {
+        const int b = threadIdx.x + it * blockDim.x;
+        const int i = b >> lh;
+        const int j = (i << (lt + 1)) | (b & ((t >> 1) - 1));
+        jj[it] = j;
+        w[it][0] = __ldg(tw + m + i);
+        w[it][1] = __ldg(tws + m + i);
+        w[it][2] = __ldg(tw + 2 * m + 2 * i);
+        w[it][3] = __ldg(tws + 2 * m + 2 * i);
+        w[it][4] = __ldg(tw + 2 * m + 2 * i + 1);
+        w[it][5] = __ldg(tws + 2 * m + 2 * i + 1);
+        x[it][0] = a[j];
+        x[it][1] = a[j + (t >> 1)];
+        x[it][2] = a[j + t];
+        x[it][3] = a[j + t + (t >> 1)];
+      }
+#pragma unroll
+      for (int it = 0; it < ITERS; ++it) {
+        uint32_t x0 = x[it][0], x1 = x[it][1], x2 = x[it][2], x3 = x[it][3];
+        uint32_t v = shoup_mul(x2, w[it][0], w[it][1], p);
+        x2 = sub_mod(x0, v, p);
+        x0 = add_mod(x0, v, p);
+        v = shoup_mul(x3, w[it][0], w[it][1], p);
+        x3 = sub_mod(x1, v, p);
+        x1 = add_mod(x1, v, p);
+        const int j = jj[it];
+        v = shoup_mul(x1, w[it][2], w[it][3], p);
+        a[j + (t >> 1)] = sub_mod(x0, v, p);
+        a[j] = add_mod(x0, v, p);
+        v = shoup_mul(x3, w[it][4], w[it][5], p);
+        a[j + t + (t >> 1)] = sub_mod(x2, v, p);
+        a[j + t] = add_mod(x2, v, p);
+      }
+      __syncthreads();
+    }
+    if (lt == 0) {  // one radix-2 stage left (t = 1)
+      uint32_t u[2 * ITERS], v[2 * ITERS], w[2 * ITERS], ws[2 * ITERS];
+#pragma unroll
+      for (int it = 0; it < 2 * ITERS; ++it) {
+        const int b = threadIdx.x + it * blockDim.x;
+        u[it] = a[2 * b];
+        v[it] = a[2 * b + 1];
+        w[it] = __ldg(tw + m + b);
+        ws[it] = __ldg(tws + m + b);
+      }
+#pragma unroll
+      for (int it = 0; it < 2 * ITERS; ++it) {
+        const int b = threadIdx.x + it * blockDim.x;
+        const uint32_t y = shoup_mul(v[it], w[it], ws[it], p);
+        a[2 * b] = add_mod(u[it], y, p);
+        a[2 * b + 1] = sub_mod(u[it], y, p);
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <int ITERS>
+__device__ __forceinline__ void ntt_inverse_t(uint32_t* a, const NttCtx& c,
+                                              int pi) {
+  if constexpr (ITERS == 0) {
+    ntt_inverse(a, c, pi);
+  } else {
+    const uint32_t p = c.p[pi];
+    const int d = 1 << c.logd;
+    const uint32_t* itw = c.tables + static_cast<size_t>(pi) * 4 * d + 2 * d;
+    const uint32_t* itws = itw + d;
+    __syncthreads();
+    int lt = 0;
+    int h = d >> 1;
+    for (; lt + 1 < c.logd; lt += 2, h >>= 2) {
+      const int t = 1 << lt;
+      uint32_t x[ITERS][4], w[ITERS][6];
+      int jj[ITERS];
+#pragma unroll
+      for (int it = 0; it < ITERS; ++it) {
+        const int b = threadIdx.x + it * blockDim.x;
+        const int i = b >> lt;
+        const int j = (i << (lt + 2)) | (b & (t - 1));
+        jj[it] = j;
+        w[it][0] = __ldg(itw + h + 2 * i);
+        w[it][1] = __ldg(itws + h + 2 * i);
+        w[it][2] = __ldg(itw + h + 2 * i + 1);
+        w[it][3] = __ldg(itws + h + 2 * i + 1);
+        w[it][4] = __ldg(itw + (h >> 1) + i);
+        w[it][5] = __ldg(itws + (h >> 1) + i);
+        x[it][0] = a[j];
+        x[it][1] = a[j + t];
+        x[it][2] = a[j + 2 * t];
+        x[it][3] = a[j + 3 * t];
+      }
+#pragma unroll
+      for (int it = 0; it < ITERS; ++it) {
+        const uint32_t y0 = add_mod(x[it][0], x[it][1], p);
+        const uint32_t y1 =
+            shoup_mul(sub_mod(x[it][0], x[it][1], p), w[it][0], w[it][1], p);
+        const uint32_t y2 = add_mod(x[it][2], x[it][3], p);
+        const uint32_t y3 =
+            shoup_mul(sub_mod(x[it][2], x[it][3], p), w[it][2], w[it][3], p);
+        const int j = jj[it];
+        a[j] = add_mod(y0, y2, p);
+        a[j + 2 * t] = shoup_mul(sub_mod(y0, y2, p), w[it][4], w[it][5], p);
+        a[j + t] = add_mod(y1, y3, p);
+        a[j + 3 * t] = shoup_mul(sub_mod(y1, y3, p), w[it][4], w[it][5], p);
+      }
+      __syncthreads();
+    }
+    if (lt < c.logd) {  // one radix-2 stage left (h = 1, t = d/2)
+      const int t = 1 << lt;
+      const uint32_t w = __ldg(itw + 1), ws = __ldg(itws + 1);
+      uint32_t u[2 * ITERS], v[2 * ITERS];
+#pragma unroll
+      for (int it = 0; it < 2 * ITERS; ++it) {
+        const int b = threadIdx.x + it * blockDim.x;
+        u[it] = a[b];
+        v[it] = a[b + t];
+      }
+#pragma unroll
+      for (int it = 0; it < 2 * ITERS; ++it) {
+        const int b = threadIdx.x + it * blockDim.x;
+        a[b] = add_mod(u[it], v[it], p);
+        a[b + t] = shoup_mul(sub_mod(u[it], v[it], p), w, ws, p);
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // Garner reconstruction: x[i] < p_i -> the integer in
 // [-(p_{r-1}-1)/2 * P', (p_{r-1}+1)/2 * P') (P' = product of the other
 // primes) congruent to x, reduced mod 2^w.

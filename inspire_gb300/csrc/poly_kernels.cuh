@@ -17,6 +17,19 @@ namespace inspire {
 constexpr int kPolyThreads = 512;
 constexpr int kMaxPer = 16;  // d / kPolyThreads for d <= 8192
 
+// Kernels templated on ITERS (quads per thread per NTT double stage, so
+// blockDim.x = d / (4 * ITERS)) keep PolyPer<ITERS> coefficients per thread;
+// ITERS == 0 is the generic form (any block size, up to kMaxPer each).
+// ITERS == 4 is the throughput shape of d <= 4096 (d/16 <= 256 threads,
+// three blocks per SM); 1 and 2 run up to 1024 threads per block.
+template <int ITERS>
+struct PolyShape {
+  static constexpr int kPer = ITERS == 0 ? kMaxPer : 4 * ITERS;
+  static constexpr int kMaxThreads =
+      ITERS == 4 ? 256 : ((ITERS == 1 || ITERS == 2) ? 1024 : kPolyThreads);
+  static constexpr int kMinBlocks = ITERS == 4 ? 3 : 1;
+};
+
 template <typename T>
 struct Bits {
   static constexpr int value = 8 * sizeof(T);
@@ -70,8 +83,8 @@ __device__ __forceinline__ T gadget_digit(T c, int log_modulus, int log_digit,
 
 // Forward NTT of CoeffType polynomials (masked to the bits the reference's
 // chunk rule reads). grid.x = npoly * r, grid.y = batch.
-template <typename T>
-__global__ void __launch_bounds__(kPolyThreads)
+template <typename T, int ITERS = 0>
+__global__ void __launch_bounds__(PolyShape<ITERS>::kMaxThreads, PolyShape<ITERS>::kMinBlocks)
 ntt_coeffs_kernel(const T* __restrict__ src, int64_t src_qstride,
                   int64_t src_off, int npoly, T mask, uint32_t* __restrict__ dst,
                   int64_t poly_stride, NttCtx c) {
@@ -85,7 +98,7 @@ ntt_coeffs_kernel(const T* __restrict__ src, int64_t src_qstride,
   for (int j = threadIdx.x; j < d; j += blockDim.x) {
     smem[j] = to_residue<T>(in[j] & mask, p);
   }
-  ntt_forward(smem, c, pi);
+  ntt_forward_t<ITERS>(smem, c, pi);
   uint32_t* out = dst + ((static_cast<int64_t>(q) * npoly + poly) * c.r + pi) * d;
   for (int j = threadIdx.x; j < d; j += blockDim.x) out[j] = smem[j];
 }
@@ -151,8 +164,8 @@ inner_product_finish_kernel(const uint32_t* __restrict__ U,
 // gemv already holds b' + b_agg_partial (optionally split in two vectors).
 // grid.x = l * t slices, grid.y = batch. Th: [l*t][k][r][d] (Montgomery-free
 // plain residues), Yh: [batch][k][r][d].
-template <typename T>
-__global__ void __launch_bounds__(kPolyThreads)
+template <typename T, int ITERS = 0>
+__global__ void __launch_bounds__(PolyShape<ITERS>::kMaxThreads, PolyShape<ITERS>::kMinBlocks)
 finalize_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ Yh,
                 int k, const T* __restrict__ gemv, const T* __restrict__ gemv2,
                 int64_t gemv_qstride, T* __restrict__ packed_b,
@@ -173,7 +186,7 @@ finalize_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ Yh
       }
       a[j] = acc;
     }
-    ntt_inverse(a, c, pi);
+    ntt_inverse_t<ITERS>(a, c, pi);
   }
   const int64_t base = q * gemv_qstride + static_cast<int64_t>(s) * d;
   T* outp = packed_b + (static_cast<int64_t>(q) * gridDim.x + s) * d;
@@ -259,8 +272,8 @@ __device__ __forceinline__ void horner_state(
 // grid = (r, l, batch). RGSWa: [2ne][r][d] (server; rgswa_qstride = 0) or
 // [batch][2ne][r][d] (rgswa_qstride = 2ne*r*d), RGSWb: [batch][2ne][r][d]. coeff_a/coeff_b select the packed
 // ciphertext added to the previous product (or the initial state).
-template <typename T>
-__global__ void __launch_bounds__(kPolyThreads)
+template <typename T, int ITERS = 0>
+__global__ void __launch_bounds__(PolyShape<ITERS>::kMaxThreads, PolyShape<ITERS>::kMinBlocks)
 ext_step_kernel(bool first, const uint32_t* __restrict__ resid_in,
                 uint32_t* __restrict__ resid_out,
                 const T* __restrict__ coeff_a, int64_t coeff_a_q_stride,
@@ -289,9 +302,10 @@ ext_step_kernel(bool first, const uint32_t* __restrict__ resid_in,
     sa[j] = low_bits<T>(ra, e.log_q);
     sb[j] = low_bits<T>(rb, e.log_q);
   }
-  uint32_t acc_a[kMaxPer], acc_b[kMaxPer];
+  constexpr int kPer = PolyShape<ITERS>::kPer;
+  uint32_t acc_a[kPer], acc_b[kPer];
 #pragma unroll
-  for (int m = 0; m < kMaxPer; ++m) acc_a[m] = acc_b[m] = 0;
+  for (int m = 0; m < kPer; ++m) acc_a[m] = acc_b[m] = 0;
 
   const int ng = 2 * e.num_digits;
   for (int g = 0; g < ng; ++g) {
@@ -303,13 +317,13 @@ ext_step_kernel(bool first, const uint32_t* __restrict__ resid_in,
       const T dig = gadget_digit<T>(src[j], e.log_q, e.log_digit, e.num_digits, dg);
       smem[j] = to_residue<T>(dig & static_cast<T>(e.umask), p);
     }
-    ntt_forward(smem, c, pi);
+    ntt_forward_t<ITERS>(smem, c, pi);
     const uint32_t* wa =
         RGSWa + q * rgswa_qstride + (static_cast<int64_t>(g) * c.r + pi) * d;
     const uint32_t* wb =
         RGSWb + ((static_cast<int64_t>(q) * ng + g) * c.r + pi) * d;
 #pragma unroll
-    for (int m = 0; m < kMaxPer; ++m) {
+    for (int m = 0; m < kPer; ++m) {
       const int j = threadIdx.x + m * blockDim.x;
       if (j < d) {
         const uint32_t x = smem[j];
@@ -322,11 +336,11 @@ ext_step_kernel(bool first, const uint32_t* __restrict__ resid_in,
   for (int half = 0; half < 2; ++half) {
     __syncthreads();
 #pragma unroll
-    for (int m = 0; m < kMaxPer; ++m) {
+    for (int m = 0; m < kPer; ++m) {
       const int j = threadIdx.x + m * blockDim.x;
       if (j < d) smem[j] = half == 0 ? acc_a[m] : acc_b[m];
     }
-    ntt_inverse(smem, c, pi);
+    ntt_inverse_t<ITERS>(smem, c, pi);
     for (int j = threadIdx.x; j < d; j += blockDim.x) {
       out[half * d + j] = shoup_mul(smem[j], c.scale[pi], c.scale_s[pi], p);
     }

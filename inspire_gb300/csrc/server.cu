@@ -361,6 +361,7 @@ struct inspire_pir_server {
   int interpolated_rows = 0;
   inspire::Status deferred;  // error the reference reports per request
   inspire::Status eval_rule;  // chunk rule of the eval-gadget inner product
+  int sms = 152;               // streaming multiprocessors of the device
 
   inspire::DevBuf db, pack, a_tilde, th_ntt, rgswa_ntt;
   std::unique_ptr<inspire::NttTables> tables;
@@ -389,6 +390,68 @@ namespace {
 // that batches fill the SMs without a wave tail.
 inline int PolyThreads(int d) { return d <= 16 * 256 ? 256 : kPolyThreads; }
 
+// Block shape of an NTT kernel launch of `ctas` blocks. Throughput shape
+// while the launch has at least one block per SM: d/16 threads for
+// 512 <= d <= 4096 (16 coefficients each, three blocks per SM), 1024 threads
+// for d = 8192. Latency shape for smaller launches: d/4 threads (up to 1024),
+// which shortens the chain of the few blocks of a small batch. iters = quads
+// per thread per NTT double stage (0: the generic loops).
+struct PolyLaunch {
+  int nt;
+  int iters;
+};
+PolyLaunch PolyShapeFor(int d, int64_t ctas, int sms) {
+  int nt;
+  if (ctas < sms) {
+    nt = std::min(1024, std::max(1, d / 4));
+  } else if (d >= 512 && d <= 4096) {
+    nt = d / 16;
+  } else if (d == 8192) {
+    nt = 1024;
+  } else {
+    nt = PolyThreads(d);
+  }
+  const int q = d / 4;
+  const int it = q % nt == 0 ? q / nt : 0;
+  if (it == 1 || it == 2 || it == 4) return PolyLaunch{nt, it};
+  return PolyLaunch{PolyThreads(d), 0};
+}
+
+#define INSPIRE_ITERS_DISPATCH(iters, ...)  \
+  switch (iters) {                          \
+    case 1: {                               \
+      constexpr int IT = 1;                 \
+      __VA_ARGS__;                          \
+    } break;                                \
+    case 2: {                               \
+      constexpr int IT = 2;                 \
+      __VA_ARGS__;                          \
+    } break;                                \
+    case 4: {                               \
+      constexpr int IT = 4;                 \
+      __VA_ARGS__;                          \
+    } break;                                \
+    default: {                              \
+      constexpr int IT = 0;                 \
+      __VA_ARGS__;                          \
+    } break;                                \
+  }
+
+// Forward NTTs of npoly CoeffType polynomials per request (stride
+// poly_stride words, masked), batch requests src_qstride words apart.
+template <typename T>
+Status NttCoeffs(const inspire_pir_server* s, const T* src, int64_t src_qstride,
+                 int64_t src_off, int npoly, T mask, uint32_t* dst,
+                 int64_t poly_stride, const NttCtx& c, int batch, cudaStream_t st) {
+  const int d = s->d;
+  const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(npoly) * c.r * batch, s->sms);
+  dim3 grid(npoly * c.r, batch);
+  INSPIRE_ITERS_DISPATCH(pl.iters, ntt_coeffs_kernel<T, IT><<<grid, pl.nt, d * 4, st>>>(
+                                       src, src_qstride, src_off, npoly, mask, dst,
+                                       poly_stride, c));
+  return Cuda(cudaGetLastError(), "forward NTT");
+}
+
 // FinalizeMatrixPack for every shard of every request of a batch
 // (lwes_to_rlwe.cc:448-479): w->packed[q][shard] = b_agg.
 template <typename T>
@@ -396,24 +459,21 @@ Status FinalizeStage(inspire_pir_server* s, Workspace* w, int batch,
                      const T* pkey, const T* gemv, cudaStream_t st) {
   const int d = s->d, t = s->t, l = s->l, k = s->k;
   const int log_q = s->prm.log_modulus;
-  const int nt = PolyThreads(d);
   // y_h = packing_key[k..2k): forward NTT over the finalize primes.
-  {
-    const NttCtx& c = s->ctx_f;
-    dim3 grid(k * c.r, batch);
-    ntt_coeffs_kernel<T><<<grid, nt, d * 4, st>>>(
-        pkey, static_cast<int64_t>(2 * k) * d, static_cast<int64_t>(k) * d, k,
-        static_cast<T>(s->vmask_f), w->yh.get<uint32_t>(), d, c);
-    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "ntt(y_h)"));
-  }
+  RETURN_IF_ERROR(NttCoeffs<T>(s, pkey, static_cast<int64_t>(2 * k) * d,
+                               static_cast<int64_t>(k) * d, k,
+                               static_cast<T>(s->vmask_f), w->yh.get<uint32_t>(), d,
+                               s->ctx_f, batch, st));
   {
     const NttCtx& c = s->ctx_f;
     const size_t smem = static_cast<size_t>(c.r) * d * 4;
-    RETURN_IF_ERROR(SetSmem(finalize_kernel<T>, smem));
+    const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(l) * t * batch, s->sms);
     dim3 grid(l * t, batch);
-    finalize_kernel<T><<<grid, nt, smem, st>>>(
-        s->th_ntt.get<uint32_t>(), w->yh.get<uint32_t>(), k, gemv, nullptr,
-        s->rows, w->packed.get<T>(), log_q, c);
+    INSPIRE_ITERS_DISPATCH(
+        pl.iters, RETURN_IF_ERROR(SetSmem(finalize_kernel<T, IT>, smem));
+        finalize_kernel<T, IT><<<grid, pl.nt, smem, st>>>(
+            s->th_ntt.get<uint32_t>(), w->yh.get<uint32_t>(), k, gemv, nullptr, s->rows,
+            w->packed.get<T>(), log_q, c));
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "finalize"));
   }
   return Status{};
@@ -435,25 +495,25 @@ Status RunPolyStage(inspire_pir_server* s, Workspace* w, int batch,
   uint32_t* resid[2] = {w->resid0.get<uint32_t>(), w->resid1.get<uint32_t>()};
   if (t > 1) {
     const NttCtx& c = s->ctx_e;
-    dim3 g1(2 * ne * c.r, batch);
-    ntt_coeffs_kernel<T><<<g1, nt, d * 4, st>>>(
-        sdim, static_cast<int64_t>(2 * ne) * d, 0, 2 * ne,
-        static_cast<T>(s->vmask_e), w->rgswb.get<uint32_t>(), d, c);
-    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "ntt(rgsw)"));
+    RETURN_IF_ERROR(NttCoeffs<T>(s, sdim, static_cast<int64_t>(2 * ne) * d, 0, 2 * ne,
+                                 static_cast<T>(s->vmask_e), w->rgswb.get<uint32_t>(),
+                                 d, c, batch, st));
     ExtArgs e{log_q, s->prm.eval_log_digit, ne,
               LiveDigits(log_q, s->prm.eval_log_digit, ne), s->umask_e};
     const size_t smem = static_cast<size_t>(d) * 4 + 2ull * d * sizeof(T);
-    RETURN_IF_ERROR(SetSmem(ext_step_kernel<T>, smem));
+    const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(c.r) * l * batch, s->sms);
     dim3 grid(c.r, l, batch);
-    for (int i = t - 2; i >= 0; --i) {
-      const bool first = i == t - 2;
-      ext_step_kernel<T><<<grid, nt, smem, st>>>(
-          first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
-          a_tilde + static_cast<int64_t>(i + 1) * d, 0, a_stride,
-          packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
-          s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
-      RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
-    }
+    INSPIRE_ITERS_DISPATCH(
+        pl.iters, RETURN_IF_ERROR(SetSmem(ext_step_kernel<T, IT>, smem));
+        for (int i = t - 2; i >= 0; --i) {
+          const bool first = i == t - 2;
+          ext_step_kernel<T, IT><<<grid, pl.nt, smem, st>>>(
+              first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
+              a_tilde + static_cast<int64_t>(i + 1) * d, 0, a_stride,
+              packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
+              s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
+          RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
+        });
   }
   {
     dim3 grid(l, batch);
@@ -639,23 +699,22 @@ Status ExternalOnDevice(inspire_pir_server* s, Workspace* w, int batch,
     using T = decltype(tag);
     const T* rg = static_cast<const T*>(rgsw);
     const int64_t qs = static_cast<int64_t>(2 * ng) * d;
-    ntt_coeffs_kernel<T><<<dim3(ng * c.r, batch), nt, d * 4, st>>>(
-        rg, qs, 0, ng, static_cast<T>(s->vmask_e), w->rgswa.get<uint32_t>(),
-        2 * d, c);
-    ntt_coeffs_kernel<T><<<dim3(ng * c.r, batch), nt, d * 4, st>>>(
-        rg, qs, d, ng, static_cast<T>(s->vmask_e), w->rgswb.get<uint32_t>(),
-        2 * d, c);
-    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "ntt(rgsw)"));
+    RETURN_IF_ERROR(NttCoeffs<T>(s, rg, qs, 0, ng, static_cast<T>(s->vmask_e),
+                                 w->rgswa.get<uint32_t>(), 2 * d, c, batch, st));
+    RETURN_IF_ERROR(NttCoeffs<T>(s, rg, qs, d, ng, static_cast<T>(s->vmask_e),
+                                 w->rgswb.get<uint32_t>(), 2 * d, c, batch, st));
     ExtArgs e{s->prm.log_modulus, s->prm.eval_log_digit, ne,
               LiveDigits(s->prm.log_modulus, s->prm.eval_log_digit, ne),
               s->umask_e};
     const size_t smem = static_cast<size_t>(d) * 4 + 2ull * d * sizeof(T);
-    RETURN_IF_ERROR(SetSmem(ext_step_kernel<T>, smem));
     const T* cta = static_cast<const T*>(ct);
-    ext_step_kernel<T><<<dim3(c.r, 1, batch), nt, smem, st>>>(
-        true, nullptr, w->resid0.get<uint32_t>(), cta, 2 * d, 0, cta + d, 2 * d,
-        0, w->rgswa.get<uint32_t>(), static_cast<int64_t>(ng) * c.r * d,
-        w->rgswb.get<uint32_t>(), e, c);
+    const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(c.r) * batch, s->sms);
+    INSPIRE_ITERS_DISPATCH(
+        pl.iters, RETURN_IF_ERROR(SetSmem(ext_step_kernel<T, IT>, smem));
+        ext_step_kernel<T, IT><<<dim3(c.r, 1, batch), pl.nt, smem, st>>>(
+            true, nullptr, w->resid0.get<uint32_t>(), cta, 2 * d, 0, cta + d, 2 * d, 0,
+            w->rgswa.get<uint32_t>(), static_cast<int64_t>(ng) * c.r * d,
+            w->rgswb.get<uint32_t>(), e, c));
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
     finish_kernel<T><<<dim3(1, batch), nt, 0, st>>>(
         true, w->resid0.get<uint32_t>(), nullptr, 0, nullptr, 0, 0, false, 0, 0,
@@ -882,6 +941,12 @@ Status CreateServer(const inspire_pir_params* prm, const void* db,
         &r_e));
   }
   RETURN_IF_ERROR(NttTables::Create(prm->log_degree, &s->tables));
+  {
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) {
+      cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+  }
   s->ctx_f = s->tables->Ctx(r_f);
   s->ctx_e = s->tables->Ctx(r_e);
 

@@ -275,6 +275,32 @@ def test_server_short_first_dimension_is_zero_padded():
     _server_case(params, np.uint16, np.int32, seed=91, batch=1, pad_to=96)
 
 
+@pytest.mark.parametrize("d,n,t", [(4096, 2 * 4096, 2), (8192, 2 * 1024, 2),
+                                   (2048, 4 * 2048, 4)])
+def test_batch_shapes_of_the_polynomial_stage(d, n, t):
+    # Large batches run the NTT kernels in their throughput shape (d/16
+    # threads per block, or 1024 at d = 8192), single requests in the latency
+    # shape (d/4 threads): both must give the oracle's bytes.
+    params = synthetic.make_params(d=d, n=n, t=t, coeff_bits=32)
+    mat = synthetic.make_material(params, seed=d + t)
+    srv = pir.PirServer.CreateCombined(params, mat.db, mat.pack,
+                                       mat.a_tilde_agg, mat.t_vec_h,
+                                       mat.second_dim_a)
+    batch = 64
+    fd, sd, pk = synthetic.make_requests(params, batch, seed=d + 1,
+                                         full_range=True)
+    got = srv.process_arrays(fd, sd, pk)
+    for i in (0, 37, 63):
+        one = srv.process_arrays(fd[i:i + 1], sd[i:i + 1], pk[i:i + 1])[0]
+        assert np.array_equal(got[i], one), i
+    op = oparams(params)
+    for i in (0, 63):
+        want = orc.process_response(op, mat.db, mat.pack, mat.a_tilde_agg,
+                                    mat.t_vec_h, mat.second_dim_a, fd[i],
+                                    sd[i], pk[i])
+        assert np.array_equal(got[i], want), i
+
+
 @pytest.mark.parametrize("engine", [pir.ENGINE_PLAIN, pir.ENGINE_TENSOR])
 def test_device_call_short_first_dimension(engine):
     # Device-pointer call with n/t < DB columns: the padding is zeroed on the

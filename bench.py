@@ -296,6 +296,90 @@ def run_pack_workload(args):
     print(json.dumps(line))
 
 
+def run_interpolate_workload(args):
+    """Offline DB interpolation + transposition (PreprocessingServer's
+    InterpolateAndTranspose) of an n = 2^20, d = 4096, t = 8, l = 1 u16 DB
+    (8 GiB in, 8 GiB out), device-resident, against the HBM roofline."""
+    import torch
+    from inspire_gb300 import _lib, build, pir, synthetic
+    build.build()
+    n, d, t, l, p = N_ENTRIES, DEGREE, INTERP, 1, 65535
+    raw = synthetic.parallel_integers((n * l * d,), 0, p, np.uint16, 41)
+    dev = torch.device("cuda", 0)
+    t_raw = torch.from_numpy(raw.view(np.int16)).to(dev)
+    t_out = torch.empty((l * t * d, n // t), dtype=torch.int16, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    lib = _lib.load()
+    err = ctypes.create_string_buffer(256)
+
+    def step():
+        rc = lib.inspire_interpolate_db(
+            16, ctypes.c_void_p(t_raw.data_ptr()), raw.size, n, d, t, l, p,
+            ctypes.c_void_p(t_out.data_ptr()), n // t, 1,
+            ctypes.c_void_p(stream.cuda_stream), err, len(err))
+        if rc:
+            raise SystemExit(err.value)
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    moved = 2 * raw.nbytes
+    hbm, _, peak_kind = peaks()
+    gbs = moved / (ms / 1000.0) / 1e9
+    line = {
+        "metric": "DB interpolation + transposition GB/s (n=2^20, d=4096, "
+                  "t=8, u16 records), bit-exact",
+        "value": gbs, "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u16",
+        "data": "synthetic (seeded uniform records in [0, p))",
+        "config": {"workload": "interpolate_n2^20_d4096_t8_l1_u16",
+                   "records_per_s": n / (ms / 1000.0),
+                   "l2": "inputs larger than L2 (8 GiB)"},
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm,
+                     "unit": "GB/s", "frac": gbs / hbm, "traffic": None,
+                     "peak_kind": peak_kind},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle as orc
+        groups = raw.reshape(n // t, t * d)
+        threads = os.cpu_count() or 1
+        done = [0]
+        lock = threading.Lock()
+        deadline = time.perf_counter() + 10.0
+
+        def work(i):
+            j = i
+            while time.perf_counter() < deadline:
+                orc.interpolate(groups[j % groups.shape[0]], d, t, p)
+                with lock:
+                    done[0] += 1
+                j += threads
+        t0 = time.perf_counter()
+        ts = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+        for th in ts:
+            th.start()
+        for th in ts:
+            th.join()
+        el = time.perf_counter() - t0
+        cpu_gbs = done[0] * t * d * 2 * 2 / el / 1e9
+        line["cpu_baseline"] = {
+            "value": cpu_gbs, "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": "%d groups of t records in %.1f s on %d host threads "
+                      "(oracle Interpolate, transposition not included)"
+                      % (done[0], el, threads)}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -305,12 +389,17 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=10)
-    ap.add_argument("--workload", default="answer", choices=["answer", "pack"],
+    ap.add_argument("--workload", default="answer",
+                    choices=["answer", "pack", "interpolate"],
                     help="answer: the online answer (default); pack: the "
-                         "packing micro-workload")
+                         "packing micro-workload; interpolate: the offline "
+                         "DB interpolation")
     args = ap.parse_args()
     if args.workload == "pack" and args.impl == "ours":
         run_pack_workload(args)
+        return
+    if args.workload == "interpolate" and args.impl == "ours":
+        run_interpolate_workload(args)
         return
 
     rank = int(os.environ.get("RANK", "0"))

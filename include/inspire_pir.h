@@ -99,6 +99,33 @@ int inspire_pir_server_create(const inspire_pir_params* params,
 void inspire_pir_server_destroy(inspire_pir_server* server);
 
 /*
+ * PirServer::LoadFromBuffer / LoadFromFile (crypto/pir/server/
+ * pir_server.cc:590-791): a server from a SaveToFile image. The DB section
+ * is copied from the image straight into GPU memory and the bit-packed pack
+ * matrix is unpacked on the GPU. Truncated images give INTERNAL "Error
+ * reading from buffer"; an unreadable file "Failed to read file.".
+ */
+int inspire_pir_server_load(const inspire_pir_params* params,
+                            const void* buffer, size_t size,
+                            inspire_pir_server** out, char* err,
+                            size_t err_len);
+int inspire_pir_server_load_file(const inspire_pir_params* params,
+                                 const char* path, inspire_pir_server** out,
+                                 char* err, size_t err_len);
+
+/*
+ * PirServer::SaveToFile (crypto/pir/server/pir_server.cc:434-588): the
+ * server's image, byte-compatible with the reference's loader. With buffer
+ * NULL (or too small: RESOURCE_EXHAUSTED) *size receives the image size.
+ * A server loaded from an image saves the same bytes.
+ */
+int inspire_pir_server_save(inspire_pir_server* server, void* buffer,
+                            size_t capacity, size_t* size, char* err,
+                            size_t err_len);
+int inspire_pir_server_save_file(inspire_pir_server* server, const char* path,
+                                 char* err, size_t err_len);
+
+/*
  * PirServer::ProcessResponse (crypto/pir/server/pir_server.cc:154-306) for
  * one request in host memory. first_dim has first_dim_len CoeffType words,
  * second_dim second_dim_count polynomials, packing_key packing_key_count
@@ -219,6 +246,26 @@ int inspire_graph_launch(inspire_graph* graph, void* stream, char* err,
 void inspire_graph_destroy(inspire_graph* graph);
 int inspire_pir_server_check(inspire_pir_server* server, char* err,
                              size_t err_len);
+
+/*
+ * VpirServer::ProcessResponse (crypto/vpir/server/vpir_server.cc:102-195)
+ * for `batch` requests in host memory, on a server created with
+ * interpolation_degree 1 and entry_size_multiple = ell (DB: ell*d rows x N
+ * columns): b' = DB * q1 and b_agg_partial = P * y_g, then per shard
+ * LowBits(b' + b_agg_partial) when local_finalize, else FinalizeMatrixPack's
+ * b. first_dim: N words per request (the flattened first-dimension
+ * polynomials); packing_key: pack_num_digits polynomials per request when
+ * local_finalize, else 2*pack_num_digits. b_responses: ell*d words per
+ * request (the VpirResponse b polynomials). The reference's messages:
+ * "Packing key must contain K polynomials.", "Flattened first dimension
+ * query must match DB matrix columns (N).".
+ */
+int inspire_vpir_process_batch(inspire_pir_server* server, int32_t batch,
+                               const void* first_dim, int64_t first_dim_len,
+                               const void* packing_key,
+                               int64_t packing_key_count,
+                               int32_t local_finalize, void* b_responses,
+                               int32_t engine, char* err, size_t err_len);
 
 /*
  * Workspaces: the state of one in-flight batch (device buffers, the tensor
@@ -379,6 +426,38 @@ int inspire_finalize_matrix_pack(const inspire_pir_params* params,
                                  const void* b, const void* b_agg_partial,
                                  const void* y_vec_h, const void* t_vec_h,
                                  void* out_b, char* err, size_t err_len);
+
+/*
+ * Offline DB preparation: PreprocessingServer::Preprocess's interpolation
+ * and transposition for every shard (crypto/pir/server/
+ * preprocessing_server.h:68-95, 174-209) on the GPU. db_raw holds
+ * num_entries records of entry_size_multiple * ring_degree values
+ * (value_bits = 8, 16 or 32), record-major as Preprocess takes it;
+ * db_raw_len counts values. out receives the combined DB matrix of
+ * l*t*d rows and out_cols columns (>= num_entries / t; columns past it are
+ * zeroed, the padding Preprocess adds for u64 coefficients), row-major:
+ * row k*t*d + j*d + c, column i = coefficient c of the j-th interpolated
+ * polynomial of records i*t .. i*t+t-1 in shard k (Interpolate,
+ * crypto/db_row_interpolation.cc:115-228). on_device = 1: device pointers,
+ * enqueued on `stream`; 0: host pointers, synchronous. Errors carry the
+ * reference's messages ("Invalid raw database size.", "ring_degree must be
+ * a power of two.", ...).
+ */
+int inspire_interpolate_db(int32_t value_bits, const void* db_raw,
+                           int64_t db_raw_len, int64_t num_entries,
+                           int32_t ring_degree, int32_t interpolation_degree,
+                           int32_t entry_size_multiple,
+                           uint32_t plaintext_modulus, void* out,
+                           int64_t out_cols, int32_t on_device, void* stream,
+                           char* err, size_t err_len);
+
+/* Interpolate (crypto/db_row_interpolation.h) of one row of t*d values,
+ * host pointers: out[j*d + c] = coefficient c of polynomial j. */
+int inspire_interpolate(int32_t value_bits, const void* db_row,
+                        int64_t db_row_len, int32_t ring_degree,
+                        int32_t interpolation_degree,
+                        uint32_t plaintext_modulus, void* out, char* err,
+                        size_t err_len);
 
 /*
  * InnerProductFft that allocates no GPU memory, for callers that cannot call

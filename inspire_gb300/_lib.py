@@ -21,6 +21,10 @@ SIGNATURES = {
         [_vp, _vp, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp,
          _i64, _vp, _cp, _sz], ctypes.c_int),
     "inspire_pir_server_destroy": ([_vp], None),
+    "inspire_pir_server_load": ([_vp, _vp, _sz, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_server_load_file": ([_vp, _cp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_server_save": ([_vp, _vp, _sz, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_server_save_file": ([_vp, _cp, _cp, _sz], ctypes.c_int),
     "inspire_pir_process_response": (
         [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _cp, _sz], ctypes.c_int),
     "inspire_pir_process_batch": (
@@ -29,6 +33,9 @@ SIGNATURES = {
     "inspire_pir_process_batch_device": (
         [_vp, _i32, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _i32, _vp, _cp,
          _sz], ctypes.c_int),
+    "inspire_vpir_process_batch": (
+        [_vp, _i32, _vp, _i64, _vp, _i64, _i32, _vp, _i32, _cp, _sz],
+        ctypes.c_int),
     "inspire_pir_products_device": (
         [_vp, _i32, _vp, _vp, _vp, _i32, _vp, _cp, _sz], ctypes.c_int),
     "inspire_pir_pack_batch_device": (
@@ -77,6 +84,12 @@ SIGNATURES = {
     "inspire_inner_product_noalloc": (
         [_i32, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp, _cp,
          _sz], ctypes.c_int),
+    "inspire_interpolate_db": (
+        [_i32, _vp, _i64, _i64, _i32, _i32, _i32, ctypes.c_uint32, _vp, _i64,
+         _i32, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_interpolate": (
+        [_i32, _vp, _i64, _i32, _i32, ctypes.c_uint32, _vp, _cp, _sz],
+        ctypes.c_int),
     "inspire_finalize_matrix_pack": (
         [_vp, _vp, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),
 }

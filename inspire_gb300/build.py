@@ -17,7 +17,8 @@ LIB_DIR = os.path.join(HERE, "lib")
 OBJ_DIR = os.path.join(HERE, "lib", "obj")
 LIB_PATH = os.path.join(LIB_DIR, "libinspire_gb300.so")
 
-SOURCES = ["server.cu", "gemv.cu", "limb_gemm.cu", "noalloc.cu", "serving.cu"]
+SOURCES = ["server.cu", "gemv.cu", "limb_gemm.cu", "noalloc.cu", "serving.cu",
+           "interpolate.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",

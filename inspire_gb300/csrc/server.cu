@@ -300,6 +300,14 @@ class DevBuf {
     ptr_ = nullptr;
     bytes_ = 0;
   }
+  // Moves another buffer's allocation into this one.
+  void Take(DevBuf* other) {
+    Free();
+    ptr_ = other->ptr_;
+    bytes_ = other->bytes_;
+    other->ptr_ = nullptr;
+    other->bytes_ = 0;
+  }
   template <typename P = void>
   P* get() const {
     return static_cast<P*>(ptr_);
@@ -362,6 +370,11 @@ struct inspire_pir_server {
   inspire::Status deferred;  // error the reference reports per request
   inspire::Status eval_rule;  // chunk rule of the eval-gadget inner product
   int sms = 152;               // streaming multiprocessors of the device
+  std::vector<uint8_t> t_vec_h_raw, second_dim_a_raw;  // host copies
+  // SaveToFile header fields (from the loaded image, or the defaults the
+  // reference's Preprocess produces: a condensed DB for u64 coefficients).
+  bool db_condensed = false, pack_condensed = false;
+  int32_t db_orig_cols = 0, pack_bits = 0;
 
   inspire::DevBuf db, pack, a_tilde, th_ntt, rgswa_ntt;
   std::unique_ptr<inspire::NttTables> tables;
@@ -596,16 +609,17 @@ Status ValidateRequest(const inspire_pir_server* s, int64_t first_dim_len,
 // Stage 1: out[q] = DB * q1[q] + P * y_g[q] for the whole batch.
 Status Products(inspire_pir_server* s, Workspace* ws, int batch,
                 const void* q1, const void* pkey, void* out, int engine,
-                cudaStream_t st) {
+                cudaStream_t st, int64_t pk_stride = -1) {
   const int cb = s->prm.coeff_bits;
+  // Words between consecutive requests' packing keys (2k polynomials).
+  if (pk_stride < 0) pk_stride = static_cast<int64_t>(2 * s->k) * s->d;
   if (engine == INSPIRE_ENGINE_TENSOR) {
     if (!s->limb) {
       return Err(INSPIRE_FAILED_PRECONDITION,
                  "tensor engine unavailable for these parameters");
     }
     if (!ws->limb) ws->limb = s->limb->NewScratch();
-    return Cuda(s->limb->Run(batch, q1, s->db_cols, pkey,
-                             static_cast<int64_t>(2 * s->k) * s->d, out,
+    return Cuda(s->limb->Run(batch, q1, s->db_cols, pkey, pk_stride, out,
                              ws->limb.get(), st),
                 "limb gemm");
   }
@@ -614,10 +628,47 @@ Status Products(inspire_pir_server* s, Workspace* ws, int batch,
   }
   return Cuda(launch_fused_gemv(cb, s->prm.db_kind, s->db.get(), s->db_cols, q1,
                                 s->db_cols, s->prm.mat_kind, s->pack.get(),
-                                s->pack_cols, pkey,
-                                static_cast<int64_t>(2 * s->k) * s->d, out,
+                                s->pack_cols, pkey, pk_stride, out,
                                 s->rows, s->rows, batch, st),
               "fused gemv");
+}
+
+// LowBits of the stage-1 words: vPIR's local finalize (b' + b_agg_partial
+// reduced mod 2^log_q).
+template <typename T>
+__global__ void low_bits_kernel(const T* __restrict__ in, int64_t n, int log_q,
+                                T* __restrict__ out) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    out[i] = low_bits<T>(in[i], log_q);
+  }
+}
+
+// VpirServer::ProcessResponse (crypto/vpir/server/vpir_server.cc:102-195) on
+// the device: DB and pack products, then per shard either LowBits(b' +
+// b_agg_partial) (LocalFinalize) or FinalizeMatrixPack's b. out: batch x
+// rows words (rows = ell * d).
+Status VpirOnDevice(inspire_pir_server* s, Workspace* w, int batch, const void* q1,
+                    const void* pkey, int64_t pk_stride, bool local, void* out,
+                    int engine, cudaStream_t st) {
+  RETURN_IF_ERROR(Products(s, w, batch, q1, pkey, w->gemv.get(), engine, st, pk_stride));
+  auto run = [&](auto tag) -> Status {
+    using T = decltype(tag);
+    const int64_t n = static_cast<int64_t>(batch) * s->rows;
+    if (local) {
+      const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((n + 255) / 256, 152 * 8));
+      low_bits_kernel<T><<<blocks, 256, 0, st>>>(w->gemv.get<T>(), n, s->prm.log_modulus,
+                                                 static_cast<T*>(out));
+      return Cuda(cudaGetLastError(), "local finalize");
+    }
+    // FinalizeStage reads y_h at offset k*d of each request's key.
+    RETURN_IF_ERROR(FinalizeStage<T>(s, w, batch, static_cast<const T*>(pkey),
+                                     w->gemv.get<T>(), st));
+    return Cuda(cudaMemcpyAsync(out, w->packed.get(), n * sizeof(T),
+                                cudaMemcpyDeviceToDevice, st),
+                "finalize output");
+  };
+  return s->prm.coeff_bits == 32 ? run(uint32_t{}) : run(uint64_t{});
 }
 
 // The device part of a batch: products, polynomial stage, rescale.
@@ -823,7 +874,8 @@ Status CreateServer(const inspire_pir_params* prm, const void* db,
                     const void* a_tilde_agg, int64_t a_count,
                     const void* t_vec_h, int64_t th_count,
                     const void* second_dim_a, int64_t sda_count,
-                    std::unique_ptr<inspire_pir_server>* out) {
+                    std::unique_ptr<inspire_pir_server>* out,
+                    DevBuf* db_dev = nullptr, DevBuf* pack_dev = nullptr) {
   if (prm == nullptr) return Err(INSPIRE_INVALID_ARGUMENT, "params is null.");
   if (prm->coeff_bits != 32 && prm->coeff_bits != 64) {
     return Err(INSPIRE_INVALID_ARGUMENT, "coeff_bits must be 32 or 64.");
@@ -911,6 +963,9 @@ Status CreateServer(const inspire_pir_params* prm, const void* db,
   s->db_cols = db_cols;
   s->pack_cols = pack_cols;
   s->interpolated_rows = prm->num_entries / t;
+  s->db_orig_cols = static_cast<int32_t>(std::min<int64_t>(db_cols, s->interpolated_rows));
+  s->db_condensed = prm->coeff_bits == 64;
+  s->pack_condensed = prm->mat_kind == INSPIRE_I16 || prm->mat_kind == INSPIRE_I32;
 
   // Chunk rules of the two inner products and the prime counts that make
   // the NTT route exact for every operand those rules admit.
@@ -951,10 +1006,28 @@ Status CreateServer(const inspire_pir_params* prm, const void* db,
   s->ctx_e = s->tables->Ctx(r_e);
 
   const size_t w = Words(cb);
-  RETURN_IF_ERROR(s->db.Upload(db, static_cast<size_t>(db_rows) * db_cols *
-                                       elem_size(prm->db_kind)));
-  RETURN_IF_ERROR(s->pack.Upload(pack, static_cast<size_t>(pack_rows) *
-                                           pack_cols * elem_size(prm->mat_kind)));
+  const size_t db_bytes = static_cast<size_t>(db_rows) * db_cols * elem_size(prm->db_kind);
+  const size_t pack_bytes =
+      static_cast<size_t>(pack_rows) * pack_cols * elem_size(prm->mat_kind);
+  if (db_dev != nullptr && pack_dev != nullptr) {
+    // Matrices already in GPU memory (the image loader) move in.
+    if (db_dev->bytes() < db_bytes || pack_dev->bytes() < pack_bytes) {
+      return Err(INSPIRE_INTERNAL, "device matrices smaller than their shapes.");
+    }
+    s->db.Take(db_dev);
+    s->pack.Take(pack_dev);
+  } else {
+    RETURN_IF_ERROR(s->db.Upload(db, db_bytes));
+    RETURN_IF_ERROR(s->pack.Upload(pack, pack_bytes));
+  }
+  // Raw copies of the small polynomial material, for SaveToFile images.
+  s->t_vec_h_raw.assign(static_cast<const uint8_t*>(t_vec_h),
+                        static_cast<const uint8_t*>(t_vec_h) + th_count * d * w);
+  if (sda_count > 0) {
+    s->second_dim_a_raw.assign(static_cast<const uint8_t*>(second_dim_a),
+                               static_cast<const uint8_t*>(second_dim_a) +
+                                   sda_count * d * w);
+  }
   RETURN_IF_ERROR(s->a_tilde.Upload(a_tilde_agg, static_cast<size_t>(a_count) * d * w));
   if (sf.ok() && (t == 1 || se.ok())) {
     if (cb == 32) {
@@ -973,6 +1046,346 @@ Status CreateServer(const inspire_pir_params* prm, const void* db,
   LimbGemm::Create(cb, prm->db_kind, s->db.get(), db_rows, db_cols,
                    prm->mat_kind, s->pack.get(), pack_cols, &s->limb);
   *out = std::move(s);
+  return Status{};
+}
+
+// ---------------------------------------------------------------------------
+// The PirServer file image: PirServer::SaveToFile / LoadFromBuffer
+// (crypto/pir/server/pir_server.cc:434-588, 590-780). Little-endian fields;
+// the DB as its raw (or condensed u64) words; the pack matrix as signed
+// entries of pack_log_digit + bit_width(d - 1) bits and the polynomials as
+// log_modulus-bit coefficients, least-significant bit first
+// (BitPackSigned / BitPackCoefficients, pir_server.cc:310-431). The two
+// large sections go straight between the image and GPU memory; the pack
+// matrix is bit-packed and unpacked by kernels.
+// ---------------------------------------------------------------------------
+// Entry i of `bits` bits starts at bit i * bits (sign-extended).
+template <typename M>
+__global__ void bit_unpack_signed_kernel(const uint8_t* __restrict__ packed,
+                                         int64_t packed_len, int64_t n, int bits,
+                                         M* __restrict__ out) {
+  const uint64_t mask = bits >= 64 ? ~0ull : ((1ull << bits) - 1);
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t bit = static_cast<uint64_t>(i) * bits;
+    const int64_t byte0 = static_cast<int64_t>(bit >> 3);
+    const int shift = static_cast<int>(bit & 7);
+    uint64_t lo = 0, hi = 0;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      if (byte0 + b < packed_len) lo |= static_cast<uint64_t>(packed[byte0 + b]) << (8 * b);
+    }
+    if (byte0 + 8 < packed_len) hi = packed[byte0 + 8];
+    uint64_t v = (lo >> shift) | (shift ? (hi << (64 - shift)) : 0);
+    v &= mask;
+    if (bits < 64 && ((v >> (bits - 1)) & 1)) v |= ~mask;
+    out[i] = static_cast<M>(static_cast<int64_t>(v));
+  }
+}
+
+// Output word w (bits 64w .. 64w+63) gathers the entries overlapping it.
+template <typename M>
+__global__ void bit_pack_kernel(const M* __restrict__ in, int64_t n, int bits,
+                                int64_t words, uint64_t* __restrict__ out) {
+  const uint64_t mask = bits >= 64 ? ~0ull : ((1ull << bits) - 1);
+  for (int64_t w = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       w < words; w += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t bit0 = w * 64;
+    const int64_t e0 = bit0 / bits;
+    const int64_t e1 = min(n, (bit0 + 64 + bits - 1) / bits);
+    uint64_t acc = 0;
+    for (int64_t e = e0; e < e1; ++e) {
+      const uint64_t v =
+          static_cast<uint64_t>(static_cast<int64_t>(in[e])) & mask;
+      const int64_t start = e * bits - bit0;
+      if (start >= 0) {
+        if (start < 64) acc |= v << start;
+      } else if (-start < 64) {
+        acc |= v >> (-start);
+      }
+    }
+    out[w] = acc;
+  }
+}
+
+struct ImageReader {
+  const uint8_t* p;
+  size_t size, off = 0;
+  bool ok = true;
+  template <typename V>
+  V get() {
+    V v{};
+    if (off + sizeof(V) > size) {
+      ok = false;
+      return v;
+    }
+    std::memcpy(&v, p + off, sizeof(V));
+    off += sizeof(V);
+    return v;
+  }
+  const uint8_t* take(size_t n) {
+    if (!ok || off + n > size) {
+      ok = false;
+      return nullptr;
+    }
+    const uint8_t* q = p + off;
+    off += n;
+    return q;
+  }
+};
+
+// BitUnpackCoefficients (below the coefficient width; raw words otherwise).
+void UnpackCoeffs(const uint8_t* data, size_t packed_len, uint64_t n, int bits,
+                  int coeff_bits, std::vector<uint8_t>* out) {
+  const size_t w = coeff_bits / 8;
+  const size_t at = out->size();
+  out->resize(at + n * w, 0);
+  uint8_t* dst = out->data() + at;
+  if (bits >= coeff_bits) {
+    std::memcpy(dst, data, std::min<size_t>(packed_len, n * w));
+    return;
+  }
+  uint64_t bit = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    uint64_t v = 0;
+    for (int b = 0; b < bits; ++b, ++bit) {
+      const size_t byte = bit >> 3;
+      if (byte < packed_len && ((data[byte] >> (bit & 7)) & 1)) v |= uint64_t{1} << b;
+    }
+    std::memcpy(dst + i * w, &v, w);  // little-endian low bytes
+  }
+}
+
+std::vector<uint8_t> PackCoeffs(const uint8_t* src, uint64_t n, int bits, int coeff_bits) {
+  const size_t w = coeff_bits / 8;
+  if (bits >= coeff_bits) return std::vector<uint8_t>(src, src + n * w);
+  std::vector<uint8_t> out((n * bits + 7) / 8, 0);
+  uint64_t bit = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    uint64_t v = 0;
+    std::memcpy(&v, src + i * w, w);
+    for (int b = 0; b < bits; ++b, ++bit) {
+      if ((v >> b) & 1) out[bit >> 3] |= static_cast<uint8_t>(1u << (bit & 7));
+    }
+  }
+  return out;
+}
+
+Status LoadImage(const inspire_pir_params* prm, const uint8_t* buf, size_t size,
+                 std::unique_ptr<inspire_pir_server>* out) {
+  if (prm == nullptr || buf == nullptr) {
+    return Err(INSPIRE_INTERNAL, "Failed to read buffer");
+  }
+  const Status bad = Err(INSPIRE_INTERNAL, "Error reading from buffer");
+  ImageReader r{buf, size};
+  const int cb = prm->coeff_bits;
+  // 1. The DB matrix.
+  const int32_t db_rows = r.get<int32_t>();
+  const int32_t db_phys = r.get<int32_t>();
+  const uint8_t db_cond = r.get<uint8_t>();
+  const int32_t db_orig = r.get<int32_t>();
+  const uint64_t db_n = r.get<uint64_t>();
+  const size_t es = elem_size(prm->db_kind);
+  const size_t db_bytes = db_n * (db_cond ? 8 : es);
+  const int64_t db_cols = db_cond ? static_cast<int64_t>(db_phys) * 8 / es : db_phys;
+  const uint8_t* db_src = r.take(db_bytes);
+  if (!r.ok || static_cast<size_t>(db_rows) * db_cols * es != db_bytes) return bad;
+  DevBuf db;
+  RETURN_IF_ERROR(db.Alloc(db_bytes));
+  RETURN_IF_ERROR(Cuda(cudaMemcpy(db.get(), db_src, db_bytes, cudaMemcpyHostToDevice),
+                       "DB upload"));
+  // 2. The pack matrix, bit-unpacked on the GPU.
+  const int32_t prow = r.get<int32_t>();
+  const int32_t pcol = r.get<int32_t>();
+  const int32_t pphys = r.get<int32_t>();
+  const uint8_t pcond = r.get<uint8_t>();
+  const int32_t porig = r.get<int32_t>();
+  const int32_t pbits = r.get<int32_t>();
+  const uint64_t plen = r.get<uint64_t>();
+  const uint8_t* psrc = r.take(plen);
+  const int64_t pn = static_cast<int64_t>(prow) * pcol;
+  if (!r.ok || pbits <= 0 || pbits > 64 || (pn * pbits + 7) / 8 > static_cast<int64_t>(plen)) {
+    return bad;
+  }
+  (void)pphys;
+  (void)porig;
+  DevBuf packed, pack;
+  RETURN_IF_ERROR(packed.Upload(psrc, plen));
+  RETURN_IF_ERROR(pack.Alloc(pn * elem_size(prm->mat_kind)));
+  if (pn > 0) {
+    const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((pn + 255) / 256, 152 * 32));
+    switch (prm->mat_kind) {
+      case INSPIRE_I16:
+        bit_unpack_signed_kernel<int16_t><<<blocks, 256>>>(packed.get<uint8_t>(), plen, pn,
+                                                           pbits, pack.get<int16_t>());
+        break;
+      case INSPIRE_I32:
+        bit_unpack_signed_kernel<int32_t><<<blocks, 256>>>(packed.get<uint8_t>(), plen, pn,
+                                                           pbits, pack.get<int32_t>());
+        break;
+      case INSPIRE_U32:
+        bit_unpack_signed_kernel<uint32_t><<<blocks, 256>>>(packed.get<uint8_t>(), plen, pn,
+                                                            pbits, pack.get<uint32_t>());
+        break;
+      default:
+        bit_unpack_signed_kernel<uint64_t><<<blocks, 256>>>(packed.get<uint8_t>(), plen, pn,
+                                                            pbits, pack.get<uint64_t>());
+    }
+    RETURN_IF_ERROR(Cuda(cudaDeviceSynchronize(), "pack matrix unpack"));
+  }
+  packed.Free();
+  // 3. Per shard and slice: a_tilde_agg and t_vec_h.
+  const int32_t log_q = r.get<int32_t>();
+  const int32_t shards = r.get<int32_t>();
+  std::vector<uint8_t> a_tilde, t_vec_h, sda;
+  int64_t a_count = 0, th_count = 0, sda_count = 0;
+  auto poly = [&](std::vector<uint8_t>* dst) {
+    const uint64_t len = r.get<uint64_t>();
+    const uint64_t plen2 = r.get<uint64_t>();
+    const uint8_t* data = r.take(plen2);
+    if (r.ok) UnpackCoeffs(data, plen2, len, log_q, cb, dst);
+  };
+  for (int32_t k = 0; k < shards && r.ok; ++k) {
+    const int32_t slices = r.get<int32_t>();
+    for (int32_t i = 0; i < slices && r.ok; ++i) {
+      poly(&a_tilde);
+      ++a_count;
+      const uint64_t tn = r.get<uint64_t>();
+      for (uint64_t j = 0; j < tn && r.ok; ++j) {
+        poly(&t_vec_h);
+        ++th_count;
+      }
+    }
+  }
+  // 4. second_dim_a.
+  const uint64_t nsd = r.get<uint64_t>();
+  for (uint64_t j = 0; j < nsd && r.ok; ++j) {
+    poly(&sda);
+    ++sda_count;
+  }
+  if (!r.ok) return bad;
+  RETURN_IF_ERROR(CreateServer(prm, db.get(), db_rows, db_cols, pack.get(), prow, pcol,
+                               a_tilde.data(), a_count, t_vec_h.data(), th_count,
+                               sda.data(), sda_count, out, &db, &pack));
+  (*out)->db_condensed = db_cond != 0;
+  (*out)->pack_condensed = pcond != 0;
+  (*out)->db_orig_cols = db_orig;
+  (*out)->pack_bits = pbits;
+  return Status{};
+}
+
+// Writes the image into dst (or only counts its bytes when dst is null).
+struct ImageWriter {
+  uint8_t* dst;
+  size_t cap, off = 0;
+  bool fits() const { return dst != nullptr && off <= cap; }
+  void put(const void* p, size_t n) {
+    if (dst != nullptr && off + n <= cap) std::memcpy(dst + off, p, n);
+    off += n;
+  }
+  template <typename V>
+  void val(V v) {
+    put(&v, sizeof(V));
+  }
+};
+
+Status SaveImage(inspire_pir_server* s, uint8_t* dst, size_t cap, size_t* size) {
+  ImageWriter w{dst, cap};
+  const int cb = s->prm.coeff_bits;
+  const size_t cw = cb / 8;
+  const int d = s->d;
+  const size_t es = elem_size(s->prm.db_kind);
+  const bool dcond = s->db_condensed && (s->db_cols * es) % 8 == 0;
+  // 1. DB.
+  w.val<int32_t>(static_cast<int32_t>(s->rows));
+  w.val<int32_t>(static_cast<int32_t>(dcond ? s->db_cols * es / 8 : s->db_cols));
+  w.val<uint8_t>(dcond ? 1 : 0);
+  w.val<int32_t>(s->db_orig_cols);
+  const size_t db_bytes = static_cast<size_t>(s->rows) * s->db_cols * es;
+  w.val<uint64_t>(dcond ? db_bytes / 8 : static_cast<uint64_t>(s->rows) * s->db_cols);
+  if (dst != nullptr && w.off + db_bytes <= cap && db_bytes > 0) {
+    RETURN_IF_ERROR(Cuda(cudaMemcpy(dst + w.off, s->db.get(), db_bytes,
+                                    cudaMemcpyDeviceToHost),
+                         "DB download"));
+  }
+  w.off += db_bytes;
+  // 2. Pack matrix, bit-packed on the GPU.
+  const size_t ms = elem_size(s->prm.mat_kind);
+  const bool pcond = s->pack_condensed && (s->pack_cols * ms) % 8 == 0;
+  int bits = s->pack_bits;
+  if (bits <= 0) {
+    int bw = 0;
+    while ((1 << bw) < d) ++bw;  // bit_width(d - 1) for a power of two d
+    bits = s->prm.pack_log_digit + bw;
+  }
+  w.val<int32_t>(static_cast<int32_t>(s->rows));
+  w.val<int32_t>(static_cast<int32_t>(s->pack_cols));
+  w.val<int32_t>(static_cast<int32_t>(pcond ? s->pack_cols * ms / 8 : s->pack_cols));
+  w.val<uint8_t>(pcond ? 1 : 0);
+  w.val<int32_t>(static_cast<int32_t>(s->pack_cols));
+  w.val<int32_t>(bits);
+  const int64_t pn = s->rows * s->pack_cols;
+  const uint64_t plen = (static_cast<uint64_t>(pn) * bits + 7) / 8;
+  w.val<uint64_t>(plen);
+  if (dst != nullptr && w.off + plen <= cap && plen > 0) {
+    const int64_t words = static_cast<int64_t>((plen + 7) / 8);
+    DevBuf packed;
+    RETURN_IF_ERROR(packed.Alloc(words * 8));
+    const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((words + 255) / 256, 152 * 32));
+    switch (s->prm.mat_kind) {
+      case INSPIRE_I16:
+        bit_pack_kernel<int16_t><<<blocks, 256>>>(s->pack.get<int16_t>(), pn, bits, words,
+                                                  packed.get<uint64_t>());
+        break;
+      case INSPIRE_I32:
+        bit_pack_kernel<int32_t><<<blocks, 256>>>(s->pack.get<int32_t>(), pn, bits, words,
+                                                  packed.get<uint64_t>());
+        break;
+      case INSPIRE_U32:
+        bit_pack_kernel<int32_t><<<blocks, 256>>>(s->pack.get<int32_t>(), pn, bits, words,
+                                                  packed.get<uint64_t>());
+        break;
+      default:
+        bit_pack_kernel<int64_t><<<blocks, 256>>>(s->pack.get<int64_t>(), pn, bits, words,
+                                                  packed.get<uint64_t>());
+    }
+    RETURN_IF_ERROR(Cuda(cudaMemcpy(dst + w.off, packed.get(), plen, cudaMemcpyDeviceToHost),
+                         "pack matrix download"));
+  }
+  w.off += plen;
+  // 3. a_tilde_agg and t_vec_h per shard and slice.
+  const int log_q = s->prm.log_modulus;
+  w.val<int32_t>(log_q);
+  w.val<int32_t>(s->l);
+  std::vector<uint8_t> a_host(static_cast<size_t>(s->l) * s->t * d * cw);
+  RETURN_IF_ERROR(Cuda(cudaMemcpy(a_host.data(), s->a_tilde.get(), a_host.size(),
+                                  cudaMemcpyDeviceToHost),
+                       "a_tilde download"));
+  auto poly = [&](const uint8_t* src) {
+    const std::vector<uint8_t> b = PackCoeffs(src, d, log_q, cb);
+    w.val<uint64_t>(d);
+    w.val<uint64_t>(b.size());
+    w.put(b.data(), b.size());
+  };
+  for (int k = 0; k < s->l; ++k) {
+    w.val<int32_t>(s->t);
+    for (int i = 0; i < s->t; ++i) {
+      const size_t slice = static_cast<size_t>(k) * s->t + i;
+      poly(a_host.data() + slice * d * cw);
+      w.val<uint64_t>(s->k);
+      for (int j = 0; j < s->k; ++j) {
+        poly(s->t_vec_h_raw.data() + (slice * s->k + j) * d * cw);
+      }
+    }
+  }
+  // 4. second_dim_a.
+  const uint64_t nsd = s->second_dim_a_raw.size() / (d * cw);
+  w.val<uint64_t>(nsd);
+  for (uint64_t j = 0; j < nsd; ++j) poly(s->second_dim_a_raw.data() + j * d * cw);
+  *size = w.off;
+  if (dst != nullptr && w.off > cap) {
+    return Err(INSPIRE_RESOURCE_EXHAUSTED, "image buffer too small.");
+  }
   return Status{};
 }
 
@@ -1123,6 +1536,94 @@ int inspire_pir_server_create(const inspire_pir_params* params, const void* db,
 }
 
 void inspire_pir_server_destroy(inspire_pir_server* server) { delete server; }
+
+int inspire_pir_server_load(const inspire_pir_params* params, const void* buffer,
+                            size_t size, inspire_pir_server** out, char* err,
+                            size_t err_len) {
+  using namespace inspire;
+  if (out == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "out is null."), err, err_len);
+  }
+  *out = nullptr;
+  std::unique_ptr<inspire_pir_server> s;
+  Status st = LoadImage(params, static_cast<const uint8_t*>(buffer), size, &s);
+  if (st.ok()) *out = s.release();
+  return Report(st, err, err_len);
+}
+
+int inspire_pir_server_load_file(const inspire_pir_params* params, const char* path,
+                                 inspire_pir_server** out, char* err,
+                                 size_t err_len) {
+  using namespace inspire;
+  if (out == nullptr || path == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "out and path must be set."), err,
+                  err_len);
+  }
+  *out = nullptr;
+  // LoadFromFile (pir_server.cc:782-791): the whole file into (pinned)
+  // host memory, then LoadFromBuffer.
+  FILE* f = std::fopen(path, "rb");
+  if (f == nullptr) return Report(Err(INSPIRE_INTERNAL, "Failed to read file."), err, err_len);
+  std::fseek(f, 0, SEEK_END);
+  const long len = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  void* host = nullptr;
+  Status st;
+  if (len < 0 || cudaMallocHost(&host, len > 0 ? len : 1) != cudaSuccess) {
+    st = Err(INSPIRE_INTERNAL, "Failed to read file.");
+  } else if (len > 0 && std::fread(host, 1, len, f) != static_cast<size_t>(len)) {
+    st = Err(INSPIRE_INTERNAL, "Failed to read file.");
+  }
+  std::fclose(f);
+  std::unique_ptr<inspire_pir_server> s;
+  if (st.ok()) st = LoadImage(params, static_cast<const uint8_t*>(host), len, &s);
+  if (host) cudaFreeHost(host);
+  if (st.ok()) *out = s.release();
+  return Report(st, err, err_len);
+}
+
+int inspire_pir_server_save(inspire_pir_server* server, void* buffer,
+                            size_t capacity, size_t* size, char* err,
+                            size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr || size == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server and size must be set."), err,
+                  err_len);
+  }
+  std::lock_guard<std::mutex> lock(server->mu);
+  return Report(SaveImage(server, static_cast<uint8_t*>(buffer), capacity, size), err,
+                err_len);
+}
+
+int inspire_pir_server_save_file(inspire_pir_server* server, const char* path,
+                                 char* err, size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr || path == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server and path must be set."), err,
+                  err_len);
+  }
+  std::lock_guard<std::mutex> lock(server->mu);
+  size_t size = 0;
+  Status st = SaveImage(server, nullptr, 0, &size);
+  void* host = nullptr;
+  if (st.ok() && cudaMallocHost(&host, size > 0 ? size : 1) != cudaSuccess) {
+    st = Err(INSPIRE_RESOURCE_EXHAUSTED, "pinned staging allocation failed.");
+  }
+  if (st.ok()) st = SaveImage(server, static_cast<uint8_t*>(host), size, &size);
+  if (st.ok()) {
+    FILE* f = std::fopen(path, "wb");
+    if (f == nullptr) {
+      st = Err(INSPIRE_INTERNAL, std::string("Failed to open file for writing: ") + path);
+    } else {
+      if (std::fwrite(host, 1, size, f) != size) {
+        st = Err(INSPIRE_INTERNAL, std::string("Error writing to file: ") + path);
+      }
+      std::fclose(f);
+    }
+  }
+  if (host) cudaFreeHost(host);
+  return Report(st, err, err_len);
+}
 
 int inspire_pir_process_response(inspire_pir_server* server,
                                  const void* first_dim, int64_t first_dim_len,
@@ -1329,6 +1830,70 @@ int inspire_pir_server_check(inspire_pir_server* server, char* err,
                   err_len);
   }
   return INSPIRE_OK;
+}
+
+int inspire_vpir_process_batch(inspire_pir_server* server, int32_t batch,
+                               const void* first_dim, int64_t first_dim_len,
+                               const void* packing_key, int64_t packing_key_count,
+                               int32_t local_finalize, void* b_responses,
+                               int32_t engine, char* err, size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr || batch <= 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server is null or batch <= 0."),
+                  err, err_len);
+  }
+  inspire_pir_server* s = server;
+  const int expected = local_finalize ? s->k : 2 * s->k;
+  if (packing_key_count != expected) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT,
+                      "Packing key must contain " + std::to_string(expected) +
+                          " polynomials."),
+                  err, err_len);
+  }
+  if (first_dim_len != s->db_cols) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT,
+                      "Flattened first dimension query must match DB matrix "
+                      "columns (N)."),
+                  err, err_len);
+  }
+  if (s->t != 1) {
+    return Report(Err(INSPIRE_FAILED_PRECONDITION,
+                      "a vPIR server has interpolation_degree 1."),
+                  err, err_len);
+  }
+  Status st = s->deferred;
+  if (!st.ok()) return Report(st, err, err_len);
+  std::lock_guard<std::mutex> lock(s->mu);
+  Workspace* ws = s->ws0.get();
+  st = EnsureWorkspace(s, ws, batch);
+  const size_t w = Words(s->prm.coeff_bits);
+  const size_t d = s->d;
+  const cudaStream_t cs = ws->stream;
+  const size_t pk_bytes = static_cast<size_t>(batch) * expected * d * w;
+  if (st.ok()) {
+    st = Cuda(cudaMemcpyAsync(ws->q1.get(), first_dim, static_cast<size_t>(batch) * s->db_cols * w,
+                              cudaMemcpyHostToDevice, cs),
+              "copy first_dim");
+  }
+  if (st.ok()) {
+    st = Cuda(cudaMemcpyAsync(ws->pkey.get(), packing_key, pk_bytes, cudaMemcpyHostToDevice, cs),
+              "copy packing_key");
+  }
+  if (st.ok()) {
+    st = VpirOnDevice(s, ws, batch, ws->q1.get(), ws->pkey.get(),
+                      static_cast<int64_t>(expected) * s->d, local_finalize != 0,
+                      ws->resp.get(), engine, cs);
+  }
+  const size_t out_bytes = static_cast<size_t>(batch) * s->rows * w;
+  if (st.ok()) {
+    st = Cuda(cudaMemcpyAsync(b_responses, ws->resp.get(), out_bytes, cudaMemcpyDeviceToHost, cs),
+              "copy response");
+  }
+  if (st.ok()) st = Cuda(cudaStreamSynchronize(cs), "vpir answer");
+  if (st.ok() && engine == INSPIRE_ENGINE_TENSOR && s->limb && s->limb->CheckError() != 0) {
+    st = Err(INSPIRE_INTERNAL, "tensor engine pipeline timed out");
+  }
+  return Report(st, err, err_len);
 }
 
 int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,

@@ -259,6 +259,60 @@ class PirServer:
         _check(rc, err)
         return PirServer(h, params, db.shape[0], db.shape[1], pack.shape[1])
 
+    @staticmethod
+    def _from_handle(h, params):
+        rows, dcols, pcols = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _lib.load().inspire_pir_server_shape(h, ctypes.byref(rows),
+                                             ctypes.byref(dcols),
+                                             ctypes.byref(pcols))
+        return PirServer(h, params, rows.value, dcols.value, pcols.value)
+
+    @staticmethod
+    def LoadFromBuffer(params, buffer, db_dtype=np.uint16, mat_dtype=np.int32):
+        """PirServer::LoadFromBuffer (crypto/pir/server/pir_server.cc:590-780)
+        into GPU memory; the template types come as numpy dtypes."""
+        buf = np.frombuffer(bytes(buffer), dtype=np.uint8) \
+            if not isinstance(buffer, np.ndarray) else buffer
+        prm = c_params(params, db_dtype, mat_dtype)
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        rc = _lib.load().inspire_pir_server_load(
+            ctypes.byref(prm), _ptr(buf), buf.size, ctypes.byref(h), err,
+            len(err))
+        _check(rc, err)
+        return PirServer._from_handle(h, params)
+
+    @staticmethod
+    def LoadFromFile(params, path, db_dtype=np.uint16, mat_dtype=np.int32):
+        """PirServer::LoadFromFile (pir_server.cc:782-791)."""
+        prm = c_params(params, db_dtype, mat_dtype)
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        rc = _lib.load().inspire_pir_server_load_file(
+            ctypes.byref(prm), str(path).encode(), ctypes.byref(h), err,
+            len(err))
+        _check(rc, err)
+        return PirServer._from_handle(h, params)
+
+    def SaveToBuffer(self):
+        """The SaveToFile image (pir_server.cc:434-588) as bytes."""
+        lib = _lib.load()
+        err = _errbuf()
+        size = ctypes.c_size_t()
+        _check(lib.inspire_pir_server_save(self._h, None, 0, ctypes.byref(size),
+                                           err, len(err)), err)
+        out = np.empty(size.value, dtype=np.uint8)
+        _check(lib.inspire_pir_server_save(self._h, _ptr(out), out.size,
+                                           ctypes.byref(size), err, len(err)),
+               err)
+        return out.tobytes()
+
+    def SaveToFile(self, path):
+        """PirServer::SaveToFile (pir_server.cc:434-588)."""
+        err = _errbuf()
+        _check(_lib.load().inspire_pir_server_save_file(
+            self._h, str(path).encode(), err, len(err)), err)
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:
@@ -498,3 +552,103 @@ def finalize_matrix_pack(params: PirParams, b, b_agg_partial, y_vec_h,
                                           err, len(err))
     _check(rc, err)
     return out
+
+
+_VALUE_BITS = {np.dtype(np.uint8): 8, np.dtype(np.uint16): 16,
+               np.dtype(np.uint32): 32}
+
+
+def Interpolate(db_row, ring_degree, interpolation_degree, plaintext_modulus):
+    """Interpolate (crypto/db_row_interpolation.h): t*d evaluations -> the
+    t coefficient polynomials, on the GPU."""
+    row = np.ascontiguousarray(db_row)
+    bits = _VALUE_BITS.get(row.dtype)
+    if bits is None:
+        raise InspireError(INVALID_ARGUMENT, "value_bits must be 8, 16 or 32.")
+    out = np.zeros_like(row)
+    err = _errbuf()
+    rc = _lib.load().inspire_interpolate(bits, _ptr(row), row.size, ring_degree,
+                                         interpolation_degree,
+                                         plaintext_modulus, _ptr(out), err,
+                                         len(err))
+    _check(rc, err)
+    return out
+
+
+def interpolate_db(db_raw, params: PirParams, out_cols=None):
+    """PreprocessingServer's interpolation + transposition of every shard
+    (crypto/pir/server/preprocessing_server.h:68-95, 174-209) on the GPU:
+    the raw DB (num_entries records of l*d values, record-major) -> the
+    combined DB matrix (l*t*d, out_cols), zero-padded past n/t columns."""
+    raw = np.ascontiguousarray(db_raw).reshape(-1)
+    bits = _VALUE_BITS.get(raw.dtype)
+    if bits is None:
+        raise InspireError(INVALID_ARGUMENT, "value_bits must be 8, 16 or 32.")
+    d = params.rlwe.degree
+    t = params.interpolation_degree
+    l = params.entry_size_multiple
+    n = params.num_entries
+    cols = out_cols if out_cols is not None else n // t
+    out = np.empty((l * t * d, cols), dtype=raw.dtype)
+    err = _errbuf()
+    rc = _lib.load().inspire_interpolate_db(
+        bits, _ptr(raw), raw.size, n, d, t, l, params.plaintext_modulus,
+        _ptr(out), cols, 0, None, err, len(err))
+    _check(rc, err)
+    return out
+
+
+@dataclass
+class VpirRequest:
+    """VpirRequest (crypto/vpir/vpir_params.h:161-164)."""
+    first_dimension_query: List[np.ndarray]   # N/d polynomials
+    packing_key: List[np.ndarray]             # k (local finalize) or 2k
+
+
+@dataclass
+class VpirResponse:
+    b_responses: np.ndarray                   # (ell, d)
+
+
+class VpirServer:
+    """VpirServer's online answer (crypto/vpir/server/vpir_server.cc:102-195)
+    on the GPU: a server with interpolation degree 1 and ell shards whose
+    response is the b polynomial of each shard."""
+
+    def __init__(self, server: PirServer, local_finalize=False):
+        if server.params.interpolation_degree != 1:
+            raise InspireError(FAILED_PRECONDITION,
+                               "a vPIR server has interpolation_degree 1.")
+        self.server = server
+        self.local_finalize = local_finalize
+
+    @staticmethod
+    def CreateCombined(params, db, pack, a_tilde_agg, t_vec_h,
+                       local_finalize=False):
+        d = params.rlwe.degree
+        srv = PirServer.CreateCombined(params, db, pack, a_tilde_agg, t_vec_h,
+                                       np.zeros((0, d), params.coeff_dtype))
+        return VpirServer(srv, local_finalize)
+
+    def process_arrays(self, first_dim, packing_key, engine=ENGINE_PLAIN):
+        """(B, N) first dimensions and (B, K, d) packing keys -> (B, ell, d)."""
+        p = self.server.params
+        cdt = p.coeff_dtype
+        d = p.rlwe.degree
+        fd = np.ascontiguousarray(first_dim, dtype=cdt)
+        pk = np.ascontiguousarray(packing_key, dtype=cdt)
+        b = fd.shape[0]
+        out = np.zeros((b, p.entry_size_multiple, d), dtype=cdt)
+        err = _errbuf()
+        rc = _lib.load().inspire_vpir_process_batch(
+            self.server._h, b, _ptr(fd), fd.shape[1], _ptr(pk),
+            pk.shape[1] if pk.ndim == 3 else 0,
+            1 if self.local_finalize else 0, _ptr(out), engine, err, len(err))
+        _check(rc, err)
+        return out
+
+    def ProcessResponse(self, request: VpirRequest) -> VpirResponse:
+        fd = np.concatenate([np.asarray(x) for x in
+                             request.first_dimension_query])[None, :]
+        pk = np.stack([np.asarray(x) for x in request.packing_key])[None]
+        return VpirResponse(self.process_arrays(fd, pk)[0])

@@ -101,6 +101,10 @@ def main(argv=None):
     ap.add_argument("--pool", type=int, default=64)
     ap.add_argument("--max-batch", type=int, default=256)
     ap.add_argument("--hbm-budget-gb", type=float, default=48.0)
+    ap.add_argument("--max-wait-us", type=int, default=0,
+                    help="batching window of the serving loop")
+    ap.add_argument("--plain-max-batch", type=int, default=8,
+                    help="largest batch answered by the plain engine")
     ap.add_argument("--small", action="store_true",
                     help="shrunk shapes (n / 16) for a quick functional run")
     args = ap.parse_args(argv)
@@ -131,7 +135,9 @@ def main(argv=None):
     loads = []
     with serving.ServingEngine(servers, max_batch=args.max_batch,
                                hbm_budget=int(args.hbm_budget_gb * (1 << 30)),
-                               max_workspaces=3, plain_max_batch=4) as eng:
+                               max_workspaces=3,
+                               plain_max_batch=args.plain_max_batch,
+                               max_wait_us=args.max_wait_us) as eng:
         for frac in [float(x) for x in args.loads.split(",")]:
             eng.reset_stats()
             n, t_sub, t_all, results = run_load(
@@ -160,6 +166,8 @@ def main(argv=None):
                    "servers": [dict(zip(("name", "n", "d", "t", "l", "share"),
                                         s)) for s in SERVERS],
                    "max_batch": args.max_batch,
+                   "max_wait_us": args.max_wait_us,
+                   "plain_max_batch": args.plain_max_batch,
                    "hbm_budget_gb": args.hbm_budget_gb,
                    "workspaces": ws},
         "peak_qps": peak,

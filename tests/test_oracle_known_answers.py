@@ -265,3 +265,47 @@ def test_rescale_rounds_half_up():
     got = orc.rescale(c, 32, 20, 1)
     want = [(x * 2 + (1 << 19)) // (1 << 20) for x in c.tolist()]
     assert got.tolist() == want
+
+
+# --------------------------------------------------------- Interpolate ----
+def _evaluate(P, power, d, p):
+    """sum_i P_i * X^(i*power) in Z_p[X]/(X^d+1)
+    (crypto/db_row_interpolation_test.cc:36-82)."""
+    out = np.zeros(d, dtype=np.int64)
+    for i, poly in enumerate(P):
+        k = (i * power) % (2 * d)
+        sign = 1
+        if k >= d:
+            sign, k = -1, k - d
+        rot = np.concatenate([-poly[d - k:], poly[:d - k]]) if k else poly
+        out = (out + sign * rot.astype(np.int64)) % p
+    return out
+
+
+@pytest.mark.parametrize("dtype", [np.uint16, np.uint32])
+@pytest.mark.parametrize("d,t,p", [(32, 16, 1031), (64, 32, 2031),
+                                   (128, 64, 65535)])
+def test_oracle_interpolate_reference_property(dtype, d, t, p):
+    # crypto/db_row_interpolation_test.cc:91-142: evaluating random P_i at
+    # w^j = X^(j*2d/t) and interpolating returns the P_i.
+    rng = np.random.default_rng(d * t)
+    P = rng.integers(0, p, size=(t, d)).astype(np.int64)
+    evals = np.concatenate([_evaluate(P, j * 2 * d // t, d, p)
+                            for j in range(t)]).astype(dtype)
+    got = orc.interpolate(evals, d, t, p)
+    assert np.array_equal(got.reshape(t, d), P.astype(dtype))
+
+
+def test_oracle_interpolate_invalid_arguments():
+    # crypto/db_row_interpolation_test.cc:144-190.
+    row = (np.arange(32 * 16) % 1031).astype(np.uint16)
+    orc.interpolate(row, 32, 16, 1031)
+    with pytest.raises(orc.OracleError, match="ring_degree must be a power"):
+        orc.interpolate(np.zeros(31 * 16, np.uint16), 31, 16, 1031)
+    with pytest.raises(orc.OracleError,
+                       match="interpolation_degree must be a power"):
+        orc.interpolate(np.zeros(32 * 15, np.uint16), 32, 15, 1031)
+    with pytest.raises(orc.OracleError, match="less than or equal to 2"):
+        orc.interpolate(np.zeros(32 * 128, np.uint16), 32, 128, 1031)
+    with pytest.raises(orc.OracleError, match="plaintext_modulus must be odd"):
+        orc.interpolate(row, 32, 16, 1030)

@@ -96,6 +96,17 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
+def replica_time(ms, dist, device):
+    """The job's time for a step: the slowest replica's (max over ranks).
+    Replicas share nothing on the data path; this is the only collective."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.item()
+
+
 def make_workload(seed=2026, batch=256):
     from inspire_gb300 import synthetic
     params = synthetic.make_params(d=DEGREE, n=N_ENTRIES, t=INTERP,
@@ -303,7 +314,7 @@ def run_interpolate_workload(args):
     import torch
     from inspire_gb300 import _lib, build, pir, synthetic
     build.build()
-    n, d, t, l, p = N_ENTRIES, DEGREE, INTERP, 1, 65535
+    n, d, t, l, p = args.entries, DEGREE, INTERP, 1, 65535
     raw = synthetic.parallel_integers((n * l * d,), 0, p, np.uint16, 41)
     dev = torch.device("cuda", 0)
     t_raw = torch.from_numpy(raw.view(np.int16)).to(dev)
@@ -341,7 +352,7 @@ def run_interpolate_workload(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u16",
         "data": "synthetic (seeded uniform records in [0, p))",
-        "config": {"workload": "interpolate_n2^20_d4096_t8_l1_u16",
+        "config": {"workload": "interpolate_n%d_d4096_t8_l1_u16" % n,
                    "records_per_s": n / (ms / 1000.0),
                    "l2": "inputs larger than L2 (8 GiB)"},
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm,
@@ -380,6 +391,75 @@ def run_interpolate_workload(args):
     print(json.dumps(line))
 
 
+def run_hint_workload(args):
+    """Offline hint matrix (ComputeHintMatrix) of the n = 2^20, d = 4096,
+    t = 8 DB: 32768 x 131072 u16 entries against 32 a-components of 4096
+    u32 coefficients -> 32768 x 4096 u32, device-resident."""
+    import torch
+    from inspire_gb300 import _lib, build, synthetic
+    build.build()
+    rows, d = INTERP * DEGREE, DEGREE
+    cols = args.entries // INTERP
+    n = cols // d
+    db = synthetic.parallel_integers((rows, cols), 0, 65535, np.uint16, 51)
+    a = synthetic.parallel_integers((n, d), 0, 1 << 32, np.uint64, 52).astype(np.uint32)
+    dev = torch.device("cuda", 0)
+    t_db = torch.from_numpy(db.view(np.int16)).to(dev)
+    t_a = torch.from_numpy(a.view(np.int32)).to(dev)
+    t_out = torch.empty((rows, d), dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    lib = _lib.load()
+    err = ctypes.create_string_buffer(256)
+
+    def step():
+        rc = lib.inspire_compute_hint_matrix(
+            1, 32, ctypes.c_void_p(t_db.data_ptr()), rows, cols,
+            ctypes.c_void_p(t_a.data_ptr()), n, d,
+            ctypes.c_void_p(t_out.data_ptr()), 1,
+            ctypes.c_void_p(stream.cuda_stream), err, len(err))
+        if rc:
+            raise SystemExit(err.value)
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            step()
+    ms = (time.perf_counter() - t0) * 1000 / args.steps
+    line = {
+        "metric": "hint matrix rows/s (ComputeHintMatrix, 32768 x 131072 "
+                  "u16 DB, 32 a-components, d=4096, Z_2^32), exact",
+        "value": rows / (ms / 1000.0), "unit": "rows/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic (seeded uniform DB and "
+                                "a-components)",
+        "config": {"workload": "hint_n%d_d4096_t8_u32" % args.entries,
+                   "rows": rows,
+                   "cols": cols, "a_components": n,
+                   "ntts_per_step": rows * (n + 1) * 3,
+                   "timing": "host clock around synchronous calls"},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle as orc
+        vinv = np.concatenate([a[:, :1], (0 - a[:, :0:-1].astype(np.uint64))
+                               .astype(np.uint32)], axis=1)
+        chunk = min(20, int((53.0 - np.log2(n) - np.log2(d)) / 2.0))
+        t0 = time.perf_counter()
+        done = 0
+        while time.perf_counter() - t0 < 10.0:
+            orc.inner_product(db[done].reshape(n, d).astype(np.uint32), vinv,
+                              32, 16, 32, chunk)
+            done += 1
+        el = time.perf_counter() - t0
+        line["cpu_baseline"] = {
+            "value": done / el, "unit": "rows/s", "cores": 1, "kind": "port",
+            "sample": "%d rows in %.1f s on one host thread (oracle exact "
+                      "inner product per row)" % (done, el)}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -389,8 +469,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-steps", type=int, default=10)
+    ap.add_argument("--entries", type=int, default=N_ENTRIES,
+                    help="records of the interpolate / hint workloads")
     ap.add_argument("--workload", default="answer",
-                    choices=["answer", "pack", "interpolate"],
+                    choices=["answer", "pack", "interpolate", "hint"],
                     help="answer: the online answer (default); pack: the "
                          "packing micro-workload; interpolate: the offline "
                          "DB interpolation")
@@ -400,6 +482,9 @@ def main():
         return
     if args.workload == "interpolate" and args.impl == "ours":
         run_interpolate_workload(args)
+        return
+    if args.workload == "hint" and args.impl == "ours":
+        run_hint_workload(args)
         return
 
     rank = int(os.environ.get("RANK", "0"))
@@ -482,11 +567,7 @@ def main():
         e1.record(stream)
         e1.synchronize()
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        if dist:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = t.item()
+        ms = replica_time(e0.elapsed_time(e1), dist, dev)
         return ms / steps
 
     hbm, tflops, peak_kind = peaks()

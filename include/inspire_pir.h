@@ -451,6 +451,22 @@ int inspire_interpolate_db(int32_t value_bits, const void* db_raw,
                            int64_t out_cols, int32_t on_device, void* stream,
                            char* err, size_t err_len);
 
+/*
+ * ComputeHintMatrix (crypto/hint_computation.cc:78-160) on the GPU: for a
+ * database of `rows` x `cols` entries (db_kind = INSPIRE_U8, _U16 or _U32)
+ * and n a-components of d CoeffType coefficients (cols = n * d), row i of
+ * the rows x d result is sum_k (row i's k-th block of d entries) times the
+ * negacyclic matrix of a_k, mod 2^coeff_bits (the reference's naive
+ * definition, hint_computation_test.cc:36-176), computed exactly with
+ * multi-prime NTTs. on_device = 1: device pointers on `stream`; 0: host
+ * pointers. The reference's error messages.
+ */
+int inspire_compute_hint_matrix(int32_t db_kind, int32_t coeff_bits,
+                                const void* db, int64_t rows, int64_t cols,
+                                const void* a_components, int32_t n,
+                                int32_t d, void* out, int32_t on_device,
+                                void* stream, char* err, size_t err_len);
+
 /* Interpolate (crypto/db_row_interpolation.h) of one row of t*d values,
  * host pointers: out[j*d + c] = coefficient c of polynomial j. */
 int inspire_interpolate(int32_t value_bits, const void* db_row,

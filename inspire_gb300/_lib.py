@@ -84,6 +84,9 @@ SIGNATURES = {
     "inspire_inner_product_noalloc": (
         [_i32, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _vp, _cp,
          _sz], ctypes.c_int),
+    "inspire_compute_hint_matrix": (
+        [_i32, _i32, _vp, _i64, _i64, _vp, _i32, _i32, _vp, _i32, _vp, _cp,
+         _sz], ctypes.c_int),
     "inspire_interpolate_db": (
         [_i32, _vp, _i64, _i64, _i32, _i32, _i32, ctypes.c_uint32, _vp, _i64,
          _i32, _vp, _cp, _sz], ctypes.c_int),

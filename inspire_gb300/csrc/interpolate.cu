@@ -147,7 +147,7 @@ interpolate_kernel(const V* __restrict__ raw, InterpArgs a, V* __restrict__ out)
 // stores run over kFastG consecutive groups (DB columns).
 constexpr int kFastR = 32;   // classes per block (one warp's lanes)
 constexpr int kFastGW = 8;   // groups in flight (warps per block)
-constexpr int kFastG = 32;   // groups per block
+constexpr int kFastG = 16;   // groups per block
 
 // Modular helpers; SMALL: p < 2^31, so sums and Shoup remainders fit in 32
 // bits.

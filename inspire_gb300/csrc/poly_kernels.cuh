@@ -223,6 +223,71 @@ pack_out_kernel(const T* __restrict__ a, const T* __restrict__ b, int d,
   }
 }
 
+// ComputeHintMatrix (crypto/hint_computation.cc:78-160) per (DB row,
+// prime): sum over the n column blocks of NTT(row block) . V_k, then the
+// inverse NTT. V: [n][r][d] transforms of the inverted a-components
+// (v_k[0] = a_k[0], v_k[j] = -a_k[d-j]); out: [rows][r][d] residues.
+// grid = (r, rows).
+template <typename S, int ITERS = 0>
+__global__ void __launch_bounds__(PolyShape<ITERS>::kMaxThreads, PolyShape<ITERS>::kMinBlocks)
+hint_rows_kernel(const S* __restrict__ db, int64_t cols, int n,
+                 const uint32_t* __restrict__ V, uint32_t* __restrict__ out,
+                 NttCtx c) {
+  extern __shared__ uint32_t smem[];
+  const int d = 1 << c.logd;
+  const int pi = blockIdx.x;
+  const int64_t row = blockIdx.y;
+  const uint32_t p = c.p[pi];
+  const uint32_t pinv = c.pinv[pi];
+  constexpr int kPer = PolyShape<ITERS>::kPer;
+  uint32_t acc[kPer];
+#pragma unroll
+  for (int m = 0; m < kPer; ++m) acc[m] = 0;
+  const S* src = db + row * cols;
+  for (int k = 0; k < n; ++k) {
+    __syncthreads();
+    for (int j = threadIdx.x; j < d; j += blockDim.x) {
+      smem[j] = reduce_u32(static_cast<uint32_t>(src[static_cast<int64_t>(k) * d + j]), p);
+    }
+    ntt_forward_t<ITERS>(smem, c, pi);
+    const uint32_t* vk = V + (static_cast<int64_t>(k) * c.r + pi) * d;
+#pragma unroll
+    for (int m = 0; m < kPer; ++m) {
+      const int j = threadIdx.x + m * blockDim.x;
+      if (j < d) acc[m] = add_mod(acc[m], mont_mul(smem[j], __ldg(vk + j), p, pinv), p);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < kPer; ++m) {
+    const int j = threadIdx.x + m * blockDim.x;
+    if (j < d) smem[j] = acc[m];
+  }
+  ntt_inverse_t<ITERS>(smem, c, pi);
+  uint32_t* o = out + (row * c.r + pi) * d;
+  for (int j = threadIdx.x; j < d; j += blockDim.x) {
+    o[j] = shoup_mul(smem[j], c.scale[pi], c.scale_s[pi], p);
+  }
+}
+
+// CRT of the hint residues: out[row][j] = the integer mod 2^w.
+template <typename T>
+__global__ void hint_crt_kernel(const uint32_t* __restrict__ res, int64_t rows, int d,
+                                T* __restrict__ out, NttCtx c) {
+  const int64_t total = rows * d;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t row = i / d;
+    const int j = static_cast<int>(i % d);
+    uint32_t x[kMaxPrimes] = {0, 0, 0, 0, 0};
+#pragma unroll
+    for (int pi = 0; pi < kMaxPrimes; ++pi) {
+      if (pi < c.r) x[pi] = res[(row * c.r + pi) * d + j];
+    }
+    out[i] = crt_reconstruct<T>(x, c);
+  }
+}
+
 struct ExtArgs {
   int log_q;         // LowBits width and GadgetInv log_modulus
   int log_digit;

@@ -2165,6 +2165,139 @@ int inspire_inner_product(int32_t coeff_bits, const void* u, const void* v,
   return Report(st, err, err_len);
 }
 
+int inspire_compute_hint_matrix(int32_t db_kind, int32_t coeff_bits, const void* db,
+                                int64_t rows, int64_t cols, const void* a_components,
+                                int32_t n, int32_t d, void* out, int32_t on_device,
+                                void* stream, char* err, size_t err_len) {
+  using namespace inspire;
+  // Checks in the reference's order (hint_computation.cc:81-97).
+  if (rows <= 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "Database matrix cannot be empty."), err,
+                  err_len);
+  }
+  if (n <= 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "a_components cannot be empty."), err,
+                  err_len);
+  }
+  if (cols != static_cast<int64_t>(d) * n) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT,
+                      "Database columns must match d * n where d is the polynomial "
+                      "length and n is the number of polynomials."),
+                  err, err_len);
+  }
+  if (coeff_bits != 32 && coeff_bits != 64) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "coeff_bits must be 32 or 64."), err,
+                  err_len);
+  }
+  if (db_kind != INSPIRE_U8 && db_kind != INSPIRE_U16 && db_kind != INSPIRE_U32) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "database type must be u8, u16 or u32."),
+                  err, err_len);
+  }
+  int logd = 0;
+  while ((1 << logd) < d) ++logd;
+  if (d < 2 || (1 << logd) != d || logd > 13) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "polynomial length must be a power of two "
+                                                "between 2 and 8192."),
+                  err, err_len);
+  }
+  const int s_bits = 8 * elem_size(db_kind);
+  int r = 0;
+  Status st = PrimesFor(BoundBits(n, d, s_bits, coeff_bits), &r);
+  if (!st.ok()) return Report(st, err, err_len);
+  std::unique_ptr<NttTables> tabs;
+  st = NttTables::Create(logd, &tabs);
+  if (!st.ok()) return Report(st, err, err_len);
+  NttCtx c = tabs->Ctx(r);
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) {
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const size_t w = coeff_bits / 8;
+  const size_t es = elem_size(db_kind);
+  // The a-components on the host (a device copy comes back first: they are
+  // n * d words).
+  std::vector<uint8_t> a_host(static_cast<size_t>(n) * d * w);
+  if (on_device) {
+    st = Cuda(cudaMemcpy(a_host.data(), a_components, a_host.size(), cudaMemcpyDeviceToHost),
+              "a-components download");
+    if (!st.ok()) return Report(st, err, err_len);
+  } else {
+    std::memcpy(a_host.data(), a_components, a_host.size());
+  }
+  // v_k[0] = a_k[0], v_k[j] = -a_k[d - j] (hint_computation.cc:110-119).
+  std::vector<uint8_t> vinv(static_cast<size_t>(n) * d * w);
+  for (int k = 0; k < n; ++k) {
+    for (int j = 0; j < d; ++j) {
+      const int src = j == 0 ? 0 : d - j;
+      const uint8_t* a = a_host.data() + (static_cast<size_t>(k) * d + src) * w;
+      uint8_t* v = vinv.data() + (static_cast<size_t>(k) * d + j) * w;
+      if (w == 4) {
+        uint32_t x;
+        std::memcpy(&x, a, 4);
+        x = j == 0 ? x : 0u - x;
+        std::memcpy(v, &x, 4);
+      } else {
+        uint64_t x;
+        std::memcpy(&x, a, 8);
+        x = j == 0 ? x : 0ull - x;
+        std::memcpy(v, &x, 8);
+      }
+    }
+  }
+  const cudaStream_t cs = on_device ? static_cast<cudaStream_t>(stream) : nullptr;
+  DevBuf dv, dV, dres, ddb, dout;
+  st = dv.Upload(vinv.data(), vinv.size());
+  if (st.ok()) st = dV.Alloc(static_cast<size_t>(n) * r * d * 4);
+  if (st.ok()) st = dres.Alloc(static_cast<size_t>(rows) * r * d * 4);
+  const void* db_dev = db;
+  void* out_dev = out;
+  if (st.ok() && !on_device) {
+    st = ddb.Upload(db, static_cast<size_t>(rows) * cols * es);
+    if (st.ok()) st = dout.Alloc(static_cast<size_t>(rows) * d * w);
+    db_dev = ddb.get();
+    out_dev = dout.get();
+  }
+  if (st.ok()) {
+    auto run = [&](auto ttag, auto stag) -> Status {
+      using T = decltype(ttag);
+      using S = decltype(stag);
+      ntt_coeffs_kernel<T><<<dim3(n * r, 1), PolyThreads(d), d * 4, cs>>>(
+          dv.get<T>(), 0, 0, n, static_cast<T>(~0ull), dV.get<uint32_t>(), d, c);
+      RETURN_IF_ERROR(Cuda(cudaGetLastError(), "a-component transforms"));
+      const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(r) * rows, sms);
+      const dim3 grid(r, static_cast<unsigned>(rows));
+      INSPIRE_ITERS_DISPATCH(
+          pl.iters, RETURN_IF_ERROR(SetSmem(hint_rows_kernel<S, IT>, d * 4));
+          hint_rows_kernel<S, IT><<<grid, pl.nt, d * 4, cs>>>(
+              static_cast<const S*>(db_dev), cols, n, dV.get<uint32_t>(),
+              dres.get<uint32_t>(), c));
+      RETURN_IF_ERROR(Cuda(cudaGetLastError(), "hint rows"));
+      const int64_t total = rows * static_cast<int64_t>(d);
+      const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 152 * 8));
+      hint_crt_kernel<T><<<blocks, 256, 0, cs>>>(dres.get<uint32_t>(), rows, d,
+                                                  static_cast<T*>(out_dev), c);
+      return Cuda(cudaGetLastError(), "hint CRT");
+    };
+    if (coeff_bits == 32) {
+      st = db_kind == INSPIRE_U8    ? run(uint32_t{}, uint8_t{})
+           : db_kind == INSPIRE_U16 ? run(uint32_t{}, uint16_t{})
+                                    : run(uint32_t{}, uint32_t{});
+    } else {
+      st = db_kind == INSPIRE_U8    ? run(uint64_t{}, uint8_t{})
+           : db_kind == INSPIRE_U16 ? run(uint64_t{}, uint16_t{})
+                                    : run(uint64_t{}, uint32_t{});
+    }
+  }
+  // The temporaries are freed on return: wait for the work that uses them.
+  if (st.ok()) st = Cuda(on_device ? cudaStreamSynchronize(cs) : cudaDeviceSynchronize(), "hint");
+  if (st.ok() && !on_device) {
+    st = Cuda(cudaMemcpy(out, dout.get(), static_cast<size_t>(rows) * d * w,
+                         cudaMemcpyDeviceToHost),
+              "copy out");
+  }
+  return Report(st, err, err_len);
+}
+
 int inspire_external_product(const inspire_pir_params* params,
                              const void* ct_a, const void* ct_b,
                              const void* rgsw, void* out_a, void* out_b,

@@ -652,3 +652,26 @@ class VpirServer:
                              request.first_dimension_query])[None, :]
         pk = np.stack([np.asarray(x) for x in request.packing_key])[None]
         return VpirResponse(self.process_arrays(fd, pk)[0])
+
+
+def ComputeHintMatrix(database, a_components):
+    """ComputeHintMatrix (crypto/hint_computation.cc:78-160) on the GPU:
+    database (rows, n*d) of u8/u16/u32, a_components (n, d) of u32/u64 ->
+    (rows, d) in the a-components' type."""
+    db = np.ascontiguousarray(database)
+    a = np.ascontiguousarray(a_components)
+    kind = {np.dtype(np.uint8): 0, np.dtype(np.uint16): 1,
+            np.dtype(np.uint32): 2}.get(db.dtype)
+    if kind is None or a.dtype not in (np.dtype(np.uint32), np.dtype(np.uint64)):
+        raise InspireError(INVALID_ARGUMENT,
+                           "database must be u8/u16/u32, a_components u32/u64.")
+    rows = db.shape[0] if db.ndim == 2 else 0
+    cols = db.shape[1] if db.ndim == 2 else 0
+    n, d = (a.shape if a.ndim == 2 and a.size else (0, 0))
+    out = np.zeros((rows, d), dtype=a.dtype)
+    err = _errbuf()
+    rc = _lib.load().inspire_compute_hint_matrix(
+        kind, a.dtype.itemsize * 8, _ptr(db), rows, cols, _ptr(a), n, d,
+        _ptr(out), 0, None, err, len(err))
+    _check(rc, err)
+    return out

@@ -160,6 +160,21 @@ def test_tensor_products_match_exact_integer_gemm():
         assert np.array_equal(got[q], (want & m).astype(np.uint32)), q
 
 
+@pytest.mark.parametrize("batch", [128, 192, 256])
+def test_tensor_cluster_shapes(batch):
+    # The request tiles of a row pair share their DB / pack tiles through
+    # cluster multicast: 2 tiles (128 requests), none (192: 3 tiles), 4 (256).
+    params = synthetic.make_params(d=128, n=2 * 8192, t=2, coeff_bits=32)
+    mat = synthetic.make_material(params, seed=batch)
+    srv = _server(params, mat)
+    fd, sd, pk = synthetic.make_requests(params, batch, seed=batch + 1,
+                                         full_range=True)
+    got_t = srv.process_arrays(fd, sd, pk, pir.ENGINE_TENSOR)
+    got_p = srv.process_arrays(fd, sd, pk, pir.ENGINE_PLAIN)
+    assert np.array_equal(got_t, got_p)
+    srv.check()
+
+
 def test_tensor_engine_repeated_batches_reuse_buffers():
     # A large batch followed by smaller ones: the request byte planes are
     # reused, stale rows must not leak into the smaller batches.

@@ -71,7 +71,8 @@ constexpr int kStageK = 32;        // K per pipeline stage (64-byte rows)
 constexpr int kUnitK = 128;        // K per exact accumulation unit
 constexpr int kStagesPerUnit = kUnitK / kStageK;
 constexpr int kStages = 4;
-constexpr int kATileBytes = kBlockRows * kStageK * 2;      // 8 KB
+constexpr int kATileBytes = kBlockRows * kStageK * 2;      // 8 KB per plane
+constexpr int kABoxBytes = 2 * kATileBytes;                // both planes: 16 KB
 constexpr int kBLimbBytes = kTileQ * kStageK * 2;          // 4 KB
 constexpr int kStageBytes = kRowBlocks * 2 * kATileBytes + 4 * kBLimbBytes;  // 48 KB
 constexpr int kThreads = 384;
@@ -207,6 +208,18 @@ __device__ __forceinline__ void tmem_wait_ld() {
 
 // Shared-memory matrix descriptor: K-major, 64-byte swizzle (rows of 64
 // bytes, 8-row groups 512 bytes apart = SBO), descriptor version 1.
+// K-major, 128-byte swizzle (rows of 128 bytes, 8-row groups 1024 bytes
+// apart): the A tiles, whose rows hold the two digit planes of a K chunk.
+__device__ __forceinline__ uint64_t smem_desc128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= static_cast<uint64_t>((addr >> 4) & 0x3FFF);
+  d |= static_cast<uint64_t>(1) << 16;                 // LBO (unused: swizzled)
+  d |= static_cast<uint64_t>(1024 >> 4) << 32;         // SBO
+  d |= static_cast<uint64_t>(1) << 46;                 // version
+  d |= static_cast<uint64_t>(2) << 61;                 // SWIZZLE_128B
+  return d;
+}
+
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   uint64_t d = 0;
   d |= static_cast<uint64_t>((addr >> 4) & 0x3FFF);
@@ -244,14 +257,16 @@ __device__ __forceinline__ void issue_block(uint32_t st, int rb, int kind,
   constexpr uint32_t id192 = instr_desc(192, kBlockRows);
   constexpr uint32_t id128 = instr_desc(128, kBlockRows);
   constexpr uint32_t id64 = instr_desc(64, kBlockRows);
-  const uint32_t a0 = st + (rb * 2 + 0) * kATileBytes;
-  const uint32_t a1 = st + (rb * 2 + 1) * kATileBytes;
-  const uint32_t bq = st + kRowBlocks * 2 * kATileBytes;
+  // Row block rb's A box: 128 rows of 128 bytes, plane 0 (x0 / p0 or p2)
+  // in the first 64 bytes of each row, plane 1 (x1 / p1 or p3) in the last.
+  const uint32_t a0 = st + rb * kABoxBytes;
+  const uint32_t a1 = a0 + 64;
+  const uint32_t bq = st + kRowBlocks * kABoxBytes;
 #pragma unroll
   for (int kk = 0; kk < kStageK / 16; ++kk) {
     const uint32_t acc = (first_stage && kk == 0) ? 0u : 1u;
-    const uint64_t da0 = smem_desc(a0 + kk * 32);
-    const uint64_t da1 = smem_desc(a1 + kk * 32);
+    const uint64_t da0 = smem_desc128(a0 + kk * 32);
+    const uint64_t da1 = smem_desc128(a1 + kk * 32);
     const uint64_t dbq = smem_desc(bq + kk * 32);
     if (kind != 2) {
       mma_f16(d, da0, dbq, id256, acc);          // x0 * [y0..y3] -> blocks 0..3
@@ -322,7 +337,10 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       const int nb = kind == 2 ? 2 : 4;  // request-byte planes this unit reads
       const CUtensorMap* am = kind == 0 ? &tm_db : &tm_pk;
       const CUtensorMap* bm = kind == 0 ? &tm_q : &tm_y;
-      const int plane0 = kind == 2 ? 2 : 0;
+      // A rows interleave the digit planes per 32-wide K chunk: the DB as
+      // [x0 | x1], the pack matrix as [p0 | p1 | p2 | p3].
+      const int a_chunk = kind == 0 ? 2 * kStageK : 4 * kStageK;
+      const int a_off = kind == 2 ? 2 * kStageK : 0;
       for (int h = 0; h < kStagesPerUnit; ++h) {
         const int g = kStagesPerUnit * i + h;
         const int s = g % kStages;
@@ -332,16 +350,13 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
         }
         unsigned char* st = smem + s * kStageBytes;
         const int x = kb * kUnitK + h * kStageK;
-        mbar_expect_tx(&full[s], kRowBlocks * 2 * kATileBytes + nb * kBLimbBytes);
+        mbar_expect_tx(&full[s], kRowBlocks * kABoxBytes + nb * kBLimbBytes);
+        const int ax = (x / kStageK) * a_chunk + a_off;
         for (int rb = 0; rb < kRowBlocks; ++rb) {
-          for (int pl = 0; pl < 2; ++pl) {
-            tma_load_2d(am, &full[s], st + (rb * 2 + pl) * kATileBytes, x,
-                        (plane0 + pl) * a.rows + row0 + rb * kBlockRows);
-          }
+          tma_load_2d(am, &full[s], st + rb * kABoxBytes, ax, row0 + rb * kBlockRows);
         }
         for (int j = 0; j < nb; ++j) {
-          tma_load_2d(bm, &full[s],
-                      st + kRowBlocks * 2 * kATileBytes + j * kBLimbBytes, x,
+          tma_load_2d(bm, &full[s], st + kRowBlocks * kABoxBytes + j * kBLimbBytes, x,
                       j * a.qcap + q0);
         }
         last_g[s] = g;
@@ -449,8 +464,9 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
 }
 
 // Digit planes of a u16 matrix: x - 2^15 = x0 + 2^8 x1 (x0 in [-128, 127],
-// x1 in [-128, 128]) as [2][rows][cols_pad] fp16; zero past cols (padding
-// columns meet zero query words, so their value does not matter).
+// x1 in [-128, 128]) as fp16, interleaved per 32-wide K chunk so that one
+// 128-byte row carries both planes of a chunk: [rows][cols_pad/32][2][32];
+// zero past cols (padding columns meet zero query words).
 __global__ void split_u16_kernel(const uint16_t* __restrict__ src,
                                  int64_t rows, int64_t cols,
                                  int64_t cols_pad, __half* __restrict__ dst) {
@@ -461,8 +477,9 @@ __global__ void split_u16_kernel(const uint16_t* __restrict__ src,
     const int v = c < cols ? static_cast<int>(src[r * cols + c]) - 32768 : 0;
     const int x0 = ((v + 128) & 255) - 128;
     const int x1 = (v - x0) / 256;
-    dst[i] = __int2half_rn(x0);
-    dst[total + i] = __int2half_rn(x1);
+    const int64_t o = r * 2 * cols_pad + (c / 32) * 64 + (c % 32);
+    dst[o] = __int2half_rn(x0);
+    dst[o + 32] = __int2half_rn(x1);
   }
 }
 
@@ -489,10 +506,13 @@ __global__ void row_sum_kernel(const uint32_t* __restrict__ q1, int64_t cols,
 // dropped: mod 2^32) of the u32 two's complement of a matrix of `kind`:
 // plane j holds rows_pad x cols_pad fp16 (zero outside rows x cols) and
 // starts at row j * plane_rows.
+// With interleave (the pack matrix, an A operand) the planes share rows
+// instead: [rows][cols_pad/32][4][32].
 __global__ void split_u32_kernel(const void* __restrict__ src, int kind,
                                  int64_t rows, int64_t cols, int64_t stride,
                                  int64_t rows_pad, int64_t plane_rows,
-                                 int64_t cols_pad, __half* __restrict__ dst) {
+                                 int64_t cols_pad, __half* __restrict__ dst,
+                                 int interleave = 0) {
   const int64_t total = rows_pad * cols_pad;
   const int64_t plane = plane_rows * cols_pad;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
@@ -514,7 +534,9 @@ __global__ void split_u32_kernel(const void* __restrict__ src, int kind,
       int b = static_cast<int>((x >> (8 * j)) & 255u) + carry;
       carry = b >= 128 ? 1 : 0;
       b -= carry << 8;
-      dst[j * plane + i] = __int2half_rn(b);
+      const int64_t o = interleave ? r * 4 * cols_pad + (c / 32) * 128 + j * 32 + (c % 32)
+                                   : j * plane + i;
+      dst[o] = __int2half_rn(b);
     }
   }
 }
@@ -536,17 +558,21 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // 2-D fp16 tensor [rows][cols], box box_rows x 32, 64-byte swizzle.
+// box_cols = kStageK (64-byte rows, 64-byte swizzle: the request planes) or
+// 2 * kStageK (128-byte rows, 128-byte swizzle: the interleaved A planes).
 bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols,
-              uint32_t box_rows) {
+              uint32_t box_rows, uint32_t box_cols = kStageK) {
   auto fn = encode_fn();
   if (fn == nullptr) return false;
   cuuint64_t dims[2] = {cols, rows};
   cuuint64_t strides[1] = {cols * 2};
-  cuuint32_t box[2] = {static_cast<cuuint32_t>(kStageK), box_rows};
+  cuuint32_t box[2] = {box_cols, box_rows};
   cuuint32_t elem[2] = {1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base),
                   dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  box_cols == 2 * kStageK ? CU_TENSOR_MAP_SWIZZLE_128B
+                                          : CU_TENSOR_MAP_SWIZZLE_64B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
@@ -589,10 +615,10 @@ class LimbGemmImpl : public LimbGemm {
     split_u16_kernel<<<152 * 16, 256>>>(static_cast<const uint16_t*>(db), rows,
                                         db_cols, cpad_, db_planes_);
     split_u32_kernel<<<152 * 16, 256>>>(pack, mat_kind, rows, pack_cols, pack_cols,
-                                        rows, rows, kpad_, pk_planes_);
+                                        rows, rows, kpad_, pk_planes_, 1);
     if (cudaDeviceSynchronize() != cudaSuccess) return false;
-    if (!make_map(&tm_db_, db_planes_, 2ull * rows, cpad_, kBlockRows)) return false;
-    if (!make_map(&tm_pk_, pk_planes_, 4ull * rows, kpad_, kBlockRows)) return false;
+    if (!make_map(&tm_db_, db_planes_, rows, 2ull * cpad_, kBlockRows, 2 * kStageK)) return false;
+    if (!make_map(&tm_pk_, pk_planes_, rows, 4ull * kpad_, kBlockRows, 2 * kStageK)) return false;
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev);

@@ -30,13 +30,20 @@
 // like the DB; then p2 -> blocks 2..3 and p3 -> block 3).
 //
 // Kernel structure. Each CTA covers two 128-row blocks that share one
-// 64-request tile (fewer operand bytes moved from L2 per MAC). 12 warps:
-//   warp 0     TMA producer: 4-stage ring of 48 KB (per stage, K = 32: four
-//              128x32 A tiles and a 4 x 64x32 tile of request digits,
-//              64-byte swizzled); four stages make one exact K=128 unit
+// 64-request tile (fewer operand bytes moved from L2 per MAC). Every operand
+// tile has 128-byte rows (128-byte swizzle): an A box row holds two digit
+// planes of a 32-wide K chunk, a request row 64 K of one plane. Shared
+// memory (224 KB) holds one ring of A boxes per row block (4 x 16 KB, one
+// per K=32 step of a unit, filled and released in pairs) and 3 request
+// slots of 32 KB (K = 64 x 4 planes x 64 requests). The MMA pipe runs row
+// block 0 over a unit, then row block 1, so a row block's boxes are
+// refilled a whole row-block pass before they are read again. 12 warps:
+//   warp 0     TMA producer, issuing loads in the order the MMA pipe frees
+//              their buffers
 //   warp 1     MMA issuer: one thread issues tcgen05.mma (M=128, K=16,
-//              N=256/192 or 128/64) for row block 0 into TMEM columns
-//              0..255, commits, then row block 1 into columns 256..511, so
+//              N=256/192 or 128/64) with descriptors that are the ring
+//              base plus compile-time offsets, row block 0 into TMEM
+//              columns 0..255, then row block 1 into columns 256..511, so
 //              one epilogue group drains a block while the other is filled
 //   warp 2     TMEM allocator (512 columns)
 //   warps 4-7  epilogue for row block 0, warps 8-11 for row block 1:
@@ -67,18 +74,29 @@ constexpr int kBlockRows = 128;    // rows per MMA (M)
 constexpr int kRowBlocks = 2;      // row blocks per CTA sharing a request tile
 constexpr int kTileRows = kBlockRows * kRowBlocks;
 constexpr int kTileQ = 64;         // requests per CTA
-constexpr int kStageK = 32;        // K per pipeline stage (64-byte rows)
+constexpr int kStageK = 32;        // K per A stage (two planes: 128-byte rows)
 constexpr int kUnitK = 128;        // K per exact accumulation unit
 constexpr int kStagesPerUnit = kUnitK / kStageK;
-constexpr int kStages = 4;
 constexpr int kATileBytes = kBlockRows * kStageK * 2;      // 8 KB per plane
 constexpr int kABoxBytes = 2 * kATileBytes;                // both planes: 16 KB
-constexpr int kBLimbBytes = kTileQ * kStageK * 2;          // 4 KB
-constexpr int kStageBytes = kRowBlocks * 2 * kATileBytes + 4 * kBLimbBytes;  // 48 KB
+// One ring of A boxes per row block, one box per step of a unit (so the box
+// of step h is h), filled and released in pairs of steps, and a ring of
+// request slots: the digit planes load K = 64 at a time (128-byte rows),
+// slot n serving steps 2n and 2n + 1 of both row blocks.
+constexpr int kAStages = kStagesPerUnit;
+constexpr int kAPairs = kAStages / 2;
+constexpr int kARingBytes = kAStages * kABoxBytes;         // 64 KB per row block
+constexpr int kBSlotK = 2 * kStageK;
+constexpr int kBPlaneBytes = kTileQ * kBSlotK * 2;         // 8 KB
+constexpr int kBSlotBytes = 4 * kBPlaneBytes;              // 32 KB
+constexpr int kBSlots = 3;
+constexpr int kBHalves = kStagesPerUnit / 2;               // request slots per unit
+constexpr int kRingBytes = kRowBlocks * kARingBytes + kBSlots * kBSlotBytes;  // 224 KB
 constexpr int kThreads = 384;
 constexpr int kTmemCols = 512;     // one 256-column accumulator per row block
 constexpr uint32_t kSpinLimit = 1u << 22;
-constexpr size_t kSmemBytes = kStages * kStageBytes + 1024 + 256;
+constexpr size_t kSmemBytes = kRingBytes + 1024 + 256;
+static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
 
 // ------------------------------------------------------------------ PTX --
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -165,17 +183,6 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a_desc,
-                                        uint64_t b_desc, uint32_t idesc,
-                                        uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 "
@@ -206,30 +213,6 @@ __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// Shared-memory matrix descriptor: K-major, 64-byte swizzle (rows of 64
-// bytes, 8-row groups 512 bytes apart = SBO), descriptor version 1.
-// K-major, 128-byte swizzle (rows of 128 bytes, 8-row groups 1024 bytes
-// apart): the A tiles, whose rows hold the two digit planes of a K chunk.
-__device__ __forceinline__ uint64_t smem_desc128(uint32_t addr) {
-  uint64_t d = 0;
-  d |= static_cast<uint64_t>((addr >> 4) & 0x3FFF);
-  d |= static_cast<uint64_t>(1) << 16;                 // LBO (unused: swizzled)
-  d |= static_cast<uint64_t>(1024 >> 4) << 32;         // SBO
-  d |= static_cast<uint64_t>(1) << 46;                 // version
-  d |= static_cast<uint64_t>(2) << 61;                 // SWIZZLE_128B
-  return d;
-}
-
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  uint64_t d = 0;
-  d |= static_cast<uint64_t>((addr >> 4) & 0x3FFF);
-  d |= static_cast<uint64_t>(1) << 16;                 // LBO (unused: swizzled)
-  d |= static_cast<uint64_t>(512 >> 4) << 32;          // SBO
-  d |= static_cast<uint64_t>(1) << 46;                 // version
-  d |= static_cast<uint64_t>(4) << 61;                 // SWIZZLE_64B
-  return d;
-}
-
 // Instruction descriptor of kind::f16: fp16 A/B, fp32 D, both K-major.
 __host__ __device__ constexpr uint32_t instr_desc(int n, int m) {
   return (1u << 4) | (static_cast<uint32_t>(n >> 3) << 17) |
@@ -250,32 +233,55 @@ __device__ __forceinline__ int unit_kind(int u, int n_db_units) {
   return u < n_db_units ? 0 : 1 + ((u - n_db_units) & 1);
 }
 
-// The MMAs of one 32-deep stage for one row block into accumulator d.
-__device__ __forceinline__ void issue_block(uint32_t st, int rb, int kind,
-                                            uint32_t d, bool first_stage) {
-  constexpr uint32_t id256 = instr_desc(256, kBlockRows);
-  constexpr uint32_t id192 = instr_desc(192, kBlockRows);
-  constexpr uint32_t id128 = instr_desc(128, kBlockRows);
-  constexpr uint32_t id64 = instr_desc(64, kBlockRows);
-  // Row block rb's A box: 128 rows of 128 bytes, plane 0 (x0 / p0 or p2)
-  // in the first 64 bytes of each row, plane 1 (x1 / p1 or p3) in the last.
-  const uint32_t a0 = st + rb * kABoxBytes;
-  const uint32_t a1 = a0 + 64;
-  const uint32_t bq = st + kRowBlocks * kABoxBytes;
-#pragma unroll
-  for (int kk = 0; kk < kStageK / 16; ++kk) {
-    const uint32_t acc = (first_stage && kk == 0) ? 0u : 1u;
-    const uint64_t da0 = smem_desc128(a0 + kk * 32);
-    const uint64_t da1 = smem_desc128(a1 + kk * 32);
-    const uint64_t dbq = smem_desc(bq + kk * 32);
-    if (kind != 2) {
-      mma_f16(d, da0, dbq, id256, acc);          // x0 * [y0..y3] -> blocks 0..3
-      mma_f16(d + 64, da1, dbq, id192, 1);       // x1 * [y0..y2] -> blocks 1..3
-    } else {
-      mma_f16(d + 128, da0, dbq, id128, acc);    // p2 * [y0 y1]  -> blocks 2..3
-      mma_f16(d + 192, da1, dbq, id64, 1);       // p3 * [y0]     -> block 3
-    }
-  }
+// Shared-memory matrix descriptors, K-major and swizzled: bits 0-13 the
+// address >> 4, 16-29 LBO >> 4 (1: unused when swizzled), 32-45 SBO >> 4
+// (the distance of 8-row groups), bit 46 the version, 61-63 the swizzle.
+// Every operand tile has 128-byte rows (128-byte swizzle, SBO 1024): an A
+// row holds two digit planes of a 32-wide K chunk, a request row 64 K of one
+// plane. The upper word is therefore one constant; the lower word is
+// (address >> 4) | 1 << 16, so every descriptor of the ring is a fixed
+// offset from the lower word of the ring base.
+constexpr uint32_t kDescHi128 = (1024 >> 4) | (1u << 14) | (2u << 29);
+
+__device__ __forceinline__ void mma_f16_w(uint32_t d_tmem, uint32_t a_lo,
+                                          uint32_t b_lo, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t.reg .b64 da, db;\n\t"
+      "mov.b64 da, {%1, %2};\n\t"
+      "mov.b64 db, {%3, %4};\n\t"
+      "setp.ne.b32 p, %6, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], da, db, %5, p;\n\t}" ::"r"(d_tmem),
+      "r"(a_lo), "r"(kDescHi128), "r"(b_lo), "r"(kDescHi128), "r"(idesc),
+      "r"(accumulate)
+      : "memory");
+}
+
+// Where the operands of unit u live: the A map and its x coordinate for
+// step 0 (A rows interleave the digit planes per 32-wide K chunk: the DB as
+// [x0 | x1], the pack matrix as [p0 | p1 | p2 | p3]), the request map and
+// its x for step 0, and how many request planes the unit reads.
+struct UnitSrc {
+  const CUtensorMap* am;
+  const CUtensorMap* bm;
+  int ax, a_step, bx, nb;
+};
+
+__device__ __forceinline__ UnitSrc unit_src(int u, int n_db_units,
+                                            const CUtensorMap* tm_db,
+                                            const CUtensorMap* tm_pk,
+                                            const CUtensorMap* tm_q,
+                                            const CUtensorMap* tm_y) {
+  const int kind = unit_kind(u, n_db_units);
+  const int kb = kind == 0 ? u : (u - n_db_units) >> 1;
+  UnitSrc r;
+  r.am = kind == 0 ? tm_db : tm_pk;
+  r.bm = kind == 0 ? tm_q : tm_y;
+  r.a_step = kind == 0 ? 2 * kStageK : 4 * kStageK;
+  r.ax = kb * kStagesPerUnit * r.a_step + (kind == 2 ? 2 * kStageK : 0);
+  r.bx = kb * kUnitK;
+  r.nb = kind == 2 ? 2 : 4;
+  return r;
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
@@ -288,9 +294,11 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
-  uint64_t* empty = full + kStages;
-  uint64_t* acc_full = empty + kStages;
+  uint64_t* a_full = reinterpret_cast<uint64_t*>(smem + kRingBytes);  // [rb][pair]
+  uint64_t* a_empty = a_full + kRowBlocks * kAPairs;
+  uint64_t* b_full = a_empty + kRowBlocks * kAPairs;                     // [slot]
+  uint64_t* b_empty = b_full + kBSlots;
+  uint64_t* acc_full = b_empty + kBSlots;
   uint64_t* acc_empty = acc_full + kRowBlocks;
   uint64_t* mma_done = acc_empty + kRowBlocks;
   uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
@@ -298,10 +306,15 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const int nqt = (a.batch + kTileQ - 1) / kTileQ;
+  // CTA order: request tile fastest (the tiles of a row pair read the same
+  // A boxes at about the same time), then row pair, then K slice: the
+  // resident CTAs all read one K slice of the request planes, which stays
+  // in L2 while every row pair passes over it.
+  const int n_pairs = a.rows / kTileRows;
   const int qt = blockIdx.x % nqt;
   const int rest = blockIdx.x / nqt;
-  const int ks = rest % a.ksplit;
-  const int row0 = (rest / a.ksplit) * kTileRows;
+  const int ks = rest / n_pairs;
+  const int row0 = (rest % n_pairs) * kTileRows;
   const int q0 = qt * kTileQ;
   const int n_units = a.n_db_units + 2 * a.n_pk_blocks;
   const int per = (n_units + a.ksplit - 1) / a.ksplit;
@@ -309,9 +322,13 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   const int nu = max(0, min(n_units, u0 + per) - u0);
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+    for (int s = 0; s < kRowBlocks * kAPairs; ++s) {
+      mbar_init(&a_full[s], 1);
+      mbar_init(&a_empty[s], 1);
+    }
+    for (int s = 0; s < kBSlots; ++s) {
+      mbar_init(&b_full[s], 1);
+      mbar_init(&b_empty[s], 1);
     }
     for (int b = 0; b < kRowBlocks; ++b) {
       mbar_init(&acc_full[b], 1);
@@ -326,68 +343,119 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   tc_fence_after();
   const uint32_t tmem = *tmem_base_slot;
 
+  // The MMA pipe runs row block 0 over a unit, then row block 1 over it. A
+  // box pair (rb, p) is refilled once row block rb has used it, a whole
+  // row-block pass before it is read again; request half n of unit i (steps
+  // 2n, 2n+1) lives in slot (kBHalves * i + n) % kBSlots, refilled after
+  // row block 1 has read its previous half.
   if (warp == 0 && lane == 0) {
     // ---------------------------------------------------- TMA producer --
-    int last_g[kStages] = {-1, -1, -1, -1};
+    // Loads go out in the order the MMA pipe frees their buffers: the row
+    // block 0 boxes of the unit, then per pair its request half and its row
+    // block 1 boxes.
+    int a_last[kRowBlocks * kAPairs];
+    int b_last[kBSlots];
+    for (int s = 0; s < kRowBlocks * kAPairs; ++s) a_last[s] = -1;
+    for (int s = 0; s < kBSlots; ++s) b_last[s] = -1;
     bool ok = true;
+    auto load_pair = [&](int rb, int p, const UnitSrc& src, int i) {
+      const int s = rb * kAPairs + p;
+      if (!mbar_wait(&a_empty[s], (i & 1) ^ 1, err)) return false;
+      mbar_expect_tx(&a_full[s], 2 * kABoxBytes);
+      for (int hh = 0; hh < 2; ++hh) {
+        const int h = 2 * p + hh;
+        tma_load_2d(src.am, &a_full[s], smem + rb * kARingBytes + h * kABoxBytes,
+                    src.ax + h * src.a_step, row0 + rb * kBlockRows);
+      }
+      a_last[s] = i;
+      return true;
+    };
     for (int i = 0; i < nu && ok; ++i) {
-      const int u = u0 + i;
-      const int kind = unit_kind(u, a.n_db_units);
-      const int kb = kind == 0 ? u : (u - a.n_db_units) >> 1;
-      const int nb = kind == 2 ? 2 : 4;  // request-byte planes this unit reads
-      const CUtensorMap* am = kind == 0 ? &tm_db : &tm_pk;
-      const CUtensorMap* bm = kind == 0 ? &tm_q : &tm_y;
-      // A rows interleave the digit planes per 32-wide K chunk: the DB as
-      // [x0 | x1], the pack matrix as [p0 | p1 | p2 | p3].
-      const int a_chunk = kind == 0 ? 2 * kStageK : 4 * kStageK;
-      const int a_off = kind == 2 ? 2 * kStageK : 0;
-      for (int h = 0; h < kStagesPerUnit; ++h) {
-        const int g = kStagesPerUnit * i + h;
-        const int s = g % kStages;
-        if (!mbar_wait(&empty[s], ((g / kStages) & 1) ^ 1, err)) {
+      const UnitSrc src = unit_src(u0 + i, a.n_db_units, &tm_db, &tm_pk, &tm_q, &tm_y);
+      for (int p = 0; p < kAPairs && ok; ++p) ok = load_pair(0, p, src, i);
+      for (int p = 0; p < kAPairs && ok; ++p) {
+        const int n = kBHalves * i + p;
+        const int slot = n % kBSlots;
+        if (!mbar_wait(&b_empty[slot], ((n / kBSlots) & 1) ^ 1, err)) {
           ok = false;
           break;
         }
-        unsigned char* st = smem + s * kStageBytes;
-        const int x = kb * kUnitK + h * kStageK;
-        mbar_expect_tx(&full[s], kRowBlocks * kABoxBytes + nb * kBLimbBytes);
-        const int ax = (x / kStageK) * a_chunk + a_off;
-        for (int rb = 0; rb < kRowBlocks; ++rb) {
-          tma_load_2d(am, &full[s], st + rb * kABoxBytes, ax, row0 + rb * kBlockRows);
-        }
-        for (int j = 0; j < nb; ++j) {
-          tma_load_2d(bm, &full[s], st + kRowBlocks * kABoxBytes + j * kBLimbBytes, x,
+        mbar_expect_tx(&b_full[slot], src.nb * kBPlaneBytes);
+        unsigned char* bs = smem + kRowBlocks * kARingBytes + slot * kBSlotBytes;
+        for (int j = 0; j < src.nb; ++j) {
+          tma_load_2d(src.bm, &b_full[slot], bs + j * kBPlaneBytes, src.bx + p * kBSlotK,
                       j * a.qcap + q0);
         }
-        last_g[s] = g;
+        b_last[slot] = n;
+        ok = load_pair(1, p, src, i);
       }
     }
     // Drain: every copy this thread issued has landed before the CTA exits.
-    for (int s = 0; s < kStages; ++s) {
-      if (last_g[s] >= 0) mbar_wait(&full[s], (last_g[s] / kStages) & 1, nullptr);
+    for (int s = 0; s < kRowBlocks * kAPairs; ++s) {
+      if (a_last[s] >= 0) mbar_wait(&a_full[s], a_last[s] & 1, nullptr);
+    }
+    for (int s = 0; s < kBSlots; ++s) {
+      if (b_last[s] >= 0) mbar_wait(&b_full[s], (b_last[s] / kBSlots) & 1, nullptr);
     }
   } else if (warp == 1 && lane == 0) {
     // ------------------------------------------------------ MMA issuer --
+    // The A descriptors are the ring base plus compile-time offsets and the
+    // request descriptors one slot offset per half: straight-line MMAs,
+    // which keep the one issuing thread ahead of the tensor pipe. The ring
+    // waits need no tcgen05 fence (the copies and the MMAs are both in the
+    // async proxy, ordered by the mbarrier); the accumulator hand-off does.
+    constexpr uint32_t id256 = instr_desc(256, kBlockRows);
+    constexpr uint32_t id192 = instr_desc(192, kBlockRows);
+    constexpr uint32_t id128 = instr_desc(128, kBlockRows);
+    constexpr uint32_t id64 = instr_desc(64, kBlockRows);
+    const uint32_t lo0 = (smem_addr(smem) >> 4) | (1u << 16);
     bool ok = true;
     for (int i = 0; i < nu && ok; ++i) {
-      const int kind = unit_kind(u0 + i, a.n_db_units);
-      for (int rb = 0; rb < kRowBlocks && ok; ++rb) {
-        if (!mbar_wait(&acc_empty[rb], (i & 1) ^ 1, err)) {
-          ok = false;
-          break;
-        }
+      // DB and low pack units: x0 * [y0..y3] -> blocks 0..3, then
+      // x1 * [y0..y2] -> blocks 1..3; high pack units: p2 * [y0 y1] ->
+      // blocks 2..3, then p3 * [y0] -> block 3.
+      const bool high = unit_kind(u0 + i, a.n_db_units) == 2;
+      const uint32_t id_0 = high ? id128 : id256, id_1 = high ? id64 : id192;
+      const uint32_t c_0 = high ? 128u : 0u, c_1 = high ? 192u : 64u;
+      int slot[kBHalves];
+      uint32_t b_lo[kBHalves];
+#pragma unroll
+      for (int p = 0; p < kBHalves; ++p) {
+        slot[p] = (kBHalves * i + p) % kBSlots;
+        b_lo[p] = lo0 + ((kRowBlocks * kARingBytes + slot[p] * kBSlotBytes) >> 4);
+      }
+#pragma unroll
+      for (int rb = 0; rb < kRowBlocks; ++rb) {
+        ok = ok && mbar_wait(&acc_empty[rb], (i & 1) ^ 1, err);
         tc_fence_after();
         const uint32_t d = tmem + rb * 256;
-        for (int h = 0; h < kStagesPerUnit; ++h) {
-          const int g = kStagesPerUnit * i + h;
-          const int s = g % kStages;
-          if (rb == 0 && !mbar_wait(&full[s], (g / kStages) & 1, err)) {
-            ok = false;
-            break;
+#pragma unroll
+        for (int p = 0; p < kAPairs; ++p) {
+          if (rb == 0) {
+            const int n = kBHalves * i + p;
+            ok = ok && mbar_wait(&b_full[slot[p]], (n / kBSlots) & 1, err);
           }
-          tc_fence_after();
-          issue_block(smem_addr(smem + s * kStageBytes), rb, kind, d, h == 0);
-          if (rb == kRowBlocks - 1) mma_commit(&empty[s]);
+          ok = ok && mbar_wait(&a_full[rb * kAPairs + p], i & 1, err);
+          if (ok) {
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+              const int h = 2 * p + hh;
+              const uint32_t ab = lo0 + ((rb * kARingBytes + h * kABoxBytes) >> 4);
+              // Odd steps read the second 64 bytes of the request rows.
+              const uint32_t bs = b_lo[p] + ((hh * 64) >> 4);
+#pragma unroll
+              for (int kk = 0; kk < kStageK / 16; ++kk) {
+                // An A box: 128 rows of 128 bytes, plane 0 in the first 64
+                // bytes of each row, plane 1 in the last.
+                const uint32_t a0 = ab + ((kk * 32) >> 4);
+                const uint32_t bq = bs + ((kk * 32) >> 4);
+                mma_f16_w(d + c_0, a0, bq, id_0, (h | kk) != 0 ? 1u : 0u);
+                mma_f16_w(d + c_1, a0 + (64 >> 4), bq, id_1, 1u);
+              }
+            }
+            mma_commit(&a_empty[rb * kAPairs + p]);
+            if (rb == kRowBlocks - 1) mma_commit(&b_empty[slot[p]]);
+          }
         }
         if (ok) mma_commit(&acc_full[rb]);
       }
@@ -558,10 +626,9 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // 2-D fp16 tensor [rows][cols], box box_rows x 32, 64-byte swizzle.
-// box_cols = kStageK (64-byte rows, 64-byte swizzle: the request planes) or
-// 2 * kStageK (128-byte rows, 128-byte swizzle: the interleaved A planes).
+// Box box_rows x box_cols with 128-byte rows and the 128-byte swizzle.
 bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols,
-              uint32_t box_rows, uint32_t box_cols = kStageK) {
+              uint32_t box_rows, uint32_t box_cols) {
   auto fn = encode_fn();
   if (fn == nullptr) return false;
   cuuint64_t dims[2] = {cols, rows};
@@ -570,8 +637,7 @@ bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols,
   cuuint32_t elem[2] = {1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base),
                   dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  box_cols == 2 * kStageK ? CU_TENSOR_MAP_SWIZZLE_128B
-                                          : CU_TENSOR_MAP_SWIZZLE_64B,
+                  CU_TENSOR_MAP_SWIZZLE_128B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
@@ -657,8 +723,8 @@ class LimbGemmImpl : public LimbGemm {
     if (e != cudaSuccess) return e;
     e = cudaMalloc(&sc->qsum, 4ull * need);
     if (e != cudaSuccess) return e;
-    if (!make_map(&sc->tm_q, sc->q_planes, 4ull * need, cpad_, kTileQ) ||
-        !make_map(&sc->tm_y, sc->y_planes, 4ull * need, kpad_, kTileQ)) {
+    if (!make_map(&sc->tm_q, sc->q_planes, 4ull * need, cpad_, kTileQ, kBSlotK) ||
+        !make_map(&sc->tm_y, sc->y_planes, 4ull * need, kpad_, kTileQ, kBSlotK)) {
       return cudaErrorInvalidValue;
     }
     sc->qcap = need;

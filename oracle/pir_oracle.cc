@@ -802,6 +802,198 @@ Status Interpolate(const V* row, int d, int t, uint32_t pmod, V* out) {
   return Status{};
 }
 
+// ---------------------------------------------------------------------------
+// PreprocessMatrixPack (crypto/lwes_to_rlwe.cc:163-446): PreprocessPack,
+// then BuildPreprocessMatrix; and Pack (lwes_to_rlwe.cc:356-412), the
+// automorphism route the matrix replaces.
+// ---------------------------------------------------------------------------
+// 5^k mod 2d (ComputePower, lwes_to_rlwe.cc:77-83).
+int PowerOf5(int k, int two_d) {
+  int64_t r = 1;
+  for (int i = 0; i < k; ++i) r = (r * 5) % two_d;
+  return static_cast<int>(r);
+}
+
+// p * X^e in Z_{2^w}[X]/(X^d + 1), 0 <= e < 2d.
+template <typename T>
+void TimesXPower(const T* p, int d, int e, T* out) {
+  const bool flip = e >= d;
+  if (flip) e -= d;
+  for (int i = 0; i < d; ++i) {
+    T v = i < e ? static_cast<T>(T{0} - p[d - e + i]) : p[i - e];
+    out[i] = flip ? static_cast<T>(T{0} - v) : v;
+  }
+}
+
+// The values P(X^{2m}), m < d, of P(Z) = sum_i c[i] Z^i whose coefficients
+// c[i] are ring elements (what EvaluateNttInPlace computes,
+// lwes_to_rlwe.cc:88-119), by direct summation: out[m] = sum_i c[i] X^{2im}.
+template <typename T>
+void EvaluateAtEvenPowers(const std::vector<T>& c, int d, std::vector<T>* out) {
+  out->assign(static_cast<size_t>(d) * d, T{0});
+  std::vector<T> tmp(d);
+  for (int m = 0; m < d; ++m) {
+    T* o = out->data() + static_cast<size_t>(m) * d;
+    for (int i = 0; i < d; ++i) {
+      const int e = static_cast<int>((2ll * i * m) % (2 * d));
+      TimesXPower(c.data() + static_cast<size_t>(i) * d, d, e, tmp.data());
+      for (int r = 0; r < d; ++r) o[r] += tmp[r];
+    }
+  }
+}
+
+// Odd power of slot k of the packing order: 5^k for k < d/2, (2d-1) 5^{k-d/2}
+// after (lwes_to_rlwe.cc:297-308).
+int SlotPower(int k, int d) {
+  if (k < d / 2) return PowerOf5(k, 2 * d);
+  return static_cast<int>((static_cast<int64_t>(PowerOf5(k - d / 2, 2 * d)) *
+                           (2 * d - 1)) % (2 * d));
+}
+
+// sum_l digits[l] (*) Automorph(w[l], power) as the InnerProduct wrapper
+// computes it (a_bits = log_digit, b_bits = log_q, signed digits).
+template <typename T>
+Status AutInner(int mode, const T* digits, const T* w, int k, int d, int power,
+                int log_digit, int log_q, T* out) {
+  std::vector<T> aut(static_cast<size_t>(k) * d);
+  for (int l = 0; l < k; ++l) {
+    Status s = Automorph<T>(w + static_cast<size_t>(l) * d, d, power,
+                            aut.data() + static_cast<size_t>(l) * d);
+    if (!s.ok()) return s;
+  }
+  return InnerProduct<T>(mode, digits, aut.data(), k, d, log_digit, log_q,
+                         ChunkFor(k, d), true, out);
+}
+
+// PreprocessPack (lwes_to_rlwe.cc:229-353). a_is: d rows of d words; w_g,
+// w_h: k = num_digits polynomials. t_vec_g / t_vec_gh: (d/2 - 1) x k x d.
+template <typename T>
+Status PreprocessPack(int mode, int log_q, int log_digit, int k, int d,
+                      const T* a_is, const T* w_g, const T* w_h, T* a_tilde_agg,
+                      T* t_vec_g, T* t_vec_gh, T* t_vec_h) {
+  int log2_d = 0;
+  while ((1 << log2_d) < d) ++log2_d;
+  const size_t dd = static_cast<size_t>(d) * d;
+  // 1-2) a_tilde_j = LowBits(RightShift(LowBits(sum_m a_j[m] X^{-m}), log d)).
+  std::vector<T> a_tilde(dd);
+  for (int j = 0; j < d; ++j) {
+    const T* a = a_is + static_cast<size_t>(j) * d;
+    T* o = a_tilde.data() + static_cast<size_t>(j) * d;
+    for (int m = 0; m < d; ++m) {
+      const T v = m == 0 ? a[0] : static_cast<T>(T{0} - a[d - m]);
+      o[m] = LowBitsOf<T>(static_cast<T>(LowBitsOf<T>(v, log_q) >> log2_d), log_q);
+    }
+  }
+  // 3) P_m = X^m sum_j a_tilde_j[m] X^j, evaluated at Z = X^{2i}; slot order.
+  std::vector<T> pk(dd), col(d), prime;
+  for (int m = 0; m < d; ++m) {
+    for (int j = 0; j < d; ++j) col[j] = a_tilde[static_cast<size_t>(j) * d + m];
+    TimesXPower(col.data(), d, m, pk.data() + static_cast<size_t>(m) * d);
+  }
+  EvaluateAtEvenPowers(pk, d, &prime);
+  auto hat = [&](int kk) {
+    return prime.data() + static_cast<size_t>((SlotPower(kk, d) - 1) / 2) * d;
+  };
+  // 4) The two reduction chains.
+  std::vector<T> tg(hat(d / 2 - 1), hat(d / 2 - 1) + d);
+  std::vector<T> tgh(hat(d - 1), hat(d - 1) + d);
+  std::vector<T> low(d), inner(d);
+  for (int i = d / 2 - 2; i >= 0; --i) {
+    const int pg = PowerOf5(i, 2 * d);
+    const int pgh = static_cast<int>((static_cast<int64_t>(pg) * (2 * d - 1)) % (2 * d));
+    T* dg = t_vec_g + static_cast<size_t>(i) * k * d;
+    for (int r = 0; r < d; ++r) low[r] = LowBitsOf<T>(tg[r], log_q);
+    Status s = SignedGadgetInv<T>(low.data(), d, log_q, log_digit, k, dg);
+    if (!s.ok()) return s;
+    s = AutInner<T>(mode, dg, w_g, k, d, pg, log_digit, log_q, inner.data());
+    if (!s.ok()) return s;
+    const T* ag = hat(i);
+    for (int r = 0; r < d; ++r) tg[r] = static_cast<T>(ag[r] + inner[r]);
+
+    T* dgh = t_vec_gh + static_cast<size_t>(i) * k * d;
+    for (int r = 0; r < d; ++r) low[r] = LowBitsOf<T>(tgh[r], log_q);
+    s = SignedGadgetInv<T>(low.data(), d, log_q, log_digit, k, dgh);
+    if (!s.ok()) return s;
+    s = AutInner<T>(mode, dgh, w_g, k, d, pgh, log_digit, log_q, inner.data());
+    if (!s.ok()) return s;
+    const T* agh = hat(d / 2 + i);
+    for (int r = 0; r < d; ++r) tgh[r] = static_cast<T>(agh[r] + inner[r]);
+  }
+  for (int r = 0; r < d; ++r) low[r] = LowBitsOf<T>(tgh[r], log_q);
+  Status s = SignedGadgetInv<T>(low.data(), d, log_q, log_digit, k, t_vec_h);
+  if (!s.ok()) return s;
+  s = InnerProduct<T>(mode, t_vec_h, w_h, k, d, log_digit, log_q, ChunkFor(k, d),
+                      true, inner.data());
+  if (!s.ok()) return s;
+  for (int r = 0; r < d; ++r) {
+    a_tilde_agg[r] = LowBitsOf<T>(static_cast<T>(tg[r] + inner[r]), log_q);
+  }
+  return Status{};
+}
+
+// BuildPreprocessMatrix (lwes_to_rlwe.cc:136-227): d x (k d) entries,
+// centred mod 2^log_q, as signed 64-bit values (the caller narrows them to
+// the matrix element type).
+template <typename T>
+void BuildPreprocessMatrix(int log_q, int k, int d, const T* t_vec_g,
+                           const T* t_vec_gh, int64_t* matrix) {
+  const size_t dd = static_cast<size_t>(d) * d;
+  std::vector<T> t(dd), ev, colp(d);
+  const int w = kBits<T>;
+  const T threshold = (log_q == 0 || log_q >= w) ? (T{1} << (w - 1))
+                                                : (T{1} << (log_q - 1));
+  for (int l = 0; l < k; ++l) {
+    std::fill(t.begin(), t.end(), T{0});
+    for (int j = 0; j <= d / 2 - 2; ++j) {
+      const int pg = PowerOf5(j, 2 * d);
+      const int pgh = static_cast<int>((static_cast<int64_t>(pg) * (2 * d - 1)) % (2 * d));
+      const T* src_g = t_vec_g + (static_cast<size_t>(j) * k + l) * d;
+      const T* src_gh = t_vec_gh + (static_cast<size_t>(j) * k + l) * d;
+      std::copy(src_g, src_g + d, t.data() + static_cast<size_t>((pg - 1) / 2) * d);
+      std::copy(src_gh, src_gh + d, t.data() + static_cast<size_t>((pgh - 1) / 2) * d);
+    }
+    EvaluateAtEvenPowers(t, d, &ev);
+    for (int c = 0; c < d; ++c) {
+      TimesXPower(ev.data() + static_cast<size_t>(c) * d, d, c, colp.data());
+      for (int r = 0; r < d; ++r) {
+        T v = colp[r];
+        if (v >= threshold && log_q < w) v = static_cast<T>(v - (T{1} << log_q));
+        using S = std::make_signed_t<T>;
+        matrix[static_cast<size_t>(r) * k * d + static_cast<size_t>(l) * d + c] =
+            static_cast<int64_t>(static_cast<S>(v));
+      }
+    }
+  }
+}
+
+// Pack (lwes_to_rlwe.cc:356-412): the b part of the packed ciphertext.
+template <typename T>
+Status Pack(int mode, int log_q, int log_digit, int k, int d, const T* b,
+            const T* y_g, const T* y_h, const T* t_vec_g, const T* t_vec_gh,
+            const T* t_vec_h, T* b_agg) {
+  std::vector<T> acc(d), inner(d);
+  for (int r = 0; r < d; ++r) acc[r] = LowBitsOf<T>(b[r], log_q);
+  for (int j = 0; j <= d / 2 - 2; ++j) {
+    const int pg = PowerOf5(j, 2 * d);
+    const int pgh = static_cast<int>((static_cast<int64_t>(pg) * (2 * d - 1)) % (2 * d));
+    Status s = AutInner<T>(mode, t_vec_g + static_cast<size_t>(j) * k * d, y_g, k,
+                           d, pg, log_digit, log_q, inner.data());
+    if (!s.ok()) return s;
+    for (int r = 0; r < d; ++r) acc[r] = LowBitsOf<T>(static_cast<T>(acc[r] + inner[r]), log_q);
+    s = AutInner<T>(mode, t_vec_gh + static_cast<size_t>(j) * k * d, y_g, k, d,
+                    pgh, log_digit, log_q, inner.data());
+    if (!s.ok()) return s;
+    for (int r = 0; r < d; ++r) acc[r] = LowBitsOf<T>(static_cast<T>(acc[r] + inner[r]), log_q);
+  }
+  Status s = InnerProduct<T>(mode, t_vec_h, y_h, k, d, log_digit, log_q,
+                             ChunkFor(k, d), true, inner.data());
+  if (!s.ok()) return s;
+  for (int r = 0; r < d; ++r) {
+    b_agg[r] = LowBitsOf<T>(static_cast<T>(acc[r] + inner[r]), log_q);
+  }
+  return Status{};
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -960,6 +1152,65 @@ int orc_process_response(const orc_params* prm, int mode, int db_kind,
         first_dim_len, static_cast<const T*>(second_dim), second_dim_count,
         static_cast<const T*>(packing_key), packing_key_count,
         static_cast<T*>(out), 1);
+  }
+  return Report(s, err, err_len);
+}
+
+int orc_preprocess_matrix_pack(int coeff_bits, int mode, int log_modulus,
+                               int log_digit, int num_digits, int d,
+                               const void* a_is, const void* w_vec_g,
+                               const void* w_vec_h, void* a_tilde_agg,
+                               int64_t* matrix, void* t_vec_h, void* t_vec_g,
+                               void* t_vec_gh, char* err, size_t err_len) {
+  if (d < 4 || (d & (d - 1)) != 0) {
+    return Report(Error(kInvalidArgument, "d must be a power of two >= 4."), err,
+                  err_len);
+  }
+  const size_t n = static_cast<size_t>(d / 2 - 1) * num_digits * d;
+  Status s;
+  auto run = [&](auto tag) {
+    using T = decltype(tag);
+    std::vector<T> g(n), gh(n);
+    s = PreprocessPack<T>(mode, log_modulus, log_digit, num_digits, d,
+                          static_cast<const T*>(a_is), static_cast<const T*>(w_vec_g),
+                          static_cast<const T*>(w_vec_h), static_cast<T*>(a_tilde_agg),
+                          g.data(), gh.data(), static_cast<T*>(t_vec_h));
+    if (!s.ok()) return;
+    if (matrix != nullptr) {
+      BuildPreprocessMatrix<T>(log_modulus, num_digits, d, g.data(), gh.data(), matrix);
+    }
+    if (t_vec_g != nullptr) std::copy(g.begin(), g.end(), static_cast<T*>(t_vec_g));
+    if (t_vec_gh != nullptr) std::copy(gh.begin(), gh.end(), static_cast<T*>(t_vec_gh));
+  };
+  if (coeff_bits == 32) {
+    run(uint32_t{});
+  } else if (coeff_bits == 64) {
+    run(uint64_t{});
+  } else {
+    s = Error(kInvalidArgument, "coeff_bits must be 32 or 64.");
+  }
+  return Report(s, err, err_len);
+}
+
+int orc_pack(int coeff_bits, int mode, int log_modulus, int log_digit,
+             int num_digits, int d, const void* b, const void* y_vec_g,
+             const void* y_vec_h, const void* t_vec_g, const void* t_vec_gh,
+             const void* t_vec_h, void* b_agg, char* err, size_t err_len) {
+  Status s;
+  if (coeff_bits == 32) {
+    using T = uint32_t;
+    s = Pack<T>(mode, log_modulus, log_digit, num_digits, d, static_cast<const T*>(b),
+                static_cast<const T*>(y_vec_g), static_cast<const T*>(y_vec_h),
+                static_cast<const T*>(t_vec_g), static_cast<const T*>(t_vec_gh),
+                static_cast<const T*>(t_vec_h), static_cast<T*>(b_agg));
+  } else if (coeff_bits == 64) {
+    using T = uint64_t;
+    s = Pack<T>(mode, log_modulus, log_digit, num_digits, d, static_cast<const T*>(b),
+                static_cast<const T*>(y_vec_g), static_cast<const T*>(y_vec_h),
+                static_cast<const T*>(t_vec_g), static_cast<const T*>(t_vec_gh),
+                static_cast<const T*>(t_vec_h), static_cast<T*>(b_agg));
+  } else {
+    s = Error(kInvalidArgument, "coeff_bits must be 32 or 64.");
   }
   return Report(s, err, err_len);
 }

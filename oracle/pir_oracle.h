@@ -129,6 +129,27 @@ int orc_interpolate(int value_bits, const void* db_row, int d, int t,
                     uint32_t plaintext_modulus, void* out, char* err,
                     size_t err_len);
 
+// PreprocessMatrixPack (crypto/lwes_to_rlwe.cc:163-446) for one slice:
+//   a_is     : d LWE a-vectors of d words (row i = a_i)
+//   w_vec_g  : num_digits polynomials (key-switching a-parts for X -> X^5)
+//   w_vec_h  : num_digits polynomials (for X -> X^{2d-1})
+// Writes a_tilde_agg (d words), t_vec_h (num_digits polynomials), and when
+// not null the d x (num_digits*d) matrix as centred signed 64-bit entries and
+// the (d/2-1) x num_digits x d digit polynomials t_vec_g / t_vec_gh.
+int orc_preprocess_matrix_pack(int coeff_bits, int mode, int log_modulus,
+                               int log_digit, int num_digits, int d,
+                               const void* a_is, const void* w_vec_g,
+                               const void* w_vec_h, void* a_tilde_agg,
+                               int64_t* matrix, void* t_vec_h, void* t_vec_g,
+                               void* t_vec_gh, char* err, size_t err_len);
+
+// Pack (crypto/lwes_to_rlwe.cc:356-412): b_agg of the packed ciphertext from
+// the LWE b-values and the key-switching b-parts, by automorphisms.
+int orc_pack(int coeff_bits, int mode, int log_modulus, int log_digit,
+             int num_digits, int d, const void* b, const void* y_vec_g,
+             const void* y_vec_h, const void* t_vec_g, const void* t_vec_gh,
+             const void* t_vec_h, void* b_agg, char* err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

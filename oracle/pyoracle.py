@@ -61,6 +61,10 @@ def lib():
                                      vp, vp, i64, vp, i64, vp, i64, vp, cp,
                                      sz],
             "orc_interpolate": [ci, vp, ci, ci, ctypes.c_uint32, vp, cp, sz],
+            "orc_preprocess_matrix_pack": [ci, ci, ci, ci, ci, ci, vp, vp, vp,
+                                           vp, vp, vp, vp, vp, cp, sz],
+            "orc_pack": [ci, ci, ci, ci, ci, ci, vp, vp, vp, vp, vp, vp, vp,
+                         cp, sz],
         }
         for name, args in sigs.items():
             fn = getattr(_lib, name)
@@ -154,6 +158,50 @@ def automorph(p, coeff_bits, power):
     out = np.zeros_like(p)
     _call(lib().orc_automorph, coeff_bits, _ptr(p), p.shape[0], power,
           _ptr(out))
+    return out
+
+
+def preprocess_matrix_pack(a_is, w_vec_g, w_vec_h, coeff_bits, log_modulus,
+                           log_digit, num_digits, mode=MODE_EXACT,
+                           with_matrix=True):
+    """PreprocessMatrixPack (crypto/lwes_to_rlwe.cc:163-446) for one slice.
+
+    Returns a dict: a_tilde_agg (d), t_vec_h (k x d), t_vec_g / t_vec_gh
+    ((d/2-1) x k x d digit polynomials) and, with with_matrix, the
+    d x (k*d) matrix as centred int64 entries."""
+    dt = _cdt(coeff_bits)
+    a_is = np.ascontiguousarray(a_is, dtype=dt)
+    d = a_is.shape[0]
+    k = num_digits
+    w_vec_g = np.ascontiguousarray(w_vec_g, dtype=dt).reshape(k, d)
+    w_vec_h = np.ascontiguousarray(w_vec_h, dtype=dt).reshape(k, d)
+    a_tilde = np.zeros(d, dtype=dt)
+    t_h = np.zeros((k, d), dtype=dt)
+    t_g = np.zeros((d // 2 - 1, k, d), dtype=dt)
+    t_gh = np.zeros((d // 2 - 1, k, d), dtype=dt)
+    mat = np.zeros((d, k * d), dtype=np.int64) if with_matrix else None
+    _call(lib().orc_preprocess_matrix_pack, coeff_bits, mode, log_modulus,
+          log_digit, num_digits, d, _ptr(a_is), _ptr(w_vec_g), _ptr(w_vec_h),
+          _ptr(a_tilde), _ptr(mat) if with_matrix else None, _ptr(t_h),
+          _ptr(t_g), _ptr(t_gh))
+    return {"a_tilde_agg": a_tilde, "t_vec_h": t_h, "t_vec_g": t_g,
+            "t_vec_gh": t_gh, "matrix": mat}
+
+
+def pack(b, y_vec_g, y_vec_h, pre, coeff_bits, log_modulus, log_digit,
+         num_digits, mode=MODE_EXACT):
+    """Pack (crypto/lwes_to_rlwe.cc:356-412): b_agg by automorphisms."""
+    dt = _cdt(coeff_bits)
+    b = np.ascontiguousarray(b, dtype=dt)
+    d = b.shape[0]
+    y_vec_g = np.ascontiguousarray(y_vec_g, dtype=dt)
+    y_vec_h = np.ascontiguousarray(y_vec_h, dtype=dt)
+    out = np.zeros(d, dtype=dt)
+    _call(lib().orc_pack, coeff_bits, mode, log_modulus, log_digit,
+          num_digits, d, _ptr(b), _ptr(y_vec_g), _ptr(y_vec_h),
+          _ptr(np.ascontiguousarray(pre["t_vec_g"], dtype=dt)),
+          _ptr(np.ascontiguousarray(pre["t_vec_gh"], dtype=dt)),
+          _ptr(np.ascontiguousarray(pre["t_vec_h"], dtype=dt)), _ptr(out))
     return out
 
 

@@ -467,6 +467,30 @@ int inspire_compute_hint_matrix(int32_t db_kind, int32_t coeff_bits,
                                 int32_t d, void* out, int32_t on_device,
                                 void* stream, char* err, size_t err_len);
 
+/*
+ * PreprocessMatrixPack (crypto/lwes_to_rlwe.cc:414-446, called per slice by
+ * PreprocessingServer::ComputePreprocessedOutputs,
+ * crypto/pir/server/preprocessing_server.h:248-271) for `slices` slices at
+ * once, exact (multi-prime NTT products, integer transforms):
+ *   hint    : slices*d rows of >= d CoeffType words, row stride hint_stride
+ *             (the hint matrix; slice i reads rows i*d .. i*d+d-1, columns
+ *             0..d-1, as its d LWE a-vectors)
+ *   pack_a  : 2*num_digits polynomials: w_vec_g then w_vec_h
+ *   a_tilde_agg : slices x d words;  t_vec_h : slices x num_digits x d words
+ *   matrix  : (slices*d) x (num_digits*d) entries of mat_kind (the
+ *             coefficient type, INSPIRE_I16 or INSPIRE_I32): the slices'
+ *             matrices stacked, i.e. the server's pack matrix
+ * on_device = 1: device pointers, work on `stream`; 0: host pointers.
+ */
+int inspire_preprocess_matrix_pack(int32_t coeff_bits, int32_t mat_kind,
+                                   int32_t log_modulus, int32_t log_digit,
+                                   int32_t num_digits, int32_t d, int32_t slices,
+                                   const void* hint, int64_t hint_stride,
+                                   const void* pack_a, int64_t pack_a_count,
+                                   void* a_tilde_agg, void* matrix, void* t_vec_h,
+                                   int32_t on_device, void* stream, char* err,
+                                   size_t err_len);
+
 /* Interpolate (crypto/db_row_interpolation.h) of one row of t*d values,
  * host pointers: out[j*d + c] = coefficient c of polynomial j. */
 int inspire_interpolate(int32_t value_bits, const void* db_row,

@@ -95,6 +95,9 @@ SIGNATURES = {
         ctypes.c_int),
     "inspire_finalize_matrix_pack": (
         [_vp, _vp, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_preprocess_matrix_pack": (
+        [_i32, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _i64, _vp, _i64, _vp,
+         _vp, _vp, _i32, _vp, _cp, _sz], ctypes.c_int),
 }
 
 

@@ -28,6 +28,7 @@
 #include "limb_gemm.h"
 #include "ntt.cuh"
 #include "poly_kernels.cuh"
+#include "preprocess_kernels.cuh"
 #include "server_api.h"
 
 namespace inspire {
@@ -2375,6 +2376,203 @@ int inspire_external_product(const inspire_pir_params* params,
   if (st.ok())
     st = Cuda(cudaMemcpy(out_b, dout.get<char>() + d * w, d * w, cudaMemcpyDeviceToHost),
               "copy");
+  return Report(st, err, err_len);
+}
+
+int inspire_preprocess_matrix_pack(int32_t coeff_bits, int32_t mat_kind,
+                                   int32_t log_modulus, int32_t log_digit,
+                                   int32_t num_digits, int32_t d, int32_t slices,
+                                   const void* hint, int64_t hint_stride,
+                                   const void* pack_a, int64_t pack_a_count,
+                                   void* a_tilde_agg, void* matrix, void* t_vec_h,
+                                   int32_t on_device, void* stream, char* err,
+                                   size_t err_len) {
+  using namespace inspire;
+  auto fail = [&](const char* m) { return Report(Err(INSPIRE_INVALID_ARGUMENT, m), err, err_len); };
+  if (coeff_bits != 32 && coeff_bits != 64) return fail("coeff_bits must be 32 or 64.");
+  const int coeff_kind = coeff_bits == 32 ? INSPIRE_U32 : INSPIRE_U64;
+  if (mat_kind != coeff_kind && mat_kind != INSPIRE_I16 && mat_kind != INSPIRE_I32) {
+    return fail("matrix type must be the coefficient type, i16 or i32.");
+  }
+  if (log_digit <= 0 || num_digits <= 0) {
+    return fail("log_digit and num_digits must be positive.");
+  }
+  if (pack_a_count != 2ll * num_digits) {
+    return fail("InnerProduct: size mismatch or empty");
+  }
+  if (num_digits > 64 || log_digit >= coeff_bits) {
+    return fail("gadget larger than the coefficient width.");
+  }
+  if (log_modulus <= 0 || log_modulus > coeff_bits) {
+    return fail("log_modulus must be in (0, coeff_bits].");
+  }
+  int logd = 0;
+  while ((1 << logd) < d) ++logd;
+  if (d < 4 || (1 << logd) != d || logd > 13) {
+    return fail("polynomial length must be a power of two between 4 and 8192.");
+  }
+  if (slices <= 0) return fail("slices must be positive.");
+  if (hint_stride < d) return fail("hint rows must hold d coefficients.");
+  if (hint == nullptr || pack_a == nullptr || a_tilde_agg == nullptr ||
+      matrix == nullptr || t_vec_h == nullptr) {
+    return fail("null buffer.");
+  }
+  const int k = num_digits;
+  int r = 0;
+  Status st = PrimesFor(BoundBits(k, d, log_digit, coeff_bits), &r);
+  if (!st.ok()) return Report(st, err, err_len);
+  const int iters = d > 4096 ? 2 : 1;
+  const int threads = d / (4 * iters);
+  const size_t w = coeff_bits / 8;
+  const size_t chain_smem = d * w + static_cast<size_t>(d) * 4 * (1 + r);
+  if (chain_smem > 227 * 1024) return fail("ring degree and gadget too large.");
+  std::unique_ptr<NttTables> tabs;
+  st = NttTables::Create(logd, &tabs);
+  if (!st.ok()) return Report(st, err, err_len);
+  const NttCtx c = tabs->Ctx(r);
+  const cudaStream_t cs = on_device ? static_cast<cudaStream_t>(stream) : nullptr;
+  const size_t mw = elem_size(mat_kind);
+  const size_t dd = static_cast<size_t>(d) * d;
+  const int64_t chain_stride = static_cast<int64_t>(d / 2 - 1) * k * d;
+
+  // Index tables: a_hat_agg[k] sits in transform slot bitrev((power_k - 1)/2);
+  // 5^i mod 2d; matrix block input i <- t_vec_g[j] (2j) / t_vec_gh[j] (2j+1).
+  std::vector<int> hat(d), pow5(d / 2), src_of(d, -1);
+  {
+    int64_t p5 = 1;
+    for (int i = 0; i < d / 2; ++i) {
+      pow5[i] = static_cast<int>(p5);
+      p5 = p5 * 5 % (2 * d);
+    }
+    for (int kk = 0; kk < d; ++kk) {
+      const int64_t power = kk < d / 2 ? pow5[kk]
+                                      : static_cast<int64_t>(pow5[kk - d / 2]) * (2 * d - 1) % (2 * d);
+      hat[kk] = BitRev(static_cast<int>((power - 1) / 2), logd);
+    }
+    for (int j = 0; j <= d / 2 - 2; ++j) {
+      const int64_t pg = pow5[j];
+      const int64_t pgh = pg * (2 * d - 1) % (2 * d);
+      src_of[(pg - 1) / 2] = 2 * j;
+      src_of[(pgh - 1) / 2] = 2 * j + 1;
+    }
+  }
+  DevBuf dhat, dpow, dsrc, dhint, dpa, dW, dev0, dev1, dtg, dtgh, dfin;
+  DevBuf da, dm, dth;
+  st = dhat.Upload(hat.data(), hat.size() * 4);
+  if (st.ok()) st = dpow.Upload(pow5.data(), pow5.size() * 4);
+  if (st.ok()) st = dsrc.Upload(src_of.data(), src_of.size() * 4);
+  const void* hint_dev = hint;
+  const void* pa_dev = pack_a;
+  void* a_out = a_tilde_agg;
+  void* m_out = matrix;
+  void* th_out = t_vec_h;
+  if (st.ok() && !on_device) {
+    st = dhint.Upload(hint, static_cast<size_t>(slices) * d * hint_stride * w);
+    if (st.ok()) st = dpa.Upload(pack_a, static_cast<size_t>(2 * k) * d * w);
+    if (st.ok()) st = da.Alloc(static_cast<size_t>(slices) * d * w);
+    if (st.ok()) st = dm.Alloc(static_cast<size_t>(slices) * d * k * d * mw);
+    if (st.ok()) st = dth.Alloc(static_cast<size_t>(slices) * k * d * w);
+    hint_dev = dhint.get();
+    pa_dev = dpa.get();
+    a_out = da.get();
+    m_out = dm.get();
+    th_out = dth.get();
+  }
+  if (st.ok()) st = dW.Alloc(static_cast<size_t>(2 * k) * r * d * 4);
+  if (st.ok()) st = dev0.Alloc(slices * dd * w);
+  if (st.ok()) st = dev1.Alloc(slices * dd * w);
+  if (st.ok()) st = dtg.Alloc(static_cast<size_t>(slices) * chain_stride * w);
+  if (st.ok()) st = dtgh.Alloc(static_cast<size_t>(slices) * chain_stride * w);
+  if (st.ok()) st = dfin.Alloc(static_cast<size_t>(slices) * 2 * d * w);
+
+  auto run = [&](auto tag) -> Status {
+    using T = decltype(tag);
+    // The transform of every key part (w_vec_g then w_vec_h), plain residues.
+    ntt_coeffs_kernel<T><<<dim3(2 * k * r, 1), PolyThreads(d), d * 4, cs>>>(
+        static_cast<const T*>(pa_dev), 0, 0, 2 * k, static_cast<T>(~0ull),
+        dW.get<uint32_t>(), d, c);
+    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "key part transforms"));
+    // Polynomial transform of d x d words per slice, log d DIF stages from
+    // `in` (rotated on input when rot) ping-ponging through dev0/dev1;
+    // returns the buffer holding the result.
+    auto transform = [&](DevBuf* in, bool rot) -> DevBuf* {
+      DevBuf* src = in;
+      DevBuf* dst = in == &dev0 ? &dev1 : &dev0;
+      const int64_t cells = static_cast<int64_t>(d / 2) * d;
+      const dim3 grid(static_cast<unsigned>((cells + 255) / 256), slices);
+      for (int lh = logd - 1; lh >= 0; --lh) {
+        pp_dif_stage_kernel<T><<<grid, 256, 0, cs>>>(src->get<T>(), dst->get<T>(), d, logd,
+                                                      lh, rot && lh == logd - 1 ? 1 : 0);
+        std::swap(src, dst);
+      }
+      return src;
+    };
+    const dim3 tgrid((d + 31) / 32, (d + 31) / 32, slices);
+    pp_atilde_kernel<T><<<tgrid, dim3(32, 8), 0, cs>>>(static_cast<const T*>(hint_dev),
+                                                       hint_stride, d, logd, log_modulus,
+                                                       dev0.get<T>());
+    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "a_tilde"));
+    DevBuf* ev = transform(&dev0, true);
+    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "a_hat_agg transform"));
+    ChainArgs ca;
+    ca.d = d;
+    ca.log_d = logd;
+    ca.log_q = log_modulus;
+    ca.log_digit = log_digit;
+    ca.k = k;
+    ca.chain_stride = chain_stride;
+    ca.hat_row = dhat.get<int>();
+    ca.pow5 = dpow.get<int>();
+    ca.Wg = dW.get<uint32_t>();
+    ca.Wh = dW.get<uint32_t>() + static_cast<size_t>(k) * r * d;
+    auto chains = [&](auto itag) -> Status {
+      constexpr int IT = decltype(itag)::value;
+      RETURN_IF_ERROR(SetSmem(pp_chain_kernel<T, IT>, chain_smem));
+      RETURN_IF_ERROR(SetSmem(pp_tail_kernel<T, IT>, chain_smem));
+      pp_chain_kernel<T, IT><<<dim3(2, slices), threads, chain_smem, cs>>>(
+          ev->get<T>(), ca, c, dtg.get<T>(), dtgh.get<T>(), dfin.get<T>());
+      RETURN_IF_ERROR(Cuda(cudaGetLastError(), "reduction chains"));
+      pp_tail_kernel<T, IT><<<slices, threads, chain_smem, cs>>>(
+          dfin.get<T>(), ca, c, static_cast<T*>(th_out), static_cast<T*>(a_out));
+      return Cuda(cudaGetLastError(), "a_tilde_agg");
+    };
+    if (iters == 2) {
+      RETURN_IF_ERROR(chains(std::integral_constant<int, 2>{}));
+    } else {
+      RETURN_IF_ERROR(chains(std::integral_constant<int, 1>{}));
+    }
+    // BuildPreprocessMatrix, one d x d block per digit plane l.
+    for (int l = 0; l < k; ++l) {
+      const int64_t cells = static_cast<int64_t>(d) * d;
+      pp_block_input_kernel<T><<<dim3(static_cast<unsigned>((cells + 255) / 256), slices), 256,
+                                 0, cs>>>(dtg.get<T>(), dtgh.get<T>(), dsrc.get<int>(), d, logd,
+                                          k, l, chain_stride, dev0.get<T>());
+      DevBuf* mev = transform(&dev0, false);
+      switch (mat_kind) {
+        case INSPIRE_I16:
+          pp_matrix_kernel<T, int16_t><<<tgrid, dim3(32, 8), 0, cs>>>(
+              mev->get<T>(), d, logd, log_modulus, k, l, static_cast<int16_t*>(m_out));
+          break;
+        case INSPIRE_I32:
+          pp_matrix_kernel<T, int32_t><<<tgrid, dim3(32, 8), 0, cs>>>(
+              mev->get<T>(), d, logd, log_modulus, k, l, static_cast<int32_t*>(m_out));
+          break;
+        default:
+          pp_matrix_kernel<T, T><<<tgrid, dim3(32, 8), 0, cs>>>(
+              mev->get<T>(), d, logd, log_modulus, k, l, static_cast<T*>(m_out));
+      }
+      RETURN_IF_ERROR(Cuda(cudaGetLastError(), "matrix block"));
+    }
+    return Status{};
+  };
+  if (st.ok()) st = coeff_bits == 32 ? run(uint32_t{}) : run(uint64_t{});
+  if (st.ok()) st = Cuda(cs == nullptr ? cudaDeviceSynchronize() : cudaStreamSynchronize(cs),
+                         "PreprocessMatrixPack");
+  if (st.ok() && !on_device) {
+    st = Cuda(cudaMemcpy(a_tilde_agg, da.get(), da.bytes(), cudaMemcpyDeviceToHost), "copy");
+    if (st.ok()) st = Cuda(cudaMemcpy(matrix, dm.get(), dm.bytes(), cudaMemcpyDeviceToHost), "copy");
+    if (st.ok()) st = Cuda(cudaMemcpy(t_vec_h, dth.get(), dth.bytes(), cudaMemcpyDeviceToHost), "copy");
+  }
   return Report(st, err, err_len);
 }
 

@@ -654,6 +654,43 @@ class VpirServer:
         return VpirResponse(self.process_arrays(fd, pk)[0])
 
 
+def PreprocessMatrixPack(hint, pack_a, log_modulus, log_digit, num_digits,
+                         mat_dtype=None, slices=None):
+    """PreprocessMatrixPack (crypto/lwes_to_rlwe.cc:414-446) on the GPU for
+    every slice of a hint matrix, as PreprocessingServer does
+    (crypto/pir/server/preprocessing_server.h:248-271).
+
+    hint: (slices*d, >= d) u32/u64 (slice i's LWE a-vectors are rows
+    i*d .. i*d+d-1, columns 0..d-1); pack_a: (2*num_digits, d), w_vec_g then
+    w_vec_h. Returns (a_tilde_agg (slices, d), matrix (slices*d,
+    num_digits*d) of mat_dtype (default: the coefficient type; int16 or
+    int32 also), t_vec_h (slices, num_digits, d))."""
+    h = np.ascontiguousarray(hint)
+    pa = np.ascontiguousarray(pack_a)
+    if h.dtype not in (np.dtype(np.uint32), np.dtype(np.uint64)) or h.ndim != 2:
+        raise InspireError(INVALID_ARGUMENT, "hint must be a 2-D u32/u64 matrix.")
+    pa = pa.astype(h.dtype, copy=False)
+    if pa.ndim != 2:
+        raise InspireError(INVALID_ARGUMENT, "pack_a must be (count, d).")
+    count, d = pa.shape
+    if slices is None:
+        slices = h.shape[0] // d if d else 0
+    mdt = np.dtype(mat_dtype) if mat_dtype is not None else h.dtype
+    kind = {np.dtype(np.uint32): 2, np.dtype(np.uint64): 3,
+            np.dtype(np.int16): 4, np.dtype(np.int32): 5}.get(mdt, -1)
+    a_tilde = np.zeros((max(slices, 0), d), dtype=h.dtype)
+    mat = np.zeros((max(slices, 0) * d, max(num_digits, 0) * d), dtype=mdt)
+    t_h = np.zeros((max(slices, 0), max(num_digits, 0), d), dtype=h.dtype)
+    err = _errbuf()
+    rc = _lib.load().inspire_preprocess_matrix_pack(
+        h.dtype.itemsize * 8, kind, log_modulus, log_digit, num_digits, d,
+        slices, _ptr(h), h.shape[1], _ptr(pa), count, _ptr(a_tilde),
+        _ptr(mat), _ptr(t_h), 0,
+        None, err, len(err))
+    _check(rc, err)
+    return a_tilde, mat, t_h
+
+
 def ComputeHintMatrix(database, a_components):
     """ComputeHintMatrix (crypto/hint_computation.cc:78-160) on the GPU:
     database (rows, n*d) of u8/u16/u32, a_components (n, d) of u32/u64 ->

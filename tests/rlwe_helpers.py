@@ -55,8 +55,10 @@ class Rlwe:
     """One key and the key-switching keys of the packing (X -> X^5 and
     X -> X^{2d-1})."""
 
-    def __init__(self, d, bits, log_q, log_digit, num_digits, seed):
+    def __init__(self, d, bits, log_q, log_digit, num_digits, seed,
+                 ksk_noise=2):
         self.d, self.bits, self.log_q = d, bits, log_q
+        self.ksk_noise = ksk_noise
         self.log_digit, self.num_digits = log_digit, num_digits
         self.rng = np.random.default_rng(seed)
         self.dt = dtype_of(bits)
@@ -88,7 +90,7 @@ class Rlwe:
                 ws = negacyclic(w[i], self.s, self.bits).astype(np.uint64)
                 tgt = (s_target.astype(np.uint64)
                        << np.uint64(i * self.log_digit + offset)) & wmask(self.bits)
-                e = self.small(2).astype(np.uint64)
+                e = self.small(self.ksk_noise).astype(np.uint64)
                 y[i] = ((np.uint64(0) - ws + e + tgt) & wmask(self.bits)).astype(self.dt)
         return w, y
 

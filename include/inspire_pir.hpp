@@ -234,6 +234,61 @@ class PirServer {
   inspire_pir_server* h_;
 };
 
+// GadgetParams (crypto/encryption.h) and PreprocessMatrixPackOutput
+// (crypto/lwes_to_rlwe.h:42-47); the matrix is row-major d x (num_digits*d).
+struct GadgetParams {
+  int log_digit = 19;
+  int num_digits = 2;
+};
+
+template <typename CoeffType, typename MatCoeffType>
+struct PreprocessMatrixPackOutput {
+  std::vector<CoeffType> a_tilde_agg;
+  std::vector<MatCoeffType> matrix;
+  int64_t rows = 0, cols = 0;
+  std::vector<std::vector<CoeffType>> t_vec_h;
+};
+
+// PreprocessMatrixPack (crypto/lwes_to_rlwe.cc:414-446) of one slice on the
+// GPU: a_is are the slice's d LWE a-vectors (d words each), w_vec_g / w_vec_h
+// the key-switching a-parts (num_digits polynomials each). The reference's
+// RlweParams enters as its log modulus.
+template <typename CoeffType, typename MatCoeffType>
+StatusOr<PreprocessMatrixPackOutput<CoeffType, MatCoeffType>> PreprocessMatrixPack(
+    int log_modulus, const std::vector<std::vector<CoeffType>>& a_is,
+    const std::vector<std::vector<CoeffType>>& w_vec_g,
+    const std::vector<std::vector<CoeffType>>& w_vec_h, const GadgetParams& gadget) {
+  const int d = static_cast<int>(a_is.size());
+  const int k = gadget.num_digits;
+  std::vector<CoeffType> hint;
+  for (const auto& row : a_is) hint.insert(hint.end(), row.begin(), row.end());
+  std::vector<CoeffType> pack;
+  for (const auto& p : w_vec_g) pack.insert(pack.end(), p.begin(), p.end());
+  for (const auto& p : w_vec_h) pack.insert(pack.end(), p.begin(), p.end());
+  if (static_cast<int64_t>(hint.size()) != static_cast<int64_t>(d) * d ||
+      static_cast<int64_t>(pack.size()) !=
+          static_cast<int64_t>(w_vec_g.size() + w_vec_h.size()) * d) {
+    return Status(INSPIRE_INVALID_ARGUMENT, "a_is must be d vectors of d words.");
+  }
+  PreprocessMatrixPackOutput<CoeffType, MatCoeffType> out;
+  out.rows = d;
+  out.cols = static_cast<int64_t>(k) * d;
+  out.a_tilde_agg.resize(d);
+  out.matrix.resize(static_cast<size_t>(out.rows * out.cols));
+  std::vector<CoeffType> th(static_cast<size_t>(k > 0 ? k : 0) * d);
+  char err[512];
+  const int rc = inspire_preprocess_matrix_pack(
+      8 * sizeof(CoeffType), KindOf<MatCoeffType>(), log_modulus, gadget.log_digit, k, d, 1,
+      hint.data(), d, pack.data(), static_cast<int64_t>(w_vec_g.size() + w_vec_h.size()),
+      out.a_tilde_agg.data(), out.matrix.data(), th.data(), 0, nullptr, err, sizeof(err));
+  if (rc != INSPIRE_OK) return Status(rc, err);
+  for (int l = 0; l < k; ++l) {
+    out.t_vec_h.emplace_back(th.begin() + static_cast<size_t>(l) * d,
+                             th.begin() + static_cast<size_t>(l + 1) * d);
+  }
+  return out;
+}
+
 }  // namespace inspire_gb300
 
 #endif  // INSPIRE_PIR_HPP_

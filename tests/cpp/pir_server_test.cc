@@ -144,11 +144,52 @@ void RunCase(const Case& c, const std::string& dir) {
 
 }  // namespace
 
+// PreprocessMatrixPack through the C++ mirror against the oracle's
+// restatement (d = 64, the reference test's degree; int32 matrix entries).
+void PreprocessCase(int log_q, int log_digit, int k) {
+  const int d = 64;
+  std::mt19937_64 g(1000 + log_q);
+  const uint32_t mask = log_q >= 32 ? 0xFFFFFFFFu : ((1u << log_q) - 1);
+  std::vector<std::vector<uint32_t>> a_is(d, std::vector<uint32_t>(d));
+  for (auto& row : a_is)
+    for (auto& x : row) x = static_cast<uint32_t>(g()) & mask;
+  std::vector<std::vector<uint32_t>> wg(k, std::vector<uint32_t>(d)), wh = wg;
+  for (auto* v : {&wg, &wh})
+    for (auto& p : *v)
+      for (auto& x : p) x = static_cast<uint32_t>(g()) & mask;
+  auto got = inspire_gb300::PreprocessMatrixPack<uint32_t, int32_t>(
+      log_q, a_is, wg, wh, inspire_gb300::GadgetParams{log_digit, k});
+  CHECK(got.ok(), "PreprocessMatrixPack");
+  if (!got.ok()) return;
+  std::vector<uint32_t> flat_a, flat_g, flat_h;
+  for (auto& r : a_is) flat_a.insert(flat_a.end(), r.begin(), r.end());
+  for (auto& p : wg) flat_g.insert(flat_g.end(), p.begin(), p.end());
+  for (auto& p : wh) flat_h.insert(flat_h.end(), p.begin(), p.end());
+  std::vector<uint32_t> a(d), th(static_cast<size_t>(k) * d);
+  std::vector<int64_t> mat(static_cast<size_t>(d) * k * d);
+  char err[512];
+  const int rc = orc_preprocess_matrix_pack(32, ORC_MODE_EXACT, log_q, log_digit, k, d,
+                                            flat_a.data(), flat_g.data(), flat_h.data(),
+                                            a.data(), mat.data(), th.data(), nullptr,
+                                            nullptr, err, sizeof(err));
+  CHECK(rc == 0, "oracle PreprocessMatrixPack");
+  CHECK(got->a_tilde_agg == a, "a_tilde_agg");
+  bool th_ok = true;
+  for (int l = 0; l < k; ++l)
+    for (int j = 0; j < d; ++j) th_ok &= got->t_vec_h[l][j] == th[static_cast<size_t>(l) * d + j];
+  CHECK(th_ok, "t_vec_h");
+  bool m_ok = true;
+  for (size_t i = 0; i < mat.size(); ++i) m_ok &= got->matrix[i] == static_cast<int32_t>(mat[i]);
+  CHECK(m_ok, "matrix");
+}
+
 int main(int argc, char** argv) {
   const std::string dir = argc > 1 ? argv[1] : ".";
   RunCase({8, 4, 1, 4 * 512}, dir);    // d = 256, t = 4
   RunCase({11, 2, 2, 2 * 1024}, dir);  // d = 2048, t = 2, l = 2
   RunCase({7, 1, 1, 256}, dir);        // t = 1: no EvalPoly
+  PreprocessCase(32, 19, 2);
+  PreprocessCase(27, 4, 5);
   if (failures == 0) std::printf("pir_server_test: all checks passed\n");
   return failures == 0 ? 0 : 1;
 }

@@ -491,6 +491,40 @@ int inspire_preprocess_matrix_pack(int32_t coeff_bits, int32_t mat_kind,
                                    int32_t on_device, void* stream, char* err,
                                    size_t err_len);
 
+/*
+ * A batched PIR client on the GPU, for load generation and end-to-end tests
+ * (PirClient, crypto/pir/client/pir_client.cc:61-272). Client b holds the
+ * ternary secret key secret_keys[b][0..d) (values -1, 0, 1) and asks for
+ * entry indices[b]. a_components are the public a-components the server was
+ * preprocessed with, in PreprocessingServer::Preprocess's order
+ * (preprocessing_server.h:96-112): NumFirstDimSamples first-dimension ones,
+ * 2*eval_num_digits second-dimension ones when t > 1, 2*pack_num_digits
+ * packing ones. Errors are centred binomials of `variance` from a
+ * counter-based hash of (seed, client, row, coefficient): reproducible, NOT
+ * cryptographically secure (the reference samples with ChaCha). Outputs per
+ * client: first_dim[n/t], second_dim[2*ne][d] (absent when t == 1),
+ * packing_key[2*k][d], CoeffType words. "Index out of bounds." for a bad
+ * index. on_device = 1: device pointers on `stream`; 0: host pointers.
+ */
+int inspire_client_create_requests(const inspire_pir_params* params,
+                                   const int8_t* secret_keys,
+                                   const void* a_components, int64_t a_count,
+                                   const int64_t* indices, int32_t batch,
+                                   uint64_t seed, int32_t variance,
+                                   void* first_dim, void* second_dim,
+                                   void* packing_key, int32_t on_device,
+                                   void* stream, char* err, size_t err_len);
+
+/* PirClient::ProcessResponse (DecryptAfterModulusSwitch per ciphertext,
+ * crypto/encryption.cc:330-376) for a batch: responses[b] holds
+ * entry_size_multiple ciphertexts (a then b, d words each); out[b] the
+ * entry_size_multiple*d plaintext words. */
+int inspire_client_process_responses(const inspire_pir_params* params,
+                                     const int8_t* secret_keys,
+                                     const void* responses, int32_t batch,
+                                     void* out, int32_t on_device, void* stream,
+                                     char* err, size_t err_len);
+
 /* Interpolate (crypto/db_row_interpolation.h) of one row of t*d values,
  * host pointers: out[j*d + c] = coefficient c of polynomial j. */
 int inspire_interpolate(int32_t value_bits, const void* db_row,

@@ -95,6 +95,11 @@ SIGNATURES = {
         ctypes.c_int),
     "inspire_finalize_matrix_pack": (
         [_vp, _vp, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_client_create_requests": (
+        [_vp, _vp, _vp, _i64, _vp, _i32, ctypes.c_uint64, _i32, _vp, _vp, _vp,
+         _i32, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_client_process_responses": (
+        [_vp, _vp, _vp, _i32, _vp, _i32, _vp, _cp, _sz], ctypes.c_int),
     "inspire_preprocess_matrix_pack": (
         [_i32, _i32, _i32, _i32, _i32, _i32, _i32, _vp, _i64, _vp, _i64, _vp,
          _vp, _vp, _i32, _vp, _cp, _sz], ctypes.c_int),

@@ -29,6 +29,7 @@
 #include "ntt.cuh"
 #include "poly_kernels.cuh"
 #include "preprocess_kernels.cuh"
+#include "client_kernels.cuh"
 #include "server_api.h"
 
 namespace inspire {
@@ -2572,6 +2573,188 @@ int inspire_preprocess_matrix_pack(int32_t coeff_bits, int32_t mat_kind,
     st = Cuda(cudaMemcpy(a_tilde_agg, da.get(), da.bytes(), cudaMemcpyDeviceToHost), "copy");
     if (st.ok()) st = Cuda(cudaMemcpy(matrix, dm.get(), dm.bytes(), cudaMemcpyDeviceToHost), "copy");
     if (st.ok()) st = Cuda(cudaMemcpy(t_vec_h, dth.get(), dth.bytes(), cudaMemcpyDeviceToHost), "copy");
+  }
+  return Report(st, err, err_len);
+}
+
+int inspire_client_create_requests(const inspire_pir_params* params,
+                                   const int8_t* secret_keys, const void* a_components,
+                                   int64_t a_count, const int64_t* indices, int32_t batch,
+                                   uint64_t seed, int32_t variance, void* first_dim,
+                                   void* second_dim, void* packing_key, int32_t on_device,
+                                   void* stream, char* err, size_t err_len) {
+  using namespace inspire;
+  auto fail = [&](const char* m) { return Report(Err(INSPIRE_INVALID_ARGUMENT, m), err, err_len); };
+  if (params == nullptr) return fail("params is null.");
+  const int cb = params->coeff_bits;
+  if (cb != 32 && cb != 64) return fail("coeff_bits must be 32 or 64.");
+  const int logd = params->log_degree;
+  if (logd < 2 || logd > 13) return fail("log_degree must be in [2, 13].");
+  const int d = 1 << logd;
+  const int t = params->interpolation_degree;
+  const int n = params->num_entries;
+  if (t <= 0 || n <= 0 || n % t != 0) return fail("num_entries must be a multiple of t.");
+  if (batch <= 0) return fail("batch must be positive.");
+  if (params->plaintext_modulus == 0) return fail("Plaintext modulus must be positive.");
+  const int64_t fd_len = n / t;
+  const int ns = static_cast<int>((fd_len + d - 1) / d);
+  const int ne = t > 1 ? params->eval_num_digits : 0;
+  const int kp = params->pack_num_digits;
+  const int64_t rows = ns + 2ll * ne + 2ll * kp;
+  if (a_count != rows) {
+    return fail("a_components must hold the first-dimension, second-dimension and "
+                "packing a-components in that order.");
+  }
+  std::vector<int64_t> idx(batch);
+  if (on_device) {
+    Status s0 = Cuda(cudaMemcpy(idx.data(), indices, batch * 8, cudaMemcpyDeviceToHost), "copy");
+    if (!s0.ok()) return Report(s0, err, err_len);
+  } else {
+    std::memcpy(idx.data(), indices, batch * 8);
+  }
+  for (int64_t x : idx) {
+    if (x < 0 || x >= n) {
+      return Report(Err(INSPIRE_INVALID_ARGUMENT, "Index out of bounds."), err, err_len);
+    }
+  }
+  int r = 0;
+  Status st = PrimesFor(BoundBits(1, d, cb, 2), &r);
+  if (!st.ok()) return Report(st, err, err_len);
+  std::unique_ptr<NttTables> tabs;
+  st = NttTables::Create(logd, &tabs);
+  if (!st.ok()) return Report(st, err, err_len);
+  const NttCtx c = tabs->Ctx(r);
+  const cudaStream_t cs = on_device ? static_cast<cudaStream_t>(stream) : nullptr;
+  const size_t w = cb / 8;
+  DevBuf dkeys, da, didx, dshat, dfd, dsd, dpk;
+  const int8_t* keys = secret_keys;
+  const void* a_dev = a_components;
+  void* fd_out = first_dim;
+  void* sd_out = second_dim;
+  void* pk_out = packing_key;
+  if (!on_device) {
+    st = dkeys.Upload(secret_keys, static_cast<size_t>(batch) * d);
+    if (st.ok()) st = da.Upload(a_components, rows * d * w);
+    if (st.ok()) st = didx.Upload(idx.data(), batch * 8);
+    if (st.ok()) st = dfd.Alloc(static_cast<size_t>(batch) * fd_len * w);
+    if (st.ok() && ne > 0) st = dsd.Alloc(static_cast<size_t>(batch) * 2 * ne * d * w);
+    if (st.ok()) st = dpk.Alloc(static_cast<size_t>(batch) * 2 * kp * d * w);
+    keys = dkeys.get<int8_t>();
+    a_dev = da.get();
+    fd_out = dfd.get();
+    sd_out = dsd.get();
+    pk_out = dpk.get();
+  }
+  if (st.ok()) st = dshat.Alloc(static_cast<size_t>(batch) * r * d * 4);
+  ClientArgs ca;
+  ca.d = d;
+  ca.log_d = logd;
+  ca.log_q = params->log_modulus;
+  ca.k_pack = kp;
+  ca.ne = ne;
+  ca.ns = ns;
+  ca.t = t;
+  ca.fd_len = fd_len;
+  ca.pack_log_digit = params->pack_log_digit;
+  ca.eval_log_digit = params->eval_log_digit;
+  ca.var = variance;
+  ca.seed = seed;
+  ca.plaintext_modulus = params->plaintext_modulus;
+  ca.keys = keys;
+  ca.index = on_device ? indices : didx.get<int64_t>();
+  const int iters = d > 4096 ? 2 : 1;
+  const int threads = d / (4 * iters);
+  const size_t smem = static_cast<size_t>(r) * d * 4;
+  auto run = [&](auto tag) -> Status {
+    using T = decltype(tag);
+    auto go = [&](auto itag) -> Status {
+      constexpr int IT = decltype(itag)::value;
+      RETURN_IF_ERROR(SetSmem(cl_key_ntt_kernel<IT>, d * 4));
+      RETURN_IF_ERROR(SetSmem(cl_request_kernel<T, IT>, smem));
+      cl_key_ntt_kernel<IT><<<dim3(r, batch), threads, d * 4, cs>>>(keys, c,
+                                                                     dshat.get<uint32_t>());
+      cl_request_kernel<T, IT><<<dim3(static_cast<unsigned>(rows), batch), threads, smem, cs>>>(
+          static_cast<const T*>(a_dev), dshat.get<uint32_t>(), ca, c, static_cast<T*>(fd_out),
+          static_cast<T*>(sd_out), static_cast<T*>(pk_out));
+      return Cuda(cudaGetLastError(), "client requests");
+    };
+    return iters == 2 ? go(std::integral_constant<int, 2>{}) : go(std::integral_constant<int, 1>{});
+  };
+  if (st.ok()) st = cb == 32 ? run(uint32_t{}) : run(uint64_t{});
+  if (st.ok()) st = Cuda(cs == nullptr ? cudaDeviceSynchronize() : cudaStreamSynchronize(cs),
+                         "client requests");
+  if (st.ok() && !on_device) {
+    st = Cuda(cudaMemcpy(first_dim, dfd.get(), dfd.bytes(), cudaMemcpyDeviceToHost), "copy");
+    if (st.ok() && ne > 0) {
+      st = Cuda(cudaMemcpy(second_dim, dsd.get(), dsd.bytes(), cudaMemcpyDeviceToHost), "copy");
+    }
+    if (st.ok()) st = Cuda(cudaMemcpy(packing_key, dpk.get(), dpk.bytes(), cudaMemcpyDeviceToHost), "copy");
+  }
+  return Report(st, err, err_len);
+}
+
+int inspire_client_process_responses(const inspire_pir_params* params,
+                                     const int8_t* secret_keys, const void* responses,
+                                     int32_t batch, void* out, int32_t on_device, void* stream,
+                                     char* err, size_t err_len) {
+  using namespace inspire;
+  auto fail = [&](const char* m) { return Report(Err(INSPIRE_INVALID_ARGUMENT, m), err, err_len); };
+  if (params == nullptr) return fail("params is null.");
+  const int cb = params->coeff_bits;
+  if (cb != 32 && cb != 64) return fail("coeff_bits must be 32 or 64.");
+  const int logd = params->log_degree;
+  if (logd < 2 || logd > 13) return fail("log_degree must be in [2, 13].");
+  if (params->plaintext_modulus == 0) return fail("Plaintext modulus must be positive.");
+  if (batch <= 0) return fail("batch must be positive.");
+  const int d = 1 << logd;
+  const int l = params->entry_size_multiple;
+  if (l <= 0) return fail("entry_size_multiple must be positive.");
+  int r = 0;
+  Status st = PrimesFor(BoundBits(1, d, cb, 2), &r);
+  if (!st.ok()) return Report(st, err, err_len);
+  std::unique_ptr<NttTables> tabs;
+  st = NttTables::Create(logd, &tabs);
+  if (!st.ok()) return Report(st, err, err_len);
+  const NttCtx c = tabs->Ctx(r);
+  const cudaStream_t cs = on_device ? static_cast<cudaStream_t>(stream) : nullptr;
+  const size_t w = cb / 8;
+  DevBuf dkeys, dresp, dout, dshat;
+  const int8_t* keys = secret_keys;
+  const void* resp = responses;
+  void* o = out;
+  if (!on_device) {
+    st = dkeys.Upload(secret_keys, static_cast<size_t>(batch) * d);
+    if (st.ok()) st = dresp.Upload(responses, static_cast<size_t>(batch) * l * 2 * d * w);
+    if (st.ok()) st = dout.Alloc(static_cast<size_t>(batch) * l * d * w);
+    keys = dkeys.get<int8_t>();
+    resp = dresp.get();
+    o = dout.get();
+  }
+  if (st.ok()) st = dshat.Alloc(static_cast<size_t>(batch) * r * d * 4);
+  const int iters = d > 4096 ? 2 : 1;
+  const int threads = d / (4 * iters);
+  const size_t smem = static_cast<size_t>(r) * d * 4;
+  auto run = [&](auto tag) -> Status {
+    using T = decltype(tag);
+    auto go = [&](auto itag) -> Status {
+      constexpr int IT = decltype(itag)::value;
+      RETURN_IF_ERROR(SetSmem(cl_key_ntt_kernel<IT>, d * 4));
+      RETURN_IF_ERROR(SetSmem(cl_decrypt_kernel<T, IT>, smem));
+      cl_key_ntt_kernel<IT><<<dim3(r, batch), threads, d * 4, cs>>>(keys, c,
+                                                                     dshat.get<uint32_t>());
+      cl_decrypt_kernel<T, IT><<<dim3(l, batch), threads, smem, cs>>>(
+          static_cast<const T*>(resp), dshat.get<uint32_t>(), l,
+          params->log_modulus1_after_switch, params->log_modulus2_after_switch,
+          params->plaintext_modulus, c, static_cast<T*>(o));
+      return Cuda(cudaGetLastError(), "client decryption");
+    };
+    return iters == 2 ? go(std::integral_constant<int, 2>{}) : go(std::integral_constant<int, 1>{});
+  };
+  if (st.ok()) st = cb == 32 ? run(uint32_t{}) : run(uint64_t{});
+  if (st.ok()) st = Cuda(cs == nullptr ? cudaDeviceSynchronize() : cudaStreamSynchronize(cs),
+                         "client decryption");
+  if (st.ok() && !on_device) {
+    st = Cuda(cudaMemcpy(out, dout.get(), dout.bytes(), cudaMemcpyDeviceToHost), "copy");
   }
   return Report(st, err, err_len);
 }

@@ -691,6 +691,144 @@ def PreprocessMatrixPack(hint, pack_a, log_modulus, log_digit, num_digits,
     return a_tilde, mat, t_h
 
 
+class PreprocessingServer:
+    """PreprocessingServer (crypto/pir/server/preprocessing_server.h:62-273)
+    with every stage on the GPU: interpolation and transposition, the hint
+    matrix, PreprocessMatrixPack per slice. The a-components come in as an
+    array (the reference draws them from a ChaCha PRNG seeded by prng_seed,
+    which this build does not have): NumFirstDimSamples first-dimension
+    ones, 2*eval_num_digits second-dimension ones when t > 1, then
+    2*pack_num_digits packing ones, each a polynomial of d words."""
+
+    def __init__(self, params: PirParams, a_components):
+        self.params = params
+        self.a_components = np.ascontiguousarray(a_components,
+                                                 dtype=params.coeff_dtype)
+        p = params
+        self.ns = p.NumFirstDimSamples()
+        self.ne = 2 * p.eval_gadget.num_digits if p.interpolation_degree > 1 else 0
+        self.np_ = 2 * p.pack_gadget.num_digits
+        if self.a_components.shape != (self.ns + self.ne + self.np_,
+                                       p.rlwe.degree):
+            raise InspireError(INVALID_ARGUMENT,
+                               "a_components must hold the first-dimension, "
+                               "second-dimension and packing a-components.")
+
+    @staticmethod
+    def Create(params: PirParams, a_components):
+        return PreprocessingServer(params, a_components)
+
+    def Preprocess(self, db_raw, db_dtype=np.uint16, mat_dtype=np.int32):
+        """PreprocessingServer::Preprocess: raw DB (num_entries records of
+        entry_size_multiple*d values) -> PirPreprocessedData."""
+        p = self.params
+        d, t, l = p.rlwe.degree, p.interpolation_degree, p.entry_size_multiple
+        raw = np.ascontiguousarray(db_raw, dtype=db_dtype)
+        if raw.size != p.num_entries * d * l:
+            raise InspireError(INVALID_ARGUMENT, "Invalid raw database size.")
+        padded = p.PaddedCols()
+        db_all = interpolate_db(raw, p, out_cols=padded)
+        first = self.a_components[:self.ns]
+        second = self.a_components[self.ns:self.ns + self.ne]
+        pack_a = self.a_components[self.ns + self.ne:]
+        cols = p.InterpolatedRows()
+        if p.rlwe.coeff_bits == 64 and np.dtype(db_dtype).itemsize <= 2:
+            # Condensed u64 DB rows (preprocessing_server.h:125-153).
+            simd = 64 if np.dtype(db_dtype).itemsize == 1 else 32
+            cols = (cols + simd - 1) // simd * simd
+        mats, outs = [], []
+        k = p.pack_gadget.num_digits
+        for s in range(l):
+            shard = db_all[s * t * d:(s + 1) * t * d]
+            hint = ComputeHintMatrix(shard, first)
+            a_t, mat, t_h = PreprocessMatrixPack(
+                hint, pack_a, p.rlwe.log_modulus, p.pack_gadget.log_digit, k,
+                mat_dtype=mat_dtype)
+            outs.append([PreprocessMatrixPackOutput(a_t[i], mat[i * d:(i + 1) * d],
+                                                    t_h[i]) for i in range(t)])
+            m = np.zeros((t * d, cols), dtype=db_dtype)
+            w = min(cols, padded)
+            m[:, :w] = shard[:, :w]
+            mats.append(m)
+        return PirPreprocessedData(mats, outs, second if self.ne else None)
+
+
+class PirClient:
+    """PirClient (crypto/pir/client/pir_client.h) on the GPU, batched: one
+    ternary secret key per client, requests for a batch of indices at once,
+    responses decrypted at once. The errors come from a reproducible
+    counter-based hash, not a cryptographic generator: for load generation
+    and tests. variance: the RLWE error variance (the reference's metrics
+    tools use 40, pir_metrics_tool.cc:79-87)."""
+
+    def __init__(self, params: PirParams, a_components, secret_keys,
+                 variance=40):
+        self.params = params
+        self.a_components = np.ascontiguousarray(a_components,
+                                                 dtype=params.coeff_dtype)
+        self.secret_keys = np.ascontiguousarray(secret_keys, dtype=np.int8)
+        self.variance = variance
+        self._seed = 0
+
+    @staticmethod
+    def Create(params: PirParams, a_components, clients=1, seed=0,
+               variance=40):
+        rng = np.random.default_rng(seed)
+        keys = rng.integers(-1, 2, (clients, params.rlwe.degree), dtype=np.int8)
+        c = PirClient(params, a_components, keys, variance)
+        c._seed = int(rng.integers(0, 2**63))
+        return c
+
+    def CreateRequests(self, indices, seed=None):
+        """Requests of clients 0..len(indices)-1 for their indices:
+        (first_dim (B, n/t), second_dim (B, 2ne, d), packing_key (B, 2k, d))."""
+        p = self.params
+        idx = np.ascontiguousarray(indices, dtype=np.int64).reshape(-1)
+        b = idx.size
+        if b > self.secret_keys.shape[0]:
+            raise InspireError(INVALID_ARGUMENT, "more indices than clients.")
+        d = p.rlwe.degree
+        ne = p.eval_gadget.num_digits if p.interpolation_degree > 1 else 0
+        k = p.pack_gadget.num_digits
+        cdt = p.coeff_dtype
+        fd = np.zeros((b, p.InterpolatedRows()), dtype=cdt)
+        sd = np.zeros((b, 2 * ne, d), dtype=cdt)
+        pk = np.zeros((b, 2 * k, d), dtype=cdt)
+        if seed is None:
+            self._seed += 1
+            seed = self._seed
+        prm = c_params(p)
+        err = _errbuf()
+        rc = _lib.load().inspire_client_create_requests(
+            ctypes.byref(prm), _ptr(self.secret_keys), _ptr(self.a_components),
+            self.a_components.shape[0], _ptr(idx), b, seed, self.variance,
+            _ptr(fd), _ptr(sd), _ptr(pk), 0, None, err, len(err))
+        _check(rc, err)
+        return fd, sd, pk
+
+    def CreateRequest(self, index):
+        fd, sd, pk = self.CreateRequests([index])
+        return PirRequest(fd[0], sd[0], pk[0])
+
+    def ProcessResponses(self, responses):
+        """(B, l, 2, d) ciphertexts -> (B, l*d) plaintexts."""
+        p = self.params
+        r = np.ascontiguousarray(responses, dtype=p.coeff_dtype)
+        b = r.shape[0]
+        d, l = p.rlwe.degree, p.entry_size_multiple
+        out = np.zeros((b, l * d), dtype=p.coeff_dtype)
+        prm = c_params(p)
+        err = _errbuf()
+        rc = _lib.load().inspire_client_process_responses(
+            ctypes.byref(prm), _ptr(self.secret_keys), _ptr(r), b, _ptr(out), 0,
+            None, err, len(err))
+        _check(rc, err)
+        return out
+
+    def ProcessResponse(self, response: PirResponse):
+        return self.ProcessResponses(np.asarray(response.ciphertexts)[None])[0]
+
+
 def ComputeHintMatrix(database, a_components):
     """ComputeHintMatrix (crypto/hint_computation.cc:78-160) on the GPU:
     database (rows, n*d) of u8/u16/u32, a_components (n, d) of u32/u64 ->

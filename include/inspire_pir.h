@@ -492,6 +492,32 @@ int inspire_preprocess_matrix_pack(int32_t coeff_bits, int32_t mat_kind,
                                    size_t err_len);
 
 /*
+ * PirPreprocessedData in its protobuf form (crypto/proto/pir_server.proto):
+ * DeserializePirPreprocessedData + PirServer::Create straight to GPU memory
+ * (the contents LoadPirPreprocessedDataFromFile reads,
+ * crypto/pir/server/pir_preprocessed_data.h:96-139), the directory form
+ * (metadata.bin + shard_<i>.bin, LoadPirPreprocessedDataFromDirectory,
+ * :203-267), and the reverse (SerializePirPreprocessedData,
+ * SavePirPreprocessedDataToDirectory). save: with buffer == NULL only *size
+ * is set. The reference's parse / size error messages.
+ */
+int inspire_pir_server_load_preprocessed(const inspire_pir_params* params,
+                                         const void* buffer, size_t size,
+                                         inspire_pir_server** out, char* err,
+                                         size_t err_len);
+int inspire_pir_server_load_preprocessed_dir(const inspire_pir_params* params,
+                                             const char* dir,
+                                             inspire_pir_server** out,
+                                             char* err, size_t err_len);
+int inspire_pir_server_save_preprocessed(inspire_pir_server* server,
+                                         void* buffer, size_t capacity,
+                                         size_t* size, char* err,
+                                         size_t err_len);
+int inspire_pir_server_save_preprocessed_dir(inspire_pir_server* server,
+                                             const char* dir, char* err,
+                                             size_t err_len);
+
+/*
  * A batched PIR client on the GPU, for load generation and end-to-end tests
  * (PirClient, crypto/pir/client/pir_client.cc:61-272). Client b holds the
  * ternary secret key secret_keys[b][0..d) (values -1, 0, 1) and asks for

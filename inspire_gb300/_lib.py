@@ -24,6 +24,13 @@ SIGNATURES = {
     "inspire_pir_server_load": ([_vp, _vp, _sz, _vp, _cp, _sz], ctypes.c_int),
     "inspire_pir_server_load_file": ([_vp, _cp, _vp, _cp, _sz], ctypes.c_int),
     "inspire_pir_server_save": ([_vp, _vp, _sz, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_server_load_preprocessed": (
+        [_vp, _vp, _sz, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_server_load_preprocessed_dir": (
+        [_vp, _cp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_server_save_preprocessed": (
+        [_vp, _vp, _sz, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_server_save_preprocessed_dir": ([_vp, _cp, _cp, _sz], ctypes.c_int),
     "inspire_pir_server_save_file": ([_vp, _cp, _cp, _sz], ctypes.c_int),
     "inspire_pir_process_response": (
         [_vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp, _cp, _sz], ctypes.c_int),

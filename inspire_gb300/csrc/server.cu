@@ -377,6 +377,7 @@ struct inspire_pir_server {
   // reference's Preprocess produces: a condensed DB for u64 coefficients).
   bool db_condensed = false, pack_condensed = false;
   int32_t db_orig_cols = 0, pack_bits = 0;
+  bool orig_from_file = false;  // db_orig_cols read from an image or proto
 
   inspire::DevBuf db, pack, a_tilde, th_ntt, rgswa_ntt;
   std::unique_ptr<inspire::NttTables> tables;
@@ -967,7 +968,8 @@ Status CreateServer(const inspire_pir_params* prm, const void* db,
   s->interpolated_rows = prm->num_entries / t;
   s->db_orig_cols = static_cast<int32_t>(std::min<int64_t>(db_cols, s->interpolated_rows));
   s->db_condensed = prm->coeff_bits == 64;
-  s->pack_condensed = prm->mat_kind == INSPIRE_I16 || prm->mat_kind == INSPIRE_I32;
+  // BuildPreprocessMatrix condenses int32 matrices only (lwes_to_rlwe.cc:221-226).
+  s->pack_condensed = prm->mat_kind == INSPIRE_I32;
 
   // Chunk rules of the two inner products and the prime counts that make
   // the NTT route exact for every operand those rules admit.
@@ -1272,6 +1274,7 @@ Status LoadImage(const inspire_pir_params* prm, const uint8_t* buf, size_t size,
   (*out)->db_condensed = db_cond != 0;
   (*out)->pack_condensed = pcond != 0;
   (*out)->db_orig_cols = db_orig;
+  (*out)->orig_from_file = true;
   (*out)->pack_bits = pbits;
   return Status{};
 }
@@ -1389,6 +1392,418 @@ Status SaveImage(inspire_pir_server* s, uint8_t* dst, size_t cap, size_t* size) 
     return Err(INSPIRE_RESOURCE_EXHAUSTED, "image buffer too small.");
   }
   return Status{};
+}
+
+// ---------------------------------------------------------------------------
+// PirPreprocessedData as protobuf messages (crypto/proto/pir_server.proto,
+// crypto/proto/rlwe.proto), the way SerializePirPreprocessedData /
+// DeserializePirPreprocessedData and the per-shard directory form write and
+// read them (crypto/pir/server/pir_preprocessed_data.h:52-267), through
+// Matrix::ToProto / FromProto (crypto/matrix.cc:478-520) and
+// Polynomial::ToProto / CreateFromProto (crypto/polynomial.cc:208-252,
+// 562-590). Protobuf wire format: each field is a varint key
+// (number << 3 | wire type) followed by a varint (type 0) or by a varint
+// length and that many bytes (type 2); a writer emits fields in number order
+// and, with the explicit presence of these messages, every scalar it set.
+// The matrices' bytes go to the GPU straight from the parsed buffer.
+// ---------------------------------------------------------------------------
+struct PbSpan {
+  const uint8_t* p = nullptr;
+  size_t n = 0;
+};
+
+struct PbReader {
+  const uint8_t* p;
+  size_t n;
+  size_t off = 0;
+  bool ok = true;
+  bool Varint(uint64_t* v) {
+    uint64_t x = 0;
+    for (int sh = 0; sh < 64; sh += 7) {
+      if (off >= n) break;
+      const uint8_t b = p[off++];
+      x |= static_cast<uint64_t>(b & 0x7F) << sh;
+      if ((b & 0x80) == 0) {
+        *v = x;
+        return true;
+      }
+    }
+    ok = false;
+    return false;
+  }
+  // The next field; false at the end of the message or on malformed input
+  // (then ok is false). Fixed-width fields are skipped.
+  bool Next(int* num, uint64_t* v, PbSpan* bytes) {
+    if (!ok || off >= n) return false;
+    uint64_t key = 0;
+    if (!Varint(&key)) return false;
+    *num = static_cast<int>(key >> 3);
+    switch (key & 7) {
+      case 0:
+        return Varint(v);
+      case 1:
+      case 5: {
+        const size_t w = (key & 7) == 1 ? 8 : 4;
+        if (n - off < w) break;
+        off += w;
+        *num = -1;
+        return true;
+      }
+      case 2: {
+        uint64_t len = 0;
+        if (!Varint(&len) || len > n - off) break;
+        bytes->p = p + off;
+        bytes->n = len;
+        off += len;
+        return true;
+      }
+      default:
+        break;
+    }
+    ok = false;
+    return false;
+  }
+};
+
+struct PbMatrix {
+  PbSpan bytes;
+  bool has_data = false, has_condensed = false, is_condensed = false;
+  int64_t rows = 0, cols = 0, orig = 0;
+};
+
+Status PbBad(const char* what) { return Err(INSPIRE_INVALID_ARGUMENT, what); }
+
+// Matrix::FromProto's checks, and the element columns of the matrix.
+Status ParseMatrix(PbSpan m, size_t es, PbMatrix* out, int64_t* elem_cols) {
+  PbReader r{m.p, m.n};
+  int num = 0;
+  uint64_t v = 0;
+  PbSpan b;
+  while (r.Next(&num, &v, &b)) {
+    switch (num) {
+      case 1: out->bytes = b; out->has_data = true; out->has_condensed = false; break;
+      case 2: out->bytes = b; out->has_condensed = true; out->has_data = false; break;
+      case 3: out->rows = static_cast<int32_t>(v); break;
+      case 4: out->cols = static_cast<int32_t>(v); break;
+      case 5: out->is_condensed = v != 0; break;
+      case 6: out->orig = static_cast<int32_t>(v); break;
+      default: break;
+    }
+  }
+  if (!r.ok) return PbBad("Failed to parse PirPreprocessedData.");
+  if (out->is_condensed && out->has_data) {
+    return PbBad("Condensed matrix cannot have normal data set.");
+  }
+  if (!out->is_condensed && out->has_condensed) {
+    return PbBad("Normal matrix cannot have condensed data set.");
+  }
+  if (out->bytes.n % (out->is_condensed ? 8 : es) != 0) {
+    return PbBad(out->is_condensed ? "Invalid serialized condensed_data size."
+                                   : "Invalid serialized data size.");
+  }
+  *elem_cols = out->is_condensed ? out->cols * 8 / static_cast<int64_t>(es) : out->cols;
+  if (static_cast<size_t>(out->rows) * *elem_cols * es != out->bytes.n) {
+    return PbBad("Invalid serialized data size.");
+  }
+  return Status{};
+}
+
+// Polynomial::CreateFromProto: d coefficients of log_q bits, appended to out
+// as CoeffType words.
+Status ParsePoly(PbSpan m, int d, int log_q, int cb, std::vector<uint8_t>* out) {
+  PbReader r{m.p, m.n};
+  int num = 0;
+  uint64_t v = 0;
+  PbSpan b, enc;
+  while (r.Next(&num, &v, &b)) {
+    if (num == 1) enc = b;
+  }
+  if (!r.ok) return PbBad("Failed to parse PirPreprocessedData.");
+  if (log_q <= 0 || log_q > cb) return PbBad("Invalid log_modulus.");
+  if (enc.n == 0) return PbBad("Empty serialized polynomial.");
+  if (enc.n != (static_cast<size_t>(d) * log_q + 7) / 8) {
+    return PbBad("Unexpected serialized size.");
+  }
+  UnpackCoeffs(enc.p, enc.n, d, log_q, cb, out);
+  return Status{};
+}
+
+// The material of one shard as it comes out of the messages.
+struct PbShard {
+  PbMatrix db;
+  int64_t db_cols = 0;
+  std::vector<PbMatrix> packs;
+  std::vector<int64_t> pack_cols;
+};
+
+// PreprocessMatrixPackOutput: a_tilde_agg (1), matrix (2), t_vec_h (3).
+Status ParseOutput(PbSpan m, const inspire_pir_params* prm, PbShard* sh,
+                   std::vector<uint8_t>* a_tilde, std::vector<uint8_t>* t_vec_h,
+                   int64_t* th_count) {
+  const int d = 1 << prm->log_degree;
+  PbReader r{m.p, m.n};
+  int num = 0;
+  uint64_t v = 0;
+  PbSpan b;
+  bool have_a = false, have_m = false;
+  while (r.Next(&num, &v, &b)) {
+    if (num == 1) {
+      RETURN_IF_ERROR(ParsePoly(b, d, prm->log_modulus, prm->coeff_bits, a_tilde));
+      have_a = true;
+    } else if (num == 2) {
+      sh->packs.emplace_back();
+      sh->pack_cols.push_back(0);
+      RETURN_IF_ERROR(ParseMatrix(b, elem_size(prm->mat_kind), &sh->packs.back(),
+                                  &sh->pack_cols.back()));
+      have_m = true;
+    } else if (num == 3) {
+      RETURN_IF_ERROR(ParsePoly(b, d, prm->log_modulus, prm->coeff_bits, t_vec_h));
+      ++*th_count;
+    }
+  }
+  if (!r.ok) return PbBad("Failed to parse PirPreprocessedData.");
+  if (!have_a) return PbBad("Empty serialized polynomial.");
+  if (!have_m) return PbBad("Preprocessed output without a matrix.");
+  return Status{};
+}
+
+// Builds the server from parsed shards: the matrices are copied into one
+// device buffer each (vertical concatenation), the polynomials go through
+// CreateServer.
+Status ServerFromShards(const inspire_pir_params* prm, std::vector<PbShard>& shards,
+                        const std::vector<uint8_t>& a_tilde, int64_t a_count,
+                        const std::vector<uint8_t>& t_vec_h, int64_t th_count,
+                        const std::vector<uint8_t>& sda, int64_t sda_count,
+                        std::unique_ptr<inspire_pir_server>* out) {
+  if (prm == nullptr) return PbBad("params is null.");
+  const int l = prm->entry_size_multiple;
+  const int t = prm->interpolation_degree;
+  if (static_cast<int>(shards.size()) != l) return PbBad("db_matrices size mismatch.");
+  const size_t es = elem_size(prm->db_kind), ms = elem_size(prm->mat_kind);
+  int64_t db_rows = 0, pack_rows = 0;
+  const int64_t db_cols = shards.empty() ? 0 : shards[0].db_cols;
+  const int64_t pack_cols = shards.empty() || shards[0].packs.empty() ? 0 : shards[0].pack_cols[0];
+  for (auto& sh : shards) {
+    if (sh.db_cols != db_cols) {
+      return PbBad("All DB matrices must have the same number of columns.");
+    }
+    if (static_cast<int>(sh.packs.size()) != t) {
+      return PbBad("Preprocessed outputs must be of length t.");
+    }
+    db_rows += sh.db.rows;
+    for (size_t i = 0; i < sh.packs.size(); ++i) {
+      if (sh.pack_cols[i] != pack_cols) {
+        return PbBad("All pack matrices must have the same number of columns.");
+      }
+      pack_rows += sh.packs[i].rows;
+    }
+  }
+  DevBuf db, pack;
+  RETURN_IF_ERROR(db.Alloc(static_cast<size_t>(db_rows) * db_cols * es));
+  RETURN_IF_ERROR(pack.Alloc(static_cast<size_t>(pack_rows) * pack_cols * ms));
+  size_t db_off = 0, pack_off = 0;
+  for (auto& sh : shards) {
+    if (sh.db.bytes.n > 0) {
+      RETURN_IF_ERROR(Cuda(cudaMemcpy(db.get<uint8_t>() + db_off, sh.db.bytes.p, sh.db.bytes.n,
+                                      cudaMemcpyHostToDevice),
+                           "DB upload"));
+    }
+    db_off += sh.db.bytes.n;
+    for (auto& pm : sh.packs) {
+      if (pm.bytes.n > 0) {
+        RETURN_IF_ERROR(Cuda(cudaMemcpy(pack.get<uint8_t>() + pack_off, pm.bytes.p, pm.bytes.n,
+                                        cudaMemcpyHostToDevice),
+                             "pack matrix upload"));
+      }
+      pack_off += pm.bytes.n;
+    }
+  }
+  RETURN_IF_ERROR(CreateServer(prm, db.get(), db_rows, db_cols, pack.get(), pack_rows,
+                               pack_cols, a_tilde.data(), a_count, t_vec_h.data(), th_count,
+                               sda.data(), sda_count, out, &db, &pack));
+  if (!shards.empty()) {
+    (*out)->db_condensed = shards[0].db.is_condensed;
+    (*out)->db_orig_cols = static_cast<int32_t>(shards[0].db.orig);
+    (*out)->orig_from_file = true;
+    (*out)->pack_condensed = !shards[0].packs.empty() && shards[0].packs[0].is_condensed;
+  }
+  return Status{};
+}
+
+// DeserializePirPreprocessedData + PirServer::Create from one serialized
+// proto::PirPreprocessedData.
+Status LoadPreprocessed(const inspire_pir_params* prm, const uint8_t* buf, size_t size,
+                        std::unique_ptr<inspire_pir_server>* out) {
+  if (prm == nullptr || (buf == nullptr && size > 0)) {
+    return PbBad("Failed to parse PirPreprocessedData from file.");
+  }
+  const int d = 1 << prm->log_degree;
+  std::vector<PbShard> shards;
+  std::vector<uint8_t> a_tilde, t_vec_h, sda;
+  int64_t a_count = 0, th_count = 0, sda_count = 0;
+  size_t db_seen = 0, out_seen = 0;
+  PbReader r{buf, size};
+  int num = 0;
+  uint64_t v = 0;
+  PbSpan b;
+  while (r.Next(&num, &v, &b)) {
+    if (num == 1) {  // db_matrices
+      if (shards.size() <= db_seen) shards.resize(db_seen + 1);
+      RETURN_IF_ERROR(ParseMatrix(b, elem_size(prm->db_kind), &shards[db_seen].db,
+                                  &shards[db_seen].db_cols));
+      ++db_seen;
+    } else if (num == 2) {  // preprocessed_outputs: ShardPreprocessedOutputs
+      if (shards.size() <= out_seen) shards.resize(out_seen + 1);
+      PbReader rs{b.p, b.n};
+      int n2 = 0;
+      uint64_t v2 = 0;
+      PbSpan o;
+      while (rs.Next(&n2, &v2, &o)) {
+        if (n2 == 1) {
+          RETURN_IF_ERROR(ParseOutput(o, prm, &shards[out_seen], &a_tilde, &t_vec_h, &th_count));
+          ++a_count;
+        }
+      }
+      if (!rs.ok) return PbBad("Failed to parse PirPreprocessedData from file.");
+      ++out_seen;
+    } else if (num == 3) {  // second_dim_a
+      RETURN_IF_ERROR(ParsePoly(b, d, prm->log_modulus, prm->coeff_bits, &sda));
+      ++sda_count;
+    }
+  }
+  if (!r.ok) return PbBad("Failed to parse PirPreprocessedData from file.");
+  if (db_seen != out_seen) return PbBad("preprocessed_outputs size mismatch.");
+  return ServerFromShards(prm, shards, a_tilde, a_count, t_vec_h, th_count, sda, sda_count,
+                          out);
+}
+
+// --- writer ---
+void PbPutVarint(std::vector<uint8_t>* o, uint64_t v) {
+  while (v >= 0x80) {
+    o->push_back(static_cast<uint8_t>(v | 0x80));
+    v >>= 7;
+  }
+  o->push_back(static_cast<uint8_t>(v));
+}
+void PbPutBytes(std::vector<uint8_t>* o, int num, const uint8_t* p, size_t n) {
+  PbPutVarint(o, static_cast<uint64_t>(num) << 3 | 2);
+  PbPutVarint(o, n);
+  o->insert(o->end(), p, p + n);
+}
+void PbPutInt(std::vector<uint8_t>* o, int num, int64_t v) {
+  PbPutVarint(o, static_cast<uint64_t>(num) << 3);
+  PbPutVarint(o, static_cast<uint64_t>(v));  // int32 fields: sign-extended
+}
+
+// Matrix::ToProto of rows x elem_cols elements at dev (device).
+Status PutMatrix(std::vector<uint8_t>* o, int num, const uint8_t* dev, int64_t rows,
+                 int64_t elem_cols, size_t es, bool condensed, int64_t orig) {
+  std::vector<uint8_t> m;
+  const size_t bytes = static_cast<size_t>(rows) * elem_cols * es;
+  std::vector<uint8_t> host(bytes);
+  if (bytes > 0) {
+    RETURN_IF_ERROR(Cuda(cudaMemcpy(host.data(), dev, bytes, cudaMemcpyDeviceToHost),
+                         "matrix download"));
+    PbPutBytes(&m, condensed ? 2 : 1, host.data(), bytes);
+  }
+  PbPutInt(&m, 3, rows);
+  PbPutInt(&m, 4, condensed ? elem_cols * static_cast<int64_t>(es) / 8 : elem_cols);
+  PbPutInt(&m, 5, condensed ? 1 : 0);
+  PbPutInt(&m, 6, orig);
+  PbPutBytes(o, num, m.data(), m.size());
+  return Status{};
+}
+
+// Polynomial::ToProto (log_q bits per coefficient) as field `num`.
+void PutPoly(std::vector<uint8_t>* o, int num, const uint8_t* words, int d, int log_q, int cb) {
+  const std::vector<uint8_t> enc = PackCoeffs(words, d, log_q, cb);
+  std::vector<uint8_t> m;
+  PbPutBytes(&m, 1, enc.data(), enc.size());
+  PbPutBytes(o, num, m.data(), m.size());
+}
+
+// One shard's messages: its DB matrix (field db_num) and its outputs
+// (field out_num, each a PreprocessMatrixPackOutput).
+Status PutShard(inspire_pir_server* s, int k, const std::vector<uint8_t>& a_host,
+                std::vector<uint8_t>* db_part, int db_num, std::vector<uint8_t>* out_part,
+                int out_num) {
+  const int d = s->d, t = s->t, cb = s->prm.coeff_bits;
+  const size_t cw = cb / 8;
+  const size_t es = elem_size(s->prm.db_kind), ms = elem_size(s->prm.mat_kind);
+  const int64_t shard_rows = static_cast<int64_t>(t) * d;
+  const bool dcond = s->db_condensed && (s->db_cols * es) % 8 == 0;
+  RETURN_IF_ERROR(PutMatrix(db_part, db_num,
+                            s->db.get<uint8_t>() + static_cast<size_t>(k) * shard_rows * s->db_cols * es,
+                            shard_rows, s->db_cols, es, dcond,
+                            s->orig_from_file ? s->db_orig_cols : s->db_cols));
+  const bool pcond = s->pack_condensed && (s->pack_cols * ms) % 8 == 0;
+  for (int i = 0; i < t; ++i) {
+    const size_t slice = static_cast<size_t>(k) * t + i;
+    std::vector<uint8_t> m;
+    PutPoly(&m, 1, a_host.data() + slice * d * cw, d, s->prm.log_modulus, cb);
+    RETURN_IF_ERROR(PutMatrix(&m, 2,
+                              s->pack.get<uint8_t>() + slice * d * s->pack_cols * ms, d,
+                              s->pack_cols, ms, pcond, s->pack_cols));
+    for (int j = 0; j < s->k; ++j) {
+      PutPoly(&m, 3, s->t_vec_h_raw.data() + (slice * s->k + j) * d * cw, d,
+              s->prm.log_modulus, cb);
+    }
+    PbPutBytes(out_part, out_num, m.data(), m.size());
+  }
+  return Status{};
+}
+
+Status SavePreprocessed(inspire_pir_server* s, std::vector<uint8_t>* out) {
+  const int d = s->d, cb = s->prm.coeff_bits;
+  const size_t cw = cb / 8;
+  std::vector<uint8_t> a_host(static_cast<size_t>(s->l) * s->t * d * cw);
+  RETURN_IF_ERROR(Cuda(cudaMemcpy(a_host.data(), s->a_tilde.get(), a_host.size(),
+                                  cudaMemcpyDeviceToHost),
+                       "a_tilde download"));
+  std::vector<uint8_t> dbs, outs;
+  for (int k = 0; k < s->l; ++k) {
+    std::vector<uint8_t> shard_outs;
+    RETURN_IF_ERROR(PutShard(s, k, a_host, &dbs, 1, &shard_outs, 1));
+    PbPutBytes(&outs, 2, shard_outs.data(), shard_outs.size());
+  }
+  out->clear();
+  out->insert(out->end(), dbs.begin(), dbs.end());
+  out->insert(out->end(), outs.begin(), outs.end());
+  const size_t nsd = s->second_dim_a_raw.size() / (d * cw);
+  for (size_t j = 0; j < nsd; ++j) {
+    PutPoly(out, 3, s->second_dim_a_raw.data() + j * d * cw, d, s->prm.log_modulus, cb);
+  }
+  return Status{};
+}
+
+Status ReadWholeFile(const std::string& path, std::vector<uint8_t>* out) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (f == nullptr) return Err(INSPIRE_INTERNAL, "Failed to read file: " + path);
+  std::fseek(f, 0, SEEK_END);
+  const long len = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  Status st;
+  if (len < 0) {
+    st = Err(INSPIRE_INTERNAL, "Failed to read file: " + path);
+  } else {
+    out->resize(static_cast<size_t>(len));
+    if (len > 0 && std::fread(out->data(), 1, len, f) != static_cast<size_t>(len)) {
+      st = Err(INSPIRE_INTERNAL, "Failed to read file: " + path);
+    }
+  }
+  std::fclose(f);
+  return st;
+}
+
+Status WriteWholeFile(const std::string& path, const std::vector<uint8_t>& data) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (f == nullptr) return Err(INSPIRE_INTERNAL, "Failed to open file for writing: " + path);
+  Status st;
+  if (!data.empty() && std::fwrite(data.data(), 1, data.size(), f) != data.size()) {
+    st = Err(INSPIRE_INTERNAL, "Error writing to file: " + path);
+  }
+  std::fclose(f);
+  return st;
 }
 
 }  // namespace
@@ -1581,6 +1996,147 @@ int inspire_pir_server_load_file(const inspire_pir_params* params, const char* p
   if (st.ok()) st = LoadImage(params, static_cast<const uint8_t*>(host), len, &s);
   if (host) cudaFreeHost(host);
   if (st.ok()) *out = s.release();
+  return Report(st, err, err_len);
+}
+
+int inspire_pir_server_load_preprocessed(const inspire_pir_params* params,
+                                         const void* buffer, size_t size,
+                                         inspire_pir_server** out, char* err,
+                                         size_t err_len) {
+  using namespace inspire;
+  if (out == nullptr) return Report(Err(INSPIRE_INVALID_ARGUMENT, "out is null."), err, err_len);
+  *out = nullptr;
+  std::unique_ptr<inspire_pir_server> s;
+  Status st = LoadPreprocessed(params, static_cast<const uint8_t*>(buffer), size, &s);
+  if (st.ok()) *out = s.release();
+  return Report(st, err, err_len);
+}
+
+int inspire_pir_server_load_preprocessed_dir(const inspire_pir_params* params,
+                                             const char* dir, inspire_pir_server** out,
+                                             char* err, size_t err_len) {
+  using namespace inspire;
+  if (out == nullptr || dir == nullptr || params == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "params, dir and out must be set."), err,
+                  err_len);
+  }
+  *out = nullptr;
+  // LoadPirPreprocessedDataFromDirectory (pir_preprocessed_data.h:203-267):
+  // metadata.bin (second_dim_a), then shard_<i>.bin per shard.
+  const std::string base(dir);
+  const int d = 1 << params->log_degree;
+  std::vector<uint8_t> meta;
+  Status st = ReadWholeFile(base + "/metadata.bin", &meta);
+  std::vector<uint8_t> sda;
+  int64_t sda_count = 0;
+  if (st.ok()) {
+    PbReader r{meta.data(), meta.size()};
+    int num = 0;
+    uint64_t v = 0;
+    PbSpan b;
+    while (st.ok() && r.Next(&num, &v, &b)) {
+      if (num == 1) {
+        st = ParsePoly(b, d, params->log_modulus, params->coeff_bits, &sda);
+        ++sda_count;
+      }
+    }
+    if (st.ok() && !r.ok) {
+      st = Err(INSPIRE_INVALID_ARGUMENT, "Failed to parse PirPreprocessedMetadata.");
+    }
+  }
+  const int l = params->entry_size_multiple;
+  std::vector<std::vector<uint8_t>> files(l > 0 ? l : 0);
+  std::vector<PbShard> shards(files.size());
+  std::vector<uint8_t> a_tilde, t_vec_h;
+  int64_t a_count = 0, th_count = 0;
+  for (int i = 0; st.ok() && i < l; ++i) {
+    st = ReadWholeFile(base + "/shard_" + std::to_string(i) + ".bin", &files[i]);
+    if (!st.ok()) break;
+    PbReader r{files[i].data(), files[i].size()};
+    int num = 0;
+    uint64_t v = 0;
+    PbSpan b;
+    bool have_db = false;
+    while (st.ok() && r.Next(&num, &v, &b)) {
+      if (num == 1) {
+        st = ParseMatrix(b, elem_size(params->db_kind), &shards[i].db, &shards[i].db_cols);
+        have_db = true;
+      } else if (num == 2) {
+        st = ParseOutput(b, params, &shards[i], &a_tilde, &t_vec_h, &th_count);
+        ++a_count;
+      }
+    }
+    if (st.ok() && (!r.ok || !have_db)) {
+      st = Err(INSPIRE_INVALID_ARGUMENT,
+               "Failed to parse PirPreprocessedShard " + std::to_string(i));
+    }
+  }
+  std::unique_ptr<inspire_pir_server> s;
+  if (st.ok()) {
+    st = ServerFromShards(params, shards, a_tilde, a_count, t_vec_h, th_count, sda, sda_count,
+                          &s);
+  }
+  if (st.ok()) *out = s.release();
+  return Report(st, err, err_len);
+}
+
+int inspire_pir_server_save_preprocessed(inspire_pir_server* server, void* buffer,
+                                         size_t capacity, size_t* size, char* err,
+                                         size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr || size == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server and size must be set."), err,
+                  err_len);
+  }
+  std::lock_guard<std::mutex> lock(server->mu);
+  std::vector<uint8_t> bytes;
+  Status st = SavePreprocessed(server, &bytes);
+  if (st.ok()) {
+    *size = bytes.size();
+    if (buffer != nullptr) {
+      if (capacity < bytes.size()) {
+        st = Err(INSPIRE_RESOURCE_EXHAUSTED, "buffer too small.");
+      } else {
+        std::memcpy(buffer, bytes.data(), bytes.size());
+      }
+    }
+  }
+  return Report(st, err, err_len);
+}
+
+int inspire_pir_server_save_preprocessed_dir(inspire_pir_server* server, const char* dir,
+                                             char* err, size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr || dir == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server and dir must be set."), err, err_len);
+  }
+  std::lock_guard<std::mutex> lock(server->mu);
+  // SavePirPreprocessedDataToDirectory (pir_preprocessed_data.h:141-201).
+  const std::string base(dir);
+  const int d = server->d, cb = server->prm.coeff_bits;
+  const size_t cw = cb / 8;
+  std::vector<uint8_t> meta;
+  const size_t nsd = server->second_dim_a_raw.size() / (d * cw);
+  for (size_t j = 0; j < nsd; ++j) {
+    PutPoly(&meta, 1, server->second_dim_a_raw.data() + j * d * cw, d,
+            server->prm.log_modulus, cb);
+  }
+  Status st = WriteWholeFile(base + "/metadata.bin", meta);
+  std::vector<uint8_t> a_host(static_cast<size_t>(server->l) * server->t * d * cw);
+  if (st.ok()) {
+    st = Cuda(cudaMemcpy(a_host.data(), server->a_tilde.get(), a_host.size(),
+                         cudaMemcpyDeviceToHost),
+              "a_tilde download");
+  }
+  for (int k = 0; st.ok() && k < server->l; ++k) {
+    std::vector<uint8_t> shard;
+    std::vector<uint8_t> outs;
+    st = PutShard(server, k, a_host, &shard, 1, &outs, 2);
+    if (st.ok()) {
+      shard.insert(shard.end(), outs.begin(), outs.end());
+      st = WriteWholeFile(base + "/shard_" + std::to_string(k) + ".bin", shard);
+    }
+  }
   return Report(st, err, err_len);
 }
 

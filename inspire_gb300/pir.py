@@ -313,6 +313,69 @@ class PirServer:
         _check(_lib.load().inspire_pir_server_save_file(
             self._h, str(path).encode(), err, len(err)), err)
 
+    @staticmethod
+    def FromPirPreprocessedData(params, data, db_dtype=np.uint16,
+                                mat_dtype=np.int32):
+        """A serialized proto::PirPreprocessedData (what
+        LoadPirPreprocessedDataFromFile reads,
+        crypto/pir/server/pir_preprocessed_data.h:96-139) straight into a
+        GPU server (DeserializePirPreprocessedData + PirServer::Create)."""
+        buf = np.frombuffer(bytes(data), dtype=np.uint8)
+        prm = c_params(params, db_dtype, mat_dtype)
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        rc = _lib.load().inspire_pir_server_load_preprocessed(
+            ctypes.byref(prm), _ptr(buf), buf.size, ctypes.byref(h), err,
+            len(err))
+        _check(rc, err)
+        return PirServer._from_handle(h, params)
+
+    @staticmethod
+    def FromPirPreprocessedDataFile(params, path, db_dtype=np.uint16,
+                                    mat_dtype=np.int32):
+        with open(path, "rb") as f:
+            return PirServer.FromPirPreprocessedData(params, f.read(),
+                                                     db_dtype, mat_dtype)
+
+    @staticmethod
+    def FromPirPreprocessedDataDirectory(params, path, db_dtype=np.uint16,
+                                         mat_dtype=np.int32):
+        """LoadPirPreprocessedDataFromDirectory (metadata.bin +
+        shard_<i>.bin, pir_preprocessed_data.h:203-267) into a GPU server."""
+        prm = c_params(params, db_dtype, mat_dtype)
+        h = ctypes.c_void_p()
+        err = _errbuf()
+        rc = _lib.load().inspire_pir_server_load_preprocessed_dir(
+            ctypes.byref(prm), str(path).encode(), ctypes.byref(h), err,
+            len(err))
+        _check(rc, err)
+        return PirServer._from_handle(h, params)
+
+    def SerializePirPreprocessedData(self):
+        """SerializePirPreprocessedData(...).SerializeAsString() of the
+        server's material."""
+        lib = _lib.load()
+        err = _errbuf()
+        size = ctypes.c_size_t()
+        _check(lib.inspire_pir_server_save_preprocessed(
+            self._h, None, 0, ctypes.byref(size), err, len(err)), err)
+        out = np.empty(size.value, dtype=np.uint8)
+        _check(lib.inspire_pir_server_save_preprocessed(
+            self._h, _ptr(out), out.size, ctypes.byref(size), err, len(err)),
+            err)
+        return out.tobytes()
+
+    def SavePirPreprocessedDataToFile(self, path):
+        with open(path, "wb") as f:
+            f.write(self.SerializePirPreprocessedData())
+
+    def SavePirPreprocessedDataToDirectory(self, path):
+        """SavePirPreprocessedDataToDirectory (pir_preprocessed_data.h:141-201);
+        the directory must exist."""
+        err = _errbuf()
+        _check(_lib.load().inspire_pir_server_save_preprocessed_dir(
+            self._h, str(path).encode(), err, len(err)), err)
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h:

@@ -27,7 +27,7 @@ def bitpack(values, num_bits):
     """BitPackSigned / BitPackCoefficients below the word width."""
     if len(values) == 0 or num_bits <= 0:
         return b""
-    mask = np.uint64((1 << num_bits) - 1) if num_bits < 64 else np.uint64(~0)
+    mask = np.uint64((1 << num_bits) - 1) if num_bits < 64 else np.uint64((1 << 64) - 1)
     v = np.asarray(values).astype(np.int64).view(np.uint64) & mask
     return np.packbits(_bits_of(v, num_bits).reshape(-1),
                        bitorder="little").tobytes()

@@ -603,6 +603,50 @@ def main():
         e2e_step()
     e2e_s = (time.perf_counter() - t0) / max(3, args.steps // 2)
 
+    # The same host-buffer path through the asynchronous workspace C ABI
+    # with two batches in flight: each step's copies (in pinned staging,
+    # written once beforehand like the buffers above) overlap the other
+    # batch's GPU work.
+    def make_ws():
+        h = ctypes.c_void_p()
+        rc = lib.inspire_pir_workspace_create(srv._h, B, ctypes.byref(h), err,
+                                              len(err))
+        if rc:
+            raise SystemExit(err.value)
+        ptrs = [ctypes.c_void_p() for _ in range(4)]
+        lib.inspire_pir_workspace_host_buffers(h, *[ctypes.byref(x) for x in ptrs])
+        row = srv.db_cols * np.dtype(cdt).itemsize
+        dst = (ctypes.c_uint8 * (B * row)).from_address(ptrs[0].value)
+        buf = np.frombuffer(dst, dtype=cdt).reshape(B, srv.db_cols)
+        buf[:, :n1] = fd
+        buf[:, n1:] = 0
+        ctypes.memmove(ptrs[1].value, sd.ctypes.data, sd.nbytes)
+        ctypes.memmove(ptrs[2].value, pk.ctypes.data, pk.nbytes)
+        return h
+    wss = [make_ws(), make_ws()]
+
+    def submit(h):
+        if lib.inspire_pir_workspace_submit(h, B, engine, err, len(err)):
+            raise SystemExit(err.value)
+
+    def wait(h):
+        if lib.inspire_pir_workspace_wait(h, err, len(err)):
+            raise SystemExit(err.value)
+    for h in wss:
+        submit(h)
+    for h in wss:
+        wait(h)
+    pipe_steps = max(4, args.steps)
+    t0 = time.perf_counter()
+    submit(wss[0])
+    for i in range(1, pipe_steps):
+        submit(wss[i % 2])
+        wait(wss[(i - 1) % 2])
+    wait(wss[(pipe_steps - 1) % 2])
+    pipe_s = (time.perf_counter() - t0) / pipe_steps
+    for h in wss:
+        lib.inspire_pir_workspace_destroy(h)
+
     rows, cols = db.shape
     db_bytes = db.nbytes + pack.nbytes
     qps = world * B / (ms_step / 1000.0)
@@ -635,6 +679,11 @@ def main():
                 "h2d_bytes_per_step": int(h_fd.nbytes + h_sd.nbytes +
                                           h_pk.nbytes),
                 "d2h_bytes_per_step": int(h_out.nbytes)},
+        "e2e_pipelined": {"value": world * B / pipe_s, "unit": "queries/s",
+                          "workspaces_in_flight": 2,
+                          "h2d_bytes_per_step": int(h_fd.nbytes + h_sd.nbytes +
+                                                    h_pk.nbytes),
+                          "d2h_bytes_per_step": int(h_out.nbytes)},
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(

@@ -40,6 +40,18 @@ def limb_ops(rows, db_cols, pack_cols, batch):
     return 2.0 * (7 * rows * db_cols + 10 * rows * pack_cols) * batch
 
 
+# DRAM traffic per unit of work from one ncu capture of a smaller case of the
+# same kernel, scaled by the units a full launch processes (both kernels
+# stream their matrices once, so traffic grows in proportion):
+#  * limb GEMM, n=2^18 d=2048 t=8 B=256 (ncu --set full, one launch):
+#    dram read 2.998676 GB + write 0.113170 GB over R (C + 2K) =
+#    16384 * 40960 row-column units;
+#  * fused GEMV, n=2^18 d=4096 t=8 (ncu --set full, one launch): read
+#    3.221 GB + write 2.9 MB against 3.222 GB of algorithmic bytes.
+LIMB_TRAFFIC_PER_UNIT = (2.998676e9 + 0.113170e9) / (16384 * 40960)
+GEMV_TRAFFIC_PER_ALG_BYTE = (3.221e9 + 2.9e6) / 3.222e9
+
+
 def launches_per_step(engine, t):
     # products (1 launch, or the limb engine's 1) + NTT(y_h) + finalize
     # + NTT(rgsw) + (t-1) external products + rescale
@@ -90,12 +102,17 @@ def kernel_times(srv, engine, batch, t_fd, t_sd, t_pk, t_out, stream, n1,
         kernels["limb_gemm_b%d" % batch] = {"ms": ms_t, "limb_ops": ops,
                                             "tflops": ach,
                                             "frac_tensor": ach / tfl}
+        units = rows * (srv.db_cols + 2 * srv.pack_cols)
         roof = {"bound": "tensor", "achieved": ach, "peak": tfl,
-                "unit": "TFLOP/s", "frac": ach / tfl, "traffic": None,
+                "unit": "TFLOP/s", "frac": ach / tfl,
+                "traffic": LIMB_TRAFFIC_PER_UNIT * units,
+                "traffic_source": "ncu small case scaled by R*(C+2K)",
                 "kernel": "limb_gemm", "peak_kind": kind + " bf16 dense"}
     else:
         roof = {"bound": "hbm", "achieved": plain_gbs, "peak": hbm,
-                "unit": "GB/s", "frac": plain_gbs / hbm, "traffic": None,
+                "unit": "GB/s", "frac": plain_gbs / hbm,
+                "traffic": GEMV_TRAFFIC_PER_ALG_BYTE * pb,
+                "traffic_source": "ncu small case scaled by algorithmic bytes",
                 "kernel": "fused_gemv", "peak_kind": kind + " copy"}
     return {"roofline": roof, "kernels": kernels,
             "launches_per_step": launches_per_step(engine,

@@ -551,22 +551,70 @@ __global__ void split_u16_kernel(const uint16_t* __restrict__ src,
   }
 }
 
-// sum_c q1[q][c] mod 2^32 per request (the DB offset term). One CTA per
-// request; blockDim.x = 256.
-__global__ void row_sum_kernel(const uint32_t* __restrict__ q1, int64_t cols,
-                               int64_t stride, uint32_t* __restrict__ sum) {
-  __shared__ uint32_t part[8];
-  const uint32_t* row = q1 + blockIdx.x * stride;
-  uint32_t s = 0;
-  for (int64_t c = threadIdx.x; c < cols; c += blockDim.x) s += row[c];
+// Balanced base-256 digits of one u32 word (mod 2^32) as fp16 values.
+__device__ __forceinline__ void u32_digits(uint32_t x, __half (&h)[4]) {
+  int carry = 0;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  for (int j = 0; j < 4; ++j) {
+    int b = static_cast<int>((x >> (8 * j)) & 255u) + carry;
+    carry = b >= 128 ? 1 : 0;
+    b -= carry << 8;
+    h[j] = __int2half_rn(b);
+  }
+}
+
+// The requests' first-dimension words as the four digit planes (plane j at
+// j * plane_rows rows, cols_pad columns, zero past cols and for requests
+// batch..rows_pad) and their sums mod 2^32 (the DB offset term; qsum must
+// be zeroed). Each thread takes 4 consecutive columns of one request:
+// 16-byte loads when the rows allow them, 8-byte stores per plane.
+// grid = (ceil(cols_pad / 1024), rows_pad), block = 256.
+__global__ void split_queries_kernel(const uint32_t* __restrict__ q1, int64_t cols,
+                                     int64_t stride, int batch, int64_t plane_rows,
+                                     int64_t cols_pad, __half* __restrict__ dst,
+                                     uint32_t* __restrict__ qsum) {
+  __shared__ uint32_t part[8];
+  const int q = blockIdx.y;
+  const int64_t c0 = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) * 4;
+  uint32_t x[4] = {0, 0, 0, 0};
+  if (q < batch && c0 < cols) {
+    const uint32_t* row = q1 + q * stride;
+    if (c0 + 4 <= cols && ((reinterpret_cast<uintptr_t>(row + c0) & 15) == 0)) {
+      const uint4 v = *reinterpret_cast<const uint4*>(row + c0);
+      x[0] = v.x;
+      x[1] = v.y;
+      x[2] = v.z;
+      x[3] = v.w;
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) x[i] = c0 + i < cols ? row[c0 + i] : 0u;
+    }
+  }
+  if (c0 < cols_pad) {
+    __half h[4][4];  // [column][plane]
+#pragma unroll
+    for (int i = 0; i < 4; ++i) u32_digits(x[i], h[i]);
+    const int64_t plane = plane_rows * cols_pad;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      __half2 lo = __halves2half2(h[0][j], h[1][j]);
+      __half2 hi = __halves2half2(h[2][j], h[3][j]);
+      uint2 w;
+      w.x = *reinterpret_cast<uint32_t*>(&lo);
+      w.y = *reinterpret_cast<uint32_t*>(&hi);
+      *reinterpret_cast<uint2*>(dst + j * plane + q * cols_pad + c0) = w;
+    }
+  }
+  if (q >= batch) return;  // uniform per block
+  uint32_t sum = x[0] + x[1] + x[2] + x[3];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = sum;
   __syncthreads();
   if (threadIdx.x == 0) {
     uint32_t t = 0;
-    for (int w = 0; w < 8; ++w) t += part[w];
-    sum[blockIdx.x] = t;
+    for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) t += part[w];
+    atomicAdd(qsum + q, t);
   }
 }
 
@@ -801,12 +849,15 @@ class LimbGemmImpl : public LimbGemm {
     if (e != cudaSuccess) return e;
     const int64_t bpad = round_up(batch, kTileQ);
     // Byte planes of the requests, qcap rows apart; rows batch..bpad are 0.
-    split_u32_kernel<<<152 * 8, 256, 0, st>>>(q1, kU32, batch, db_cols_, q1_stride,
-                                              bpad, sc->qcap, cpad_, sc->q_planes);
+    e = cudaMemsetAsync(sc->qsum, 0, 4ull * batch, st);
+    if (e != cudaSuccess) return e;
+    split_queries_kernel<<<dim3(static_cast<unsigned>((cpad_ + 1023) / 1024),
+                                static_cast<unsigned>(bpad)),
+                           256, 0, st>>>(static_cast<const uint32_t*>(q1), db_cols_,
+                                         q1_stride, batch, sc->qcap, cpad_, sc->q_planes,
+                                         sc->qsum);
     split_u32_kernel<<<152 * 8, 256, 0, st>>>(yg, kU32, batch, pk_cols_, yg_stride,
                                               bpad, sc->qcap, kpad_, sc->y_planes);
-    row_sum_kernel<<<batch, 256, 0, st>>>(static_cast<const uint32_t*>(q1), db_cols_,
-                                         q1_stride, sc->qsum);
     LimbArgs a;
     a.rows = static_cast<int>(rows_);
     a.n_db_units = static_cast<int>(cpad_ / kUnitK);

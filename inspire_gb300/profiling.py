@@ -53,9 +53,11 @@ GEMV_TRAFFIC_PER_ALG_BYTE = (3.221e9 + 2.9e6) / 3.222e9
 
 
 def launches_per_step(engine, t):
-    # products (1 launch, or the limb engine's 1) + NTT(y_h) + finalize
+    # products: the fused GEMV, or the tensor engine's query-digit split,
+    # pack-key digit split and limb GEMM; then NTT(y_h) + finalize
     # + NTT(rgsw) + (t-1) external products + rescale
-    return 1 + 2 + (1 + (t - 1) if t > 1 else 0) + 1
+    products = 3 if engine == pir.ENGINE_TENSOR else 1
+    return products + 2 + (1 + (t - 1) if t > 1 else 0) + 1
 
 
 def kernel_times(srv, engine, batch, t_fd, t_sd, t_pk, t_out, stream, n1,

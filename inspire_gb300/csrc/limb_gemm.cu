@@ -63,6 +63,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <type_traits>
 
 #include "internal.h"
 #include "limb_gemm.h"
@@ -73,7 +74,6 @@ namespace {
 constexpr int kBlockRows = 128;    // rows per MMA (M)
 constexpr int kRowBlocks = 2;      // row blocks per CTA sharing a request tile
 constexpr int kTileRows = kBlockRows * kRowBlocks;
-constexpr int kTileQ = 64;         // requests per CTA
 constexpr int kStageK = 32;        // K per A stage (two planes: 128-byte rows)
 constexpr int kUnitK = 128;        // K per exact accumulation unit
 constexpr int kStagesPerUnit = kUnitK / kStageK;
@@ -87,8 +87,8 @@ constexpr int kAStages = kStagesPerUnit;
 constexpr int kAPairs = kAStages / 2;
 constexpr int kARingBytes = kAStages * kABoxBytes;         // 64 KB per row block
 constexpr int kBSlotK = 2 * kStageK;
-constexpr int kBPlaneBytes = kTileQ * kBSlotK * 2;         // 8 KB
-constexpr int kBSlotBytes = 4 * kBPlaneBytes;              // 32 KB
+constexpr int kBRows = 256;        // request-tile rows of the B operand
+constexpr int kBSlotBytes = kBRows * kBSlotK * 2;          // 32 KB
 constexpr int kBSlots = 3;
 constexpr int kBHalves = kStagesPerUnit / 2;               // request slots per unit
 constexpr int kRingBytes = kRowBlocks * kARingBytes + kBSlots * kBSlotBytes;  // 224 KB
@@ -97,6 +97,18 @@ constexpr int kTmemCols = 512;     // one 256-column accumulator per row block
 constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr size_t kSmemBytes = kRingBytes + 1024 + 256;
 static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
+
+// Request words split into NQ balanced base-256 digit planes: NQ = 4 for
+// Z_2^32 words, 8 for Z_2^64. A request tile holds TQ = 256 / NQ requests,
+// so its B operand always has 256 rows (NQ planes x TQ requests), the DB /
+// low-pack MMA has N = 256 and the accumulator of a row block NQ weight
+// blocks of TQ columns (256 TMEM columns).
+template <int NQ>
+struct LimbShape {
+  static constexpr int kTQ = kBRows / NQ;
+  static constexpr int kBPlaneBytes = kTQ * kBSlotK * 2;  // 8 or 4 KB
+  using Acc = typename std::conditional<NQ == 4, uint32_t, unsigned long long>::type;
+};
 
 // ------------------------------------------------------------------ PTX --
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -267,6 +279,7 @@ struct UnitSrc {
   int ax, a_step, bx, nb;
 };
 
+template <int NQ>
 __device__ __forceinline__ UnitSrc unit_src(int u, int n_db_units,
                                             const CUtensorMap* tm_db,
                                             const CUtensorMap* tm_pk,
@@ -280,17 +293,21 @@ __device__ __forceinline__ UnitSrc unit_src(int u, int n_db_units,
   r.a_step = kind == 0 ? 2 * kStageK : 4 * kStageK;
   r.ax = kb * kStagesPerUnit * r.a_step + (kind == 2 ? 2 * kStageK : 0);
   r.bx = kb * kUnitK;
-  r.nb = kind == 2 ? 2 : 4;
+  r.nb = kind == 2 ? NQ - 2 : NQ;
   return r;
 }
 
+template <int NQ>
 __global__ void __launch_bounds__(kThreads, 1)
 limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
                  const __grid_constant__ CUtensorMap tm_pk,
                  const __grid_constant__ CUtensorMap tm_q,
                  const __grid_constant__ CUtensorMap tm_y, LimbArgs a,
-                 const uint32_t* __restrict__ qsum,
-                 uint32_t* __restrict__ out, int* __restrict__ err) {
+                 const typename LimbShape<NQ>::Acc* __restrict__ qsum,
+                 typename LimbShape<NQ>::Acc* __restrict__ out, int* __restrict__ err) {
+  using Acc = typename LimbShape<NQ>::Acc;
+  constexpr int kTileQ = LimbShape<NQ>::kTQ;
+  constexpr int kBPlaneBytes = LimbShape<NQ>::kBPlaneBytes;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -371,7 +388,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       return true;
     };
     for (int i = 0; i < nu && ok; ++i) {
-      const UnitSrc src = unit_src(u0 + i, a.n_db_units, &tm_db, &tm_pk, &tm_q, &tm_y);
+      const UnitSrc src = unit_src<NQ>(u0 + i, a.n_db_units, &tm_db, &tm_pk, &tm_q, &tm_y);
       for (int p = 0; p < kAPairs && ok; ++p) ok = load_pair(0, p, src, i);
       for (int p = 0; p < kAPairs && ok; ++p) {
         const int n = kBHalves * i + p;
@@ -404,19 +421,21 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     // which keep the one issuing thread ahead of the tensor pipe. The ring
     // waits need no tcgen05 fence (the copies and the MMAs are both in the
     // async proxy, ordered by the mbarrier); the accumulator hand-off does.
-    constexpr uint32_t id256 = instr_desc(256, kBlockRows);
-    constexpr uint32_t id192 = instr_desc(192, kBlockRows);
-    constexpr uint32_t id128 = instr_desc(128, kBlockRows);
-    constexpr uint32_t id64 = instr_desc(64, kBlockRows);
+    // N of the four MMA shapes: all NQ request planes (DB x0, pack p0),
+    // one fewer (x1, p1), and for the high pack planes NQ-2 (p2), NQ-3 (p3).
+    constexpr uint32_t id_n0 = instr_desc(NQ * kTileQ, kBlockRows);
+    constexpr uint32_t id_n1 = instr_desc((NQ - 1) * kTileQ, kBlockRows);
+    constexpr uint32_t id_n2 = instr_desc((NQ - 2) * kTileQ, kBlockRows);
+    constexpr uint32_t id_n3 = instr_desc((NQ - 3) * kTileQ, kBlockRows);
     const uint32_t lo0 = (smem_addr(smem) >> 4) | (1u << 16);
     bool ok = true;
     for (int i = 0; i < nu && ok; ++i) {
-      // DB and low pack units: x0 * [y0..y3] -> blocks 0..3, then
-      // x1 * [y0..y2] -> blocks 1..3; high pack units: p2 * [y0 y1] ->
-      // blocks 2..3, then p3 * [y0] -> block 3.
+      // DB and low pack units: x0 * [y0..y_{NQ-1}] -> weight blocks
+      // 0..NQ-1, then x1 * [y0..y_{NQ-2}] -> blocks 1..NQ-1; high pack
+      // units: p2 * [y0..y_{NQ-3}] -> blocks 2.., then p3 -> blocks 3..
       const bool high = unit_kind(u0 + i, a.n_db_units) == 2;
-      const uint32_t id_0 = high ? id128 : id256, id_1 = high ? id64 : id192;
-      const uint32_t c_0 = high ? 128u : 0u, c_1 = high ? 192u : 64u;
+      const uint32_t id_0 = high ? id_n2 : id_n0, id_1 = high ? id_n3 : id_n1;
+      const uint32_t c_0 = high ? 2u * kTileQ : 0u, c_1 = high ? 3u * kTileQ : 1u * kTileQ;
       int slot[kBHalves];
       uint32_t b_lo[kBHalves];
 #pragma unroll
@@ -466,7 +485,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     // -------------------------------------------------------- epilogue --
     const int e = (warp - 4) / 4;   // row block
     const int ew = (warp - 4) % 4;  // TMEM lanes 32*ew .. 32*ew+31
-    uint32_t acc[kTileQ];
+    Acc acc[kTileQ];
 #pragma unroll
     for (int i = 0; i < kTileQ; ++i) acc[i] = 0;
     bool ok = true;
@@ -484,18 +503,20 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       const uint32_t base =
           tmem + (static_cast<uint32_t>(ew * 32) << 16) + e * 256;
 #pragma unroll
-      for (int sblk = 0; sblk < 4; ++sblk) {
+      for (int sblk = 0; sblk < NQ; ++sblk) {
         if (kind == 2 && sblk < 2) continue;
-        uint32_t v0[32], v1[32];
-        tmem_ld_x32(base + sblk * 64, v0);
-        tmem_ld_x32(base + sblk * 64 + 32, v1);
+        uint32_t v[kTileQ / 32][32];
+#pragma unroll
+        for (int c = 0; c < kTileQ / 32; ++c) tmem_ld_x32(base + sblk * kTileQ + 32 * c, v[c]);
         tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          acc[j] += __float_as_uint(__uint_as_float(v0[j]) + 12582912.0f)
-                    << (8 * sblk);
-          acc[32 + j] += __float_as_uint(__uint_as_float(v1[j]) + 12582912.0f)
-                         << (8 * sblk);
+        for (int c = 0; c < kTileQ / 32; ++c) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            acc[32 * c + j] +=
+                static_cast<Acc>(__float_as_uint(__uint_as_float(v[c][j]) + 12582912.0f))
+                << (8 * sblk);
+          }
         }
       }
       tc_fence_before();
@@ -504,18 +525,21 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     }
     if (ok && *reinterpret_cast<volatile int*>(err) == 0) {
       // Every decoded value carried 0x4B400000 (the bits of 1.5 * 2^23),
-      // shifted by its block weight: remove them all at once, mod 2^32.
-      const uint32_t m = 0x4B400000u;
-      const uint32_t corr = n01 * m + n01 * (m << 8) + n23 * (m << 16) +
-                            n23 * (m << 24);
+      // shifted by its block weight: remove them all at once, mod 2^w.
+      const Acc m = 0x4B400000u;
+      Acc corr = 0;
+#pragma unroll
+      for (int sblk = 0; sblk < NQ; ++sblk) {
+        corr += static_cast<Acc>(sblk < 2 ? n01 : n23) * (m << (8 * sblk));
+      }
       const int row = row0 + e * kBlockRows + ew * 32 + lane;
 #pragma unroll
       for (int j = 0; j < kTileQ; ++j) {
         const int q = q0 + j;
         if (q < a.batch) {
-          uint32_t* o = out + q * a.out_stride + row;
+          Acc* o = out + q * a.out_stride + row;
           // The DB offset 2^15 * sum_c q1[c], once per output word.
-          const uint32_t v = acc[j] - corr + (ks == 0 ? __ldg(qsum + q) << 15 : 0u);
+          const Acc v = acc[j] - corr + (ks == 0 ? __ldg(qsum + q) << 15 : Acc{0});
           if (a.ksplit == 1) {
             *o = v;
           } else {
@@ -551,11 +575,13 @@ __global__ void split_u16_kernel(const uint16_t* __restrict__ src,
   }
 }
 
-// Balanced base-256 digits of one u32 word (mod 2^32) as fp16 values.
-__device__ __forceinline__ void u32_digits(uint32_t x, __half (&h)[4]) {
+// Balanced base-256 digits of a word (mod 2^(8 NQ): the top carry drops)
+// as fp16 values.
+template <int NQ, typename T>
+__device__ __forceinline__ void word_digits(T x, __half (&h)[NQ]) {
   int carry = 0;
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < NQ; ++j) {
     int b = static_cast<int>((x >> (8 * j)) & 255u) + carry;
     carry = b >= 128 ? 1 : 0;
     b -= carry << 8;
@@ -563,40 +589,44 @@ __device__ __forceinline__ void u32_digits(uint32_t x, __half (&h)[4]) {
   }
 }
 
-// The requests' first-dimension words as the four digit planes (plane j at
+// The requests' first-dimension words as the NQ digit planes (plane j at
 // j * plane_rows rows, cols_pad columns, zero past cols and for requests
-// batch..rows_pad) and their sums mod 2^32 (the DB offset term; qsum must
+// batch..rows_pad) and their sums mod 2^w (the DB offset term; qsum must
 // be zeroed). Each thread takes 4 consecutive columns of one request:
 // 16-byte loads when the rows allow them, 8-byte stores per plane.
 // grid = (ceil(cols_pad / 1024), rows_pad), block = 256.
-__global__ void split_queries_kernel(const uint32_t* __restrict__ q1, int64_t cols,
+template <typename T, int NQ>
+__global__ void split_queries_kernel(const T* __restrict__ q1, int64_t cols,
                                      int64_t stride, int batch, int64_t plane_rows,
                                      int64_t cols_pad, __half* __restrict__ dst,
-                                     uint32_t* __restrict__ qsum) {
-  __shared__ uint32_t part[8];
+                                     T* __restrict__ qsum) {
+  __shared__ T part[8];
   const int q = blockIdx.y;
   const int64_t c0 = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) * 4;
-  uint32_t x[4] = {0, 0, 0, 0};
+  T x[4] = {0, 0, 0, 0};
   if (q < batch && c0 < cols) {
-    const uint32_t* row = q1 + q * stride;
+    const T* row = q1 + q * stride;
     if (c0 + 4 <= cols && ((reinterpret_cast<uintptr_t>(row + c0) & 15) == 0)) {
-      const uint4 v = *reinterpret_cast<const uint4*>(row + c0);
-      x[0] = v.x;
-      x[1] = v.y;
-      x[2] = v.z;
-      x[3] = v.w;
+      constexpr int kVec = 16 / sizeof(T);
+#pragma unroll
+      for (int v = 0; v < 4; v += kVec) {
+        const uint4 w = *reinterpret_cast<const uint4*>(row + c0 + v);
+        const T* e = reinterpret_cast<const T*>(&w);
+#pragma unroll
+        for (int i = 0; i < kVec; ++i) x[v + i] = e[i];
+      }
     } else {
 #pragma unroll
-      for (int i = 0; i < 4; ++i) x[i] = c0 + i < cols ? row[c0 + i] : 0u;
+      for (int i = 0; i < 4; ++i) x[i] = c0 + i < cols ? row[c0 + i] : T{0};
     }
   }
   if (c0 < cols_pad) {
-    __half h[4][4];  // [column][plane]
+    __half h[4][NQ];  // [column][plane]
 #pragma unroll
-    for (int i = 0; i < 4; ++i) u32_digits(x[i], h[i]);
+    for (int i = 0; i < 4; ++i) word_digits<NQ>(x[i], h[i]);
     const int64_t plane = plane_rows * cols_pad;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < NQ; ++j) {
       __half2 lo = __halves2half2(h[0][j], h[1][j]);
       __half2 hi = __halves2half2(h[2][j], h[3][j]);
       uint2 w;
@@ -606,15 +636,34 @@ __global__ void split_queries_kernel(const uint32_t* __restrict__ q1, int64_t co
     }
   }
   if (q >= batch) return;  // uniform per block
-  uint32_t sum = x[0] + x[1] + x[2] + x[3];
+  T sum = x[0] + x[1] + x[2] + x[3];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
   if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = sum;
   __syncthreads();
   if (threadIdx.x == 0) {
-    uint32_t t = 0;
+    T t = 0;
     for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) t += part[w];
     atomicAdd(qsum + q, t);
+  }
+}
+
+// The same NQ digit planes of any request-word matrix (the packing keys' y_g
+// words), one word per iteration. Planes plane_rows x cols_pad apart.
+template <typename T, int NQ>
+__global__ void split_words_kernel(const T* __restrict__ src, int64_t rows, int64_t cols,
+                                   int64_t stride, int64_t rows_pad, int64_t plane_rows,
+                                   int64_t cols_pad, __half* __restrict__ dst) {
+  const int64_t total = rows_pad * cols_pad;
+  const int64_t plane = plane_rows * cols_pad;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+       i < total; i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = i / cols_pad, c = i % cols_pad;
+    const T x = r < rows && c < cols ? src[r * stride + c] : T{0};
+    __half h[NQ];
+    word_digits<NQ>(x, h);
+#pragma unroll
+    for (int j = 0; j < NQ; ++j) dst[j * plane + i] = h[j];
   }
 }
 
@@ -628,7 +677,7 @@ __global__ void split_u32_kernel(const void* __restrict__ src, int kind,
                                  int64_t rows, int64_t cols, int64_t stride,
                                  int64_t rows_pad, int64_t plane_rows,
                                  int64_t cols_pad, __half* __restrict__ dst,
-                                 int interleave = 0) {
+                                 int interleave = 0, int exact_top = 0) {
   const int64_t total = rows_pad * cols_pad;
   const int64_t plane = plane_rows * cols_pad;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
@@ -644,12 +693,19 @@ __global__ void split_u32_kernel(const void* __restrict__ src, int kind,
         default: x = static_cast<const uint32_t*>(src)[o]; break;
       }
     }
+    // With exact_top the signed entry itself is the sum of its digits (the
+    // top digit takes the remainder, in [-128, 128]): products with 64-bit
+    // request words need the integer, not its value mod 2^32.
+    const int64_t sv = static_cast<int32_t>(x);
+    int64_t low = 0;
     int carry = 0;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       int b = static_cast<int>((x >> (8 * j)) & 255u) + carry;
       carry = b >= 128 ? 1 : 0;
       b -= carry << 8;
+      if (exact_top && j == 3) b = static_cast<int>((sv - low) >> 24);
+      low += static_cast<int64_t>(b) << (8 * j);
       const int64_t o = interleave ? r * 4 * cols_pad + (c / 32) * 128 + j * 32 + (c % 32)
                                    : j * plane + i;
       dst[o] = __int2half_rn(b);
@@ -703,7 +759,7 @@ class LimbScratchImpl : public LimbScratch {
   int64_t qcap = 0;
   __half* q_planes = nullptr;
   __half* y_planes = nullptr;
-  uint32_t* qsum = nullptr;  // sum_c q1[q][c] per request
+  void* qsum = nullptr;  // sum_c q1[q][c] per request (coefficient words)
   CUtensorMap tm_q{}, tm_y{};
 };
 
@@ -715,8 +771,11 @@ class LimbGemmImpl : public LimbGemm {
     if (err_) cudaFree(err_);
   }
 
-  bool Init(const void* db, int64_t rows, int64_t db_cols, int mat_kind,
+  bool Init(int nq, const void* db, int64_t rows, int64_t db_cols, int mat_kind,
             const void* pack, int64_t pack_cols) {
+    nq_ = nq;
+    tq_ = kBRows / nq;
+    word_ = nq == 4 ? 4 : 8;
     rows_ = rows;
     db_cols_ = db_cols;
     pk_cols_ = pack_cols;
@@ -729,17 +788,21 @@ class LimbGemmImpl : public LimbGemm {
     split_u16_kernel<<<152 * 16, 256>>>(static_cast<const uint16_t*>(db), rows,
                                         db_cols, cpad_, db_planes_);
     split_u32_kernel<<<152 * 16, 256>>>(pack, mat_kind, rows, pack_cols, pack_cols,
-                                        rows, rows, kpad_, pk_planes_, 1);
+                                        rows, rows, kpad_, pk_planes_, 1, nq == 8 ? 1 : 0);
     if (cudaDeviceSynchronize() != cudaSuccess) return false;
     if (!make_map(&tm_db_, db_planes_, rows, 2ull * cpad_, kBlockRows, 2 * kStageK)) return false;
     if (!make_map(&tm_pk_, pk_planes_, rows, 4ull * kpad_, kBlockRows, 2 * kStageK)) return false;
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaFuncSetAttribute(limb_gemm_kernel,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(kSmemBytes)) != cudaSuccess)
-      return false;
+    const cudaError_t fe =
+        nq == 4 ? cudaFuncSetAttribute(limb_gemm_kernel<4>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(kSmemBytes))
+                : cudaFuncSetAttribute(limb_gemm_kernel<8>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(kSmemBytes));
+    if (fe != cudaSuccess) return false;
     return true;
   }
 
@@ -748,8 +811,8 @@ class LimbGemmImpl : public LimbGemm {
   }
 
   int64_t ScratchBytes(int batch) const override {
-    const int64_t need = round_up(batch, kTileQ);
-    return 4 * need * (cpad_ + kpad_) * 2 + 4 * need;
+    const int64_t need = round_up(batch, tq_);
+    return nq_ * need * (cpad_ + kpad_) * 2 + word_ * need;
   }
 
   cudaError_t Reserve(LimbScratch* scratch, int batch) override {
@@ -757,7 +820,7 @@ class LimbGemmImpl : public LimbGemm {
   }
 
   cudaError_t EnsureQueries(LimbScratchImpl* sc, int batch) {
-    const int64_t need = round_up(batch, kTileQ);
+    const int64_t need = round_up(batch, tq_);
     if (need <= sc->qcap) return cudaSuccess;
     if (sc->q_planes) cudaFree(sc->q_planes);
     if (sc->y_planes) cudaFree(sc->y_planes);
@@ -765,14 +828,16 @@ class LimbGemmImpl : public LimbGemm {
     sc->q_planes = sc->y_planes = nullptr;
     sc->qsum = nullptr;
     sc->qcap = 0;
-    cudaError_t e = cudaMalloc(&sc->q_planes, 4ull * need * cpad_ * 2);
+    cudaError_t e = cudaMalloc(&sc->q_planes, static_cast<size_t>(nq_) * need * cpad_ * 2);
     if (e != cudaSuccess) return e;
-    e = cudaMalloc(&sc->y_planes, 4ull * need * kpad_ * 2);
+    e = cudaMalloc(&sc->y_planes, static_cast<size_t>(nq_) * need * kpad_ * 2);
     if (e != cudaSuccess) return e;
-    e = cudaMalloc(&sc->qsum, 4ull * need);
+    e = cudaMalloc(&sc->qsum, static_cast<size_t>(word_) * need);
     if (e != cudaSuccess) return e;
-    if (!make_map(&sc->tm_q, sc->q_planes, 4ull * need, cpad_, kTileQ, kBSlotK) ||
-        !make_map(&sc->tm_y, sc->y_planes, 4ull * need, kpad_, kTileQ, kBSlotK)) {
+    if (!make_map(&sc->tm_q, sc->q_planes, static_cast<uint64_t>(nq_) * need, cpad_, tq_,
+                  kBSlotK) ||
+        !make_map(&sc->tm_y, sc->y_planes, static_cast<uint64_t>(nq_) * need, kpad_, tq_,
+                  kBSlotK)) {
       return cudaErrorInvalidValue;
     }
     sc->qcap = need;
@@ -793,8 +858,8 @@ class LimbGemmImpl : public LimbGemm {
                    int64_t yg_stride, void* out, LimbScratch* scratch,
                    cudaStream_t st, int* chosen, float* best_ms) override {
     if (batch <= 0) return cudaErrorInvalidValue;
-    const int64_t bpad = round_up(batch, kTileQ);
-    const int64_t tiles = (rows_ / kTileRows) * (bpad / kTileQ);
+    const int64_t bpad = round_up(batch, tq_);
+    const int64_t tiles = (rows_ / kTileRows) * (bpad / tq_);
     const int n_units = static_cast<int>((cpad_ + 2 * kpad_) / kUnitK);
     const int sms = sms_ > 0 ? sms_ : 148;
     const int heuristic = ChooseSplit(tiles, n_units);
@@ -847,17 +912,27 @@ class LimbGemmImpl : public LimbGemm {
     LimbScratchImpl* sc = static_cast<LimbScratchImpl*>(scratch);
     cudaError_t e = EnsureQueries(sc, batch);
     if (e != cudaSuccess) return e;
-    const int64_t bpad = round_up(batch, kTileQ);
+    const int64_t bpad = round_up(batch, tq_);
     // Byte planes of the requests, qcap rows apart; rows batch..bpad are 0.
-    e = cudaMemsetAsync(sc->qsum, 0, 4ull * batch, st);
+    e = cudaMemsetAsync(sc->qsum, 0, static_cast<size_t>(word_) * batch, st);
     if (e != cudaSuccess) return e;
-    split_queries_kernel<<<dim3(static_cast<unsigned>((cpad_ + 1023) / 1024),
-                                static_cast<unsigned>(bpad)),
-                           256, 0, st>>>(static_cast<const uint32_t*>(q1), db_cols_,
-                                         q1_stride, batch, sc->qcap, cpad_, sc->q_planes,
-                                         sc->qsum);
-    split_u32_kernel<<<152 * 8, 256, 0, st>>>(yg, kU32, batch, pk_cols_, yg_stride,
-                                              bpad, sc->qcap, kpad_, sc->y_planes);
+    const dim3 qgrid(static_cast<unsigned>((cpad_ + 1023) / 1024), static_cast<unsigned>(bpad));
+    if (nq_ == 4) {
+      split_queries_kernel<uint32_t, 4><<<qgrid, 256, 0, st>>>(
+          static_cast<const uint32_t*>(q1), db_cols_, q1_stride, batch, sc->qcap, cpad_,
+          sc->q_planes, static_cast<uint32_t*>(sc->qsum));
+      split_words_kernel<uint32_t, 4><<<152 * 8, 256, 0, st>>>(
+          static_cast<const uint32_t*>(yg), batch, pk_cols_, yg_stride, bpad, sc->qcap, kpad_,
+          sc->y_planes);
+    } else {
+      using U = unsigned long long;
+      split_queries_kernel<U, 8><<<qgrid, 256, 0, st>>>(
+          static_cast<const U*>(q1), db_cols_, q1_stride, batch, sc->qcap, cpad_, sc->q_planes,
+          static_cast<U*>(sc->qsum));
+      split_words_kernel<U, 8><<<152 * 8, 256, 0, st>>>(
+          static_cast<const U*>(yg), batch, pk_cols_, yg_stride, bpad, sc->qcap, kpad_,
+          sc->y_planes);
+    }
     LimbArgs a;
     a.rows = static_cast<int>(rows_);
     a.n_db_units = static_cast<int>(cpad_ / kUnitK);
@@ -865,18 +940,25 @@ class LimbGemmImpl : public LimbGemm {
     a.qcap = static_cast<int>(sc->qcap);
     a.batch = batch;
     a.out_stride = rows_;
-    const int nqt = static_cast<int>(bpad / kTileQ);
+    const int nqt = static_cast<int>(bpad / tq_);
     const int64_t tiles = (rows_ / kTileRows) * nqt;
     a.ksplit = force_split > 0 ? force_split
                                : Split(bpad, tiles, a.n_db_units + 2 * a.n_pk_blocks);
     if (a.ksplit > 1) {
-      e = cudaMemsetAsync(out, 0, static_cast<size_t>(batch) * rows_ * 4, st);
+      e = cudaMemsetAsync(out, 0, static_cast<size_t>(batch) * rows_ * word_, st);
       if (e != cudaSuccess) return e;
     }
     const unsigned grid = static_cast<unsigned>(tiles * a.ksplit);
-    limb_gemm_kernel<<<grid, kThreads, kSmemBytes, st>>>(
-        tm_db_, tm_pk_, sc->tm_q, sc->tm_y, a, sc->qsum, static_cast<uint32_t*>(out),
-        err_);
+    if (nq_ == 4) {
+      limb_gemm_kernel<4><<<grid, kThreads, kSmemBytes, st>>>(
+          tm_db_, tm_pk_, sc->tm_q, sc->tm_y, a, static_cast<const uint32_t*>(sc->qsum),
+          static_cast<uint32_t*>(out), err_);
+    } else {
+      using U = unsigned long long;
+      limb_gemm_kernel<8><<<grid, kThreads, kSmemBytes, st>>>(
+          tm_db_, tm_pk_, sc->tm_q, sc->tm_y, a, static_cast<const U*>(sc->qsum),
+          static_cast<U*>(out), err_);
+    }
     return cudaGetLastError();
   }
 
@@ -920,6 +1002,7 @@ class LimbGemmImpl : public LimbGemm {
  private:
   int64_t rows_ = 0, db_cols_ = 0, pk_cols_ = 0, cpad_ = 0, kpad_ = 0;
   int sms_ = 0;
+  int nq_ = 4, tq_ = 64, word_ = 4;  // request digit planes, requests per tile, word bytes
   __half *db_planes_ = nullptr, *pk_planes_ = nullptr;
   int* err_ = nullptr;
   CUtensorMap tm_db_{}, tm_pk_{};
@@ -933,9 +1016,17 @@ void LimbGemm::Create(int coeff_bits, int db_kind, const void* db, int64_t rows,
                       int64_t db_cols, int mat_kind, const void* pack,
                       int64_t pack_cols, std::unique_ptr<LimbGemm>* out) {
   out->reset();
-  // Z_{2^32} with a u16 DB: the configuration the byte-limb plan covers.
-  if (coeff_bits != 32 || db_kind != kU16) return;
-  if (mat_kind != kI16 && mat_kind != kI32 && mat_kind != kU32) return;
+  // A u16 DB over Z_{2^32} (4 request digit planes; int16, int32 or u32
+  // pack matrices) or Z_{2^64} (8 planes; int16 or int32 pack matrices,
+  // split into digits whose sum is the entry itself).
+  if (db_kind != kU16) return;
+  if (coeff_bits == 32) {
+    if (mat_kind != kI16 && mat_kind != kI32 && mat_kind != kU32) return;
+  } else if (coeff_bits == 64) {
+    if (mat_kind != kI16 && mat_kind != kI32) return;
+  } else {
+    return;
+  }
   if (rows % kTileRows != 0 || db_cols <= 0 || pack_cols <= 0) return;
   int dev = 0, major = 0, minor = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return;
@@ -943,7 +1034,7 @@ void LimbGemm::Create(int coeff_bits, int db_kind, const void* db, int64_t rows,
   cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
   if (major != 10) return;
   std::unique_ptr<LimbGemmImpl> impl(new LimbGemmImpl());
-  if (!impl->Init(db, rows, db_cols, mat_kind, pack, pack_cols)) {
+  if (!impl->Init(coeff_bits == 32 ? 4 : 8, db, rows, db_cols, mat_kind, pack, pack_cols)) {
     cudaGetLastError();
     return;
   }

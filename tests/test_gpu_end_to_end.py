@@ -47,14 +47,17 @@ def _a_components(params, seed):
         p.coeff_dtype)
 
 
-# Decryption needs the 52-bit modulus: over Z_2^32 (the throughput
+# Decryption needs a modulus above 2^32: over Z_2^32 (the throughput
 # configurations) the first-dimension noise of 16-bit records summed over the
-# DB columns exceeds the message scale 2^32 / 65535, so the tensor engine
-# (Z_2^32 only) is checked against the oracle elsewhere, not by decryption.
+# DB columns exceeds the message scale 2^32 / 65535. Both engines run here
+# over Z_2^64 (the tensor engine with eight request digit planes).
 @pytest.mark.parametrize("d,t,n,l,engine", [
     (2048, 2, 4096, 1, pir.ENGINE_PLAIN),      # the C1 shape
     (1024, 4, 8192, 2, pir.ENGINE_PLAIN),      # two shards
     (2048, 8, 65536, 1, pir.ENGINE_PLAIN),     # t = 8: seven external products
+    (2048, 2, 4096, 1, pir.ENGINE_TENSOR),
+    (1024, 4, 8192, 2, pir.ENGINE_TENSOR),
+    (2048, 8, 65536, 1, pir.ENGINE_TENSOR),
 ])
 def test_decrypted_records_equal_database(d, t, n, l, engine):
     params = _params(d, t, n, l)

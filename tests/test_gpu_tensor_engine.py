@@ -198,9 +198,11 @@ def test_autotuned_split_keeps_responses_identical():
                           srv.process_arrays(fd, sd, pk, pir.ENGINE_PLAIN))
 
 
-def test_tensor_engine_unavailable_for_u64():
+def test_tensor_engine_unavailable_for_full_width_pack_words():
+    # Over Z_2^64 the engine takes int16 / int32 pack matrices (four digits
+    # whose sum is the entry); full u64 words would need eight.
     params = synthetic.make_params(d=128, n=8192, t=2, coeff_bits=64, log_q=52)
-    mat = synthetic.make_material(params, seed=1, pad_to=32)
+    mat = synthetic.make_material(params, seed=1, pad_to=32, mat_dtype=np.uint64)
     srv = _server(params, mat)
     fd, sd, pk = synthetic.make_requests(params, 1)
     with pytest.raises(pir.InspireError, match="tensor engine unavailable"):

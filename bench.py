@@ -32,7 +32,21 @@ sys.path.insert(0, ROOT)
 N_ENTRIES = 1 << 20
 DEGREE = 4096
 INTERP = 8
-COEFF_BITS = 32
+COEFF_BITS = 32   # --coeff-bits 64 answers over Z_2^64 with q = 2^56
+LOG_Q = 32
+
+
+def word_tag():
+    return "u%d" % COEFF_BITS
+
+
+def ring_tag():
+    return "Z_2^32" if COEFF_BITS == 32 else "Z_2^64, q=2^%d" % LOG_Q
+
+
+def workload_name():
+    return "pir_answer_n2^20_d4096_t8_l1_" + word_tag() + \
+        ("" if COEFF_BITS == 32 else "_q2^%d" % LOG_Q)
 
 
 def peaks():
@@ -110,7 +124,7 @@ def replica_time(ms, dist, device):
 def make_workload(seed=2026, batch=256):
     from inspire_gb300 import synthetic
     params = synthetic.make_params(d=DEGREE, n=N_ENTRIES, t=INTERP,
-                                   coeff_bits=COEFF_BITS)
+                                   coeff_bits=COEFF_BITS, log_q=LOG_Q)
     rows = INTERP * DEGREE
     cols = N_ENTRIES // INTERP
     # Uniform already-interpolated DB values in [0, p) (p = 65535).
@@ -121,7 +135,7 @@ def make_workload(seed=2026, batch=256):
                                        np.int32, seed + 7)
     mat = synthetic.make_material(
         synthetic.make_params(d=DEGREE, n=DEGREE * INTERP, t=INTERP,
-                              coeff_bits=COEFF_BITS), seed=seed + 1)
+                              coeff_bits=COEFF_BITS, log_q=LOG_Q), seed=seed + 1)
     fd, sd, pk = synthetic.make_requests(params, batch, seed=seed + 2)
     return params, db, pack, mat.a_tilde_agg, mat.t_vec_h, mat.second_dim_a, \
         fd, sd, pk
@@ -165,13 +179,13 @@ def run_reference(args):
     qps = threads * args.steps / total
     line = {
         "impl": "reference",
-        "metric": "queries/s (online answer, n=2^20 d=4096 t=8, Z_2^32)",
+        "metric": "queries/s (online answer, n=2^20 d=4096 t=8, %s)" % ring_tag(),
         "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "scaling": "weak", "vs_baseline": None, "dtype": word_tag(),
         "data": "synthetic (seeded uniform DB / queries)",
-        "config": {"workload": "pir_answer_n2^20_d4096_t8_l1_u32",
+        "config": {"workload": workload_name(),
                    "n": N_ENTRIES, "d": DEGREE, "t": INTERP, "l": 1,
                    "requests_per_step": threads},
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads,
@@ -476,7 +490,13 @@ def main():
                     help="answer: the online answer (default); pack: the "
                          "packing micro-workload; interpolate: the offline "
                          "DB interpolation")
+    ap.add_argument("--coeff-bits", type=int, default=32, choices=[32, 64],
+                    help="answer workload: CoeffType u32 (q = 2^32) or u64 "
+                         "(q = 2^56, the reference's real parameters)")
     args = ap.parse_args()
+    global COEFF_BITS, LOG_Q
+    COEFF_BITS = args.coeff_bits
+    LOG_Q = 32 if COEFF_BITS == 32 else 56
     if args.workload == "pack" and args.impl == "ours":
         run_pack_workload(args)
         return
@@ -511,15 +531,17 @@ def main():
     B = args.batch
     d = DEGREE
     n1 = fd.shape[1]
-    cdt = np.uint32
+    cdt = params.coeff_dtype
+    iv = np.int32 if COEFF_BITS == 32 else np.int64
+    tdt = torch.int32 if COEFF_BITS == 32 else torch.int64
     l = 1
 
     # Device-resident requests and responses.
     dev = torch.device("cuda", local)
-    t_fd = torch.from_numpy(fd.view(np.int32)).to(dev)
-    t_sd = torch.from_numpy(sd.view(np.int32)).to(dev)
-    t_pk = torch.from_numpy(pk.view(np.int32)).to(dev)
-    t_out = torch.empty((B, l, 2, d), dtype=torch.int32, device=dev)
+    t_fd = torch.from_numpy(fd.view(iv)).to(dev)
+    t_sd = torch.from_numpy(sd.view(iv)).to(dev)
+    t_pk = torch.from_numpy(pk.view(iv)).to(dev)
+    t_out = torch.empty((B, l, 2, d), dtype=tdt, device=dev)
     stream = torch.cuda.Stream(device=dev)
     sptr = stream.cuda_stream
 
@@ -582,10 +604,10 @@ def main():
                                   stream, n1, sd.shape[1], pk.shape[1])
 
     # e2e through the host-buffer C ABI (pinned host memory).
-    h_fd = torch.from_numpy(fd.view(np.int32)).pin_memory().numpy().view(cdt)
-    h_sd = torch.from_numpy(sd.view(np.int32)).pin_memory().numpy().view(cdt)
-    h_pk = torch.from_numpy(pk.view(np.int32)).pin_memory().numpy().view(cdt)
-    h_out = torch.empty((B, l, 2, d), dtype=torch.int32).pin_memory().numpy()
+    h_fd = torch.from_numpy(fd.view(iv)).pin_memory().numpy().view(cdt)
+    h_sd = torch.from_numpy(sd.view(iv)).pin_memory().numpy().view(cdt)
+    h_pk = torch.from_numpy(pk.view(iv)).pin_memory().numpy().view(cdt)
+    h_out = torch.empty((B, l, 2, d), dtype=tdt).pin_memory().numpy()
     lib = __import__("inspire_gb300._lib", fromlist=["load"]).load()
     err = ctypes.create_string_buffer(256)
 
@@ -652,14 +674,14 @@ def main():
     qps = world * B / (ms_step / 1000.0)
     plain_qps = 1000.0 / ms_plain
     line = {
-        "metric": "queries/s (online answer, n=2^20 d=4096 t=8, Z_2^32): "
-                  "batched tensor-core vs plain, bit-exact",
+        "metric": "queries/s (online answer, n=2^20 d=4096 t=8, %s): "
+                  "batched tensor-core vs plain, bit-exact" % ring_tag(),
         "value": qps, "unit": "queries/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u32", "data": "synthetic (seeded uniform DB, pack matrix, "
-                                "queries)",
-        "config": {"workload": "pir_answer_n2^20_d4096_t8_l1_u32",
+        "dtype": word_tag(), "data": "synthetic (seeded uniform DB, pack matrix, "
+                                     "queries)",
+        "config": {"workload": workload_name(),
                    "n": N_ENTRIES, "d": DEGREE, "t": INTERP, "l": 1,
                    "batch": B, "engine": "tensor" if engine else "plain",
                    "db_matrix": [rows, cols], "pack_matrix": list(pack.shape),

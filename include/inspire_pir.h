@@ -49,6 +49,8 @@ extern "C" {
 /* Answer engines for the batched entry points. */
 #define INSPIRE_ENGINE_PLAIN 0  /* fused CUDA-core GEMV, HBM-bound        */
 #define INSPIRE_ENGINE_TENSOR 1 /* 8-bit limbs on the tcgen05 tensor cores */
+/* (u16 DB; i16/i32/u32 pack matrices over Z_2^32, i16/i32 over Z_2^64;
+ * l*t*d a multiple of 256. Other servers return FAILED_PRECONDITION.) */
 
 /* PirParams<CoeffType> (crypto/pir/pir_params.h:36-105) together with the
  * template arguments of PirServer<DbDataType, CoeffType, MatCoeffType>. */

@@ -9,7 +9,9 @@ Algorithmic work per request (rows R = l*t*d, DB columns C, pack columns K):
   bytes (plain)  = 2*R*C (u16 DB) + 4*R*K (i32 pack) + 4*(C + K) + 4*R
   limb-ops (tensor, Z_2^32) = 2*(7*R*C + 10*R*K)
     (DB: low byte x 4 query limbs + high byte x 3; pack: 4+3+2+1 byte pairs,
-     only pairs whose weight 2^(8(i+j)) is below 2^32 contribute).
+     only pairs whose weight 2^(8(i+j)) is below 2^32 contribute);
+  limb-ops (tensor, Z_2^64) = 2*(15*R*C + 26*R*K)
+    (8 query limbs: DB 8+7, pack 8+7+6+5 byte pairs below 2^64).
 """
 import ctypes
 import json
@@ -36,8 +38,9 @@ def plain_bytes(rows, db_cols, pack_cols, db_elem=2, pack_elem=4, word=4):
             (db_cols + pack_cols) * word + rows * word)
 
 
-def limb_ops(rows, db_cols, pack_cols, batch):
-    return 2.0 * (7 * rows * db_cols + 10 * rows * pack_cols) * batch
+def limb_ops(rows, db_cols, pack_cols, batch, coeff_bits=32):
+    db_pairs, pk_pairs = (7, 10) if coeff_bits == 32 else (15, 26)
+    return 2.0 * (db_pairs * rows * db_cols + pk_pairs * rows * pack_cols) * batch
 
 
 # DRAM traffic per unit of work from one ncu capture of a smaller case of the
@@ -46,9 +49,12 @@ def limb_ops(rows, db_cols, pack_cols, batch):
 #  * limb GEMM, n=2^18 d=2048 t=8 B=256 (ncu --set full, one launch):
 #    dram read 2.998676 GB + write 0.113170 GB over R (C + 2K) =
 #    16384 * 40960 row-column units;
+#  * limb GEMM over Z_2^64, same shape: read 3.490142 GB + write
+#    0.163364 GB;
 #  * fused GEMV, n=2^18 d=4096 t=8 (ncu --set full, one launch): read
 #    3.221 GB + write 2.9 MB against 3.222 GB of algorithmic bytes.
 LIMB_TRAFFIC_PER_UNIT = (2.998676e9 + 0.113170e9) / (16384 * 40960)
+LIMB64_TRAFFIC_PER_UNIT = (3.490142e9 + 0.163364e9) / (16384 * 40960)
 GEMV_TRAFFIC_PER_ALG_BYTE = (3.221e9 + 2.9e6) / 3.222e9
 
 
@@ -67,7 +73,10 @@ def kernel_times(srv, engine, batch, t_fd, t_sd, t_pk, t_out, stream, n1,
     err = ctypes.create_string_buffer(256)
     rows = srv.rows
     dev = t_fd.device
-    out = torch.empty((batch, rows), dtype=torch.int32, device=dev)
+    cb = srv.params.rlwe.coeff_bits
+    word = cb // 8
+    out = torch.empty((batch, rows),
+                      dtype=torch.int32 if cb == 32 else torch.int64, device=dev)
     sptr = stream.cuda_stream
 
     def run(b, eng):
@@ -92,22 +101,23 @@ def kernel_times(srv, engine, batch, t_fd, t_sd, t_pk, t_out, stream, n1,
 
     hbm, tfl, kind = peaks()
     ms_plain = time_it(1, pir.ENGINE_PLAIN)
-    pb = plain_bytes(rows, srv.db_cols, srv.pack_cols)
+    pb = plain_bytes(rows, srv.db_cols, srv.pack_cols, word=word)
     plain_gbs = pb / (ms_plain / 1e3) / 1e9
     kernels = {"fused_gemv_b1": {"ms": ms_plain, "bytes": pb,
                                  "gbs": plain_gbs,
                                  "frac_hbm": plain_gbs / hbm}}
     if engine == pir.ENGINE_TENSOR:
         ms_t = time_it(batch, engine)
-        ops = limb_ops(rows, srv.db_cols, srv.pack_cols, batch)
+        ops = limb_ops(rows, srv.db_cols, srv.pack_cols, batch, cb)
         ach = ops / (ms_t / 1e3) / 1e12
         kernels["limb_gemm_b%d" % batch] = {"ms": ms_t, "limb_ops": ops,
                                             "tflops": ach,
                                             "frac_tensor": ach / tfl}
         units = rows * (srv.db_cols + 2 * srv.pack_cols)
+        per_unit = LIMB_TRAFFIC_PER_UNIT if cb == 32 else LIMB64_TRAFFIC_PER_UNIT
         roof = {"bound": "tensor", "achieved": ach, "peak": tfl,
                 "unit": "TFLOP/s", "frac": ach / tfl,
-                "traffic": LIMB_TRAFFIC_PER_UNIT * units,
+                "traffic": per_unit * units,
                 "traffic_source": "ncu small case scaled by R*(C+2K)",
                 "kernel": "limb_gemm", "peak_kind": kind + " bf16 dense"}
     else:

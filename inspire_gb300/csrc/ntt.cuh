@@ -24,6 +24,9 @@ struct NttCtx {
   uint32_t garner[kMaxPrimes][kMaxPrimes];  // [j][i] = p_j^-1 * 2^32 mod p_i
   uint64_t pm[kMaxPrimes];                  // prod_{j<i} p_j mod 2^64
   const uint32_t* tables;  // [prime][4][d]: psi_rev, shoup, ipsi_rev, shoup
+  // The same tables permuted for the radix-16 transform of ntt16.cuh
+  // ([prime][4][d]); null unless d = 4096.
+  const uint32_t* tables16;
 };
 
 #ifdef __CUDACC__

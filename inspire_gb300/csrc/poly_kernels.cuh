@@ -11,6 +11,7 @@
 
 #include "arith.cuh"
 #include "ntt.cuh"
+#include "ntt16.cuh"
 
 namespace inspire {
 
@@ -408,6 +409,94 @@ ext_step_kernel(bool first, const uint32_t* __restrict__ resid_in,
     ntt_inverse_t<ITERS>(smem, c, pi);
     for (int j = threadIdx.x; j < d; j += blockDim.x) {
       out[half * d + j] = shoup_mul(smem[j], c.scale[pi], c.scale_s[pi], p);
+    }
+  }
+}
+
+// The external product of ext_step_kernel for d = 4096, one block per
+// (shard, request) over all primes: the Horner state is reconstructed once
+// (not once per prime), every NTT runs in registers with the radix-16
+// passes of ntt16.cuh, the RGSW products are taken in the layout the forward
+// transform leaves (16 consecutive slots per thread, 16-byte loads) and the
+// inverse starts from the accumulators without a trip through shared
+// memory. Same residues as ext_step_kernel. grid = (l, batch), 256 threads,
+// needs c.tables16.
+template <typename T>
+__global__ void __launch_bounds__(kNtt16Threads, 2)
+ext_step16_kernel(bool first, const uint32_t* __restrict__ resid_in,
+                  uint32_t* __restrict__ resid_out,
+                  const T* __restrict__ coeff_a, int64_t coeff_a_q_stride,
+                  int64_t coeff_a_shard_stride,
+                  const T* __restrict__ coeff_b, int64_t coeff_b_q_stride,
+                  int64_t coeff_b_shard_stride,
+                  const uint32_t* __restrict__ RGSWa, int64_t rgswa_qstride,
+                  const uint32_t* __restrict__ RGSWb, ExtArgs e, NttCtx c) {
+  extern __shared__ uint32_t smem[];
+  constexpr int d = kNtt16D;
+  uint32_t* xs = smem;                           // exchange buffer
+  T* sa = reinterpret_cast<T*>(smem + d);        // LowBits of the state
+  T* sb = sa + d;
+  const int tid = threadIdx.x;
+  const int shard = blockIdx.x;
+  const int q = blockIdx.y;
+  const int l = gridDim.x;
+  const T* ca = coeff_a + q * coeff_a_q_stride + shard * coeff_a_shard_stride;
+  const T* cb = coeff_b + q * coeff_b_q_stride + shard * coeff_b_shard_stride;
+  const int64_t rbase = (static_cast<int64_t>(q) * l + shard) * c.r * 2 * d;
+  for (int j = tid; j < d; j += kNtt16Threads) {
+    T ra, rb;
+    horner_state<T>(first, resid_in, rbase, d, j, ca, cb, c, ra, rb);
+    sa[j] = low_bits<T>(ra, e.log_q);
+    sb[j] = low_bits<T>(rb, e.log_q);
+  }
+  // Each thread reads back only the words it wrote: no barrier needed.
+  const int ng = 2 * e.num_digits;
+  for (int pi = 0; pi < c.r; ++pi) {
+    const uint32_t p = c.p[pi];
+    const uint32_t pinv = c.pinv[pi];
+    const uint32_t* tab16 = c.tables16 + static_cast<size_t>(pi) * 4 * d;
+    uint32_t acc_a[16], acc_b[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc_a[k] = acc_b[k] = 0;
+    for (int g = 0; g < ng; ++g) {
+      const T* src = g < e.num_digits ? sa : sb;
+      const int dg = g < e.num_digits ? g : g - e.num_digits;
+      if (dg >= e.live_digits) continue;
+      uint32_t x[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        const T dig = gadget_digit<T>(src[tid + 256 * k], e.log_q, e.log_digit,
+                                      e.num_digits, dg);
+        x[k] = to_residue<T>(dig & static_cast<T>(e.umask), p);
+      }
+      ntt16_forward(x, xs, tab16, p, tid);
+      const uint4* wa = reinterpret_cast<const uint4*>(
+          RGSWa + q * rgswa_qstride + (static_cast<int64_t>(g) * c.r + pi) * d + 16 * tid);
+      const uint4* wb = reinterpret_cast<const uint4*>(
+          RGSWb + ((static_cast<int64_t>(q) * ng + g) * c.r + pi) * d + 16 * tid);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const uint4 va = __ldg(wa + v), vb = __ldg(wb + v);
+        const uint32_t ra[4] = {va.x, va.y, va.z, va.w};
+        const uint32_t rb[4] = {vb.x, vb.y, vb.z, vb.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int k = 4 * v + i;
+          acc_a[k] = add_mod(acc_a[k], mont_mul(x[k], ra[i], p, pinv), p);
+          acc_b[k] = add_mod(acc_b[k], mont_mul(x[k], rb[i], p, pinv), p);
+        }
+      }
+    }
+    uint32_t* out = resid_out + rbase + static_cast<int64_t>(pi) * 2 * d;
+    ntt16_inverse(acc_a, xs, tab16, p, tid);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      out[tid + 256 * k] = shoup_mul(acc_a[k], c.scale[pi], c.scale_s[pi], p);
+    }
+    ntt16_inverse(acc_b, xs, tab16, p, tid);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      out[d + tid + 256 * k] = shoup_mul(acc_b[k], c.scale[pi], c.scale_s[pi], p);
     }
   }
 }

@@ -150,6 +150,31 @@ class NttTables {
         tab[3 * d + i] = Shoup(iw, p);
       }
     }
+    if (logd == kNtt16LogD) {
+      // The radix-16 order of ntt16.cuh, appended after the plain tables:
+      // W[16^P 2^s + g 2^s + x] at ntt16_twiddle_slot(P, s, x, g).
+      const size_t plain = host.size();
+      host.resize(2 * plain, 0);
+      for (int pi = 0; pi < kMaxPrimes; ++pi) {
+        const uint32_t* tab = host.data() + static_cast<size_t>(pi) * 4 * d;
+        uint32_t* t16 = host.data() + plain + static_cast<size_t>(pi) * 4 * d;
+        for (int pass = 0; pass < 3; ++pass) {
+          const int m0 = 1 << (4 * pass);
+          for (int st = 0; st < 4; ++st) {
+            for (int x = 0; x < (1 << st); ++x) {
+              for (int g = 0; g < m0; ++g) {
+                const int slot = ntt16_twiddle_slot(pass, st, x, g);
+                const int idx = (m0 << st) + (g << st) + x;
+                for (int part = 0; part < 4; ++part) {
+                  t16[part * d + slot] = tab[part * d + idx];
+                }
+              }
+            }
+          }
+        }
+      }
+      t->has16_ = true;
+    }
     RETURN_IF_ERROR(Cuda(cudaMalloc(&t->dev_, host.size() * 4), "cudaMalloc"));
     RETURN_IF_ERROR(Cuda(cudaMemcpy(t->dev_, host.data(), host.size() * 4,
                                     cudaMemcpyHostToDevice),
@@ -184,12 +209,14 @@ class NttTables {
       }
     }
     c.tables = dev_;
+    c.tables16 = has16_ ? dev_ + static_cast<size_t>(kMaxPrimes) * 4 * d : nullptr;
     return c;
   }
 
  private:
   NttTables() = default;
   int logd_ = 0;
+  bool has16_ = false;
   uint32_t* dev_ = nullptr;
 };
 
@@ -517,19 +544,34 @@ Status RunPolyStage(inspire_pir_server* s, Workspace* w, int batch,
     ExtArgs e{log_q, s->prm.eval_log_digit, ne,
               LiveDigits(log_q, s->prm.eval_log_digit, ne), s->umask_e};
     const size_t smem = static_cast<size_t>(d) * 4 + 2ull * d * sizeof(T);
-    const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(c.r) * l * batch, s->sms);
-    dim3 grid(c.r, l, batch);
-    INSPIRE_ITERS_DISPATCH(
-        pl.iters, RETURN_IF_ERROR(SetSmem(ext_step_kernel<T, IT>, smem));
-        for (int i = t - 2; i >= 0; --i) {
-          const bool first = i == t - 2;
-          ext_step_kernel<T, IT><<<grid, pl.nt, smem, st>>>(
-              first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
-              a_tilde + static_cast<int64_t>(i + 1) * d, 0, a_stride,
-              packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
-              s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
-          RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
-        });
+    if (d == kNtt16D && c.tables16 != nullptr &&
+        static_cast<int64_t>(l) * batch >= s->sms) {
+      // Enough requests to fill the GPU with one block per (shard, request).
+      RETURN_IF_ERROR(SetSmem(ext_step16_kernel<T>, smem));
+      for (int i = t - 2; i >= 0; --i) {
+        const bool first = i == t - 2;
+        ext_step16_kernel<T><<<dim3(l, batch), kNtt16Threads, smem, st>>>(
+            first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
+            a_tilde + static_cast<int64_t>(i + 1) * d, 0, a_stride,
+            packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
+            s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
+        RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
+      }
+    } else {
+      const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(c.r) * l * batch, s->sms);
+      dim3 grid(c.r, l, batch);
+      INSPIRE_ITERS_DISPATCH(
+          pl.iters, RETURN_IF_ERROR(SetSmem(ext_step_kernel<T, IT>, smem));
+          for (int i = t - 2; i >= 0; --i) {
+            const bool first = i == t - 2;
+            ext_step_kernel<T, IT><<<grid, pl.nt, smem, st>>>(
+                first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
+                a_tilde + static_cast<int64_t>(i + 1) * d, 0, a_stride,
+                packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
+                s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
+            RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
+          });
+    }
   }
   {
     dim3 grid(l, batch);

@@ -1,0 +1,63 @@
+"""The d = 4096 external-product kernel with the register-resident radix-16
+NTT (one block per shard and request over all primes), which the answer
+takes once shards x requests fill the GPU, against the per-prime kernel it
+replaces (taken for small batches) and the CPU oracle
+(crypto/external_product.cc:35-114 inside EvalPoly,
+crypto/pir/server/pir_server.cc:128-150).
+"""
+import numpy as np
+import pytest
+
+from inspire_gb300 import build, pir, synthetic
+from oracle import pyoracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    build.build()
+
+
+def _oparams(params):
+    r = params.rlwe
+    return orc.make_params(
+        coeff_bits=r.coeff_bits, log_degree=r.degree.bit_length() - 1,
+        log_modulus=r.log_modulus,
+        log_modulus1_after_switch=r.log_modulus1_after_switch,
+        log_modulus2_after_switch=r.log_modulus2_after_switch,
+        pack_log_digit=params.pack_gadget.log_digit,
+        pack_num_digits=params.pack_gadget.num_digits,
+        eval_log_digit=params.eval_gadget.log_digit,
+        eval_num_digits=params.eval_gadget.num_digits,
+        num_entries=params.num_entries,
+        interpolation_degree=params.interpolation_degree,
+        entry_size_multiple=params.entry_size_multiple)
+
+
+@pytest.mark.parametrize("coeff_bits,log_q,t,l,batch", [
+    (32, 32, 4, 1, 160),
+    (32, 32, 8, 2, 80),
+    (64, 56, 4, 1, 160),
+])
+def test_radix16_external_product_matches_small_batches_and_oracle(
+        coeff_bits, log_q, t, l, batch):
+    d = 4096
+    params = synthetic.make_params(d=d, n=t * 2048, t=t, l=l,
+                                   coeff_bits=coeff_bits, log_q=log_q)
+    mat = synthetic.make_material(params, seed=t + l)
+    srv = pir.PirServer.CreateCombined(params, mat.db, mat.pack, mat.a_tilde_agg,
+                                       mat.t_vec_h, mat.second_dim_a)
+    fd, sd, pk = synthetic.make_requests(params, batch, seed=batch + t,
+                                         full_range=True)
+    big = srv.process_arrays(fd, sd, pk, pir.ENGINE_PLAIN)
+    small = np.concatenate([
+        srv.process_arrays(fd[i:i + 8], sd[i:i + 8], pk[i:i + 8], pir.ENGINE_PLAIN)
+        for i in range(0, batch, 8)])
+    assert np.array_equal(big, small)
+    op = _oparams(params)
+    for i in (0, batch - 1):
+        want = orc.process_response(op, mat.db, mat.pack, mat.a_tilde_agg,
+                                    mat.t_vec_h, mat.second_dim_a, fd[i], sd[i],
+                                    pk[i])
+        assert np.array_equal(big[i], want), i

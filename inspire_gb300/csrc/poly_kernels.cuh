@@ -104,6 +104,38 @@ ntt_coeffs_kernel(const T* __restrict__ src, int64_t src_qstride,
   for (int j = threadIdx.x; j < d; j += blockDim.x) out[j] = smem[j];
 }
 
+// ntt_coeffs_kernel for d = 4096 with the radix-16 transform of ntt16.cuh,
+// one block per polynomial over all primes (the input is read once).
+// grid = (npoly, batch), 256 threads, needs c.tables16.
+template <typename T>
+__global__ void __launch_bounds__(kNtt16Threads, 2)
+ntt_coeffs16_kernel(const T* __restrict__ src, int64_t src_qstride,
+                    int64_t src_off, int npoly, T mask, uint32_t* __restrict__ dst,
+                    int64_t poly_stride, NttCtx c) {
+  __shared__ uint32_t xs[kNtt16D];
+  constexpr int d = kNtt16D;
+  const int tid = threadIdx.x;
+  const int poly = blockIdx.x;
+  const int q = blockIdx.y;
+  const T* in = src + q * src_qstride + src_off + poly * poly_stride;
+  T v[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = in[tid + 256 * k] & mask;
+  for (int pi = 0; pi < c.r; ++pi) {
+    const uint32_t p = c.p[pi];
+    uint32_t x[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) x[k] = to_residue<T>(v[k], p);
+    ntt16_forward(x, xs, c.tables16 + static_cast<size_t>(pi) * 4 * d, p, tid);
+    uint4* out = reinterpret_cast<uint4*>(
+        dst + ((static_cast<int64_t>(q) * npoly + poly) * c.r + pi) * d + 16 * tid);
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      out[w] = make_uint4(x[4 * w], x[4 * w + 1], x[4 * w + 2], x[4 * w + 3]);
+    }
+  }
+}
+
 // Forward NTT of signed 64-bit polynomials (host-prepared operands).
 // Internal linkage: the header is shared by several translation units.
 static __global__ void __launch_bounds__(kPolyThreads)
@@ -199,6 +231,67 @@ finalize_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ Yh
         x[pi] = shoup_mul(smem[static_cast<int64_t>(pi) * d + j], c.scale[pi],
                           c.scale_s[pi], c.p[pi]);
       }
+    }
+    const T inner = crt_reconstruct<T>(x, c);
+    T g = gemv[base + j];
+    if (gemv2 != nullptr) g += gemv2[base + j];
+    outp[j] = low_bits<T>(static_cast<T>(low_bits<T>(g, log_q) + inner), log_q);
+  }
+}
+
+// finalize_kernel for d = 4096 with the radix-16 inverse of ntt16.cuh: the
+// products are taken in the slot layout the inverse starts from (16
+// consecutive slots per thread, 16-byte loads), each prime's scaled result is
+// kept in shared memory at the positions its thread reads back for the CRT.
+// grid = (l * t, batch), 256 threads, (1 + r) * d words of shared memory,
+// needs c.tables16.
+template <typename T>
+__global__ void __launch_bounds__(kNtt16Threads, 2)
+finalize16_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ Yh,
+                  int k, const T* __restrict__ gemv, const T* __restrict__ gemv2,
+                  int64_t gemv_qstride, T* __restrict__ packed_b, int log_q,
+                  NttCtx c) {
+  extern __shared__ uint32_t smem[];  // exchange buffer, then [r][d] results
+  constexpr int d = kNtt16D;
+  uint32_t* xs = smem;
+  uint32_t* res = smem + d;
+  const int tid = threadIdx.x;
+  const int s = blockIdx.x;
+  const int q = blockIdx.y;
+  for (int pi = 0; pi < c.r; ++pi) {
+    const uint32_t p = c.p[pi];
+    const uint32_t pinv = c.pinv[pi];
+    uint32_t acc[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc[j] = 0;
+    for (int i = 0; i < k; ++i) {
+      const uint4* th = reinterpret_cast<const uint4*>(
+          Th + ((static_cast<int64_t>(s) * k + i) * c.r + pi) * d + 16 * tid);
+      const uint4* yh = reinterpret_cast<const uint4*>(
+          Yh + ((static_cast<int64_t>(q) * k + i) * c.r + pi) * d + 16 * tid);
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const uint4 a = __ldg(th + w), b = __ldg(yh + w);
+        acc[4 * w] = add_mod(acc[4 * w], mont_mul(a.x, b.x, p, pinv), p);
+        acc[4 * w + 1] = add_mod(acc[4 * w + 1], mont_mul(a.y, b.y, p, pinv), p);
+        acc[4 * w + 2] = add_mod(acc[4 * w + 2], mont_mul(a.z, b.z, p, pinv), p);
+        acc[4 * w + 3] = add_mod(acc[4 * w + 3], mont_mul(a.w, b.w, p, pinv), p);
+      }
+    }
+    ntt16_inverse(acc, xs, c.tables16 + static_cast<size_t>(pi) * 4 * d, p, tid);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      res[pi * d + tid + 256 * j] = shoup_mul(acc[j], c.scale[pi], c.scale_s[pi], p);
+    }
+  }
+  const int64_t base = q * gemv_qstride + static_cast<int64_t>(s) * d;
+  T* outp = packed_b + (static_cast<int64_t>(q) * gridDim.x + s) * d;
+  for (int jj = 0; jj < 16; ++jj) {
+    const int j = tid + 256 * jj;
+    uint32_t x[kMaxPrimes] = {0, 0, 0, 0, 0};
+#pragma unroll
+    for (int pi = 0; pi < kMaxPrimes; ++pi) {
+      if (pi < c.r) x[pi] = res[pi * d + j];
     }
     const T inner = crt_reconstruct<T>(x, c);
     T g = gemv[base + j];

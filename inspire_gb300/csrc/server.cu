@@ -487,6 +487,12 @@ Status NttCoeffs(const inspire_pir_server* s, const T* src, int64_t src_qstride,
                  int64_t src_off, int npoly, T mask, uint32_t* dst,
                  int64_t poly_stride, const NttCtx& c, int batch, cudaStream_t st) {
   const int d = s->d;
+  if (d == kNtt16D && c.tables16 != nullptr &&
+      static_cast<int64_t>(npoly) * batch >= s->sms) {
+    ntt_coeffs16_kernel<T><<<dim3(npoly, batch), kNtt16Threads, 0, st>>>(
+        src, src_qstride, src_off, npoly, mask, dst, poly_stride, c);
+    return Cuda(cudaGetLastError(), "forward NTT");
+  }
   const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(npoly) * c.r * batch, s->sms);
   dim3 grid(npoly * c.r, batch);
   INSPIRE_ITERS_DISPATCH(pl.iters, ntt_coeffs_kernel<T, IT><<<grid, pl.nt, d * 4, st>>>(
@@ -507,7 +513,16 @@ Status FinalizeStage(inspire_pir_server* s, Workspace* w, int batch,
                                static_cast<int64_t>(k) * d, k,
                                static_cast<T>(s->vmask_f), w->yh.get<uint32_t>(), d,
                                s->ctx_f, batch, st));
-  {
+  if (d == kNtt16D && s->ctx_f.tables16 != nullptr &&
+      static_cast<int64_t>(l) * t * batch >= s->sms) {
+    const NttCtx& c = s->ctx_f;
+    const size_t smem = static_cast<size_t>(c.r + 1) * d * 4;
+    RETURN_IF_ERROR(SetSmem(finalize16_kernel<T>, smem));
+    finalize16_kernel<T><<<dim3(l * t, batch), kNtt16Threads, smem, st>>>(
+        s->th_ntt.get<uint32_t>(), w->yh.get<uint32_t>(), k, gemv, nullptr, s->rows,
+        w->packed.get<T>(), log_q, c);
+    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "finalize"));
+  } else {
     const NttCtx& c = s->ctx_f;
     const size_t smem = static_cast<size_t>(c.r) * d * 4;
     const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(l) * t * batch, s->sms);

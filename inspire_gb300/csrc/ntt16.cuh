@@ -55,6 +55,17 @@ __device__ __forceinline__ int ntt16_elem(int pass, int tid, int k) {
                    : (pass == 1 ? 256 * (tid >> 4) + (tid & 15) + 16 * k : 16 * tid + k);
 }
 
+// Barrier of the 256 threads running one transform: the whole block
+// (bar == 0) or named barrier `bar` when several groups of 256 threads run
+// transforms of their own.
+__device__ __forceinline__ void ntt16_sync(int bar) {
+  if (bar == 0) {
+    __syncthreads();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(kNtt16Threads) : "memory");
+  }
+}
+
 __device__ __forceinline__ int ntt16_group(int pass, int tid) {
   return pass == 0 ? 0 : (pass == 1 ? tid >> 4 : tid);
 }
@@ -138,40 +149,41 @@ __device__ __forceinline__ void ntt16_load(uint32_t (&x)[16], const uint32_t* xs
 // slot 16 tid + k (the bit-reversed output array of ntt_forward). `xs` is a
 // 4096-word shared buffer, free again when this returns. tab16 = the
 // prime's permuted tables [W | W shoup | IW | IW shoup], 4096 words each.
+// tid in [0, 256) within the group that synchronises on `bar`.
 __device__ __forceinline__ void ntt16_forward(uint32_t (&x)[16], uint32_t* xs,
                                               const uint32_t* __restrict__ tab16,
-                                              uint32_t p, int tid) {
+                                              uint32_t p, int tid, int bar = 0) {
   const uint32_t* tw = tab16;
   const uint32_t* tws = tab16 + kNtt16D;
   ntt16_fwd_pass<0>(x, tw, tws, p, tid);
   ntt16_store<0>(x, xs, tid);
-  __syncthreads();
+  ntt16_sync(bar);
   ntt16_load<1>(x, xs, tid);
   ntt16_fwd_pass<1>(x, tw, tws, p, tid);
   ntt16_store<1>(x, xs, tid);  // the same words this thread read
-  __syncthreads();
+  ntt16_sync(bar);
   ntt16_load<2>(x, xs, tid);
   ntt16_fwd_pass<2>(x, tw, tws, p, tid);
-  __syncthreads();
+  ntt16_sync(bar);
 }
 
 // Inverse transform without the 1/d scaling. In: x[k] = slot 16 tid + k.
 // Out: x[k] = coefficient tid + 256 k.
 __device__ __forceinline__ void ntt16_inverse(uint32_t (&x)[16], uint32_t* xs,
                                               const uint32_t* __restrict__ tab16,
-                                              uint32_t p, int tid) {
+                                              uint32_t p, int tid, int bar = 0) {
   const uint32_t* itw = tab16 + 2 * kNtt16D;
   const uint32_t* itws = tab16 + 3 * kNtt16D;
   ntt16_inv_pass<2>(x, itw, itws, p, tid);
   ntt16_store<2>(x, xs, tid);
-  __syncthreads();
+  ntt16_sync(bar);
   ntt16_load<1>(x, xs, tid);
   ntt16_inv_pass<1>(x, itw, itws, p, tid);
   ntt16_store<1>(x, xs, tid);
-  __syncthreads();
+  ntt16_sync(bar);
   ntt16_load<0>(x, xs, tid);
   ntt16_inv_pass<0>(x, itw, itws, p, tid);
-  __syncthreads();
+  ntt16_sync(bar);
 }
 #endif
 

@@ -594,6 +594,99 @@ ext_step16_kernel(bool first, const uint32_t* __restrict__ resid_in,
   }
 }
 
+// The external product for d = 4096 when a launch has fewer requests than
+// SMs: one block per (prime, shard, request) as ext_step_kernel, 512 threads
+// in two groups of 256 that run the radix-16 transforms side by side. Group 0
+// transforms the live digits of a, group 1 those of b; each keeps its partial
+// product for one output (group 0: a', group 1: b') and hands the other over
+// through shared memory, then group 0 inverts a' and group 1 b'. Same
+// residues as ext_step_kernel. grid = (r, l, batch), needs c.tables16.
+template <typename T>
+__global__ void __launch_bounds__(2 * kNtt16Threads, 1)
+ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
+                       uint32_t* __restrict__ resid_out,
+                       const T* __restrict__ coeff_a, int64_t coeff_a_q_stride,
+                       int64_t coeff_a_shard_stride,
+                       const T* __restrict__ coeff_b, int64_t coeff_b_q_stride,
+                       int64_t coeff_b_shard_stride,
+                       const uint32_t* __restrict__ RGSWa, int64_t rgswa_qstride,
+                       const uint32_t* __restrict__ RGSWb, ExtArgs e, NttCtx c) {
+  extern __shared__ uint32_t smem[];
+  constexpr int d = kNtt16D;
+  const int tid = threadIdx.x;
+  const int grp = tid >> 8;  // 0: digits of a, 1: digits of b
+  const int lt = tid & (kNtt16Threads - 1);
+  const int bar = 1 + grp;
+  uint32_t* xs = smem + grp * d;  // this group's exchange buffer
+  T* st = reinterpret_cast<T*>(smem + 2 * d);  // LowBits of a, then of b
+  const int pi = blockIdx.x;
+  const int shard = blockIdx.y;
+  const int q = blockIdx.z;
+  const int l = gridDim.y;
+  const T* ca = coeff_a + q * coeff_a_q_stride + shard * coeff_a_shard_stride;
+  const T* cb = coeff_b + q * coeff_b_q_stride + shard * coeff_b_shard_stride;
+  const int64_t rbase = (static_cast<int64_t>(q) * l + shard) * c.r * 2 * d;
+#pragma unroll 4
+  for (int j = tid; j < d; j += 2 * kNtt16Threads) {
+    T ra, rb;
+    horner_state<T>(first, resid_in, rbase, d, j, ca, cb, c, ra, rb);
+    st[j] = low_bits<T>(ra, e.log_q);
+    st[d + j] = low_bits<T>(rb, e.log_q);
+  }
+  __syncthreads();
+  const T* src = st + grp * d;
+  const uint32_t p = c.p[pi];
+  const uint32_t pinv = c.pinv[pi];
+  const uint32_t* tab16 = c.tables16 + static_cast<size_t>(pi) * 4 * d;
+  const int ng = 2 * e.num_digits;
+  uint32_t keep[16], send[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) keep[k] = send[k] = 0;
+  for (int dg = 0; dg < e.live_digits; ++dg) {
+    const int g = grp * e.num_digits + dg;
+    uint32_t x[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const T dig = gadget_digit<T>(src[lt + 256 * k], e.log_q, e.log_digit,
+                                    e.num_digits, dg);
+      x[k] = to_residue<T>(dig & static_cast<T>(e.umask), p);
+    }
+    ntt16_forward(x, xs, tab16, p, lt, bar);
+    const uint32_t* wa =
+        RGSWa + q * rgswa_qstride + (static_cast<int64_t>(g) * c.r + pi) * d + 16 * lt;
+    const uint32_t* wb =
+        RGSWb + ((static_cast<int64_t>(q) * ng + g) * c.r + pi) * d + 16 * lt;
+    const uint4* wk = reinterpret_cast<const uint4*>(grp == 0 ? wa : wb);
+    const uint4* wsd = reinterpret_cast<const uint4*>(grp == 0 ? wb : wa);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const uint4 vk = __ldg(wk + v), vs = __ldg(wsd + v);
+      const uint32_t rk[4] = {vk.x, vk.y, vk.z, vk.w};
+      const uint32_t rs[4] = {vs.x, vs.y, vs.z, vs.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int k = 4 * v + i;
+        keep[k] = add_mod(keep[k], mont_mul(x[k], rk[i], p, pinv), p);
+        send[k] = add_mod(send[k], mont_mul(x[k], rs[i], p, pinv), p);
+      }
+    }
+  }
+  // Hand over: each group leaves its partial of the other output in its own
+  // buffer (free since its last transform) and adds the other group's.
+  ntt16_store<2>(send, xs, lt);
+  __syncthreads();
+  ntt16_load<2>(send, smem + (1 - grp) * d, lt);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) keep[k] = add_mod(keep[k], send[k], p);
+  __syncthreads();
+  ntt16_inverse(keep, xs, tab16, p, lt, bar);
+  uint32_t* out = resid_out + rbase + static_cast<int64_t>(pi) * 2 * d + grp * d;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    out[lt + 256 * k] = shoup_mul(keep[k], c.scale[pi], c.scale_s[pi], p);
+  }
+}
+
 // Final Horner addition (or the single packed ciphertext when t == 1) and
 // the modulus switch of a to q1 and b to q2. grid = (l, batch).
 // With rescale == false it only reconstructs (component entry point).
@@ -615,6 +708,7 @@ finish_kernel(bool from_resid, const uint32_t* __restrict__ resid,
   const int64_t rbase = (static_cast<int64_t>(q) * l + shard) * c.r * 2 * d;
   T* oa = out + (static_cast<int64_t>(q) * l + shard) * 2 * d;
   T* ob = oa + d;
+#pragma unroll 4
   for (int j = threadIdx.x; j < d; j += blockDim.x) {
     T ra, rb;
     horner_state<T>(!from_resid, resid, rbase, d, j, ca, cb, c, ra, rb);

@@ -572,6 +572,19 @@ Status RunPolyStage(inspire_pir_server* s, Workspace* w, int batch,
             s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
         RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
       }
+    } else if (d == kNtt16D && c.tables16 != nullptr) {
+      // Few requests: one block per prime, two transforms at a time.
+      const size_t smem16 = 2ull * d * 4 + 2ull * d * sizeof(T);
+      RETURN_IF_ERROR(SetSmem(ext_step16_pair_kernel<T>, smem16));
+      for (int i = t - 2; i >= 0; --i) {
+        const bool first = i == t - 2;
+        ext_step16_pair_kernel<T><<<dim3(c.r, l, batch), 2 * kNtt16Threads, smem16, st>>>(
+            first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
+            a_tilde + static_cast<int64_t>(i + 1) * d, 0, a_stride,
+            packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
+            s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
+        RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
+      }
     } else {
       const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(c.r) * l * batch, s->sms);
       dim3 grid(c.r, l, batch);
@@ -589,8 +602,11 @@ Status RunPolyStage(inspire_pir_server* s, Workspace* w, int batch,
     }
   }
   {
+    // Few requests: the widest block, which shortens each block's chain of
+    // dependent loads.
     dim3 grid(l, batch);
-    finish_kernel<T><<<grid, nt, 0, st>>>(
+    const int fin_nt = static_cast<int64_t>(l) * batch < s->sms ? kPolyThreads : nt;
+    finish_kernel<T><<<grid, fin_nt, 0, st>>>(
         t > 1, resid[0], a_tilde, a_stride, packed, b_qstride, a_stride, true,
         log_q, s->prm.log_modulus1_after_switch,
         s->prm.log_modulus2_after_switch, resp, t > 1 ? s->ctx_e : s->ctx_f);

@@ -1,9 +1,10 @@
-"""The d = 4096 external-product kernel with the register-resident radix-16
-NTT (one block per shard and request over all primes), which the answer
-takes once shards x requests fill the GPU, against the per-prime kernel it
-replaces (taken for small batches) and the CPU oracle
-(crypto/external_product.cc:35-114 inside EvalPoly,
-crypto/pir/server/pir_server.cc:128-150).
+"""The d = 4096 external-product kernels with the register-resident radix-16
+NTT against each other and the CPU oracle (crypto/external_product.cc:35-114
+inside EvalPoly, crypto/pir/server/pir_server.cc:128-150): once shards x
+requests fill the GPU the answer takes one block per shard and request over
+all primes (and the radix-16 request NTTs and finalize); smaller batches take
+one block per prime with two transforms side by side. Every response of a
+large batch must equal the same requests answered eight at a time.
 """
 import numpy as np
 import pytest

@@ -70,9 +70,20 @@ __device__ __forceinline__ int ntt16_group(int pass, int tid) {
   return pass == 0 ? 0 : (pass == 1 ? tid >> 4 : tid);
 }
 
+// A twiddle word: read-only global memory (kSmem = false) or a copy of the
+// tables in shared memory.
+template <bool kSmem>
+__device__ __forceinline__ uint32_t ntt16_tw(const uint32_t* t, int i) {
+  if constexpr (kSmem) {
+    return t[i];
+  } else {
+    return __ldg(t + i);
+  }
+}
+
 // Four forward stages of pass P on the thread's 16 coefficients.
 // tw = permuted W, tws = its Shoup constants.
-template <int P>
+template <int P, bool kSmem = false>
 __device__ __forceinline__ void ntt16_fwd_pass(uint32_t (&x)[16],
                                                const uint32_t* __restrict__ tw,
                                                const uint32_t* __restrict__ tws,
@@ -85,8 +96,8 @@ __device__ __forceinline__ void ntt16_fwd_pass(uint32_t (&x)[16],
 #pragma unroll
     for (int b = 0; b < (1 << s); ++b) {
       const int slot = ntt16_twiddle_slot(P, s, b, g);
-      w[b] = __ldg(tw + slot);
-      ws[b] = __ldg(tws + slot);
+      w[b] = ntt16_tw<kSmem>(tw, slot);
+      ws[b] = ntt16_tw<kSmem>(tws, slot);
     }
 #pragma unroll
     for (int b = 0; b < (1 << s); ++b) {
@@ -102,7 +113,7 @@ __device__ __forceinline__ void ntt16_fwd_pass(uint32_t (&x)[16],
 }
 
 // Four inverse stages of pass P (stage s = 3 down to 0).
-template <int P>
+template <int P, bool kSmem = false>
 __device__ __forceinline__ void ntt16_inv_pass(uint32_t (&x)[16],
                                                const uint32_t* __restrict__ itw,
                                                const uint32_t* __restrict__ itws,
@@ -115,8 +126,8 @@ __device__ __forceinline__ void ntt16_inv_pass(uint32_t (&x)[16],
 #pragma unroll
     for (int b = 0; b < (1 << s); ++b) {
       const int slot = ntt16_twiddle_slot(P, s, b, g);
-      w[b] = __ldg(itw + slot);
-      ws[b] = __ldg(itws + slot);
+      w[b] = ntt16_tw<kSmem>(itw, slot);
+      ws[b] = ntt16_tw<kSmem>(itws, slot);
     }
 #pragma unroll
     for (int b = 0; b < (1 << s); ++b) {
@@ -149,41 +160,144 @@ __device__ __forceinline__ void ntt16_load(uint32_t (&x)[16], const uint32_t* xs
 // slot 16 tid + k (the bit-reversed output array of ntt_forward). `xs` is a
 // 4096-word shared buffer, free again when this returns. tab16 = the
 // prime's permuted tables [W | W shoup | IW | IW shoup], 4096 words each.
-// tid in [0, 256) within the group that synchronises on `bar`.
+// tid in [0, 256) within the group that synchronises on `bar`. kSmem: the
+// tables were copied to shared memory (tab16 points there).
+template <bool kSmem = false>
 __device__ __forceinline__ void ntt16_forward(uint32_t (&x)[16], uint32_t* xs,
                                               const uint32_t* __restrict__ tab16,
                                               uint32_t p, int tid, int bar = 0) {
   const uint32_t* tw = tab16;
   const uint32_t* tws = tab16 + kNtt16D;
-  ntt16_fwd_pass<0>(x, tw, tws, p, tid);
+  ntt16_fwd_pass<0, kSmem>(x, tw, tws, p, tid);
   ntt16_store<0>(x, xs, tid);
   ntt16_sync(bar);
   ntt16_load<1>(x, xs, tid);
-  ntt16_fwd_pass<1>(x, tw, tws, p, tid);
+  ntt16_fwd_pass<1, kSmem>(x, tw, tws, p, tid);
   ntt16_store<1>(x, xs, tid);  // the same words this thread read
   ntt16_sync(bar);
   ntt16_load<2>(x, xs, tid);
-  ntt16_fwd_pass<2>(x, tw, tws, p, tid);
+  ntt16_fwd_pass<2, kSmem>(x, tw, tws, p, tid);
   ntt16_sync(bar);
 }
 
 // Inverse transform without the 1/d scaling. In: x[k] = slot 16 tid + k.
 // Out: x[k] = coefficient tid + 256 k.
-__device__ __forceinline__ void ntt16_inverse(uint32_t (&x)[16], uint32_t* xs,
-                                              const uint32_t* __restrict__ tab16,
-                                              uint32_t p, int tid, int bar = 0) {
-  const uint32_t* itw = tab16 + 2 * kNtt16D;
-  const uint32_t* itws = tab16 + 3 * kNtt16D;
-  ntt16_inv_pass<2>(x, itw, itws, p, tid);
+// The same with the inverse twiddles and their Shoup constants given apart.
+template <bool kSmem = false>
+__device__ __forceinline__ void ntt16_inverse_tw(uint32_t (&x)[16], uint32_t* xs,
+                                                 const uint32_t* __restrict__ itw,
+                                                 const uint32_t* __restrict__ itws,
+                                                 uint32_t p, int tid, int bar = 0) {
+  ntt16_inv_pass<2, kSmem>(x, itw, itws, p, tid);
   ntt16_store<2>(x, xs, tid);
   ntt16_sync(bar);
   ntt16_load<1>(x, xs, tid);
-  ntt16_inv_pass<1>(x, itw, itws, p, tid);
+  ntt16_inv_pass<1, kSmem>(x, itw, itws, p, tid);
   ntt16_store<1>(x, xs, tid);
   ntt16_sync(bar);
   ntt16_load<0>(x, xs, tid);
-  ntt16_inv_pass<0>(x, itw, itws, p, tid);
+  ntt16_inv_pass<0, kSmem>(x, itw, itws, p, tid);
   ntt16_sync(bar);
+}
+
+// Compact forms: one pass body serves all three passes, the pass index a
+// run-time value (coefficients e_k = base + stride * k, twiddle slots
+// 16^P - 1 + 16^P (2^s - 1 + x) + g). A third of the code of the unrolled
+// transforms, for launches whose blocks each run once per SM, where the
+// fetch of the unrolled code, not the arithmetic, sets the time.
+__device__ __forceinline__ void ntt16_pass_geometry(int pass, int tid, int& base,
+                                                    int& stride, int& g) {
+  base = pass == 0 ? tid : (pass == 1 ? 256 * (tid >> 4) + (tid & 15) : 16 * tid);
+  stride = pass == 0 ? 256 : (pass == 1 ? 16 : 1);
+  g = pass == 0 ? 0 : (pass == 1 ? tid >> 4 : tid);
+}
+
+template <bool kSmem, bool kInverse>
+__device__ __forceinline__ void ntt16_pass_rt(uint32_t (&x)[16],
+                                              const uint32_t* __restrict__ tw,
+                                              const uint32_t* __restrict__ tws,
+                                              uint32_t p, int pass, int g) {
+  const int m0 = 1 << (4 * pass);
+  const int base = m0 - 1 + g;
+#pragma unroll
+  for (int si = 0; si < 4; ++si) {
+    const int s = kInverse ? 3 - si : si;
+    const int half = 8 >> s;
+    uint32_t w[8], ws[8];
+#pragma unroll
+    for (int b = 0; b < (1 << s); ++b) {
+      const int slot = base + m0 * ((1 << s) - 1 + b);
+      w[b] = ntt16_tw<kSmem>(tw, slot);
+      ws[b] = ntt16_tw<kSmem>(tws, slot);
+    }
+#pragma unroll
+    for (int b = 0; b < (1 << s); ++b) {
+#pragma unroll
+      for (int i = 0; i < half; ++i) {
+        const int k = b * 2 * half + i;
+        if (kInverse) {
+          const uint32_t u = x[k], v = x[k + half];
+          x[k] = add_mod(u, v, p);
+          x[k + half] = shoup_mul(sub_mod(u, v, p), w[b], ws[b], p);
+        } else {
+          const uint32_t v = shoup_mul(x[k + half], w[b], ws[b], p);
+          x[k + half] = sub_mod(x[k], v, p);
+          x[k] = add_mod(x[k], v, p);
+        }
+      }
+    }
+  }
+}
+
+template <bool kSmem = false>
+__device__ __forceinline__ void ntt16_forward_compact(uint32_t (&x)[16], uint32_t* xs,
+                                                      const uint32_t* __restrict__ tab16,
+                                                      uint32_t p, int tid, int bar = 0) {
+#pragma unroll 1
+  for (int pass = 0; pass < 3; ++pass) {
+    int base, stride, g;
+    ntt16_pass_geometry(pass, tid, base, stride, g);
+    if (pass > 0) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) x[k] = xs[ntt16_pos(base + stride * k)];
+    }
+    ntt16_pass_rt<kSmem, false>(x, tab16, tab16 + kNtt16D, p, pass, g);
+    if (pass < 2) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) xs[ntt16_pos(base + stride * k)] = x[k];
+    }
+    ntt16_sync(bar);
+  }
+}
+
+template <bool kSmem = false>
+__device__ __forceinline__ void ntt16_inverse_compact(uint32_t (&x)[16], uint32_t* xs,
+                                                      const uint32_t* __restrict__ itw,
+                                                      const uint32_t* __restrict__ itws,
+                                                      uint32_t p, int tid, int bar = 0) {
+#pragma unroll 1
+  for (int i = 0; i < 3; ++i) {
+    const int pass = 2 - i;
+    int base, stride, g;
+    ntt16_pass_geometry(pass, tid, base, stride, g);
+    if (i > 0) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) x[k] = xs[ntt16_pos(base + stride * k)];
+    }
+    ntt16_pass_rt<kSmem, true>(x, itw, itws, p, pass, g);
+    if (i < 2) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) xs[ntt16_pos(base + stride * k)] = x[k];
+    }
+    ntt16_sync(bar);
+  }
+}
+
+template <bool kSmem = false>
+__device__ __forceinline__ void ntt16_inverse(uint32_t (&x)[16], uint32_t* xs,
+                                              const uint32_t* __restrict__ tab16,
+                                              uint32_t p, int tid, int bar = 0) {
+  ntt16_inverse_tw<kSmem>(x, xs, tab16 + 2 * kNtt16D, tab16 + 3 * kNtt16D, p, tid, bar);
 }
 #endif
 

@@ -300,6 +300,81 @@ finalize16_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ 
   }
 }
 
+// finalize16_kernel for launches with fewer blocks than SMs: 512 threads in
+// two groups of 256, group g taking primes g, g + 2, ... side by side, each
+// with its prime's inverse tables copied to shared memory and the compact
+// inverse (a block runs once per SM: global twiddle reads would each wait on
+// L2 and the unrolled code on instruction fetch); then the whole block does
+// the CRT. grid = (l * t, batch), shared memory (2 + 4 + r) * d words, needs
+// c.tables16.
+template <typename T>
+__global__ void __launch_bounds__(2 * kNtt16Threads, 1)
+finalize16_pair_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ Yh,
+                       int k, const T* __restrict__ gemv, const T* __restrict__ gemv2,
+                       int64_t gemv_qstride, T* __restrict__ packed_b, int log_q,
+                       NttCtx c) {
+  extern __shared__ uint32_t smem[];
+  constexpr int d = kNtt16D;
+  const int tid = threadIdx.x;
+  const int grp = tid >> 8;
+  const int lt = tid & (kNtt16Threads - 1);
+  const int bar = 1 + grp;
+  uint32_t* xs = smem + grp * d;
+  uint32_t* itab = smem + 2 * d + grp * 2 * d;  // IW | IW shoup of the prime
+  uint32_t* res = smem + 6 * d;                 // [r][d] scaled residues
+  const int s = blockIdx.x;
+  const int q = blockIdx.y;
+  for (int pi = grp; pi < c.r; pi += 2) {
+    const uint32_t p = c.p[pi];
+    const uint32_t pinv = c.pinv[pi];
+    const uint4* g16 = reinterpret_cast<const uint4*>(
+        c.tables16 + static_cast<size_t>(pi) * 4 * d + 2 * d);
+    uint4* s16 = reinterpret_cast<uint4*>(itab);
+#pragma unroll
+    for (int i = 0; i < 2 * d / 4 / kNtt16Threads; ++i) {
+      s16[lt + i * kNtt16Threads] = __ldg(g16 + lt + i * kNtt16Threads);
+    }
+    uint32_t acc[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc[j] = 0;
+    for (int i = 0; i < k; ++i) {
+      const uint4* th = reinterpret_cast<const uint4*>(
+          Th + ((static_cast<int64_t>(s) * k + i) * c.r + pi) * d + 16 * lt);
+      const uint4* yh = reinterpret_cast<const uint4*>(
+          Yh + ((static_cast<int64_t>(q) * k + i) * c.r + pi) * d + 16 * lt);
+#pragma unroll
+      for (int w = 0; w < 4; ++w) {
+        const uint4 a = __ldg(th + w), b = __ldg(yh + w);
+        acc[4 * w] = add_mod(acc[4 * w], mont_mul(a.x, b.x, p, pinv), p);
+        acc[4 * w + 1] = add_mod(acc[4 * w + 1], mont_mul(a.y, b.y, p, pinv), p);
+        acc[4 * w + 2] = add_mod(acc[4 * w + 2], mont_mul(a.z, b.z, p, pinv), p);
+        acc[4 * w + 3] = add_mod(acc[4 * w + 3], mont_mul(a.w, b.w, p, pinv), p);
+      }
+    }
+    ntt16_sync(bar);  // the group's copy of the tables is complete
+    ntt16_inverse_compact<true>(acc, xs, itab, itab + d, p, lt, bar);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      res[pi * d + lt + 256 * j] = shoup_mul(acc[j], c.scale[pi], c.scale_s[pi], p);
+    }
+  }
+  __syncthreads();
+  const int64_t base = q * gemv_qstride + static_cast<int64_t>(s) * d;
+  T* outp = packed_b + (static_cast<int64_t>(q) * gridDim.x + s) * d;
+#pragma unroll 4
+  for (int j = tid; j < d; j += 2 * kNtt16Threads) {
+    uint32_t x[kMaxPrimes] = {0, 0, 0, 0, 0};
+#pragma unroll
+    for (int pi = 0; pi < kMaxPrimes; ++pi) {
+      if (pi < c.r) x[pi] = res[pi * d + j];
+    }
+    const T inner = crt_reconstruct<T>(x, c);
+    T g = gemv[base + j];
+    if (gemv2 != nullptr) g += gemv2[base + j];
+    outp[j] = low_bits<T>(static_cast<T>(low_bits<T>(g, log_q) + inner), log_q);
+  }
+}
+
 // The packed ciphertexts as (a_tilde_agg, b_agg) pairs:
 // out[q][s] = (a[s], b[q][s]). grid = (shards, batch).
 template <typename T>
@@ -599,8 +674,10 @@ ext_step16_kernel(bool first, const uint32_t* __restrict__ resid_in,
 // in two groups of 256 that run the radix-16 transforms side by side. Group 0
 // transforms the live digits of a, group 1 those of b; each keeps its partial
 // product for one output (group 0: a', group 1: b') and hands the other over
-// through shared memory, then group 0 inverts a' and group 1 b'. Same
-// residues as ext_step_kernel. grid = (r, l, batch), needs c.tables16.
+// through shared memory, then group 0 inverts a' and group 1 b'. Each block
+// runs once per SM, so the compact transforms (one pass body for all passes)
+// keep the code small. Same residues as ext_step_kernel.
+// grid = (r, l, batch), needs c.tables16.
 template <typename T>
 __global__ void __launch_bounds__(2 * kNtt16Threads, 1)
 ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
@@ -620,13 +697,14 @@ ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
   uint32_t* xs = smem + grp * d;  // this group's exchange buffer
   T* st = reinterpret_cast<T*>(smem + 2 * d);  // LowBits of a, then of b
   const int pi = blockIdx.x;
+  const uint32_t* tab16 = c.tables16 + static_cast<size_t>(pi) * 4 * d;
   const int shard = blockIdx.y;
   const int q = blockIdx.z;
   const int l = gridDim.y;
   const T* ca = coeff_a + q * coeff_a_q_stride + shard * coeff_a_shard_stride;
   const T* cb = coeff_b + q * coeff_b_q_stride + shard * coeff_b_shard_stride;
   const int64_t rbase = (static_cast<int64_t>(q) * l + shard) * c.r * 2 * d;
-#pragma unroll 4
+#pragma unroll 2
   for (int j = tid; j < d; j += 2 * kNtt16Threads) {
     T ra, rb;
     horner_state<T>(first, resid_in, rbase, d, j, ca, cb, c, ra, rb);
@@ -637,7 +715,6 @@ ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
   const T* src = st + grp * d;
   const uint32_t p = c.p[pi];
   const uint32_t pinv = c.pinv[pi];
-  const uint32_t* tab16 = c.tables16 + static_cast<size_t>(pi) * 4 * d;
   const int ng = 2 * e.num_digits;
   uint32_t keep[16], send[16];
 #pragma unroll
@@ -651,7 +728,7 @@ ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
                                     e.num_digits, dg);
       x[k] = to_residue<T>(dig & static_cast<T>(e.umask), p);
     }
-    ntt16_forward(x, xs, tab16, p, lt, bar);
+    ntt16_forward_compact(x, xs, tab16, p, lt, bar);
     const uint32_t* wa =
         RGSWa + q * rgswa_qstride + (static_cast<int64_t>(g) * c.r + pi) * d + 16 * lt;
     const uint32_t* wb =
@@ -679,7 +756,7 @@ ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
 #pragma unroll
   for (int k = 0; k < 16; ++k) keep[k] = add_mod(keep[k], send[k], p);
   __syncthreads();
-  ntt16_inverse(keep, xs, tab16, p, lt, bar);
+  ntt16_inverse_compact(keep, xs, tab16 + 2 * d, tab16 + 3 * d, p, lt, bar);
   uint32_t* out = resid_out + rbase + static_cast<int64_t>(pi) * 2 * d + grp * d;
 #pragma unroll
   for (int k = 0; k < 16; ++k) {

@@ -522,6 +522,14 @@ Status FinalizeStage(inspire_pir_server* s, Workspace* w, int batch,
         s->th_ntt.get<uint32_t>(), w->yh.get<uint32_t>(), k, gemv, nullptr, s->rows,
         w->packed.get<T>(), log_q, c);
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "finalize"));
+  } else if (d == kNtt16D && s->ctx_f.tables16 != nullptr) {
+    const NttCtx& c = s->ctx_f;
+    const size_t smem = static_cast<size_t>(6 + c.r) * d * 4;
+    RETURN_IF_ERROR(SetSmem(finalize16_pair_kernel<T>, smem));
+    finalize16_pair_kernel<T><<<dim3(l * t, batch), 2 * kNtt16Threads, smem, st>>>(
+        s->th_ntt.get<uint32_t>(), w->yh.get<uint32_t>(), k, gemv, nullptr, s->rows,
+        w->packed.get<T>(), log_q, c);
+    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "finalize"));
   } else {
     const NttCtx& c = s->ctx_f;
     const size_t smem = static_cast<size_t>(c.r) * d * 4;

@@ -181,8 +181,8 @@ __device__ __forceinline__ void ntt16_forward(uint32_t (&x)[16], uint32_t* xs,
 }
 
 // Inverse transform without the 1/d scaling. In: x[k] = slot 16 tid + k.
-// Out: x[k] = coefficient tid + 256 k.
-// The same with the inverse twiddles and their Shoup constants given apart.
+// Out: x[k] = coefficient tid + 256 k. itw / itws: the permuted inverse
+// twiddles and their Shoup constants.
 template <bool kSmem = false>
 __device__ __forceinline__ void ntt16_inverse_tw(uint32_t (&x)[16], uint32_t* xs,
                                                  const uint32_t* __restrict__ itw,
@@ -293,6 +293,7 @@ __device__ __forceinline__ void ntt16_inverse_compact(uint32_t (&x)[16], uint32_
   }
 }
 
+// The inverse with the prime's whole table block [W | W shoup | IW | IW shoup].
 template <bool kSmem = false>
 __device__ __forceinline__ void ntt16_inverse(uint32_t (&x)[16], uint32_t* xs,
                                               const uint32_t* __restrict__ tab16,

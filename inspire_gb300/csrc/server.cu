@@ -375,6 +375,10 @@ struct Workspace {
   DevBuf rgswa;  // per-request RGSW a-parts (batched ExternalProduct only)
   std::unique_ptr<LimbScratch> limb;
   cudaStream_t stream = nullptr;
+  // Second stream for the host-buffer call: the copy of the second
+  // dimension (read only by the polynomial stage) overlaps the products.
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_go = nullptr, sdim_ready = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t done = nullptr;
   void* host[4] = {nullptr, nullptr, nullptr, nullptr};  // fd, sd, pk, resp
@@ -383,7 +387,10 @@ struct Workspace {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     if (done) cudaEventDestroy(done);
+    if (copy_go) cudaEventDestroy(copy_go);
+    if (sdim_ready) cudaEventDestroy(sdim_ready);
     if (stream) cudaStreamDestroy(stream);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
     for (auto& h : host)
       if (h) cudaFreeHost(h);
   }
@@ -661,6 +668,12 @@ Status InitWorkspace(Workspace* ws) {
   RETURN_IF_ERROR(Cuda(cudaStreamCreateWithFlags(&ws->stream, cudaStreamNonBlocking),
                        "cudaStreamCreate"));
   for (auto& e : ws->ev) RETURN_IF_ERROR(Cuda(cudaEventCreate(&e), "cudaEventCreate"));
+  RETURN_IF_ERROR(Cuda(cudaStreamCreateWithFlags(&ws->copy_stream, cudaStreamNonBlocking),
+                       "cudaStreamCreate"));
+  RETURN_IF_ERROR(Cuda(cudaEventCreateWithFlags(&ws->copy_go, cudaEventDisableTiming),
+                       "cudaEventCreate"));
+  RETURN_IF_ERROR(Cuda(cudaEventCreateWithFlags(&ws->sdim_ready, cudaEventDisableTiming),
+                       "cudaEventCreate"));
   return Cuda(cudaEventCreateWithFlags(&ws->done, cudaEventDisableTiming),
               "cudaEventCreate");
 }
@@ -758,11 +771,15 @@ Status VpirOnDevice(inspire_pir_server* s, Workspace* w, int batch, const void* 
 // The device part of a batch: products, polynomial stage, rescale.
 Status AnswerOnDevice(inspire_pir_server* s, Workspace* w, int batch,
                       const void* q1, const void* pkey, const void* sdim,
-                      void* resp, int engine, cudaStream_t st, bool timed) {
+                      void* resp, int engine, cudaStream_t st, bool timed,
+                      cudaEvent_t sdim_ready = nullptr) {
   const int cb = s->prm.coeff_bits;
   if (timed) cudaEventRecord(w->ev[0], st);
   RETURN_IF_ERROR(Products(s, w, batch, q1, pkey, w->gemv.get(), engine, st));
   if (timed) cudaEventRecord(w->ev[1], st);
+  if (sdim_ready != nullptr) {
+    RETURN_IF_ERROR(Cuda(cudaStreamWaitEvent(st, sdim_ready, 0), "wait second_dim"));
+  }
   if (cb == 32) {
     RETURN_IF_ERROR(RunPolyStage<uint32_t>(
         s, w, batch, static_cast<const uint32_t*>(pkey),
@@ -889,14 +906,23 @@ Status ProcessHostBatch(inspire_pir_server* s, int batch, const void* first_dim,
                                        batch * packing_key_count * d * w,
                                        cudaMemcpyHostToDevice, st),
                        "copy packing_key"));
+  cudaEvent_t sdim_ready = nullptr;
   if (s->t > 1) {
+    // On the copy stream, after everything already queued on the workspace
+    // stream (an earlier batch may still read sdim); the polynomial stage
+    // waits for it, the products do not.
+    RETURN_IF_ERROR(Cuda(cudaEventRecord(ws->copy_go, st), "record"));
+    RETURN_IF_ERROR(Cuda(cudaStreamWaitEvent(ws->copy_stream, ws->copy_go, 0), "wait"));
     RETURN_IF_ERROR(Cuda(cudaMemcpyAsync(ws->sdim.get(), second_dim,
                                          batch * second_dim_count * d * w,
-                                         cudaMemcpyHostToDevice, st),
+                                         cudaMemcpyHostToDevice, ws->copy_stream),
                          "copy second_dim"));
+    RETURN_IF_ERROR(Cuda(cudaEventRecord(ws->sdim_ready, ws->copy_stream), "record"));
+    sdim_ready = ws->sdim_ready;
   }
   RETURN_IF_ERROR(AnswerOnDevice(s, ws, batch, ws->q1.get(), ws->pkey.get(),
-                                 ws->sdim.get(), ws->resp.get(), engine, st, true));
+                                 ws->sdim.get(), ws->resp.get(), engine, st, true,
+                                 sdim_ready));
   const size_t out_bytes = static_cast<size_t>(batch) * s->l * 2 * d * w;
   RETURN_IF_ERROR(Cuda(cudaMemcpyAsync(responses, ws->resp.get(), out_bytes,
                                        cudaMemcpyDeviceToHost, st),

@@ -474,6 +474,196 @@ def run_hint_workload(args):
     print(json.dumps(line))
 
 
+SINGLE_CONFIGS = {
+    # The reference metrics tool's shapes for a single request.
+    "c2": dict(n=65536, d=2048, t=4, l=1, coeff_bits=32, log_q=32),
+    "c1": dict(n=4096, d=2048, t=2, l=1, coeff_bits=64, log_q=52),
+}
+
+
+def run_single_workload(args):
+    """Single-request latency of the plain engine on the small shapes: c2
+    (n = 65536, d = 2048, t = 4, Z_2^32; DB 8192 x 16384 u16 + pack 8192 x
+    4096 i32) or c1 (n = 4096, d = 2048, t = 2, Z_2^64 with q = 2^52). One
+    request per step with L2 flushed (a 256 MB write) before each, each step
+    timed alone with CUDA events: device-resident requests (`value`), the
+    same calls replayed from a CUDA graph, the host-buffer C ABI (`e2e`), the
+    fused GEMV alone against the HBM roofline, and the oracle on one host
+    core (the reference is single-threaded)."""
+    import torch
+    from inspire_gb300 import build, pir, profiling, synthetic
+    cfg = SINGLE_CONFIGS[args.config]
+    build.build()
+    n, d, t, l, cb = cfg["n"], cfg["d"], cfg["t"], cfg["l"], cfg["coeff_bits"]
+    params = synthetic.make_params(d=d, n=n, t=t, l=l, coeff_bits=cb,
+                                   log_q=cfg["log_q"])
+    mat = synthetic.make_material(params, seed=71)
+    srv = pir.PirServer.CreateCombined(params, mat.db, mat.pack, mat.a_tilde_agg,
+                                       mat.t_vec_h, mat.second_dim_a)
+    nreq = 16
+    fd, sd, pk = synthetic.make_requests(params, nreq, seed=72)
+    iv = np.int32 if cb == 32 else np.int64
+    tdt = torch.int32 if cb == 32 else torch.int64
+    dev = torch.device("cuda", 0)
+    t_fd = torch.from_numpy(fd.view(iv)).to(dev)
+    t_sd = torch.from_numpy(sd.view(iv)).to(dev)
+    t_pk = torch.from_numpy(pk.view(iv)).to(dev)
+    t_out = torch.empty((nreq, l, 2, d), dtype=tdt, device=dev)
+    t_prod = torch.empty((nreq, srv.rows), dtype=tdt, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sptr = stream.cuda_stream
+    lib = __import__("inspire_gb300._lib", fromlist=["load"]).load()
+    err = ctypes.create_string_buffer(256)
+    n1, nsd, npk = fd.shape[1], sd.shape[1], pk.shape[1]
+    esz = np.dtype(params.coeff_dtype).itemsize
+
+    def answer(i):
+        srv.process_device(1, t_fd.data_ptr() + i * n1 * esz, n1,
+                           t_sd.data_ptr() + i * nsd * d * esz, nsd,
+                           t_pk.data_ptr() + i * npk * d * esz, npk,
+                           t_out.data_ptr() + i * l * 2 * d * esz,
+                           pir.ENGINE_PLAIN, sptr)
+
+    def products(i):
+        rc = lib.inspire_pir_products_device(
+            srv._h, 1, t_fd.data_ptr() + i * n1 * esz,
+            t_pk.data_ptr() + i * npk * d * esz,
+            t_prod.data_ptr() + i * srv.rows * esz, pir.ENGINE_PLAIN, sptr,
+            err, len(err))
+        if rc:
+            raise SystemExit(err.value)
+
+    def per_step(fn, steps, warm):
+        for i in range(warm):
+            fn(i % nreq)
+        stream.synchronize()
+        times = []
+        for i in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn(i % nreq)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return times
+
+    # Parity of the timed path against the oracle on the first request.
+    from oracle import pyoracle as orc
+    r = params.rlwe
+    op = orc.make_params(
+        coeff_bits=cb, log_degree=d.bit_length() - 1, log_modulus=r.log_modulus,
+        log_modulus1_after_switch=r.log_modulus1_after_switch,
+        log_modulus2_after_switch=r.log_modulus2_after_switch,
+        pack_log_digit=params.pack_gadget.log_digit,
+        pack_num_digits=params.pack_gadget.num_digits,
+        eval_log_digit=params.eval_gadget.log_digit,
+        eval_num_digits=params.eval_gadget.num_digits, num_entries=n,
+        interpolation_degree=t, entry_size_multiple=l)
+    answer(0)
+    stream.synchronize()
+    want = orc.process_response(op, mat.db, mat.pack, mat.a_tilde_agg,
+                                mat.t_vec_h, mat.second_dim_a, fd[0], sd[0], pk[0])
+    got = t_out[0].cpu().numpy().view(params.coeff_dtype)
+    if not np.array_equal(got.reshape(want.shape), want):
+        raise SystemExit("single-request response differs from the oracle")
+
+    hbm, _, peak_kind = peaks()
+    with ClockSampler(0) as clk:
+        t_ans = per_step(answer, args.steps, args.warmup)
+    t_prod_ms = per_step(products, args.steps, args.warmup)
+
+    # The same answer replayed from a CUDA graph (one launch per request).
+    graphs = []
+    for i in range(nreq):
+        with pir.Graph(sptr) as g:
+            answer(i)
+        graphs.append(g)
+    t_graph = per_step(lambda i: graphs[i].launch(sptr), args.steps, args.warmup)
+
+    # End to end through the host-buffer C ABI (pinned host memory).
+    h_fd = torch.from_numpy(fd.view(iv)).pin_memory().numpy().view(params.coeff_dtype)
+    h_sd = torch.from_numpy(sd.view(iv)).pin_memory().numpy().view(params.coeff_dtype)
+    h_pk = torch.from_numpy(pk.view(iv)).pin_memory().numpy().view(params.coeff_dtype)
+    h_out = torch.empty((nreq, l, 2, d), dtype=tdt).pin_memory().numpy()
+
+    def e2e(i):
+        rc = lib.inspire_pir_process_batch(
+            srv._h, 1, h_fd[i].ctypes.data, n1, h_sd[i].ctypes.data, nsd,
+            h_pk[i].ctypes.data, npk, h_out[i].ctypes.data, pir.ENGINE_PLAIN,
+            err, len(err))
+        if rc:
+            raise SystemExit(err.value)
+    for i in range(args.warmup):
+        e2e(i % nreq)
+    t_e2e = []
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        stream.synchronize()
+        t0 = time.perf_counter()
+        e2e(i % nreq)
+        t_e2e.append((time.perf_counter() - t0) * 1000.0)
+
+    ms = statistics.mean(t_ans)
+    ms_prod = statistics.mean(t_prod_ms)
+    rows = srv.rows
+    alg = profiling.plain_bytes(rows, srv.db_cols, srv.pack_cols, word=esz)
+    gbs = alg / (ms_prod / 1000.0) / 1e9
+
+    def pct(v, q):
+        s = sorted(v)
+        return s[min(len(s) - 1, int(q * len(s)))]
+    tag = "u%d" % cb
+    line = {
+        "metric": "queries/s (single request, plain engine, n=%d d=%d t=%d, "
+                  "Z_2^%d q=2^%d)" % (n, d, t, cb, cfg["log_q"]),
+        "value": 1000.0 / ms, "unit": "queries/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": tag, "data": "synthetic (seeded uniform DB, pack matrix, "
+                              "requests)",
+        "config": {"workload": "pir_single_n%d_d%d_t%d_l%d_%s" % (n, d, t, l, tag),
+                   "n": n, "d": d, "t": t, "l": l, "batch": 1,
+                   "engine": "plain", "db_matrix": list(mat.db.shape),
+                   "pack_matrix": list(mat.pack.shape),
+                   "l2": "flushed before every request (256 MB write)"},
+        "latency_ms": {"mean": ms, "p50": pct(t_ans, 0.5), "p99": pct(t_ans, 0.99)},
+        "graph": {"queries_per_s": 1000.0 / statistics.mean(t_graph),
+                  "latency_ms_p50": pct(t_graph, 0.5)},
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                     "frac": gbs / hbm,
+                     "traffic": profiling.GEMV_TRAFFIC_PER_ALG_BYTE * alg,
+                     "traffic_source": "ncu small case scaled by algorithmic bytes",
+                     "kernel": "fused_gemv", "ms": ms_prod, "bytes": alg,
+                     "peak_kind": peak_kind + " copy"},
+        "clocks": clk.summary(),
+        "gpu_launches": profiling.launches_per_step(pir.ENGINE_PLAIN, t) * args.steps,
+        "e2e": {"value": 1000.0 / statistics.mean(t_e2e), "unit": "queries/s",
+                "latency_ms_p50": pct(t_e2e, 0.5),
+                "h2d_bytes_per_step": int(h_fd[0].nbytes + h_sd[0].nbytes +
+                                          h_pk[0].nbytes),
+                "d2h_bytes_per_step": int(h_out[0].nbytes)},
+    }
+    if not args.no_cpu_baseline:
+        done, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < 10.0:
+            orc.process_response(op, mat.db, mat.pack, mat.a_tilde_agg,
+                                 mat.t_vec_h, mat.second_dim_a, fd[done % nreq],
+                                 sd[done % nreq], pk[done % nreq],
+                                 mode=orc.MODE_FP64)
+            done += 1
+        el = time.perf_counter() - t0
+        line["cpu_baseline"] = {
+            "value": done / el, "unit": "queries/s", "cores": 1, "kind": "port",
+            "sample": "%d requests in %.1f s on one host thread (oracle, FP64 "
+                      "FFT path, as the single-threaded reference)" % (done, el)}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -486,10 +676,13 @@ def main():
     ap.add_argument("--entries", type=int, default=N_ENTRIES,
                     help="records of the interpolate / hint workloads")
     ap.add_argument("--workload", default="answer",
-                    choices=["answer", "pack", "interpolate", "hint"],
+                    choices=["answer", "pack", "interpolate", "hint", "single"],
                     help="answer: the online answer (default); pack: the "
                          "packing micro-workload; interpolate: the offline "
-                         "DB interpolation")
+                         "DB interpolation; single: one request at a time on "
+                         "the small shapes (--config c2 or c1)")
+    ap.add_argument("--config", default="c2", choices=sorted(SINGLE_CONFIGS),
+                    help="shape of the single workload")
     ap.add_argument("--coeff-bits", type=int, default=32, choices=[32, 64],
                     help="answer workload: CoeffType u32 (q = 2^32) or u64 "
                          "(q = 2^56, the reference's real parameters)")
@@ -505,6 +698,9 @@ def main():
         return
     if args.workload == "hint" and args.impl == "ours":
         run_hint_workload(args)
+        return
+    if args.workload == "single" and args.impl == "ours":
+        run_single_workload(args)
         return
 
     rank = int(os.environ.get("RANK", "0"))

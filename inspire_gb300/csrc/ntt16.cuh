@@ -1,30 +1,29 @@
-// Register-resident negacyclic NTT for d = 4096 with 256 threads: three
-// radix-16 passes of four stages each, 16 coefficients per thread, two
-// exchanges through shared memory in between.
+// Register-resident negacyclic NTT for d = 2^LOGD (LOGD = 11, 12, 13) with
+// d / 16 threads: passes of up to four stages on 16 coefficients per
+// thread, exchanges through shared memory in between.
 //
 // The transform is the one of ntt.cuh (Cooley-Tukey forward with the
 // psi-twisted twiddles, natural order in and bit-reversed order out;
 // Gentleman-Sande inverse), so both give the same residues. Only the
-// grouping of the stages differs. Stage (m groups, distance t = d / 2m) takes
-// the pair (e, e + t) of group i = e / 2t with twiddle W[m + i]. Pass P
-// (P = 0, 1, 2) runs the stages m = 16^P * 2^s (s = 0..3) on the 16
-// coefficients e_k = 2 g t0 + o + k t0 / 8 of one thread, t0 = d / (2 * 16^P),
-// g = the thread's group, o = its offset:
-//   P = 0: e_k = tid + 256 k         (g = 0,        o = tid)
-//   P = 1: e_k = 256 g + o + 16 k    (g = tid / 16, o = tid % 16)
-//   P = 2: e_k = 16 tid + k          (g = tid,      o = 0)
-// Within a pass, stage s pairs k with k + 8 / 2^s and takes the twiddle
-// W[16^P 2^s + g 2^s + (k >> (4 - s))].
+// grouping of the stages differs. Stage j (m = 2^j groups, distance
+// t = d / 2m) takes the pair (e, e + t) of group i = e / 2t with twiddle
+// W[m + i]. A pass is a window of four stages sp .. sp + 3, of which the
+// first `skip` are left out: (0, 0), (4, 0), (8, 0), ... and, when LOGD is
+// not a multiple of 4, a last window (LOGD - 4, 4 - LOGD % 4). With
+// m0 = 2^sp and t0 = d / (2 m0), a thread holds the 16 coefficients
+// e_k = 2 g t0 + o + k t0 / 8 of group g = tid / (t0 / 8) and offset
+// o = tid % (t0 / 8). The first pass reads e_k = tid + (d / 16) k (natural
+// order, coalesced), the last one e_k = 16 tid + k. Stage s of a window
+// pairs k with k + 8 / 2^s and takes W[m0 2^s + g 2^s + (k >> (4 - s))].
 //
 // Twiddles are read from a permuted copy of the tables (built on the host):
-// pass P, stage s, sub-block x, group g at 16^P - 1 + 16^P (2^s - 1) + x 16^P
-// + g, so the 32 threads of a warp read consecutive words (pass 2), two
-// words (pass 1) or one word (pass 0).
+// window w, stage s, sub-block x, group g at base_w + m0 (2^s - 2^skip) +
+// x m0 + g, so the threads of a warp read one word, a few words or
+// consecutive words.
 //
-// Shared memory holds coefficient e at e ^ swz(e >> 5), swz(r) = (r & 15) |
-// ((r >> 3) & 1) << 4, which keeps all three access patterns free of bank
-// conflicts (pass 0 reads whole rows; pass 1 two half rows 8 rows apart;
-// pass 2 two coefficients of each of 16 consecutive rows).
+// Shared memory holds coefficient e at e ^ swz(e >> 5), with a swz per size
+// that keeps every pass's access pattern free of bank conflicts (the
+// patterns and the swz were checked exhaustively on the host).
 #pragma once
 #include <cstdint>
 
@@ -32,42 +31,69 @@
 
 namespace inspire {
 
-constexpr int kNtt16LogD = 12;
-constexpr int kNtt16D = 1 << kNtt16LogD;
-constexpr int kNtt16Threads = 256;
+constexpr int kNtt16MinLogD = 11;
+constexpr int kNtt16MaxLogD = 13;
 
-// Position of twiddle W[m + g] (stage with m = 16^P 2^s groups) in the
-// permuted table. Host and device.
-__host__ __device__ __forceinline__ int ntt16_twiddle_slot(int pass, int s, int x,
-                                                           int g) {
-  const int m0 = 1 << (4 * pass);
-  return m0 - 1 + m0 * ((1 << s) - 1) + x * m0 + g;
-}
+template <int LOGD>
+struct Ntt16 {
+  static_assert(LOGD >= kNtt16MinLogD && LOGD <= kNtt16MaxLogD, "ring degree");
+  static constexpr int kD = 1 << LOGD;
+  static constexpr int kThreads = kD / 16;
+  static constexpr int kPasses = (LOGD + 3) / 4;
+  __host__ __device__ static constexpr int Start(int w) {
+    return (w < kPasses - 1 || LOGD % 4 == 0) ? 4 * w : LOGD - 4;
+  }
+  __host__ __device__ static constexpr int Skip(int w) {
+    return (w == kPasses - 1 && LOGD % 4 != 0) ? 4 - LOGD % 4 : 0;
+  }
+  // First slot of window w: the full windows before it hold 15 m0 each.
+  __host__ __device__ static constexpr int Base(int w) {
+    int b = 0;
+    for (int i = 0; i < w; ++i) b += 15 << (4 * i);
+    return b;
+  }
+  // Slot of W[m0 2^s + g 2^s + x] (window w, stage s) in the permuted table.
+  __host__ __device__ static constexpr int Slot(int w, int s, int x, int g) {
+    return Base(w) + (1 << Start(w)) * ((1 << s) - (1 << Skip(w))) +
+           x * (1 << Start(w)) + g;
+  }
+};
 
 #ifdef __CUDACC__
+template <int LOGD>
 __device__ __forceinline__ int ntt16_pos(int e) {
   const int r = e >> 5;
-  return e ^ ((r & 15) | (((r >> 3) & 1) << 4));
+  if constexpr (LOGD == 11) {
+    return e ^ ((r & 7) | ((((r >> 3) ^ (r >> 2)) & 1) << 3) | (((r >> 3) & 1) << 4));
+  } else if constexpr (LOGD == 12) {
+    return e ^ ((r & 15) | (((r >> 3) & 1) << 4));
+  } else {
+    return e ^ ((r & 15) ^ ((r & 15) << 1));
+  }
 }
 
-__device__ __forceinline__ int ntt16_elem(int pass, int tid, int k) {
-  return pass == 0 ? tid + 256 * k
-                   : (pass == 1 ? 256 * (tid >> 4) + (tid & 15) + 16 * k : 16 * tid + k);
+// Geometry of window w for thread tid: coefficient e_k = base + stride * k,
+// group g.
+template <int LOGD>
+__device__ __forceinline__ void ntt16_geometry(int w, int tid, int& base, int& stride,
+                                               int& g) {
+  const int m0 = 1 << Ntt16<LOGD>::Start(w);
+  const int t0 = Ntt16<LOGD>::kD / (2 * m0);
+  stride = t0 / 8;
+  g = tid / stride;
+  base = 2 * g * t0 + tid % stride;
 }
 
-// Barrier of the 256 threads running one transform: the whole block
-// (bar == 0) or named barrier `bar` when several groups of 256 threads run
-// transforms of their own.
+// Barrier of the threads running one transform: the whole block (bar == 0)
+// or named barrier `bar` when several groups of threads run transforms of
+// their own.
+template <int LOGD>
 __device__ __forceinline__ void ntt16_sync(int bar) {
   if (bar == 0) {
     __syncthreads();
   } else {
-    asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(kNtt16Threads) : "memory");
+    asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(Ntt16<LOGD>::kThreads) : "memory");
   }
-}
-
-__device__ __forceinline__ int ntt16_group(int pass, int tid) {
-  return pass == 0 ? 0 : (pass == 1 ? tid >> 4 : tid);
 }
 
 // A twiddle word: read-only global memory (kSmem = false) or a copy of the
@@ -81,154 +107,29 @@ __device__ __forceinline__ uint32_t ntt16_tw(const uint32_t* t, int i) {
   }
 }
 
-// Four forward stages of pass P on the thread's 16 coefficients.
-// tw = permuted W, tws = its Shoup constants.
-template <int P, bool kSmem = false>
-__device__ __forceinline__ void ntt16_fwd_pass(uint32_t (&x)[16],
-                                               const uint32_t* __restrict__ tw,
-                                               const uint32_t* __restrict__ tws,
-                                               uint32_t p, int tid) {
-  const int g = ntt16_group(P, tid);
-#pragma unroll
-  for (int s = 0; s < 4; ++s) {
-    const int half = 8 >> s;
-    uint32_t w[8], ws[8];
-#pragma unroll
-    for (int b = 0; b < (1 << s); ++b) {
-      const int slot = ntt16_twiddle_slot(P, s, b, g);
-      w[b] = ntt16_tw<kSmem>(tw, slot);
-      ws[b] = ntt16_tw<kSmem>(tws, slot);
-    }
-#pragma unroll
-    for (int b = 0; b < (1 << s); ++b) {
-#pragma unroll
-      for (int i = 0; i < half; ++i) {
-        const int k = b * 2 * half + i;
-        const uint32_t v = shoup_mul(x[k + half], w[b], ws[b], p);
-        x[k + half] = sub_mod(x[k], v, p);
-        x[k] = add_mod(x[k], v, p);
-      }
-    }
-  }
-}
-
-// Four inverse stages of pass P (stage s = 3 down to 0).
-template <int P, bool kSmem = false>
-__device__ __forceinline__ void ntt16_inv_pass(uint32_t (&x)[16],
-                                               const uint32_t* __restrict__ itw,
-                                               const uint32_t* __restrict__ itws,
-                                               uint32_t p, int tid) {
-  const int g = ntt16_group(P, tid);
-#pragma unroll
-  for (int s = 3; s >= 0; --s) {
-    const int half = 8 >> s;
-    uint32_t w[8], ws[8];
-#pragma unroll
-    for (int b = 0; b < (1 << s); ++b) {
-      const int slot = ntt16_twiddle_slot(P, s, b, g);
-      w[b] = ntt16_tw<kSmem>(itw, slot);
-      ws[b] = ntt16_tw<kSmem>(itws, slot);
-    }
-#pragma unroll
-    for (int b = 0; b < (1 << s); ++b) {
-#pragma unroll
-      for (int i = 0; i < half; ++i) {
-        const int k = b * 2 * half + i;
-        const uint32_t u = x[k], v = x[k + half];
-        x[k] = add_mod(u, v, p);
-        x[k + half] = shoup_mul(sub_mod(u, v, p), w[b], ws[b], p);
-      }
-    }
-  }
-}
-
-template <int P>
-__device__ __forceinline__ void ntt16_store(const uint32_t (&x)[16], uint32_t* xs,
-                                            int tid) {
-#pragma unroll
-  for (int k = 0; k < 16; ++k) xs[ntt16_pos(ntt16_elem(P, tid, k))] = x[k];
-}
-
-template <int P>
-__device__ __forceinline__ void ntt16_load(uint32_t (&x)[16], const uint32_t* xs,
-                                           int tid) {
-#pragma unroll
-  for (int k = 0; k < 16; ++k) x[k] = xs[ntt16_pos(ntt16_elem(P, tid, k))];
-}
-
-// Forward transform. In: x[k] = coefficient tid + 256 k. Out: x[k] = NTT
-// slot 16 tid + k (the bit-reversed output array of ntt_forward). `xs` is a
-// 4096-word shared buffer, free again when this returns. tab16 = the
-// prime's permuted tables [W | W shoup | IW | IW shoup], 4096 words each.
-// tid in [0, 256) within the group that synchronises on `bar`. kSmem: the
-// tables were copied to shared memory (tab16 points there).
-template <bool kSmem = false>
-__device__ __forceinline__ void ntt16_forward(uint32_t (&x)[16], uint32_t* xs,
-                                              const uint32_t* __restrict__ tab16,
-                                              uint32_t p, int tid, int bar = 0) {
-  const uint32_t* tw = tab16;
-  const uint32_t* tws = tab16 + kNtt16D;
-  ntt16_fwd_pass<0, kSmem>(x, tw, tws, p, tid);
-  ntt16_store<0>(x, xs, tid);
-  ntt16_sync(bar);
-  ntt16_load<1>(x, xs, tid);
-  ntt16_fwd_pass<1, kSmem>(x, tw, tws, p, tid);
-  ntt16_store<1>(x, xs, tid);  // the same words this thread read
-  ntt16_sync(bar);
-  ntt16_load<2>(x, xs, tid);
-  ntt16_fwd_pass<2, kSmem>(x, tw, tws, p, tid);
-  ntt16_sync(bar);
-}
-
-// Inverse transform without the 1/d scaling. In: x[k] = slot 16 tid + k.
-// Out: x[k] = coefficient tid + 256 k. itw / itws: the permuted inverse
-// twiddles and their Shoup constants.
-template <bool kSmem = false>
-__device__ __forceinline__ void ntt16_inverse_tw(uint32_t (&x)[16], uint32_t* xs,
-                                                 const uint32_t* __restrict__ itw,
-                                                 const uint32_t* __restrict__ itws,
-                                                 uint32_t p, int tid, int bar = 0) {
-  ntt16_inv_pass<2, kSmem>(x, itw, itws, p, tid);
-  ntt16_store<2>(x, xs, tid);
-  ntt16_sync(bar);
-  ntt16_load<1>(x, xs, tid);
-  ntt16_inv_pass<1, kSmem>(x, itw, itws, p, tid);
-  ntt16_store<1>(x, xs, tid);
-  ntt16_sync(bar);
-  ntt16_load<0>(x, xs, tid);
-  ntt16_inv_pass<0, kSmem>(x, itw, itws, p, tid);
-  ntt16_sync(bar);
-}
-
-// Compact forms: one pass body serves all three passes, the pass index a
-// run-time value (coefficients e_k = base + stride * k, twiddle slots
-// 16^P - 1 + 16^P (2^s - 1 + x) + g). A third of the code of the unrolled
-// transforms, for launches whose blocks each run once per SM, where the
-// fetch of the unrolled code, not the arithmetic, sets the time.
-__device__ __forceinline__ void ntt16_pass_geometry(int pass, int tid, int& base,
-                                                    int& stride, int& g) {
-  base = pass == 0 ? tid : (pass == 1 ? 256 * (tid >> 4) + (tid & 15) : 16 * tid);
-  stride = pass == 0 ? 256 : (pass == 1 ? 16 : 1);
-  g = pass == 0 ? 0 : (pass == 1 ? tid >> 4 : tid);
-}
-
-template <bool kSmem, bool kInverse>
-__device__ __forceinline__ void ntt16_pass_rt(uint32_t (&x)[16],
-                                              const uint32_t* __restrict__ tw,
-                                              const uint32_t* __restrict__ tws,
-                                              uint32_t p, int pass, int g) {
-  const int m0 = 1 << (4 * pass);
-  const int base = m0 - 1 + g;
+// The stages of window w on the thread's 16 coefficients, forward (Cooley-
+// Tukey, stages skip .. 3) or inverse (Gentleman-Sande, 3 .. skip). With a
+// compile-time window every index folds; the compact transforms pass a
+// run-time one and the same instructions serve every window.
+template <int LOGD, bool kSmem, bool kInverse>
+__device__ __forceinline__ void ntt16_window(uint32_t (&x)[16],
+                                             const uint32_t* __restrict__ tw,
+                                             const uint32_t* __restrict__ tws,
+                                             uint32_t p, int w, int g) {
+  const int m0 = 1 << Ntt16<LOGD>::Start(w);
+  const int skip = Ntt16<LOGD>::Skip(w);
+  const int base = Ntt16<LOGD>::Base(w) + g - m0 * (1 << skip);
 #pragma unroll
   for (int si = 0; si < 4; ++si) {
     const int s = kInverse ? 3 - si : si;
+    if (s < skip) continue;
     const int half = 8 >> s;
-    uint32_t w[8], ws[8];
+    uint32_t wv[8], wsv[8];
 #pragma unroll
     for (int b = 0; b < (1 << s); ++b) {
-      const int slot = base + m0 * ((1 << s) - 1 + b);
-      w[b] = ntt16_tw<kSmem>(tw, slot);
-      ws[b] = ntt16_tw<kSmem>(tws, slot);
+      const int slot = base + m0 * ((1 << s) + b);
+      wv[b] = ntt16_tw<kSmem>(tw, slot);
+      wsv[b] = ntt16_tw<kSmem>(tws, slot);
     }
 #pragma unroll
     for (int b = 0; b < (1 << s); ++b) {
@@ -238,9 +139,9 @@ __device__ __forceinline__ void ntt16_pass_rt(uint32_t (&x)[16],
         if (kInverse) {
           const uint32_t u = x[k], v = x[k + half];
           x[k] = add_mod(u, v, p);
-          x[k + half] = shoup_mul(sub_mod(u, v, p), w[b], ws[b], p);
+          x[k + half] = shoup_mul(sub_mod(u, v, p), wv[b], wsv[b], p);
         } else {
-          const uint32_t v = shoup_mul(x[k + half], w[b], ws[b], p);
+          const uint32_t v = shoup_mul(x[k + half], wv[b], wsv[b], p);
           x[k + half] = sub_mod(x[k], v, p);
           x[k] = add_mod(x[k], v, p);
         }
@@ -249,56 +150,116 @@ __device__ __forceinline__ void ntt16_pass_rt(uint32_t (&x)[16],
   }
 }
 
-template <bool kSmem = false>
-__device__ __forceinline__ void ntt16_forward_compact(uint32_t (&x)[16], uint32_t* xs,
-                                                      const uint32_t* __restrict__ tab16,
-                                                      uint32_t p, int tid, int bar = 0) {
+template <int LOGD>
+__device__ __forceinline__ void ntt16_store(const uint32_t (&x)[16], uint32_t* xs, int w,
+                                            int tid) {
+  int base, stride, g;
+  ntt16_geometry<LOGD>(w, tid, base, stride, g);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) xs[ntt16_pos<LOGD>(base + stride * k)] = x[k];
+}
+
+template <int LOGD>
+__device__ __forceinline__ void ntt16_load(uint32_t (&x)[16], const uint32_t* xs, int w,
+                                           int tid) {
+  int base, stride, g;
+  ntt16_geometry<LOGD>(w, tid, base, stride, g);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) x[k] = xs[ntt16_pos<LOGD>(base + stride * k)];
+}
+
+// Forward transform. In: x[k] = coefficient tid + (d / 16) k. Out: x[k] =
+// NTT slot 16 tid + k (the bit-reversed output array of ntt_forward). `xs`
+// is a d-word shared buffer, free again when this returns. tab16 = the
+// prime's permuted tables [W | W shoup | IW | IW shoup], d words each. tid
+// in [0, d / 16) within the group that synchronises on `bar`. kSmem: the
+// tables were copied to shared memory (tab16 points there). kCompact: one
+// window body for all windows (a third of the code, for launches whose
+// blocks each run once per SM, where fetching unrolled code sets the time).
+template <int LOGD, bool kSmem = false, bool kCompact = false>
+__device__ __forceinline__ void ntt16_forward(uint32_t (&x)[16], uint32_t* xs,
+                                              const uint32_t* __restrict__ tab16,
+                                              uint32_t p, int tid, int bar = 0) {
+  using N = Ntt16<LOGD>;
+  const uint32_t* tw = tab16;
+  const uint32_t* tws = tab16 + N::kD;
+  if constexpr (kCompact) {
 #pragma unroll 1
-  for (int pass = 0; pass < 3; ++pass) {
-    int base, stride, g;
-    ntt16_pass_geometry(pass, tid, base, stride, g);
-    if (pass > 0) {
-#pragma unroll
-      for (int k = 0; k < 16; ++k) x[k] = xs[ntt16_pos(base + stride * k)];
+    for (int w = 0; w < N::kPasses; ++w) {
+      int base, stride, g;
+      ntt16_geometry<LOGD>(w, tid, base, stride, g);
+      if (w > 0) ntt16_load<LOGD>(x, xs, w, tid);
+      ntt16_window<LOGD, kSmem, false>(x, tw, tws, p, w, g);
+      if (w < N::kPasses - 1) ntt16_store<LOGD>(x, xs, w, tid);
+      ntt16_sync<LOGD>(bar);
     }
-    ntt16_pass_rt<kSmem, false>(x, tab16, tab16 + kNtt16D, p, pass, g);
-    if (pass < 2) {
+  } else {
 #pragma unroll
-      for (int k = 0; k < 16; ++k) xs[ntt16_pos(base + stride * k)] = x[k];
+    for (int w = 0; w < N::kPasses; ++w) {
+      int base, stride, g;
+      ntt16_geometry<LOGD>(w, tid, base, stride, g);
+      if (w > 0) ntt16_load<LOGD>(x, xs, w, tid);
+      ntt16_window<LOGD, kSmem, false>(x, tw, tws, p, w, g);
+      // The store goes to the words this thread read (no barrier between).
+      if (w < N::kPasses - 1) ntt16_store<LOGD>(x, xs, w, tid);
+      ntt16_sync<LOGD>(bar);
     }
-    ntt16_sync(bar);
   }
 }
 
-template <bool kSmem = false>
-__device__ __forceinline__ void ntt16_inverse_compact(uint32_t (&x)[16], uint32_t* xs,
-                                                      const uint32_t* __restrict__ itw,
-                                                      const uint32_t* __restrict__ itws,
-                                                      uint32_t p, int tid, int bar = 0) {
+// Inverse transform without the 1/d scaling. In: x[k] = slot 16 tid + k.
+// Out: x[k] = coefficient tid + (d / 16) k. itw / itws: the permuted
+// inverse twiddles and their Shoup constants.
+template <int LOGD, bool kSmem = false, bool kCompact = false>
+__device__ __forceinline__ void ntt16_inverse_tw(uint32_t (&x)[16], uint32_t* xs,
+                                                 const uint32_t* __restrict__ itw,
+                                                 const uint32_t* __restrict__ itws,
+                                                 uint32_t p, int tid, int bar = 0) {
+  using N = Ntt16<LOGD>;
+  if constexpr (kCompact) {
 #pragma unroll 1
-  for (int i = 0; i < 3; ++i) {
-    const int pass = 2 - i;
-    int base, stride, g;
-    ntt16_pass_geometry(pass, tid, base, stride, g);
-    if (i > 0) {
-#pragma unroll
-      for (int k = 0; k < 16; ++k) x[k] = xs[ntt16_pos(base + stride * k)];
+    for (int w = N::kPasses - 1; w >= 0; --w) {
+      int base, stride, g;
+      ntt16_geometry<LOGD>(w, tid, base, stride, g);
+      if (w < N::kPasses - 1) ntt16_load<LOGD>(x, xs, w, tid);
+      ntt16_window<LOGD, kSmem, true>(x, itw, itws, p, w, g);
+      if (w > 0) ntt16_store<LOGD>(x, xs, w, tid);
+      ntt16_sync<LOGD>(bar);
     }
-    ntt16_pass_rt<kSmem, true>(x, itw, itws, p, pass, g);
-    if (i < 2) {
+  } else {
 #pragma unroll
-      for (int k = 0; k < 16; ++k) xs[ntt16_pos(base + stride * k)] = x[k];
+    for (int w = N::kPasses - 1; w >= 0; --w) {
+      int base, stride, g;
+      ntt16_geometry<LOGD>(w, tid, base, stride, g);
+      if (w < N::kPasses - 1) ntt16_load<LOGD>(x, xs, w, tid);
+      ntt16_window<LOGD, kSmem, true>(x, itw, itws, p, w, g);
+      if (w > 0) ntt16_store<LOGD>(x, xs, w, tid);
+      ntt16_sync<LOGD>(bar);
     }
-    ntt16_sync(bar);
   }
 }
 
 // The inverse with the prime's whole table block [W | W shoup | IW | IW shoup].
-template <bool kSmem = false>
+template <int LOGD, bool kSmem = false, bool kCompact = false>
 __device__ __forceinline__ void ntt16_inverse(uint32_t (&x)[16], uint32_t* xs,
                                               const uint32_t* __restrict__ tab16,
                                               uint32_t p, int tid, int bar = 0) {
-  ntt16_inverse_tw<kSmem>(x, xs, tab16 + 2 * kNtt16D, tab16 + 3 * kNtt16D, p, tid, bar);
+  ntt16_inverse_tw<LOGD, kSmem, kCompact>(x, xs, tab16 + 2 * Ntt16<LOGD>::kD,
+                                          tab16 + 3 * Ntt16<LOGD>::kD, p, tid, bar);
+}
+
+// The slot layout the forward transform leaves (x[k] = slot 16 tid + k) in
+// and out of the d-word buffer `xs`, conflict-free.
+template <int LOGD>
+__device__ __forceinline__ void ntt16_store_slots(const uint32_t (&x)[16], uint32_t* xs,
+                                                  int tid) {
+  ntt16_store<LOGD>(x, xs, Ntt16<LOGD>::kPasses - 1, tid);
+}
+
+template <int LOGD>
+__device__ __forceinline__ void ntt16_load_slots(uint32_t (&x)[16], const uint32_t* xs,
+                                                 int tid) {
+  ntt16_load<LOGD>(x, xs, Ntt16<LOGD>::kPasses - 1, tid);
 }
 #endif
 

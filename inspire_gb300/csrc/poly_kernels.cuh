@@ -104,29 +104,30 @@ ntt_coeffs_kernel(const T* __restrict__ src, int64_t src_qstride,
   for (int j = threadIdx.x; j < d; j += blockDim.x) out[j] = smem[j];
 }
 
-// ntt_coeffs_kernel for d = 4096 with the radix-16 transform of ntt16.cuh,
+// ntt_coeffs_kernel for d = 2^LOGD with the radix-16 transform of ntt16.cuh,
 // one block per polynomial over all primes (the input is read once).
-// grid = (npoly, batch), 256 threads, needs c.tables16.
-template <typename T>
-__global__ void __launch_bounds__(kNtt16Threads, 2)
+// grid = (npoly, batch), d / 16 threads, needs c.tables16.
+template <typename T, int LOGD>
+__global__ void __launch_bounds__(Ntt16<LOGD>::kThreads, 512 / Ntt16<LOGD>::kThreads)
 ntt_coeffs16_kernel(const T* __restrict__ src, int64_t src_qstride,
                     int64_t src_off, int npoly, T mask, uint32_t* __restrict__ dst,
                     int64_t poly_stride, NttCtx c) {
-  __shared__ uint32_t xs[kNtt16D];
-  constexpr int d = kNtt16D;
+  constexpr int d = Ntt16<LOGD>::kD;
+  constexpr int NT = Ntt16<LOGD>::kThreads;
+  __shared__ uint32_t xs[d];
   const int tid = threadIdx.x;
   const int poly = blockIdx.x;
   const int q = blockIdx.y;
   const T* in = src + q * src_qstride + src_off + poly * poly_stride;
   T v[16];
 #pragma unroll
-  for (int k = 0; k < 16; ++k) v[k] = in[tid + 256 * k] & mask;
+  for (int k = 0; k < 16; ++k) v[k] = in[tid + NT * k] & mask;
   for (int pi = 0; pi < c.r; ++pi) {
     const uint32_t p = c.p[pi];
     uint32_t x[16];
 #pragma unroll
     for (int k = 0; k < 16; ++k) x[k] = to_residue<T>(v[k], p);
-    ntt16_forward(x, xs, c.tables16 + static_cast<size_t>(pi) * 4 * d, p, tid);
+    ntt16_forward<LOGD>(x, xs, c.tables16 + static_cast<size_t>(pi) * 4 * d, p, tid);
     uint4* out = reinterpret_cast<uint4*>(
         dst + ((static_cast<int64_t>(q) * npoly + poly) * c.r + pi) * d + 16 * tid);
 #pragma unroll
@@ -239,20 +240,21 @@ finalize_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ Yh
   }
 }
 
-// finalize_kernel for d = 4096 with the radix-16 inverse of ntt16.cuh: the
+// finalize_kernel for d = 2^LOGD with the radix-16 inverse of ntt16.cuh: the
 // products are taken in the slot layout the inverse starts from (16
 // consecutive slots per thread, 16-byte loads), each prime's scaled result is
 // kept in shared memory at the positions its thread reads back for the CRT.
-// grid = (l * t, batch), 256 threads, (1 + r) * d words of shared memory,
+// grid = (l * t, batch), d / 16 threads, (1 + r) * d words of shared memory,
 // needs c.tables16.
-template <typename T>
-__global__ void __launch_bounds__(kNtt16Threads, 2)
+template <typename T, int LOGD>
+__global__ void __launch_bounds__(Ntt16<LOGD>::kThreads, 512 / Ntt16<LOGD>::kThreads)
 finalize16_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ Yh,
                   int k, const T* __restrict__ gemv, const T* __restrict__ gemv2,
                   int64_t gemv_qstride, T* __restrict__ packed_b, int log_q,
                   NttCtx c) {
   extern __shared__ uint32_t smem[];  // exchange buffer, then [r][d] results
-  constexpr int d = kNtt16D;
+  constexpr int d = Ntt16<LOGD>::kD;
+  constexpr int NT = Ntt16<LOGD>::kThreads;
   uint32_t* xs = smem;
   uint32_t* res = smem + d;
   const int tid = threadIdx.x;
@@ -278,16 +280,16 @@ finalize16_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ 
         acc[4 * w + 3] = add_mod(acc[4 * w + 3], mont_mul(a.w, b.w, p, pinv), p);
       }
     }
-    ntt16_inverse(acc, xs, c.tables16 + static_cast<size_t>(pi) * 4 * d, p, tid);
+    ntt16_inverse<LOGD>(acc, xs, c.tables16 + static_cast<size_t>(pi) * 4 * d, p, tid);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      res[pi * d + tid + 256 * j] = shoup_mul(acc[j], c.scale[pi], c.scale_s[pi], p);
+      res[pi * d + tid + NT * j] = shoup_mul(acc[j], c.scale[pi], c.scale_s[pi], p);
     }
   }
   const int64_t base = q * gemv_qstride + static_cast<int64_t>(s) * d;
   T* outp = packed_b + (static_cast<int64_t>(q) * gridDim.x + s) * d;
   for (int jj = 0; jj < 16; ++jj) {
-    const int j = tid + 256 * jj;
+    const int j = tid + NT * jj;
     uint32_t x[kMaxPrimes] = {0, 0, 0, 0, 0};
 #pragma unroll
     for (int pi = 0; pi < kMaxPrimes; ++pi) {
@@ -300,24 +302,25 @@ finalize16_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ 
   }
 }
 
-// finalize16_kernel for launches with fewer blocks than SMs: 512 threads in
-// two groups of 256, group g taking primes g, g + 2, ... side by side, each
+// finalize16_kernel for launches with fewer blocks than SMs: d / 8 threads
+// in two groups of d / 16, group g taking primes g, g + 2, ... side by side, each
 // with its prime's inverse tables copied to shared memory and the compact
 // inverse (a block runs once per SM: global twiddle reads would each wait on
 // L2 and the unrolled code on instruction fetch); then the whole block does
 // the CRT. grid = (l * t, batch), shared memory (2 + 4 + r) * d words, needs
 // c.tables16.
-template <typename T>
-__global__ void __launch_bounds__(2 * kNtt16Threads, 1)
+template <typename T, int LOGD>
+__global__ void __launch_bounds__(2 * Ntt16<LOGD>::kThreads, 1)
 finalize16_pair_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ Yh,
                        int k, const T* __restrict__ gemv, const T* __restrict__ gemv2,
                        int64_t gemv_qstride, T* __restrict__ packed_b, int log_q,
                        NttCtx c) {
   extern __shared__ uint32_t smem[];
-  constexpr int d = kNtt16D;
+  constexpr int d = Ntt16<LOGD>::kD;
+  constexpr int NT = Ntt16<LOGD>::kThreads;
   const int tid = threadIdx.x;
-  const int grp = tid >> 8;
-  const int lt = tid & (kNtt16Threads - 1);
+  const int grp = tid / NT;
+  const int lt = tid & (NT - 1);
   const int bar = 1 + grp;
   uint32_t* xs = smem + grp * d;
   uint32_t* itab = smem + 2 * d + grp * 2 * d;  // IW | IW shoup of the prime
@@ -331,8 +334,8 @@ finalize16_pair_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restri
         c.tables16 + static_cast<size_t>(pi) * 4 * d + 2 * d);
     uint4* s16 = reinterpret_cast<uint4*>(itab);
 #pragma unroll
-    for (int i = 0; i < 2 * d / 4 / kNtt16Threads; ++i) {
-      s16[lt + i * kNtt16Threads] = __ldg(g16 + lt + i * kNtt16Threads);
+    for (int i = 0; i < 2 * d / 4 / NT; ++i) {
+      s16[lt + i * NT] = __ldg(g16 + lt + i * NT);
     }
     uint32_t acc[16];
 #pragma unroll
@@ -351,18 +354,18 @@ finalize16_pair_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restri
         acc[4 * w + 3] = add_mod(acc[4 * w + 3], mont_mul(a.w, b.w, p, pinv), p);
       }
     }
-    ntt16_sync(bar);  // the group's copy of the tables is complete
-    ntt16_inverse_compact<true>(acc, xs, itab, itab + d, p, lt, bar);
+    ntt16_sync<LOGD>(bar);  // the group's copy of the tables is complete
+    ntt16_inverse_tw<LOGD, true, true>(acc, xs, itab, itab + d, p, lt, bar);
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      res[pi * d + lt + 256 * j] = shoup_mul(acc[j], c.scale[pi], c.scale_s[pi], p);
+      res[pi * d + lt + NT * j] = shoup_mul(acc[j], c.scale[pi], c.scale_s[pi], p);
     }
   }
   __syncthreads();
   const int64_t base = q * gemv_qstride + static_cast<int64_t>(s) * d;
   T* outp = packed_b + (static_cast<int64_t>(q) * gridDim.x + s) * d;
 #pragma unroll 4
-  for (int j = tid; j < d; j += 2 * kNtt16Threads) {
+  for (int j = tid; j < d; j += 2 * NT) {
     uint32_t x[kMaxPrimes] = {0, 0, 0, 0, 0};
 #pragma unroll
     for (int pi = 0; pi < kMaxPrimes; ++pi) {
@@ -581,16 +584,16 @@ ext_step_kernel(bool first, const uint32_t* __restrict__ resid_in,
   }
 }
 
-// The external product of ext_step_kernel for d = 4096, one block per
+// The external product of ext_step_kernel for d = 2^LOGD, one block per
 // (shard, request) over all primes: the Horner state is reconstructed once
 // (not once per prime), every NTT runs in registers with the radix-16
 // passes of ntt16.cuh, the RGSW products are taken in the layout the forward
 // transform leaves (16 consecutive slots per thread, 16-byte loads) and the
 // inverse starts from the accumulators without a trip through shared
-// memory. Same residues as ext_step_kernel. grid = (l, batch), 256 threads,
+// memory. Same residues as ext_step_kernel. grid = (l, batch), d / 16 threads,
 // needs c.tables16.
-template <typename T>
-__global__ void __launch_bounds__(kNtt16Threads, 2)
+template <typename T, int LOGD>
+__global__ void __launch_bounds__(Ntt16<LOGD>::kThreads, 512 / Ntt16<LOGD>::kThreads)
 ext_step16_kernel(bool first, const uint32_t* __restrict__ resid_in,
                   uint32_t* __restrict__ resid_out,
                   const T* __restrict__ coeff_a, int64_t coeff_a_q_stride,
@@ -600,7 +603,8 @@ ext_step16_kernel(bool first, const uint32_t* __restrict__ resid_in,
                   const uint32_t* __restrict__ RGSWa, int64_t rgswa_qstride,
                   const uint32_t* __restrict__ RGSWb, ExtArgs e, NttCtx c) {
   extern __shared__ uint32_t smem[];
-  constexpr int d = kNtt16D;
+  constexpr int d = Ntt16<LOGD>::kD;
+  constexpr int NT = Ntt16<LOGD>::kThreads;
   uint32_t* xs = smem;                           // exchange buffer
   T* sa = reinterpret_cast<T*>(smem + d);        // LowBits of the state
   T* sb = sa + d;
@@ -611,7 +615,7 @@ ext_step16_kernel(bool first, const uint32_t* __restrict__ resid_in,
   const T* ca = coeff_a + q * coeff_a_q_stride + shard * coeff_a_shard_stride;
   const T* cb = coeff_b + q * coeff_b_q_stride + shard * coeff_b_shard_stride;
   const int64_t rbase = (static_cast<int64_t>(q) * l + shard) * c.r * 2 * d;
-  for (int j = tid; j < d; j += kNtt16Threads) {
+  for (int j = tid; j < d; j += NT) {
     T ra, rb;
     horner_state<T>(first, resid_in, rbase, d, j, ca, cb, c, ra, rb);
     sa[j] = low_bits<T>(ra, e.log_q);
@@ -633,11 +637,11 @@ ext_step16_kernel(bool first, const uint32_t* __restrict__ resid_in,
       uint32_t x[16];
 #pragma unroll
       for (int k = 0; k < 16; ++k) {
-        const T dig = gadget_digit<T>(src[tid + 256 * k], e.log_q, e.log_digit,
+        const T dig = gadget_digit<T>(src[tid + NT * k], e.log_q, e.log_digit,
                                       e.num_digits, dg);
         x[k] = to_residue<T>(dig & static_cast<T>(e.umask), p);
       }
-      ntt16_forward(x, xs, tab16, p, tid);
+      ntt16_forward<LOGD, false, LOGD != 12>(x, xs, tab16, p, tid);
       const uint4* wa = reinterpret_cast<const uint4*>(
           RGSWa + q * rgswa_qstride + (static_cast<int64_t>(g) * c.r + pi) * d + 16 * tid);
       const uint4* wb = reinterpret_cast<const uint4*>(
@@ -656,30 +660,31 @@ ext_step16_kernel(bool first, const uint32_t* __restrict__ resid_in,
       }
     }
     uint32_t* out = resid_out + rbase + static_cast<int64_t>(pi) * 2 * d;
-    ntt16_inverse(acc_a, xs, tab16, p, tid);
+    ntt16_inverse<LOGD, false, LOGD != 12>(acc_a, xs, tab16, p, tid);
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-      out[tid + 256 * k] = shoup_mul(acc_a[k], c.scale[pi], c.scale_s[pi], p);
+      out[tid + NT * k] = shoup_mul(acc_a[k], c.scale[pi], c.scale_s[pi], p);
     }
-    ntt16_inverse(acc_b, xs, tab16, p, tid);
+    ntt16_inverse<LOGD, false, LOGD != 12>(acc_b, xs, tab16, p, tid);
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-      out[d + tid + 256 * k] = shoup_mul(acc_b[k], c.scale[pi], c.scale_s[pi], p);
+      out[d + tid + NT * k] = shoup_mul(acc_b[k], c.scale[pi], c.scale_s[pi], p);
     }
   }
 }
 
-// The external product for d = 4096 when a launch has fewer requests than
-// SMs: one block per (prime, shard, request) as ext_step_kernel, 512 threads
-// in two groups of 256 that run the radix-16 transforms side by side. Group 0
-// transforms the live digits of a, group 1 those of b; each keeps its partial
+// The external product for d = 2^LOGD when a launch has fewer requests
+// than SMs: one block per (prime, shard, request) as ext_step_kernel, d / 8
+// threads in two groups of d / 16 that run the radix-16 transforms side by
+// side. Group 0 transforms the live digits of a, group 1 those of b; each
+// keeps its partial
 // product for one output (group 0: a', group 1: b') and hands the other over
 // through shared memory, then group 0 inverts a' and group 1 b'. Each block
 // runs once per SM, so the compact transforms (one pass body for all passes)
 // keep the code small. Same residues as ext_step_kernel.
 // grid = (r, l, batch), needs c.tables16.
-template <typename T>
-__global__ void __launch_bounds__(2 * kNtt16Threads, 1)
+template <typename T, int LOGD>
+__global__ void __launch_bounds__(2 * Ntt16<LOGD>::kThreads, 1)
 ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
                        uint32_t* __restrict__ resid_out,
                        const T* __restrict__ coeff_a, int64_t coeff_a_q_stride,
@@ -689,10 +694,11 @@ ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
                        const uint32_t* __restrict__ RGSWa, int64_t rgswa_qstride,
                        const uint32_t* __restrict__ RGSWb, ExtArgs e, NttCtx c) {
   extern __shared__ uint32_t smem[];
-  constexpr int d = kNtt16D;
+  constexpr int d = Ntt16<LOGD>::kD;
+  constexpr int NT = Ntt16<LOGD>::kThreads;
   const int tid = threadIdx.x;
-  const int grp = tid >> 8;  // 0: digits of a, 1: digits of b
-  const int lt = tid & (kNtt16Threads - 1);
+  const int grp = tid / NT;  // 0: digits of a, 1: digits of b
+  const int lt = tid & (NT - 1);
   const int bar = 1 + grp;
   uint32_t* xs = smem + grp * d;  // this group's exchange buffer
   T* st = reinterpret_cast<T*>(smem + 2 * d);  // LowBits of a, then of b
@@ -705,7 +711,7 @@ ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
   const T* cb = coeff_b + q * coeff_b_q_stride + shard * coeff_b_shard_stride;
   const int64_t rbase = (static_cast<int64_t>(q) * l + shard) * c.r * 2 * d;
 #pragma unroll 2
-  for (int j = tid; j < d; j += 2 * kNtt16Threads) {
+  for (int j = tid; j < d; j += 2 * NT) {
     T ra, rb;
     horner_state<T>(first, resid_in, rbase, d, j, ca, cb, c, ra, rb);
     st[j] = low_bits<T>(ra, e.log_q);
@@ -724,11 +730,11 @@ ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
     uint32_t x[16];
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-      const T dig = gadget_digit<T>(src[lt + 256 * k], e.log_q, e.log_digit,
+      const T dig = gadget_digit<T>(src[lt + NT * k], e.log_q, e.log_digit,
                                     e.num_digits, dg);
       x[k] = to_residue<T>(dig & static_cast<T>(e.umask), p);
     }
-    ntt16_forward_compact(x, xs, tab16, p, lt, bar);
+    ntt16_forward<LOGD, false, true>(x, xs, tab16, p, lt, bar);
     const uint32_t* wa =
         RGSWa + q * rgswa_qstride + (static_cast<int64_t>(g) * c.r + pi) * d + 16 * lt;
     const uint32_t* wb =
@@ -750,17 +756,17 @@ ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
   }
   // Hand over: each group leaves its partial of the other output in its own
   // buffer (free since its last transform) and adds the other group's.
-  ntt16_store<2>(send, xs, lt);
+  ntt16_store_slots<LOGD>(send, xs, lt);
   __syncthreads();
-  ntt16_load<2>(send, smem + (1 - grp) * d, lt);
+  ntt16_load_slots<LOGD>(send, smem + (1 - grp) * d, lt);
 #pragma unroll
   for (int k = 0; k < 16; ++k) keep[k] = add_mod(keep[k], send[k], p);
   __syncthreads();
-  ntt16_inverse_compact(keep, xs, tab16 + 2 * d, tab16 + 3 * d, p, lt, bar);
+  ntt16_inverse<LOGD, false, true>(keep, xs, tab16, p, lt, bar);
   uint32_t* out = resid_out + rbase + static_cast<int64_t>(pi) * 2 * d + grp * d;
 #pragma unroll
   for (int k = 0; k < 16; ++k) {
-    out[lt + 256 * k] = shoup_mul(keep[k], c.scale[pi], c.scale_s[pi], p);
+    out[lt + NT * k] = shoup_mul(keep[k], c.scale[pi], c.scale_s[pi], p);
   }
 }
 

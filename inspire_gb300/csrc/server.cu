@@ -121,6 +121,27 @@ int BitRev(int x, int bits) {
   return r;
 }
 
+// One prime's tables [W | W shoup | IW | IW shoup] in the window order of
+// the radix-16 transforms.
+template <int LOGD>
+void Permute16(const uint32_t* tab, uint32_t* t16) {
+  using N = Ntt16<LOGD>;
+  for (int w = 0; w < N::kPasses; ++w) {
+    const int m0 = 1 << N::Start(w);
+    for (int st = N::Skip(w); st < 4; ++st) {
+      for (int x = 0; x < (1 << st); ++x) {
+        for (int g = 0; g < m0; ++g) {
+          const int slot = N::Slot(w, st, x, g);
+          const int idx = (m0 << st) + (g << st) + x;
+          for (int part = 0; part < 4; ++part) {
+            t16[part * N::kD + slot] = tab[part * N::kD + idx];
+          }
+        }
+      }
+    }
+  }
+}
+
 // Device tables for one ring degree, all primes.
 class NttTables {
  public:
@@ -150,27 +171,20 @@ class NttTables {
         tab[3 * d + i] = Shoup(iw, p);
       }
     }
-    if (logd == kNtt16LogD) {
+    if (logd >= kNtt16MinLogD && logd <= kNtt16MaxLogD) {
       // The radix-16 order of ntt16.cuh, appended after the plain tables:
-      // W[16^P 2^s + g 2^s + x] at ntt16_twiddle_slot(P, s, x, g).
+      // W[m0 2^s + g 2^s + x] of window w at Ntt16<logd>::Slot(w, s, x, g).
       const size_t plain = host.size();
       host.resize(2 * plain, 0);
       for (int pi = 0; pi < kMaxPrimes; ++pi) {
         const uint32_t* tab = host.data() + static_cast<size_t>(pi) * 4 * d;
         uint32_t* t16 = host.data() + plain + static_cast<size_t>(pi) * 4 * d;
-        for (int pass = 0; pass < 3; ++pass) {
-          const int m0 = 1 << (4 * pass);
-          for (int st = 0; st < 4; ++st) {
-            for (int x = 0; x < (1 << st); ++x) {
-              for (int g = 0; g < m0; ++g) {
-                const int slot = ntt16_twiddle_slot(pass, st, x, g);
-                const int idx = (m0 << st) + (g << st) + x;
-                for (int part = 0; part < 4; ++part) {
-                  t16[part * d + slot] = tab[part * d + idx];
-                }
-              }
-            }
-          }
+        if (logd == 11) {
+          Permute16<11>(tab, t16);
+        } else if (logd == 12) {
+          Permute16<12>(tab, t16);
+        } else {
+          Permute16<13>(tab, t16);
         }
       }
       t->has16_ = true;
@@ -467,6 +481,37 @@ PolyLaunch PolyShapeFor(int d, int64_t ctas, int sms) {
   return PolyLaunch{PolyThreads(d), 0};
 }
 
+// Runs the statement with constexpr int LG = log2(d) for the ring degrees of
+// the radix-16 transforms (ntt16.cuh).
+#define INSPIRE_NTT16_DISPATCH(logd, ...) \
+  switch (logd) {                         \
+    case 11: {                            \
+      constexpr int LG = 11;              \
+      __VA_ARGS__;                        \
+    } break;                              \
+    case 12: {                            \
+      constexpr int LG = 12;              \
+      __VA_ARGS__;                        \
+    } break;                              \
+    default: {                            \
+      constexpr int LG = 13;              \
+      __VA_ARGS__;                        \
+    } break;                              \
+  }
+
+// The same for the two-group kernels (d / 8 threads), d <= 4096.
+#define INSPIRE_NTT16_PAIR_DISPATCH(logd, ...) \
+  switch (logd) {                              \
+    case 11: {                                 \
+      constexpr int LG = 11;                   \
+      __VA_ARGS__;                             \
+    } break;                                   \
+    default: {                                 \
+      constexpr int LG = 12;                   \
+      __VA_ARGS__;                             \
+    } break;                                   \
+  }
+
 #define INSPIRE_ITERS_DISPATCH(iters, ...)  \
   switch (iters) {                          \
     case 1: {                               \
@@ -494,10 +539,10 @@ Status NttCoeffs(const inspire_pir_server* s, const T* src, int64_t src_qstride,
                  int64_t src_off, int npoly, T mask, uint32_t* dst,
                  int64_t poly_stride, const NttCtx& c, int batch, cudaStream_t st) {
   const int d = s->d;
-  if (d == kNtt16D && c.tables16 != nullptr &&
-      static_cast<int64_t>(npoly) * batch >= s->sms) {
-    ntt_coeffs16_kernel<T><<<dim3(npoly, batch), kNtt16Threads, 0, st>>>(
-        src, src_qstride, src_off, npoly, mask, dst, poly_stride, c);
+  if (c.tables16 != nullptr && static_cast<int64_t>(npoly) * batch >= s->sms) {
+    INSPIRE_NTT16_DISPATCH(
+        c.logd, ntt_coeffs16_kernel<T, LG><<<dim3(npoly, batch), Ntt16<LG>::kThreads, 0, st>>>(
+                    src, src_qstride, src_off, npoly, mask, dst, poly_stride, c));
     return Cuda(cudaGetLastError(), "forward NTT");
   }
   const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(npoly) * c.r * batch, s->sms);
@@ -520,22 +565,25 @@ Status FinalizeStage(inspire_pir_server* s, Workspace* w, int batch,
                                static_cast<int64_t>(k) * d, k,
                                static_cast<T>(s->vmask_f), w->yh.get<uint32_t>(), d,
                                s->ctx_f, batch, st));
-  if (d == kNtt16D && s->ctx_f.tables16 != nullptr &&
-      static_cast<int64_t>(l) * t * batch >= s->sms) {
+  if (s->ctx_f.tables16 != nullptr && static_cast<int64_t>(l) * t * batch >= s->sms) {
     const NttCtx& c = s->ctx_f;
     const size_t smem = static_cast<size_t>(c.r + 1) * d * 4;
-    RETURN_IF_ERROR(SetSmem(finalize16_kernel<T>, smem));
-    finalize16_kernel<T><<<dim3(l * t, batch), kNtt16Threads, smem, st>>>(
-        s->th_ntt.get<uint32_t>(), w->yh.get<uint32_t>(), k, gemv, nullptr, s->rows,
-        w->packed.get<T>(), log_q, c);
+    INSPIRE_NTT16_DISPATCH(
+        c.logd, RETURN_IF_ERROR(SetSmem(finalize16_kernel<T, LG>, smem));
+        finalize16_kernel<T, LG><<<dim3(l * t, batch), Ntt16<LG>::kThreads, smem, st>>>(
+            s->th_ntt.get<uint32_t>(), w->yh.get<uint32_t>(), k, gemv, nullptr, s->rows,
+            w->packed.get<T>(), log_q, c));
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "finalize"));
-  } else if (d == kNtt16D && s->ctx_f.tables16 != nullptr) {
+  } else if (s->ctx_f.tables16 != nullptr && d <= 4096) {
+    // Two transform groups per block: d / 8 threads.
     const NttCtx& c = s->ctx_f;
     const size_t smem = static_cast<size_t>(6 + c.r) * d * 4;
-    RETURN_IF_ERROR(SetSmem(finalize16_pair_kernel<T>, smem));
-    finalize16_pair_kernel<T><<<dim3(l * t, batch), 2 * kNtt16Threads, smem, st>>>(
-        s->th_ntt.get<uint32_t>(), w->yh.get<uint32_t>(), k, gemv, nullptr, s->rows,
-        w->packed.get<T>(), log_q, c);
+    INSPIRE_NTT16_PAIR_DISPATCH(
+        c.logd, RETURN_IF_ERROR(SetSmem(finalize16_pair_kernel<T, LG>, smem));
+        finalize16_pair_kernel<T, LG><<<dim3(l * t, batch), 2 * Ntt16<LG>::kThreads, smem,
+                                        st>>>(s->th_ntt.get<uint32_t>(), w->yh.get<uint32_t>(),
+                                              k, gemv, nullptr, s->rows, w->packed.get<T>(),
+                                              log_q, c));
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "finalize"));
   } else {
     const NttCtx& c = s->ctx_f;
@@ -574,32 +622,35 @@ Status RunPolyStage(inspire_pir_server* s, Workspace* w, int batch,
     ExtArgs e{log_q, s->prm.eval_log_digit, ne,
               LiveDigits(log_q, s->prm.eval_log_digit, ne), s->umask_e};
     const size_t smem = static_cast<size_t>(d) * 4 + 2ull * d * sizeof(T);
-    if (d == kNtt16D && c.tables16 != nullptr &&
-        static_cast<int64_t>(l) * batch >= s->sms) {
+    if (c.tables16 != nullptr && static_cast<int64_t>(l) * batch >= s->sms) {
       // Enough requests to fill the GPU with one block per (shard, request).
-      RETURN_IF_ERROR(SetSmem(ext_step16_kernel<T>, smem));
-      for (int i = t - 2; i >= 0; --i) {
-        const bool first = i == t - 2;
-        ext_step16_kernel<T><<<dim3(l, batch), kNtt16Threads, smem, st>>>(
-            first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
-            a_tilde + static_cast<int64_t>(i + 1) * d, 0, a_stride,
-            packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
-            s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
-        RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
-      }
-    } else if (d == kNtt16D && c.tables16 != nullptr) {
-      // Few requests: one block per prime, two transforms at a time.
+      INSPIRE_NTT16_DISPATCH(
+          c.logd, RETURN_IF_ERROR(SetSmem(ext_step16_kernel<T, LG>, smem));
+          for (int i = t - 2; i >= 0; --i) {
+            const bool first = i == t - 2;
+            ext_step16_kernel<T, LG><<<dim3(l, batch), Ntt16<LG>::kThreads, smem, st>>>(
+                first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
+                a_tilde + static_cast<int64_t>(i + 1) * d, 0, a_stride,
+                packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
+                s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
+            RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
+          });
+    } else if (c.tables16 != nullptr && d <= 4096) {
+      // Few requests: one block per prime, two transforms at a time (d / 8
+      // threads).
       const size_t smem16 = 2ull * d * 4 + 2ull * d * sizeof(T);
-      RETURN_IF_ERROR(SetSmem(ext_step16_pair_kernel<T>, smem16));
-      for (int i = t - 2; i >= 0; --i) {
-        const bool first = i == t - 2;
-        ext_step16_pair_kernel<T><<<dim3(c.r, l, batch), 2 * kNtt16Threads, smem16, st>>>(
-            first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
-            a_tilde + static_cast<int64_t>(i + 1) * d, 0, a_stride,
-            packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
-            s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
-        RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
-      }
+      INSPIRE_NTT16_PAIR_DISPATCH(
+          c.logd, RETURN_IF_ERROR(SetSmem(ext_step16_pair_kernel<T, LG>, smem16));
+          for (int i = t - 2; i >= 0; --i) {
+            const bool first = i == t - 2;
+            ext_step16_pair_kernel<T, LG>
+                <<<dim3(c.r, l, batch), 2 * Ntt16<LG>::kThreads, smem16, st>>>(
+                    first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
+                    a_tilde + static_cast<int64_t>(i + 1) * d, 0, a_stride,
+                    packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
+                    s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
+            RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
+          });
     } else {
       const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(c.r) * l * batch, s->sms);
       dim3 grid(c.r, l, batch);

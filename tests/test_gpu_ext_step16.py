@@ -1,10 +1,12 @@
-"""The d = 4096 external-product kernels with the register-resident radix-16
-NTT against each other and the CPU oracle (crypto/external_product.cc:35-114
-inside EvalPoly, crypto/pir/server/pir_server.cc:128-150): once shards x
-requests fill the GPU the answer takes one block per shard and request over
-all primes (and the radix-16 request NTTs and finalize); smaller batches take
-one block per prime with two transforms side by side. Every response of a
-large batch must equal the same requests answered eight at a time.
+"""The external-product, request-NTT and finalize kernels with the
+register-resident radix-16 NTT (d = 2048, 4096, 8192) against each other,
+the radix-4 kernels and the CPU oracle (crypto/external_product.cc:35-114
+inside EvalPoly, crypto/pir/server/pir_server.cc:128-150,
+crypto/lwes_to_rlwe.cc:448-479): once shards x requests fill the GPU the
+answer takes one block per shard and request over all primes; smaller
+batches take one block per prime with two transforms side by side (d <= 4096)
+or the radix-4 kernels (d = 8192). Every response of a large batch must equal
+the same requests answered eight at a time.
 """
 import numpy as np
 import pytest
@@ -36,14 +38,17 @@ def _oparams(params):
         entry_size_multiple=params.entry_size_multiple)
 
 
-@pytest.mark.parametrize("coeff_bits,log_q,t,l,batch", [
-    (32, 32, 4, 1, 160),
-    (32, 32, 8, 2, 80),
-    (64, 56, 4, 1, 160),
+@pytest.mark.parametrize("d,coeff_bits,log_q,t,l,batch", [
+    (4096, 32, 32, 4, 1, 160),
+    (4096, 32, 32, 8, 2, 80),
+    (4096, 64, 56, 4, 1, 160),
+    (2048, 32, 32, 4, 1, 160),
+    (2048, 64, 52, 2, 2, 80),
+    (8192, 32, 32, 2, 1, 160),
+    (8192, 64, 56, 2, 1, 152),
 ])
 def test_radix16_external_product_matches_small_batches_and_oracle(
-        coeff_bits, log_q, t, l, batch):
-    d = 4096
+        d, coeff_bits, log_q, t, l, batch):
     params = synthetic.make_params(d=d, n=t * 2048, t=t, l=l,
                                    coeff_bits=coeff_bits, log_q=log_q)
     mat = synthetic.make_material(params, seed=t + l)

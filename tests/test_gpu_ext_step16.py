@@ -45,6 +45,7 @@ def _oparams(params):
     (2048, 32, 32, 4, 1, 160),
     (2048, 64, 52, 2, 2, 80),
     (8192, 32, 32, 2, 1, 160),
+    (8192, 32, 32, 2, 2, 80),
     (8192, 64, 56, 2, 1, 152),
 ])
 def test_radix16_external_product_matches_small_batches_and_oracle(

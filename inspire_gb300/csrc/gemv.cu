@@ -205,6 +205,18 @@ cudaError_t launch_typed(const void* db, int64_t db_cols, const void* q1,
                          const void* yg, int64_t yg_stride, void* out,
                          int64_t out_stride, int64_t rows,
                          cudaStream_t stream) {
+  if (NQ == 1 && rows < 16384) {
+    // Smaller matrices (e.g. 8192 rows: 2048 blocks of 4 rows are 1.7 waves)
+    // take 2 rows per block, which evens out the last wave: 0.84 instead of
+    // 0.78 of the copy peak at 8192 x 16384 u16 + 8192 x 4096 i32.
+    fused_gemv_kernel<T, DbT, MatT, 2, NQ, kThreads>
+        <<<static_cast<unsigned>((rows + 1) / 2), kThreads, 0, stream>>>(
+            static_cast<const DbT*>(db), db_cols, static_cast<const T*>(q1),
+            q1_stride, static_cast<const MatT*>(pk), pk_cols,
+            static_cast<const T*>(yg), yg_stride, static_cast<T*>(out),
+            out_stride, rows);
+    return cudaGetLastError();
+  }
   constexpr int RB = NQ >= 4 ? 2 : 4;
   const int64_t blocks = (rows + RB - 1) / RB;
   fused_gemv_kernel<T, DbT, MatT, RB, NQ, kThreads>

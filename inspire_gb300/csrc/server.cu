@@ -553,6 +553,14 @@ Status NttCoeffs(const inspire_pir_server* s, const T* src, int64_t src_qstride,
   return Cuda(cudaGetLastError(), "forward NTT");
 }
 
+// Blocks (one per shard and request) from which the external product takes
+// one block per request over all primes rather than one per prime: a block
+// per SM at d >= 4096; at d = 2048 (128-thread blocks) two per SM, below
+// which the per-prime blocks keep more warps busy.
+inline int64_t Ext16Min(const inspire_pir_server* s, int d) {
+  return static_cast<int64_t>(s->sms) * std::max(1, 4096 / d);
+}
+
 // FinalizeMatrixPack for every shard of every request of a batch
 // (lwes_to_rlwe.cc:448-479): w->packed[q][shard] = b_agg.
 template <typename T>
@@ -622,7 +630,7 @@ Status RunPolyStage(inspire_pir_server* s, Workspace* w, int batch,
     ExtArgs e{log_q, s->prm.eval_log_digit, ne,
               LiveDigits(log_q, s->prm.eval_log_digit, ne), s->umask_e};
     const size_t smem = static_cast<size_t>(d) * 4 + 2ull * d * sizeof(T);
-    if (c.tables16 != nullptr && static_cast<int64_t>(l) * batch >= s->sms) {
+    if (c.tables16 != nullptr && static_cast<int64_t>(l) * batch >= Ext16Min(s, d)) {
       // Enough requests to fill the GPU with one block per (shard, request).
       INSPIRE_NTT16_DISPATCH(
           c.logd, RETURN_IF_ERROR(SetSmem(ext_step16_kernel<T, LG>, smem));
@@ -911,13 +919,30 @@ Status ExternalOnDevice(inspire_pir_server* s, Workspace* w, int batch,
               s->umask_e};
     const size_t smem = static_cast<size_t>(d) * 4 + 2ull * d * sizeof(T);
     const T* cta = static_cast<const T*>(ct);
-    const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(c.r) * batch, s->sms);
-    INSPIRE_ITERS_DISPATCH(
-        pl.iters, RETURN_IF_ERROR(SetSmem(ext_step_kernel<T, IT>, smem));
-        ext_step_kernel<T, IT><<<dim3(c.r, 1, batch), pl.nt, smem, st>>>(
-            true, nullptr, w->resid0.get<uint32_t>(), cta, 2 * d, 0, cta + d, 2 * d, 0,
-            w->rgswa.get<uint32_t>(), static_cast<int64_t>(ng) * c.r * d,
-            w->rgswb.get<uint32_t>(), e, c));
+    const int64_t rq = static_cast<int64_t>(ng) * c.r * d;  // RGSW a per request
+    if (c.tables16 != nullptr && batch >= Ext16Min(s, d)) {
+      // The radix-16 kernels as in RunPolyStage: one block per ciphertext.
+      INSPIRE_NTT16_DISPATCH(
+          c.logd, RETURN_IF_ERROR(SetSmem(ext_step16_kernel<T, LG>, smem));
+          ext_step16_kernel<T, LG><<<dim3(1, batch), Ntt16<LG>::kThreads, smem, st>>>(
+              true, nullptr, w->resid0.get<uint32_t>(), cta, 2 * d, 0, cta + d, 2 * d, 0,
+              w->rgswa.get<uint32_t>(), rq, w->rgswb.get<uint32_t>(), e, c));
+    } else if (c.tables16 != nullptr && d <= 4096) {
+      const size_t smem16 = 2ull * d * 4 + 2ull * d * sizeof(T);
+      INSPIRE_NTT16_PAIR_DISPATCH(
+          c.logd, RETURN_IF_ERROR(SetSmem(ext_step16_pair_kernel<T, LG>, smem16));
+          ext_step16_pair_kernel<T, LG>
+              <<<dim3(c.r, 1, batch), 2 * Ntt16<LG>::kThreads, smem16, st>>>(
+                  true, nullptr, w->resid0.get<uint32_t>(), cta, 2 * d, 0, cta + d, 2 * d,
+                  0, w->rgswa.get<uint32_t>(), rq, w->rgswb.get<uint32_t>(), e, c));
+    } else {
+      const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(c.r) * batch, s->sms);
+      INSPIRE_ITERS_DISPATCH(
+          pl.iters, RETURN_IF_ERROR(SetSmem(ext_step_kernel<T, IT>, smem));
+          ext_step_kernel<T, IT><<<dim3(c.r, 1, batch), pl.nt, smem, st>>>(
+              true, nullptr, w->resid0.get<uint32_t>(), cta, 2 * d, 0, cta + d, 2 * d, 0,
+              w->rgswa.get<uint32_t>(), rq, w->rgswb.get<uint32_t>(), e, c));
+    }
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
     finish_kernel<T><<<dim3(1, batch), nt, 0, st>>>(
         true, w->resid0.get<uint32_t>(), nullptr, 0, nullptr, 0, 0, false, 0, 0,

@@ -42,8 +42,9 @@ def _oparams(params):
     (4096, 32, 32, 4, 1, 160),
     (4096, 32, 32, 8, 2, 80),
     (4096, 64, 56, 4, 1, 160),
-    (2048, 32, 32, 4, 1, 160),
-    (2048, 64, 52, 2, 2, 80),
+    (2048, 32, 32, 4, 1, 320),
+    (2048, 64, 52, 2, 2, 160),
+    (2048, 32, 32, 4, 1, 160),   # below two per SM: the per-prime kernel
     (8192, 32, 32, 2, 1, 160),
     (8192, 32, 32, 2, 2, 80),
     (8192, 64, 56, 2, 1, 152),

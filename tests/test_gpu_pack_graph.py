@@ -98,9 +98,12 @@ def test_pack_batch_matches_oracle(engine, d, n, t, l, batch):
         assert np.array_equal(got[i], oracle_pack(params, mat, fd[i], pk[i])), i
 
 
-@pytest.mark.parametrize("cb,log_q,d", [(32, 32, 2048), (32, 32, 4096),
-                                        (64, 52, 2048)])
-def test_external_product_batch_matches_oracle(cb, log_q, d):
+@pytest.mark.parametrize("cb,log_q,d,batch", [
+    (32, 32, 2048, 4), (32, 32, 4096, 4), (64, 52, 2048, 4),
+    # Enough ciphertexts for the radix-16 block-per-ciphertext kernel (one
+    # per SM, two at d = 2048).
+    (32, 32, 2048, 320), (64, 52, 4096, 160), (32, 32, 8192, 152)])
+def test_external_product_batch_matches_oracle(cb, log_q, d, batch):
     params = synthetic.make_params(d=d, n=2 * d, t=2, coeff_bits=cb,
                                    log_q=log_q)
     mat = synthetic.make_material(params, seed=3, pad_to=32 if cb == 64 else 1)
@@ -109,7 +112,6 @@ def test_external_product_batch_matches_oracle(cb, log_q, d):
     cdt = params.coeff_dtype
     rng = np.random.default_rng(d + cb)
     hi = (1 << log_q) - 1
-    batch = 4
     ct = rng.integers(0, hi, size=(batch, 2, d), dtype=cdt, endpoint=True)
     rgsw = rng.integers(0, hi, size=(batch, 2 * ne, 2, d), dtype=cdt,
                         endpoint=True)
@@ -121,7 +123,7 @@ def test_external_product_batch_matches_oracle(cb, log_q, d):
     torch.cuda.synchronize()
     got = _host(out, cdt)
     op = oparams(params)
-    for i in range(batch):
+    for i in sorted({0, 1, 2, batch - 1}):
         wa, wb = orc.external_product(op, ct[i, 0], ct[i, 1],
                                       rgsw[i].reshape(-1, d))
         assert np.array_equal(got[i, 0], wa), i

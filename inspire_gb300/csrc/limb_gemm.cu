@@ -973,13 +973,15 @@ class LimbGemmImpl : public LimbGemm {
     return ChooseSplit(tiles, n_units);
   }
 
-  // Split-K factor that fills the SMs in whole waves (one CTA per SM).
+  // Split-K factor that fills the SMs in whole waves (one CTA per SM), with
+  // at least 16 accumulation units per K slice (small products, e.g. a
+  // 2048-row pack matrix: 64 units, 32 tiles at B = 256, split 4).
   int ChooseSplit(int64_t tiles, int n_units) const {
     const int sms = sms_ > 0 ? sms_ : 148;
     int best = 1;
     double best_eff = 0;
     for (int k = 1; k <= 8; ++k) {
-      if (n_units / k < 32) break;
+      if (n_units / k < 16) break;
       const int64_t items = tiles * k;
       const int64_t waves = (items + sms - 1) / sms;
       const double eff = static_cast<double>(items) / (waves * sms);

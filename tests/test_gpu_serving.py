@@ -95,6 +95,29 @@ def test_full_batches_use_the_tensor_engine():
     assert stats["requests"] == 96
 
 
+def test_u64_server_in_the_mix_uses_the_tensor_engine():
+    # A Z_2^64 server (q = 2^56, int32 pack matrix: eight request digit
+    # planes on the tensor cores) beside a Z_2^32 one.
+    pa, _, sa = _db(256, 32768, 2, 1, seed=11)
+    p64 = synthetic.make_params(d=256, n=16384, t=2, coeff_bits=64, log_q=56)
+    m64 = synthetic.make_material(p64, seed=12)
+    s64 = pir.PirServer.CreateCombined(p64, m64.db, m64.pack, m64.a_tilde_agg,
+                                       m64.t_vec_h, m64.second_dim_a)
+    reqs = {"A": synthetic.make_requests(pa, 64, seed=13),
+            "W": synthetic.make_requests(p64, 64, seed=14)}
+    want = {"A": sa.process_arrays(*reqs["A"]), "W": s64.process_arrays(*reqs["W"])}
+    with serving.ServingEngine({"A": sa, "W": s64}, max_batch=32, max_workspaces=2,
+                               plain_max_batch=4, max_wait_us=3000) as eng:
+        futs = {n: [eng.submit(n, r[0][i], r[1][i], r[2][i]) for i in range(64)]
+                for n, r in reqs.items()}
+        got = {n: np.stack([f.result(timeout=120) for f in fs]) for n, fs in futs.items()}
+        stats = eng.stats()
+    for n in ("A", "W"):
+        assert got[n].dtype == want[n].dtype
+        assert np.array_equal(got[n], want[n]), n
+    assert stats["tensor_batches"] >= 1
+
+
 def test_short_first_dimension_and_errors_in_the_mix():
     pa, ma, sa = _db(128, 2 * 4000, 2, 1, seed=8, pad_to=256)
     assert sa.db_cols == 4096

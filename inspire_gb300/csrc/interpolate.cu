@@ -146,8 +146,15 @@ interpolate_kernel(const V* __restrict__ raw, InterpArgs a, V* __restrict__ out)
 // consecutive classes; results pass through shared memory once so that the
 // stores run over kFastG consecutive groups (DB columns).
 constexpr int kFastR = 32;   // classes per block (one warp's lanes)
-constexpr int kFastGW = 8;   // groups in flight (warps per block)
-constexpr int kFastG = 16;   // groups per block
+// Groups per block (kG: the stores run over kG consecutive columns) and
+// groups in flight (kGW warps per block). 16-bit values take 32 groups
+// (64-byte stores, a 68 KB tile at t = 8, three blocks per SM); wider values
+// 16, which keeps the tile within a block's limit.
+template <typename V>
+struct FastShape {
+  static constexpr int kG = sizeof(V) <= 2 ? 32 : 16;
+  static constexpr int kGW = 8;
+};
 
 // Modular helpers; SMALL: p < 2^31, so sums and Shoup remainders fit in 32
 // bits.
@@ -196,19 +203,23 @@ __device__ __forceinline__ uint32_t scale_p(uint32_t x, uint32_t tinv, uint32_t 
 }
 
 template <typename V, int T, bool SMALL>
-__global__ void __launch_bounds__(kFastR * kFastGW)
+__global__ void __launch_bounds__(kFastR * FastShape<V>::kGW)
 interpolate_fast_kernel(const V* __restrict__ raw, InterpArgs a, ModConsts mc,
                         V* __restrict__ out) {
   constexpr int H = T / 2;
   constexpr int LOGT = T == 2 ? 1 : (T == 4 ? 2 : 3);
+  constexpr int kFastG = FastShape<V>::kG;
+  constexpr int kFastGW = FastShape<V>::kGW;
   // [T*H rows][kFastR classes][kFastG + 1 groups] (dynamic shared memory)
   extern __shared__ __align__(16) unsigned char tile_raw[];
   V* tile = reinterpret_cast<V*>(tile_raw);
   constexpr int kRow = kFastG + 1;
   const int c0 = threadIdx.x % kFastR;
   const int gw = threadIdx.x / kFastR;
-  const int64_t g_base = static_cast<int64_t>(blockIdx.x) * kFastG;
-  const int c_start = blockIdx.y * kFastR;
+  // Class blocks fastest: blocks running together read neighbouring 64-byte
+  // pieces of the same records.
+  const int64_t g_base = static_cast<int64_t>(blockIdx.y) * kFastG;
+  const int c_start = blockIdx.x * kFastR;
   const int k = blockIdx.z;
   const int64_t rec_stride = static_cast<int64_t>(a.l) * a.d;
   const uint32_t p = a.p;
@@ -383,9 +394,10 @@ int Run(const V* raw, int64_t n, int d, int t, int l, uint32_t p, V* out,
       mc.tinv_s64 = static_cast<uint64_t>((static_cast<unsigned __int128>(a.tinv) << 64) / p);
       mc.tinv_s32 = static_cast<uint32_t>((static_cast<uint64_t>(a.tinv) << 32) / p);
       const bool small = p < (1u << 31);
-      dim3 grid(static_cast<unsigned>((groups + kFastG - 1) / kFastG),
-                static_cast<unsigned>(a.s / kFastR), static_cast<unsigned>(l));
-      const int threads = kFastR * kFastGW;
+      constexpr int kFastG = FastShape<V>::kG;
+      dim3 grid(static_cast<unsigned>(a.s / kFastR),
+                static_cast<unsigned>((groups + kFastG - 1) / kFastG), static_cast<unsigned>(l));
+      const int threads = kFastR * FastShape<V>::kGW;
       const size_t smem = static_cast<size_t>(t) * (t / 2) * kFastR * (kFastG + 1) * sizeof(V);
       auto launch = [&](auto kernel) {
         cudaError_t r = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -154,6 +154,9 @@ template <typename V>
 struct FastShape {
   static constexpr int kG = sizeof(V) <= 2 ? 32 : 16;
   static constexpr int kGW = 8;
+  // Tile row pitch in values: padded against bank conflicts, and even for
+  // 16-bit values so that two neighbouring groups read as one 32-bit word.
+  static constexpr int kRow = kG + (sizeof(V) == 2 ? 2 : 1);
 };
 
 // Modular helpers; SMALL: p < 2^31, so sums and Shoup remainders fit in 32
@@ -213,7 +216,7 @@ interpolate_fast_kernel(const V* __restrict__ raw, InterpArgs a, ModConsts mc,
   // [T*H rows][kFastR classes][kFastG + 1 groups] (dynamic shared memory)
   extern __shared__ __align__(16) unsigned char tile_raw[];
   V* tile = reinterpret_cast<V*>(tile_raw);
-  constexpr int kRow = kFastG + 1;
+  constexpr int kRow = FastShape<V>::kRow;
   const int c0 = threadIdx.x % kFastR;
   const int gw = threadIdx.x / kFastR;
   // Class blocks fastest: blocks running together read neighbouring 64-byte
@@ -285,6 +288,27 @@ interpolate_fast_kernel(const V* __restrict__ raw, InterpArgs a, ModConsts mc,
   // Stores: kFastG consecutive columns of each DB row.
   const int64_t left = a.groups - g_base;
   const int G = left < kFastG ? static_cast<int>(left) : kFastG;
+  if constexpr (sizeof(V) == 2) {
+    if ((a.out_cols & 1) == 0 && G == kFastG &&
+        (reinterpret_cast<uintptr_t>(out) & 3) == 0) {
+      // Two neighbouring groups per 32-bit store (even row pitch, g_base a
+      // multiple of 32: every store is 4-byte aligned).
+      constexpr int kPairs = kFastG / 2;
+      for (int idx = threadIdx.x; idx < T * H * kFastR * kPairs; idx += blockDim.x) {
+        const int gp = idx % kPairs;
+        const int c = (idx / kPairs) % kFastR;
+        const int rm = idx / (kPairs * kFastR);
+        const int r = rm / H, m = rm % H;
+        const int64_t row = static_cast<int64_t>(k) * T * a.d +
+                            static_cast<int64_t>(r) * a.d + c_start + c +
+                            static_cast<int64_t>(m) * a.s;
+        const uint32_t v =
+            *reinterpret_cast<const uint32_t*>(tile + (rm * kFastR + c) * kRow + 2 * gp);
+        *reinterpret_cast<uint32_t*>(out + row * a.out_cols + g_base + 2 * gp) = v;
+      }
+      return;
+    }
+  }
   for (int idx = threadIdx.x; idx < T * H * kFastR * kFastG; idx += blockDim.x) {
     const int g = idx % kFastG;
     const int c = (idx / kFastG) % kFastR;
@@ -398,7 +422,8 @@ int Run(const V* raw, int64_t n, int d, int t, int l, uint32_t p, V* out,
       dim3 grid(static_cast<unsigned>(a.s / kFastR),
                 static_cast<unsigned>((groups + kFastG - 1) / kFastG), static_cast<unsigned>(l));
       const int threads = kFastR * FastShape<V>::kGW;
-      const size_t smem = static_cast<size_t>(t) * (t / 2) * kFastR * (kFastG + 1) * sizeof(V);
+      const size_t smem =
+          static_cast<size_t>(t) * (t / 2) * kFastR * FastShape<V>::kRow * sizeof(V);
       auto launch = [&](auto kernel) {
         cudaError_t r = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem));

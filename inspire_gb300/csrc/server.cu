@@ -676,10 +676,10 @@ Status RunPolyStage(inspire_pir_server* s, Workspace* w, int batch,
     }
   }
   {
-    // Few requests: the widest block, which shortens each block's chain of
-    // dependent loads.
+    // The widest block: it shortens each block's chain of dependent loads
+    // (one block per request runs once per SM at any batch size here).
     dim3 grid(l, batch);
-    const int fin_nt = static_cast<int64_t>(l) * batch < s->sms ? kPolyThreads : nt;
+    const int fin_nt = kPolyThreads;
     finish_kernel<T><<<grid, fin_nt, 0, st>>>(
         t > 1, resid[0], a_tilde, a_stride, packed, b_qstride, a_stride, true,
         log_q, s->prm.log_modulus1_after_switch,

@@ -97,7 +97,9 @@ def run_load(eng, pools, names, weights, rate, seconds, rng):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--seconds", type=float, default=3.0)
-    ap.add_argument("--loads", default="0.1,0.25,0.5,0.75,1.0")
+    ap.add_argument("--loads", default="0.1,0.25,0.5,0.75,1.0,1.5",
+                    help="offered loads as fractions of the closed-loop peak; "
+                         "above 1 the loop saturates")
     ap.add_argument("--pool", type=int, default=64)
     ap.add_argument("--max-batch", type=int, default=256)
     ap.add_argument("--hbm-budget-gb", type=float, default=48.0)

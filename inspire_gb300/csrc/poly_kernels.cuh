@@ -674,17 +674,17 @@ ext_step16_kernel(bool first, const uint32_t* __restrict__ resid_in,
 }
 
 // The external product for d = 2^LOGD when a launch has fewer requests
-// than SMs: one block per (prime, shard, request) as ext_step_kernel, d / 8
-// threads in two groups of d / 16 that run the radix-16 transforms side by
-// side. Group 0 transforms the live digits of a, group 1 those of b; each
-// keeps its partial
-// product for one output (group 0: a', group 1: b') and hands the other over
-// through shared memory, then group 0 inverts a' and group 1 b'. Each block
-// runs once per SM, so the compact transforms (one pass body for all passes)
-// keep the code small. Same residues as ext_step_kernel.
-// grid = (r, l, batch), needs c.tables16.
-template <typename T, int LOGD>
-__global__ void __launch_bounds__(2 * Ntt16<LOGD>::kThreads, 1)
+// than SMs: one block per (prime, shard, request) as ext_step_kernel, NGR
+// groups of d / 16 threads that run the radix-16 transforms side by side
+// (NGR = 2, or 4 at d = 2048 for the fewest blocks). The live digits of a
+// and b are dealt to the groups in turn; each group keeps its partial
+// products for both outputs, the partials meet in shared memory, group 0
+// sums and inverts a' and group 1 b'. Each block runs once per SM, so the
+// compact transforms (one pass body for all passes) keep the code small.
+// Same residues as ext_step_kernel. grid = (r, l, batch), shared memory
+// 2 NGR d words + 2 d CoeffType words, needs c.tables16.
+template <typename T, int LOGD, int NGR>
+__global__ void __launch_bounds__(NGR * Ntt16<LOGD>::kThreads, 1)
 ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
                        uint32_t* __restrict__ resid_out,
                        const T* __restrict__ coeff_a, int64_t coeff_a_q_stride,
@@ -697,11 +697,13 @@ ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
   constexpr int d = Ntt16<LOGD>::kD;
   constexpr int NT = Ntt16<LOGD>::kThreads;
   const int tid = threadIdx.x;
-  const int grp = tid / NT;  // 0: digits of a, 1: digits of b
+  const int grp = tid / NT;
   const int lt = tid & (NT - 1);
   const int bar = 1 + grp;
-  uint32_t* xs = smem + grp * d;  // this group's exchange buffer
-  T* st = reinterpret_cast<T*>(smem + 2 * d);  // LowBits of a, then of b
+  // Per group: [partial a' | partial b'], the first half doubling as the
+  // group's exchange buffer while it transforms.
+  uint32_t* region = smem + grp * 2 * d;
+  T* st = reinterpret_cast<T*>(smem + NGR * 2 * d);  // LowBits of a, then of b
   const int pi = blockIdx.x;
   const uint32_t* tab16 = c.tables16 + static_cast<size_t>(pi) * 4 * d;
   const int shard = blockIdx.y;
@@ -711,22 +713,25 @@ ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
   const T* cb = coeff_b + q * coeff_b_q_stride + shard * coeff_b_shard_stride;
   const int64_t rbase = (static_cast<int64_t>(q) * l + shard) * c.r * 2 * d;
 #pragma unroll 2
-  for (int j = tid; j < d; j += 2 * NT) {
+  for (int j = tid; j < d; j += NGR * NT) {
     T ra, rb;
     horner_state<T>(first, resid_in, rbase, d, j, ca, cb, c, ra, rb);
     st[j] = low_bits<T>(ra, e.log_q);
     st[d + j] = low_bits<T>(rb, e.log_q);
   }
   __syncthreads();
-  const T* src = st + grp * d;
   const uint32_t p = c.p[pi];
   const uint32_t pinv = c.pinv[pi];
   const int ng = 2 * e.num_digits;
-  uint32_t keep[16], send[16];
+  const int n_live = 2 * e.live_digits;  // transforms: digits of a, then of b
+  uint32_t acc_a[16], acc_b[16];
 #pragma unroll
-  for (int k = 0; k < 16; ++k) keep[k] = send[k] = 0;
-  for (int dg = 0; dg < e.live_digits; ++dg) {
-    const int g = grp * e.num_digits + dg;
+  for (int k = 0; k < 16; ++k) acc_a[k] = acc_b[k] = 0;
+  for (int ti = grp; ti < n_live; ti += NGR) {
+    const int poly = ti < e.live_digits ? 0 : 1;
+    const int dg = ti - poly * e.live_digits;
+    const int g = poly * e.num_digits + dg;
+    const T* src = st + poly * d;
     uint32_t x[16];
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
@@ -734,39 +739,48 @@ ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
                                     e.num_digits, dg);
       x[k] = to_residue<T>(dig & static_cast<T>(e.umask), p);
     }
-    ntt16_forward<LOGD, false, true>(x, xs, tab16, p, lt, bar);
-    const uint32_t* wa =
-        RGSWa + q * rgswa_qstride + (static_cast<int64_t>(g) * c.r + pi) * d + 16 * lt;
-    const uint32_t* wb =
-        RGSWb + ((static_cast<int64_t>(q) * ng + g) * c.r + pi) * d + 16 * lt;
-    const uint4* wk = reinterpret_cast<const uint4*>(grp == 0 ? wa : wb);
-    const uint4* wsd = reinterpret_cast<const uint4*>(grp == 0 ? wb : wa);
+    ntt16_forward<LOGD, false, true>(x, region, tab16, p, lt, bar);
+    const uint4* wa = reinterpret_cast<const uint4*>(
+        RGSWa + q * rgswa_qstride + (static_cast<int64_t>(g) * c.r + pi) * d + 16 * lt);
+    const uint4* wb = reinterpret_cast<const uint4*>(
+        RGSWb + ((static_cast<int64_t>(q) * ng + g) * c.r + pi) * d + 16 * lt);
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const uint4 vk = __ldg(wk + v), vs = __ldg(wsd + v);
-      const uint32_t rk[4] = {vk.x, vk.y, vk.z, vk.w};
-      const uint32_t rs[4] = {vs.x, vs.y, vs.z, vs.w};
+      const uint4 va = __ldg(wa + v), vb = __ldg(wb + v);
+      const uint32_t ra[4] = {va.x, va.y, va.z, va.w};
+      const uint32_t rb[4] = {vb.x, vb.y, vb.z, vb.w};
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         const int k = 4 * v + i;
-        keep[k] = add_mod(keep[k], mont_mul(x[k], rk[i], p, pinv), p);
-        send[k] = add_mod(send[k], mont_mul(x[k], rs[i], p, pinv), p);
+        acc_a[k] = add_mod(acc_a[k], mont_mul(x[k], ra[i], p, pinv), p);
+        acc_b[k] = add_mod(acc_b[k], mont_mul(x[k], rb[i], p, pinv), p);
       }
     }
   }
-  // Hand over: each group leaves its partial of the other output in its own
-  // buffer (free since its last transform) and adds the other group's.
-  ntt16_store_slots<LOGD>(send, xs, lt);
+  // The partials meet: every group leaves both in its region (its exchange
+  // buffer is free since its last transform); group 0 sums a', group 1 b'.
+  ntt16_store_slots<LOGD>(acc_a, region, lt);
+  ntt16_store_slots<LOGD>(acc_b, region + d, lt);
   __syncthreads();
-  ntt16_load_slots<LOGD>(send, smem + (1 - grp) * d, lt);
+  uint32_t sum[16];
+  if (grp < 2) {
 #pragma unroll
-  for (int k = 0; k < 16; ++k) keep[k] = add_mod(keep[k], send[k], p);
+    for (int k = 0; k < 16; ++k) sum[k] = 0;
+    for (int o = 0; o < NGR; ++o) {
+      uint32_t part[16];
+      ntt16_load_slots<LOGD>(part, smem + o * 2 * d + grp * d, lt);
+#pragma unroll
+      for (int k = 0; k < 16; ++k) sum[k] = add_mod(sum[k], part[k], p);
+    }
+  }
   __syncthreads();
-  ntt16_inverse<LOGD, false, true>(keep, xs, tab16, p, lt, bar);
-  uint32_t* out = resid_out + rbase + static_cast<int64_t>(pi) * 2 * d + grp * d;
+  if (grp < 2) {
+    ntt16_inverse<LOGD, false, true>(sum, region, tab16, p, lt, bar);
+    uint32_t* out = resid_out + rbase + static_cast<int64_t>(pi) * 2 * d + grp * d;
 #pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    out[lt + NT * k] = shoup_mul(keep[k], c.scale[pi], c.scale_s[pi], p);
+    for (int k = 0; k < 16; ++k) {
+      out[lt + NT * k] = shoup_mul(sum[k], c.scale[pi], c.scale_s[pi], p);
+    }
   }
 }
 

@@ -553,6 +553,31 @@ Status NttCoeffs(const inspire_pir_server* s, const T* src, int64_t src_qstride,
   return Cuda(cudaGetLastError(), "forward NTT");
 }
 
+// Shared memory of ext_step16_pair_kernel with NGR transform groups: a
+// 2 d-word region per group plus the state.
+template <typename T, int LG, int NGR>
+constexpr size_t PairExtSmem() {
+  return static_cast<size_t>(NGR) * 2 * Ntt16<LG>::kD * 4 + 2ull * Ntt16<LG>::kD * sizeof(T);
+}
+
+// Launches ext_step16_pair_kernel with NGR groups: four at d = 2048 when the
+// launch has fewer blocks than SMs (each Horner step then waits on one
+// transform per group instead of two), else two.
+template <typename T, int LG, typename... A>
+Status LaunchPairExt(int64_t blocks, int sms, dim3 grid, cudaStream_t st, A... args) {
+  if (LG == 11 && blocks < sms) {
+    constexpr int NGR = LG == 11 ? 4 : 2;
+    const size_t smem = PairExtSmem<T, LG, NGR>();
+    RETURN_IF_ERROR(SetSmem(ext_step16_pair_kernel<T, LG, NGR>, smem));
+    ext_step16_pair_kernel<T, LG, NGR><<<grid, NGR * Ntt16<LG>::kThreads, smem, st>>>(args...);
+  } else {
+    const size_t smem = PairExtSmem<T, LG, 2>();
+    RETURN_IF_ERROR(SetSmem(ext_step16_pair_kernel<T, LG, 2>, smem));
+    ext_step16_pair_kernel<T, LG, 2><<<grid, 2 * Ntt16<LG>::kThreads, smem, st>>>(args...);
+  }
+  return Cuda(cudaGetLastError(), "external product");
+}
+
 // Blocks (one per shard and request) from which the external product takes
 // one block per request over all primes rather than one per prime: a block
 // per SM at d >= 4096; at d = 2048 (128-thread blocks) two per SM, below
@@ -644,20 +669,18 @@ Status RunPolyStage(inspire_pir_server* s, Workspace* w, int batch,
             RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
           });
     } else if (c.tables16 != nullptr && d <= 4096) {
-      // Few requests: one block per prime, two transforms at a time (d / 8
-      // threads).
-      const size_t smem16 = 2ull * d * 4 + 2ull * d * sizeof(T);
+      // Few requests: one block per prime, transforms side by side.
+      const int64_t blocks = static_cast<int64_t>(c.r) * l * batch;
       INSPIRE_NTT16_PAIR_DISPATCH(
-          c.logd, RETURN_IF_ERROR(SetSmem(ext_step16_pair_kernel<T, LG>, smem16));
-          for (int i = t - 2; i >= 0; --i) {
+          c.logd, for (int i = t - 2; i >= 0; --i) {
             const bool first = i == t - 2;
-            ext_step16_pair_kernel<T, LG>
-                <<<dim3(c.r, l, batch), 2 * Ntt16<LG>::kThreads, smem16, st>>>(
-                    first, first ? nullptr : resid[(i + 1) & 1], resid[i & 1],
-                    a_tilde + static_cast<int64_t>(i + 1) * d, 0, a_stride,
-                    packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
-                    s->rgswa_ntt.get<uint32_t>(), 0, w->rgswb.get<uint32_t>(), e, c);
-            RETURN_IF_ERROR(Cuda(cudaGetLastError(), "external product"));
+            RETURN_IF_ERROR((LaunchPairExt<T, LG>(
+                blocks, s->sms, dim3(c.r, l, batch), st, first,
+                first ? nullptr : static_cast<const uint32_t*>(resid[(i + 1) & 1]),
+                resid[i & 1], a_tilde + static_cast<int64_t>(i + 1) * d, int64_t{0}, a_stride,
+                packed + static_cast<int64_t>(i + 1) * d, b_qstride, a_stride,
+                static_cast<const uint32_t*>(s->rgswa_ntt.get<uint32_t>()), int64_t{0},
+                static_cast<const uint32_t*>(w->rgswb.get<uint32_t>()), e, c)));
           });
     } else {
       const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(c.r) * l * batch, s->sms);
@@ -928,13 +951,13 @@ Status ExternalOnDevice(inspire_pir_server* s, Workspace* w, int batch,
               true, nullptr, w->resid0.get<uint32_t>(), cta, 2 * d, 0, cta + d, 2 * d, 0,
               w->rgswa.get<uint32_t>(), rq, w->rgswb.get<uint32_t>(), e, c));
     } else if (c.tables16 != nullptr && d <= 4096) {
-      const size_t smem16 = 2ull * d * 4 + 2ull * d * sizeof(T);
       INSPIRE_NTT16_PAIR_DISPATCH(
-          c.logd, RETURN_IF_ERROR(SetSmem(ext_step16_pair_kernel<T, LG>, smem16));
-          ext_step16_pair_kernel<T, LG>
-              <<<dim3(c.r, 1, batch), 2 * Ntt16<LG>::kThreads, smem16, st>>>(
-                  true, nullptr, w->resid0.get<uint32_t>(), cta, 2 * d, 0, cta + d, 2 * d,
-                  0, w->rgswa.get<uint32_t>(), rq, w->rgswb.get<uint32_t>(), e, c));
+          c.logd, RETURN_IF_ERROR((LaunchPairExt<T, LG>(
+                      static_cast<int64_t>(c.r) * batch, s->sms, dim3(c.r, 1, batch), st,
+                      true, static_cast<const uint32_t*>(nullptr), w->resid0.get<uint32_t>(),
+                      cta, int64_t{2} * d, int64_t{0}, cta + d, int64_t{2} * d, int64_t{0},
+                      static_cast<const uint32_t*>(w->rgswa.get<uint32_t>()), rq,
+                      static_cast<const uint32_t*>(w->rgswb.get<uint32_t>()), e, c))));
     } else {
       const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(c.r) * batch, s->sms);
       INSPIRE_ITERS_DISPATCH(

@@ -44,6 +44,11 @@ def ring_tag():
     return "Z_2^32" if COEFF_BITS == 32 else "Z_2^64, q=2^%d" % LOG_Q
 
 
+def metric_name():
+    """The headline metric, printed identically by both arms."""
+    return "queries/s (online answer, n=2^20 d=4096 t=8, %s)" % ring_tag()
+
+
 def workload_name():
     return "pir_answer_n2^20_d4096_t8_l1_" + word_tag() + \
         ("" if COEFF_BITS == 32 else "_q2^%d" % LOG_Q)
@@ -60,41 +65,46 @@ def peaks():
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    """Samples nvidia-smi clocks and throttle reasons during the timed region
+    (one nvidia-smi process in its own loop mode, a sample every 25 ms)."""
     QUERY = ("clocks.sm,clocks.max.sm,power.draw,"
              "clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index=0):
+    def __init__(self, index=0, interval_ms=25):
         self.index = index
+        self.interval_ms = interval_ms
         self.samples = []
-        self._stop = threading.Event()
-        self._t = None
-
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(
-                    ["nvidia-smi", "-i", str(self.index),
-                     "--query-gpu=" + self.QUERY,
-                     "--format=csv,noheader,nounits"],
-                    capture_output=True, text=True, timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([x.strip() for x in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        self._proc = None
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
-        self._t.start()
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                 "-lms", str(self.interval_ms)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            # nvidia-smi prints its first sample once it has attached.
+            time.sleep(0.3)
+        except OSError:
+            self._proc = None
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        self._t.join(timeout=10)
+        if self._proc is None:
+            return
+        time.sleep(2 * self.interval_ms / 1000.0)
+        self._proc.terminate()
+        try:
+            out, _ = self._proc.communicate(timeout=10)
+        except subprocess.TimeoutExpired:
+            self._proc.kill()
+            out, _ = self._proc.communicate()
+        for ln in out.splitlines():
+            if ln.strip():
+                self.samples.append([x.strip() for x in ln.split(",")])
 
     def summary(self):
         if not self.samples:
@@ -141,36 +151,80 @@ def make_workload(seed=2026, batch=256):
         fd, sd, pk
 
 
-def run_reference(args):
-    """The reference algorithm (oracle port, FP64 FFT path) on host cores."""
+def cpu_reference_profile(params, db, pack, a_tilde, t_vec_h, sda, fd, sd,
+                          pk, reps=2):
+    """The reference algorithm (the oracle's timing build, FP64 FFT path) on
+    one host core, one request at a time as the single-threaded reference
+    runs it: mean latency and the reference's stage split (DB mult, packing,
+    poly-eval; pir_server.cc:214-285, printed by pir_metrics_tool.cc:435-447).
+    """
+    from oracle import build_oracle, pyoracle as orc
+    op = oracle_params(params)
+    condensed = params.rlwe.coeff_bits == 64
+    lat, stages = [], []
+    for i in range(reps):
+        t0 = time.perf_counter()
+        _, st = orc.process_response_staged(
+            op, db, pack, a_tilde, t_vec_h, sda, fd[i % fd.shape[0]],
+            sd[i % fd.shape[0]], pk[i % fd.shape[0]], mode=orc.MODE_FP64,
+            threads=1, condensed_db=condensed)
+        lat.append((time.perf_counter() - t0) * 1000.0)
+        stages.append(st)
+    mean = {k: statistics.mean(s[k] for s in stages) for k in stages[0]}
+    return {"single_core_ms": statistics.mean(lat),
+            "stages_ms": mean,
+            "build": build_oracle.timing_build_string(),
+            "db_product": "condensed u64 words (matrix.cc:261-318)"
+                          if condensed else
+                          "scalar u32 loop (matrix.h:183-194; the reference "
+                          "condenses the DB only for u64 CoeffType, "
+                          "preprocessing_server.h:127-153)"}
+
+
+def cpu_reference_throughput(params, db, pack, a_tilde, t_vec_h, sda, fd, sd,
+                             pk, threads, requests):
+    """`requests` full requests, one per host thread at a time on `threads`
+    threads (the reference has no threads of its own: independent requests
+    per core). Returns (seconds, requests done)."""
     from oracle import pyoracle as orc
-    params, db, pack, a_tilde, t_vec_h, sda, fd, sd, pk = make_workload(
-        batch=max(64, os.cpu_count() or 1))
-    r = params.rlwe
-    op = orc.make_params(
-        coeff_bits=COEFF_BITS, log_degree=DEGREE.bit_length() - 1,
-        log_modulus=r.log_modulus,
-        log_modulus1_after_switch=r.log_modulus1_after_switch,
-        log_modulus2_after_switch=r.log_modulus2_after_switch,
-        pack_log_digit=params.pack_gadget.log_digit,
-        pack_num_digits=params.pack_gadget.num_digits,
-        eval_log_digit=params.eval_gadget.log_digit,
-        eval_num_digits=params.eval_gadget.num_digits,
-        num_entries=N_ENTRIES, interpolation_degree=INTERP,
-        entry_size_multiple=1)
+    op = oracle_params(params)
+    condensed = params.rlwe.coeff_bits == 64
+    nxt = [0]
+    lock = threading.Lock()
+
+    def work():
+        while True:
+            with lock:
+                i = nxt[0]
+                if i >= requests:
+                    return
+                nxt[0] += 1
+            j = i % fd.shape[0]
+            orc.process_response_staged(op, db, pack, a_tilde, t_vec_h, sda,
+                                        fd[j], sd[j], pk[j],
+                                        mode=orc.MODE_FP64, threads=1,
+                                        condensed_db=condensed)
+    ts = [threading.Thread(target=work) for _ in range(threads)]
+    t0 = time.perf_counter()
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    return time.perf_counter() - t0, requests
+
+
+def run_reference(args):
+    """The reference algorithm (the oracle's timing build, FP64 FFT path) on
+    all host cores: each step answers one request per host thread."""
     threads = os.cpu_count() or 1
+    params, db, pack, a_tilde, t_vec_h, sda, fd, sd, pk = make_workload(
+        batch=max(64, threads))
+    prof = cpu_reference_profile(params, db, pack, a_tilde, t_vec_h, sda, fd,
+                                 sd, pk, reps=2)
 
     def one_step():
-        def work(i):
-            orc.process_response(op, db, pack, a_tilde, t_vec_h, sda, fd[i],
-                                 sd[i], pk[i], mode=orc.MODE_FP64)
-        ts = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
-        t0 = time.perf_counter()
-        for t in ts:
-            t.start()
-        for t in ts:
-            t.join()
-        return time.perf_counter() - t0
+        return cpu_reference_throughput(params, db, pack, a_tilde, t_vec_h,
+                                        sda, fd, sd, pk, threads, threads)[0]
 
     for _ in range(args.warmup):
         one_step()
@@ -179,63 +233,100 @@ def run_reference(args):
     qps = threads * args.steps / total
     line = {
         "impl": "reference",
-        "metric": "queries/s (online answer, n=2^20 d=4096 t=8, %s)" % ring_tag(),
+        "metric": metric_name(),
         "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": word_tag(),
-        "data": "synthetic (seeded uniform DB / queries)",
+        "data": "synthetic (seeded uniform DB, pack matrix, queries)",
         "config": {"workload": workload_name(),
                    "n": N_ENTRIES, "d": DEGREE, "t": INTERP, "l": 1,
                    "requests_per_step": threads},
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads,
                          "kind": "port",
                          "sample": "%d full requests per step, one per host "
-                                   "thread" % threads},
+                                   "thread (oracle timing build, FP64 FFT "
+                                   "path)" % threads,
+                         "single_core_ms": prof["single_core_ms"],
+                         "stages_ms": prof["stages_ms"],
+                         "build": prof["build"],
+                         "db_product": prof["db_product"]},
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
 
 
-def cpu_baseline_sample(params, db, pack, a_tilde, t_vec_h, sda, fd, sd, pk,
-                        budget_s=20.0):
-    """Oracle (FP64 reference algorithm) on all host cores, bounded."""
+def oracle_params(params):
     from oracle import pyoracle as orc
     r = params.rlwe
-    op = orc.make_params(
-        coeff_bits=COEFF_BITS, log_degree=DEGREE.bit_length() - 1,
+    return orc.make_params(
+        coeff_bits=r.coeff_bits, log_degree=r.degree.bit_length() - 1,
         log_modulus=r.log_modulus,
         log_modulus1_after_switch=r.log_modulus1_after_switch,
         log_modulus2_after_switch=r.log_modulus2_after_switch,
-        pack_log_digit=19, pack_num_digits=2, eval_log_digit=19,
-        eval_num_digits=3, num_entries=N_ENTRIES, interpolation_degree=INTERP,
-        entry_size_multiple=1)
-    threads = min(os.cpu_count() or 1, fd.shape[0])
-    done = [0]
-    lock = threading.Lock()
-    deadline = time.perf_counter() + budget_s
+        pack_log_digit=params.pack_gadget.log_digit,
+        pack_num_digits=params.pack_gadget.num_digits,
+        eval_log_digit=params.eval_gadget.log_digit,
+        eval_num_digits=params.eval_gadget.num_digits,
+        num_entries=params.num_entries,
+        interpolation_degree=params.interpolation_degree,
+        entry_size_multiple=params.entry_size_multiple)
 
-    def work(i):
-        j = i
-        while time.perf_counter() < deadline:
-            orc.process_response(op, db, pack, a_tilde, t_vec_h, sda,
-                                 fd[j % fd.shape[0]], sd[j % fd.shape[0]],
-                                 pk[j % fd.shape[0]], mode=orc.MODE_FP64)
-            with lock:
-                done[0] += 1
-            j += threads
+
+def oracle_check(params, db, pack, a_tilde, t_vec_h, sda, fd, sd, pk, got,
+                 picks):
+    """Compares responses `picks` of `got` (B, l, 2, d) with the oracle's
+    exact-product answer on the same bytes, one host thread per response."""
+    from oracle import pyoracle as orc
+    op = oracle_params(params)
+    bad = []
+    errs = []
+
+    def one(i):
+        try:
+            want = orc.process_response(op, db, pack, a_tilde, t_vec_h, sda,
+                                        fd[i], sd[i], pk[i],
+                                        mode=orc.MODE_EXACT)
+            if not np.array_equal(got[i].reshape(want.shape), want):
+                bad.append(i)
+        except Exception as e:  # reported below, never swallowed
+            errs.append("%d: %s" % (i, e))
     t0 = time.perf_counter()
-    ts = [threading.Thread(target=work, args=(i,)) for i in range(threads)]
+    ts = [threading.Thread(target=one, args=(i,)) for i in picks]
     for t in ts:
         t.start()
     for t in ts:
         t.join()
-    el = time.perf_counter() - t0
-    return {"value": done[0] / el, "unit": "queries/s", "cores": threads,
+    if errs:
+        raise SystemExit("oracle check failed: %s" % "; ".join(errs))
+    return {"responses": list(picks), "mismatches": sorted(bad),
+            "oracle": "exact-product oracle (ORC_MODE_EXACT)",
+            "seconds": round(time.perf_counter() - t0, 2)}
+
+
+def cpu_baseline_sample(params, db, pack, a_tilde, t_vec_h, sda, fd, sd, pk,
+                        budget_s=20.0):
+    """The reference algorithm on the host cores, bounded: two requests on
+    one core (latency and stage split), then one request per host thread
+    for the rest of the budget."""
+    prof = cpu_reference_profile(params, db, pack, a_tilde, t_vec_h, sda, fd,
+                                 sd, pk, reps=2)
+    threads = os.cpu_count() or 1
+    left = budget_s - 2 * prof["single_core_ms"] / 1000.0
+    per_req = prof["single_core_ms"] / 1000.0
+    requests = max(threads, int(threads * max(left, per_req) / (2 * per_req)))
+    requests = (requests + threads - 1) // threads * threads
+    el, done = cpu_reference_throughput(params, db, pack, a_tilde, t_vec_h,
+                                        sda, fd, sd, pk, threads, requests)
+    return {"value": done / el, "unit": "queries/s", "cores": threads,
             "kind": "port",
-            "sample": "%d full requests in %.1f s on %d host threads "
-                      "(oracle, FP64 FFT path)" % (done[0], el, threads)}
+            "sample": "%d full requests in %.1f s, one per host thread on %d "
+                      "threads (oracle timing build, FP64 FFT path)"
+                      % (done, el, threads),
+            "single_core_ms": prof["single_core_ms"],
+            "stages_ms": prof["stages_ms"], "build": prof["build"],
+            "db_product": prof["db_product"]}
 
 
 def run_pack_workload(args):
@@ -649,18 +740,27 @@ def run_single_workload(args):
                 "d2h_bytes_per_step": int(h_out[0].nbytes)},
     }
     if not args.no_cpu_baseline:
+        from oracle import build_oracle
         done, t0 = 0, time.perf_counter()
+        stages = []
         while time.perf_counter() - t0 < 10.0:
-            orc.process_response(op, mat.db, mat.pack, mat.a_tilde_agg,
-                                 mat.t_vec_h, mat.second_dim_a, fd[done % nreq],
-                                 sd[done % nreq], pk[done % nreq],
-                                 mode=orc.MODE_FP64)
+            _, st = orc.process_response_staged(
+                op, mat.db, mat.pack, mat.a_tilde_agg, mat.t_vec_h,
+                mat.second_dim_a, fd[done % nreq], sd[done % nreq],
+                pk[done % nreq], mode=orc.MODE_FP64, threads=1,
+                condensed_db=cb == 64)
+            stages.append(st)
             done += 1
         el = time.perf_counter() - t0
         line["cpu_baseline"] = {
             "value": done / el, "unit": "queries/s", "cores": 1, "kind": "port",
-            "sample": "%d requests in %.1f s on one host thread (oracle, FP64 "
-                      "FFT path, as the single-threaded reference)" % (done, el)}
+            "sample": "%d requests in %.1f s on one host thread (oracle timing "
+                      "build, FP64 FFT path, as the single-threaded reference)"
+                      % (done, el),
+            "single_core_ms": 1000.0 * el / done,
+            "stages_ms": {k: statistics.mean(x[k] for x in stages)
+                          for k in stages[0]},
+            "build": build_oracle.timing_build_string()}
     print(json.dumps(line))
 
 
@@ -756,8 +856,7 @@ def main():
         split, tune_ms = srv.autotune(B)
         tuned = {"split_k": split, "product_ms": tune_ms}
 
-    # Parity of the two engines on the first requests, and spot rows of the
-    # DB product against an exact host computation.
+    # Parity of the two engines on the first requests.
     check = min(B, 8)
     got_plain = srv.process_arrays(fd[:check], sd[:check], pk[:check],
                                    pir.ENGINE_PLAIN)
@@ -791,6 +890,9 @@ def main():
     hbm, tflops, peak_kind = peaks()
     with ClockSampler(local) as clk:
         ms_step = timed(lambda: step(B, engine), args.steps, args.warmup)
+    # The responses of the last timed step, checked against the oracle once
+    # every timed leg has run.
+    timed_out = t_out.cpu().numpy().view(cdt)
     # Plain single-query engine beside it (B = 1 per step).
     ms_plain = timed(lambda: step(1, pir.ENGINE_PLAIN), args.plain_steps,
                      args.warmup)
@@ -865,13 +967,23 @@ def main():
     for h in wss:
         lib.inspire_pir_workspace_destroy(h)
 
+    # Bit-exact check of the timed batch: first, middle and last response
+    # against the oracle's exact product (a run that fails exits non-zero).
+    picks = sorted({0, B // 2, B - 1})
+    ocheck = oracle_check(params, db, pack, a_tilde, t_vec_h, sda, fd, sd, pk,
+                          timed_out, picks)
+    if ocheck["mismatches"]:
+        raise SystemExit("timed responses %s differ from the oracle"
+                         % ocheck["mismatches"])
+
     rows, cols = db.shape
     db_bytes = db.nbytes + pack.nbytes
     qps = world * B / (ms_step / 1000.0)
     plain_qps = 1000.0 / ms_plain
     line = {
-        "metric": "queries/s (online answer, n=2^20 d=4096 t=8, %s): "
-                  "batched tensor-core vs plain, bit-exact" % ring_tag(),
+        "metric": metric_name(),
+        "comparison": "batched tensor-core engine (value) vs plain "
+                      "single-query engine (plain), responses bit-exact",
         "value": qps, "unit": "queries/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -893,6 +1005,7 @@ def main():
         "peak_kind": peak_kind,
         "clocks": clk.summary(),
         "gpu_launches": kern["launches_per_step"] * args.steps,
+        "oracle_check": ocheck,
         "e2e": {"value": world * B / e2e_s, "unit": "queries/s",
                 "h2d_bytes_per_step": int(h_fd.nbytes + h_sd.nbytes +
                                           h_pk.nbytes),

@@ -158,6 +158,59 @@ noalloc_ntt_u_kernel(const T* __restrict__ u, int chunk_bits, int u_chunks,
   for (int j = threadIdx.x; j < d; j += blockDim.x) out[j] = smem[j];
 }
 
+// Host-side constants of one degree: the primes' 2d-th roots and the
+// NttCtx fields that do not depend on the call (prime count and table
+// address are set per call).
+struct DegreeConsts {
+  RootSet roots;
+  NttCtx ctx;
+};
+
+// Computed once per degree (at most 13 degrees), so that a call costs only
+// its kernel launches; the generators are found once for all degrees.
+const DegreeConsts& ConstsFor(int logd) {
+  static std::once_flag gen_once;
+  static uint32_t generators[kMaxPrimes];
+  std::call_once(gen_once, [] {
+    for (int i = 0; i < kMaxPrimes; ++i) {
+      generators[i] = generator_of(kNoAllocPrimes[i]);
+    }
+  });
+  static std::once_flag once[kNoAllocLogMaxDegree + 1];
+  static DegreeConsts table[kNoAllocLogMaxDegree + 1];
+  std::call_once(once[logd], [logd] {
+    const uint64_t d = 1ull << logd;
+    DegreeConsts& k = table[logd];
+    NttCtx& c = k.ctx;
+    c.logd = logd;
+    for (int i = 0; i < kMaxPrimes; ++i) {
+      const uint32_t p = kNoAllocPrimes[i];
+      const uint64_t psi = pow_mod(generators[i], (p - 1) / (2 * d), p);
+      k.roots.p[i] = p;
+      k.roots.psi[i] = static_cast<uint32_t>(psi);
+      k.roots.psi_inv[i] = static_cast<uint32_t>(pow_mod(psi, p - 2, p));
+      c.p[i] = p;
+      uint32_t x = p;
+      for (int j = 0; j < 5; ++j) x *= 2 - p * x;
+      c.pinv[i] = x;
+      c.half[i] = (p - 1) / 2;
+      const uint64_t r32 = (1ull << 32) % p;
+      c.scale[i] = static_cast<uint32_t>(pow_mod(d, p - 2, p) * r32 % p);
+      c.scale_s[i] = shoup_of(c.scale[i], p);
+      uint64_t prod = 1;
+      for (int j = 0; j < i; ++j) prod *= kNoAllocPrimes[j];
+      c.pm[i] = prod;
+      for (int j = 0; j < kMaxPrimes; ++j) {
+        c.garner[j][i] = j == i ? 0
+                                : static_cast<uint32_t>(
+                                      pow_mod(kNoAllocPrimes[j] % p, p - 2, p) *
+                                      r32 % p);
+      }
+    }
+  });
+  return table[logd];
+}
+
 struct Status {
   int code = INSPIRE_OK;
   std::string msg;
@@ -202,35 +255,10 @@ Status Run(const void* u, const void* v, int n, int d, int logd, int u_bits,
   uint32_t* U = scratch + kTableWords;
   uint32_t* V = U + kOperandWords;
 
-  NttCtx c{};
-  c.logd = logd;
+  const DegreeConsts& k = ConstsFor(logd);
+  NttCtx c = k.ctx;
   c.r = r;
-  RootSet roots{};
-  for (int i = 0; i < kMaxPrimes; ++i) {
-    const uint32_t p = kNoAllocPrimes[i];
-    const uint64_t psi =
-        pow_mod(generator_of(p), (p - 1) / (2ull * d), p);
-    roots.p[i] = p;
-    roots.psi[i] = static_cast<uint32_t>(psi);
-    roots.psi_inv[i] = static_cast<uint32_t>(pow_mod(psi, p - 2, p));
-    c.p[i] = p;
-    uint32_t x = p;
-    for (int k = 0; k < 5; ++k) x *= 2 - p * x;
-    c.pinv[i] = x;
-    c.half[i] = (p - 1) / 2;
-    const uint64_t r32 = (1ull << 32) % p;
-    c.scale[i] = static_cast<uint32_t>(pow_mod(d, p - 2, p) * r32 % p);
-    c.scale_s[i] = shoup_of(c.scale[i], p);
-    uint64_t prod = 1;
-    for (int j = 0; j < i; ++j) prod *= kNoAllocPrimes[j];
-    c.pm[i] = prod;
-    for (int j = 0; j < kMaxPrimes; ++j) {
-      c.garner[j][i] = j == i ? 0
-                              : static_cast<uint32_t>(
-                                    pow_mod(kNoAllocPrimes[j] % p, p - 2, p) *
-                                    r32 % p);
-    }
-  }
+  const RootSet roots = k.roots;
   c.tables = tables;
 
   const int coeff_bits = 8 * static_cast<int>(sizeof(T));

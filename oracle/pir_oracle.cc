@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <chrono>
 #include <thread>
 #include <type_traits>
 #include <vector>
@@ -282,6 +283,70 @@ Status CondensedMultiply(int kind, const void* mat, int64_t rows, int64_t cols,
     out[i] = sum;
   }
   return Status{};
+}
+
+// The condensed DB product as the reference server runs it for a u64
+// CoeffType (the DB is condensed only then, preprocessing_server.h:127-153):
+// Highway's CondensedMultiply<uint16_t> (matrix.cc:261-318) or <uint8_t>
+// (matrix.cc:376-462) de-interleaves the vector once into one array per
+// field of a packed word, then sums field_k(word) * V_k[word] over a row's
+// words in u64 lanes. Here the lanes are the compiler's: the loop over a
+// row's words is a plain reduction that -O3 vectorises (mod-2^64 sums are
+// associative, so the lane split does not change the result).
+template <int kFields>
+void CondensedRows(const uint64_t* words, int64_t wpr, const uint64_t* vt,
+                   uint64_t* out, int64_t row_begin, int64_t row_end) {
+  constexpr int kFieldBits = 64 / kFields;
+  constexpr uint64_t kMask = (uint64_t{1} << kFieldBits) - 1;
+  for (int64_t i = row_begin; i < row_end; ++i) {
+    const uint64_t* row = words + i * wpr;
+    uint64_t acc = 0;
+    for (int64_t j = 0; j < wpr; ++j) {
+      const uint64_t w = row[j];
+      uint64_t s = 0;
+      for (int k = 0; k < kFields; ++k) {
+        s += ((w >> (k * kFieldBits)) & kMask) * vt[k * wpr + j];
+      }
+      acc += s;
+    }
+    out[i] = acc;
+  }
+}
+
+// Condensed product of a u8 / u16 DB with a u64 vector on `threads` threads;
+// false when the shape does not condense (the caller then uses the scalar
+// product, as the reference does for uncondensed matrices).
+bool CondensedDbProduct(int kind, const void* mat, int64_t rows, int64_t cols,
+                        const uint64_t* v, uint64_t* out, int threads) {
+  const int fields = kind == ORC_U16 ? 4 : kind == ORC_U8 ? 8 : 0;
+  if (fields == 0 || cols % fields != 0) return false;
+  const int64_t wpr = cols / fields;
+  std::vector<uint64_t> vt(static_cast<size_t>(cols));
+  for (int64_t j = 0; j < wpr; ++j) {
+    for (int k = 0; k < fields; ++k) vt[k * wpr + j] = v[j * fields + k];
+  }
+  const uint64_t* words = static_cast<const uint64_t*>(mat);
+  auto run = [&](int64_t b, int64_t e) {
+    if (fields == 4) {
+      CondensedRows<4>(words, wpr, vt.data(), out, b, e);
+    } else {
+      CondensedRows<8>(words, wpr, vt.data(), out, b, e);
+    }
+  };
+  if (threads <= 1 || rows < 2 * threads) {
+    run(0, rows);
+    return true;
+  }
+  std::vector<std::thread> pool;
+  const int64_t chunk = (rows + threads - 1) / threads;
+  for (int t = 0; t < threads; ++t) {
+    const int64_t b = t * chunk;
+    const int64_t e = std::min(rows, b + chunk);
+    if (b >= e) break;
+    pool.emplace_back([=] { run(b, e); });
+  }
+  for (auto& th : pool) th.join();
+  return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -584,7 +649,14 @@ Status ProcessResponse(const orc_params& p, int mode, int db_kind,
                        const T* second_dim_a, const T* first_dim,
                        int64_t first_dim_len, const T* second_dim,
                        int64_t second_dim_count, const T* packing_key,
-                       int64_t packing_key_count, T* out, int threads) {
+                       int64_t packing_key_count, T* out, int threads,
+                       double* stage_ms = nullptr, bool condensed_db = false) {
+  using Clock = std::chrono::steady_clock;
+  auto ms_since = [](Clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(Clock::now() - t0)
+        .count();
+  };
+  double db_ms = 0, pack_ms = 0, eval_ms = 0;
   const int d = 1 << p.log_degree;
   const int t = p.interpolation_degree;
   const int l = p.entry_size_multiple;
@@ -628,14 +700,28 @@ Status ProcessResponse(const orc_params& p, int mode, int db_kind,
                 rgsw.begin() + static_cast<size_t>(2 * i + 1) * d);
     }
   }
-  // Stage 1: the DB product with the zero-padded first dimension.
+  // Stage 1: the DB product with the zero-padded first dimension
+  // (timed as the reference's db_mult_time_, pir_server.cc:214-229).
+  const auto t_db = Clock::now();
   std::vector<T> q1(db_cols, 0);
   std::copy(first_dim, first_dim + first_dim_len, q1.begin());
   std::vector<T> b_prime(rows);
-  Status s = MatrixMultiply(db_kind, kBits<T>, db, rows, db_cols, q1.data(),
-                            b_prime.data(), threads);
-  if (!s.ok()) return s;
-  // Stage 2: the packing product with the flattened y_vec_g.
+  Status s;
+  bool condensed = false;
+  if (condensed_db && kBits<T> == 64) {
+    condensed = CondensedDbProduct(
+        db_kind, db, rows, db_cols, reinterpret_cast<const uint64_t*>(q1.data()),
+        reinterpret_cast<uint64_t*>(b_prime.data()), threads);
+  }
+  if (!condensed) {
+    s = MatrixMultiply(db_kind, kBits<T>, db, rows, db_cols, q1.data(),
+                       b_prime.data(), threads);
+    if (!s.ok()) return s;
+  }
+  db_ms = ms_since(t_db);
+  // Stage 2: the packing product with the flattened y_vec_g (packing_time_
+  // starts here, pir_server.cc:237).
+  const auto t_pack = Clock::now();
   if (pack_cols != static_cast<int64_t>(kd) * d) {
     return Error(kInvalidArgument,
                  "Vector size must match the number of matrix columns.");
@@ -656,6 +742,11 @@ Status ProcessResponse(const orc_params& p, int mode, int db_kind,
           packed_b.data() + static_cast<size_t>(i) * d);
       if (!s.ok()) return s;
     }
+    // The reference adds (now - start_pack) once per shard
+    // (pir_server.cc:276), so for l > 1 its packing time counts the earlier
+    // shards again; the same sum is kept here.
+    pack_ms += ms_since(t_pack);
+    const auto t_eval = Clock::now();
     // EvalPoly: Horner from the last coefficient, no LowBits between steps.
     const T* a_slice = a_tilde_agg + static_cast<size_t>(k) * t * d;
     std::copy(a_slice + static_cast<size_t>(t - 1) * d,
@@ -671,12 +762,18 @@ Status ProcessResponse(const orc_params& p, int mode, int db_kind,
         res_b[j] = prod_b[j] + packed_b[static_cast<size_t>(i) * d + j];
       }
     }
+    eval_ms += ms_since(t_eval);
     T* oa = out + static_cast<size_t>(2 * k) * d;
     T* ob = oa + d;
     for (int j = 0; j < d; ++j) {
       oa[j] = RescaleOf(res_a[j], p.log_modulus, p.log_modulus1_after_switch);
       ob[j] = RescaleOf(res_b[j], p.log_modulus, p.log_modulus2_after_switch);
     }
+  }
+  if (stage_ms != nullptr) {
+    stage_ms[0] = db_ms;
+    stage_ms[1] = pack_ms;
+    stage_ms[2] = eval_ms;
   }
   return Status{};
 }
@@ -1120,6 +1217,37 @@ int orc_external_product(const orc_params* prm, int mode, const void* ct_a,
         *prm, mode, static_cast<const uint64_t*>(ct_a),
         static_cast<const uint64_t*>(ct_b), static_cast<const uint64_t*>(rgsw),
         static_cast<uint64_t*>(out_a), static_cast<uint64_t*>(out_b));
+  }
+  return Report(s, err, err_len);
+}
+
+int orc_process_response_staged(
+    const orc_params* prm, int mode, int db_kind, const void* db,
+    int64_t db_cols, int pack_kind, const void* pack, int64_t pack_cols,
+    const void* a_tilde_agg, const void* t_vec_h, const void* second_dim_a,
+    const void* first_dim, int64_t first_dim_len, const void* second_dim,
+    int64_t second_dim_count, const void* packing_key,
+    int64_t packing_key_count, void* out, int threads, int condensed_db,
+    double* stage_ms, char* err, size_t err_len) {
+  Status s;
+  if (prm->coeff_bits == 32) {
+    using T = uint32_t;
+    s = ProcessResponse<T>(
+        *prm, mode, db_kind, db, db_cols, pack_kind, pack, pack_cols,
+        static_cast<const T*>(a_tilde_agg), static_cast<const T*>(t_vec_h),
+        static_cast<const T*>(second_dim_a), static_cast<const T*>(first_dim),
+        first_dim_len, static_cast<const T*>(second_dim), second_dim_count,
+        static_cast<const T*>(packing_key), packing_key_count,
+        static_cast<T*>(out), threads, stage_ms, condensed_db != 0);
+  } else {
+    using T = uint64_t;
+    s = ProcessResponse<T>(
+        *prm, mode, db_kind, db, db_cols, pack_kind, pack, pack_cols,
+        static_cast<const T*>(a_tilde_agg), static_cast<const T*>(t_vec_h),
+        static_cast<const T*>(second_dim_a), static_cast<const T*>(first_dim),
+        first_dim_len, static_cast<const T*>(second_dim), second_dim_count,
+        static_cast<const T*>(packing_key), packing_key_count,
+        static_cast<T*>(out), threads, stage_ms, condensed_db != 0);
   }
   return Report(s, err, err_len);
 }

@@ -123,6 +123,22 @@ int orc_process_response(const orc_params* prm, int mode, int db_kind,
                          int64_t packing_key_count, void* out, char* err,
                          size_t err_len);
 
+// orc_process_response with the reference's stage timers
+// (pir_server.cc:214-285): stage_ms[0] = DB product, [1] = packing (pack
+// product + FinalizeMatrixPack), [2] = EvalPoly, in milliseconds. `threads`
+// splits the two products over host threads (1 = the single-threaded
+// reference); condensed_db != 0 runs a u8 / u16 DB with a u64 CoeffType
+// through the condensed-word product the reference uses for that case
+// (matrix.cc:261-318, 376-462). Used by the CPU baseline.
+int orc_process_response_staged(
+    const orc_params* prm, int mode, int db_kind, const void* db,
+    int64_t db_cols, int pack_kind, const void* pack, int64_t pack_cols,
+    const void* a_tilde_agg, const void* t_vec_h, const void* second_dim_a,
+    const void* first_dim, int64_t first_dim_len, const void* second_dim,
+    int64_t second_dim_count, const void* packing_key,
+    int64_t packing_key_count, void* out, int threads, int condensed_db,
+    double* stage_ms, char* err, size_t err_len);
+
 // Interpolate (crypto/db_row_interpolation.cc:115-228) for one group of t
 // records of d values each, values of width value_bits (8, 16 or 32).
 int orc_interpolate(int value_bits, const void* db_row, int d, int t,

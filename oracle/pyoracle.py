@@ -36,41 +36,59 @@ class OrcParams(ctypes.Structure):
 
 
 _lib = None
+_timing_lib = None
 
 
 def lib():
+    """The checker build of the oracle."""
     global _lib
     if _lib is None:
-        path = build_oracle.build()
-        _lib = ctypes.CDLL(path)
-        vp, i64, ci = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
-        cp, sz = ctypes.c_char_p, ctypes.c_size_t
-        pp = ctypes.POINTER(OrcParams)
-        sigs = {
-            "orc_matrix_multiply": [ci, ci, vp, i64, i64, vp, vp, cp, sz],
-            "orc_condensed_multiply": [ci, vp, i64, i64, vp, vp, ci, cp, sz],
-            "orc_inner_product": [ci, ci, vp, vp, ci, ci, ci, ci, ci, ci, vp,
-                                  cp, sz],
-            "orc_gadget_inv": [ci, vp, ci, ci, ci, ci, vp, cp, sz],
-            "orc_signed_gadget_inv": [ci, vp, ci, ci, ci, ci, vp, cp, sz],
-            "orc_rescale": [ci, vp, ci, ci, ci, vp],
-            "orc_automorph": [ci, vp, ci, ci, vp, cp, sz],
-            "orc_finalize_matrix_pack": [pp, ci, vp, vp, vp, vp, vp, cp, sz],
-            "orc_external_product": [pp, ci, vp, vp, vp, vp, vp, cp, sz],
-            "orc_process_response": [pp, ci, ci, vp, i64, ci, vp, i64, vp, vp,
-                                     vp, vp, i64, vp, i64, vp, i64, vp, cp,
-                                     sz],
-            "orc_interpolate": [ci, vp, ci, ci, ctypes.c_uint32, vp, cp, sz],
-            "orc_preprocess_matrix_pack": [ci, ci, ci, ci, ci, ci, vp, vp, vp,
-                                           vp, vp, vp, vp, vp, cp, sz],
-            "orc_pack": [ci, ci, ci, ci, ci, ci, vp, vp, vp, vp, vp, vp, vp,
-                         cp, sz],
-        }
-        for name, args in sigs.items():
-            fn = getattr(_lib, name)
-            fn.argtypes = args
-            fn.restype = ci
+        _lib = _load(build_oracle.build())
     return _lib
+
+
+def timing_lib():
+    """The timing build (same source, host-tuned flags): the CPU baseline."""
+    global _timing_lib
+    if _timing_lib is None:
+        _timing_lib = _load(build_oracle.build_timing())
+    return _timing_lib
+
+
+def _load(path):
+    """Loads one build of the oracle and sets its signatures."""
+    lb = ctypes.CDLL(path)
+    vp, i64, ci = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    cp, sz = ctypes.c_char_p, ctypes.c_size_t
+    pp = ctypes.POINTER(OrcParams)
+    sigs = {
+        "orc_matrix_multiply": [ci, ci, vp, i64, i64, vp, vp, cp, sz],
+        "orc_condensed_multiply": [ci, vp, i64, i64, vp, vp, ci, cp, sz],
+        "orc_inner_product": [ci, ci, vp, vp, ci, ci, ci, ci, ci, ci, vp,
+                              cp, sz],
+        "orc_gadget_inv": [ci, vp, ci, ci, ci, ci, vp, cp, sz],
+        "orc_signed_gadget_inv": [ci, vp, ci, ci, ci, ci, vp, cp, sz],
+        "orc_rescale": [ci, vp, ci, ci, ci, vp],
+        "orc_automorph": [ci, vp, ci, ci, vp, cp, sz],
+        "orc_finalize_matrix_pack": [pp, ci, vp, vp, vp, vp, vp, cp, sz],
+        "orc_external_product": [pp, ci, vp, vp, vp, vp, vp, cp, sz],
+        "orc_process_response": [pp, ci, ci, vp, i64, ci, vp, i64, vp, vp,
+                                 vp, vp, i64, vp, i64, vp, i64, vp, cp,
+                                 sz],
+        "orc_process_response_staged": [pp, ci, ci, vp, i64, ci, vp, i64,
+                                        vp, vp, vp, vp, i64, vp, i64, vp,
+                                        i64, vp, ci, ci, vp, cp, sz],
+        "orc_interpolate": [ci, vp, ci, ci, ctypes.c_uint32, vp, cp, sz],
+        "orc_preprocess_matrix_pack": [ci, ci, ci, ci, ci, ci, vp, vp, vp,
+                                       vp, vp, vp, vp, vp, cp, sz],
+        "orc_pack": [ci, ci, ci, ci, ci, ci, vp, vp, vp, vp, vp, vp, vp,
+                     cp, sz],
+    }
+    for name, args in sigs.items():
+        fn = getattr(lb, name)
+        fn.argtypes = args
+        fn.restype = ci
+    return lb
 
 
 def _ptr(a):
@@ -265,6 +283,41 @@ def process_response(prm, db, pack, a_tilde_agg, t_vec_h, second_dim_a,
           _ptr(second_dim), second_dim.shape[0], _ptr(packing_key),
           packing_key.shape[0], _ptr(out))
     return out
+
+
+def process_response_staged(prm, db, pack, a_tilde_agg, t_vec_h,
+                            second_dim_a, first_dim, second_dim, packing_key,
+                            mode=MODE_FP64, threads=1, condensed_db=False,
+                            library=None):
+    """process_response with the reference's stage timers (pir_server.cc:
+    214-285). Returns (response, {"db_mult_ms", "packing_ms",
+    "poly_eval_ms"}). library: timing_lib() (default) or lib()."""
+    dt = _cdt(prm.coeff_bits)
+    d = 1 << prm.log_degree
+    kinds = {np.dtype(v): k for k, v in KIND_DTYPE.items()}
+    db = np.ascontiguousarray(db)
+    pack = np.ascontiguousarray(pack)
+    a_tilde_agg = np.ascontiguousarray(a_tilde_agg, dtype=dt)
+    t_vec_h = np.ascontiguousarray(t_vec_h, dtype=dt)
+    if second_dim_a is None or np.size(second_dim_a) == 0:
+        second_dim_a = np.zeros((0, d), dtype=dt)
+    second_dim_a = np.ascontiguousarray(second_dim_a, dtype=dt)
+    first_dim = np.ascontiguousarray(first_dim, dtype=dt)
+    second_dim = np.ascontiguousarray(second_dim, dtype=dt).reshape(-1, d)
+    packing_key = np.ascontiguousarray(packing_key, dtype=dt).reshape(-1, d)
+    out = np.zeros((prm.entry_size_multiple, 2, d), dtype=dt)
+    stages = np.zeros(3, dtype=np.float64)
+    lb = library or timing_lib()
+    _call(lb.orc_process_response_staged, ctypes.byref(prm), mode,
+          kinds[db.dtype], _ptr(db), db.shape[1], kinds[pack.dtype],
+          _ptr(pack), pack.shape[1], _ptr(a_tilde_agg), _ptr(t_vec_h),
+          _ptr(second_dim_a), _ptr(first_dim), first_dim.shape[0],
+          _ptr(second_dim), second_dim.shape[0], _ptr(packing_key),
+          packing_key.shape[0], _ptr(out), int(threads), int(condensed_db),
+          _ptr(stages))
+    return out, {"db_mult_ms": float(stages[0]),
+                 "packing_ms": float(stages[1]),
+                 "poly_eval_ms": float(stages[2])}
 
 
 def interpolate(db_row, d, t, plaintext_modulus):

@@ -24,11 +24,11 @@ pytestmark = pytest.mark.gpu
 P = 65535
 
 
-def _params(d, t, n, l=1, log_q=56, bits=64):
+def _params(d, t, n, l=1, log_q=56, bits=64, variance=6):
     log_d = d.bit_length() - 1
     rl = pir.RlweParams(degree=d, log_modulus=log_q,
                         log_modulus1_after_switch=16 + log_d + 2,
-                        log_modulus2_after_switch=16 + 2, variance=6,
+                        log_modulus2_after_switch=16 + 2, variance=variance,
                         coeff_bits=bits)
     return pir.PirParams(rlwe=rl, plaintext_modulus=P,
                          pack_gadget=pir.GadgetParams(19, 2),
@@ -76,6 +76,51 @@ def test_decrypted_records_equal_database(d, t, n, l, engine):
     for b in range(batch):
         assert np.array_equal(got[b].astype(np.int64),
                               db_raw[idx[b]].astype(np.int64)), (b, idx[b])
+
+
+@pytest.mark.parametrize("engine", [pir.ENGINE_PLAIN, pir.ENGINE_TENSOR])
+def test_metrics_tool_default_parameters_decrypt(engine):
+    """The reference metrics tool's default set (pir_metrics_tool.cc:74-114):
+    d = 2048, n = 4096, t = 2, l = 1, q = 2^52, error variance 40, u64
+    words, the tool's fixed index 123 among the requests. Every record
+    decrypts to the DB row and every response equals the oracle's."""
+    from oracle import pyoracle as orc
+    d, t, n = 2048, 2, 4096
+    params = _params(d, t, n, log_q=52, variance=40)
+    rng = np.random.default_rng(123)
+    db_raw = rng.integers(0, P, (n, d), dtype=np.uint16)
+    a = _a_components(params, seed=13)
+    pre = pir.PreprocessingServer.Create(params, a).Preprocess(db_raw)
+    server = pir.PirServer.Create(params, pre)
+    batch = 16
+    client = pir.PirClient.Create(params, a, clients=batch, seed=7,
+                                  variance=40)
+    idx = rng.integers(0, n, batch)
+    idx[0], idx[1], idx[2] = 123, 0, n - 1
+    fd, sd, pk = client.CreateRequests(idx)
+    responses = server.process_arrays(fd, sd, pk, engine)
+    got = client.ProcessResponses(responses)
+    for b in range(batch):
+        assert np.array_equal(got[b].astype(np.int64),
+                              db_raw[idx[b]].astype(np.int64)), (b, idx[b])
+    r = params.rlwe
+    op = orc.make_params(
+        coeff_bits=64, log_degree=11, log_modulus=52,
+        log_modulus1_after_switch=r.log_modulus1_after_switch,
+        log_modulus2_after_switch=r.log_modulus2_after_switch,
+        pack_log_digit=19, pack_num_digits=2, eval_log_digit=19,
+        eval_num_digits=3, num_entries=n, interpolation_degree=t,
+        entry_size_multiple=1)
+    db = np.concatenate(pre.db_matrices, axis=0)
+    packm = np.concatenate([o.matrix for o in pre.preprocessed_outputs[0]],
+                           axis=0)
+    a_t = np.stack([o.a_tilde_agg for o in pre.preprocessed_outputs[0]])
+    t_h = np.concatenate([o.t_vec_h for o in pre.preprocessed_outputs[0]],
+                         axis=0)
+    for b in (0, batch - 1):
+        want = orc.process_response(op, db, packm, a_t, t_h, pre.second_dim_a,
+                                    fd[b], sd[b], pk[b])
+        assert np.array_equal(responses[b], want), b
 
 
 def test_client_rejects_bad_index():

@@ -161,9 +161,9 @@ def test_tensor_products_match_exact_integer_gemm():
 
 
 @pytest.mark.parametrize("batch", [128, 192, 256])
-def test_tensor_cluster_shapes(batch):
-    # The request tiles of a row pair share their DB / pack tiles through
-    # cluster multicast: 2 tiles (128 requests), none (192: 3 tiles), 4 (256).
+def test_tensor_request_tile_counts(batch):
+    # 2, 3 and 4 request tiles per row pair; each tile's CTA issues its own
+    # TMA loads of the DB / pack tiles (no multicast).
     params = synthetic.make_params(d=128, n=2 * 8192, t=2, coeff_bits=32)
     mat = synthetic.make_material(params, seed=batch)
     srv = _server(params, mat)

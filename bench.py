@@ -158,7 +158,7 @@ def cpu_reference_profile(params, db, pack, a_tilde, t_vec_h, sda, fd, sd,
     runs it: mean latency and the reference's stage split (DB mult, packing,
     poly-eval; pir_server.cc:214-285, printed by pir_metrics_tool.cc:435-447).
     """
-    from oracle import build_oracle, pyoracle as orc
+    from oracle import pyoracle as orc
     op = oracle_params(params)
     condensed = params.rlwe.coeff_bits == 64
     lat, stages = [], []
@@ -173,7 +173,7 @@ def cpu_reference_profile(params, db, pack, a_tilde, t_vec_h, sda, fd, sd,
     mean = {k: statistics.mean(s[k] for s in stages) for k in stages[0]}
     return {"single_core_ms": statistics.mean(lat),
             "stages_ms": mean,
-            "build": build_oracle.timing_build_string(),
+            "build": orc.timing_build_string(),
             "db_product": "condensed u64 words (matrix.cc:261-318)"
                           if condensed else
                           "scalar u32 loop (matrix.h:183-194; the reference "
@@ -740,7 +740,6 @@ def run_single_workload(args):
                 "d2h_bytes_per_step": int(h_out[0].nbytes)},
     }
     if not args.no_cpu_baseline:
-        from oracle import build_oracle
         done, t0 = 0, time.perf_counter()
         stages = []
         while time.perf_counter() - t0 < 10.0:
@@ -760,7 +759,7 @@ def run_single_workload(args):
             "single_core_ms": 1000.0 * el / done,
             "stages_ms": {k: statistics.mean(x[k] for x in stages)
                           for k in stages[0]},
-            "build": build_oracle.timing_build_string()}
+            "build": orc.timing_build_string()}
     print(json.dumps(line))
 
 

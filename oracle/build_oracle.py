@@ -28,24 +28,42 @@ CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off",
 # Arm "CPU part" numbers of cores with a matching -mcpu name.
 _ARM_PARTS = {"0xd4f": "neoverse-v2", "0xd40": "neoverse-v1",
               "0xd0c": "neoverse-n1", "0xd49": "neoverse-n2"}
+# Optional extensions of those cores (gcc name, /proc/cpuinfo flag): the
+# ones the kernel does not report are switched off, since a host (or a
+# virtual machine) may hide some, and code using them would trap.
+_ARM_EXTS = [("sve", "sve"), ("sve2", "sve2"), ("i8mm", "i8mm"),
+             ("bf16", "bf16"), ("dotprod", "asimddp"), ("fp16", "asimdhp"),
+             ("rng", "rng"), ("memtag", "mte"), ("sb", "sb"),
+             ("ssbs", "ssbs"), ("pauth", "paca"), ("crypto", "aes"),
+             ("lse", "atomics"), ("rcpc", "lrcpc"), ("flagm", "flagm")]
+
+
+def _cpuinfo():
+    part, feats = None, set()
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key == "cpu part" and part is None:
+                    part = line.split(":")[1].strip().lower()
+                elif key == "features" and not feats:
+                    feats = set(line.split(":")[1].split())
+    except OSError:
+        pass
+    return part, feats
 
 
 def timing_target_flags():
     """Target flags of the timing build for this host: an -mcpu named for
-    the host's Arm core when it is a known one, else none."""
+    the host's Arm core when it is a known one, minus the extensions the
+    host does not report; else none."""
     if platform.machine() not in ("aarch64", "arm64"):
         return []
-    try:
-        with open("/proc/cpuinfo") as f:
-            for line in f:
-                if line.lower().startswith("cpu part"):
-                    part = line.split(":")[1].strip().lower()
-                    if part in _ARM_PARTS:
-                        return ["-mcpu=" + _ARM_PARTS[part]]
-                    break
-    except OSError:
-        pass
-    return []
+    part, feats = _cpuinfo()
+    if part not in _ARM_PARTS or not feats:
+        return []
+    off = "".join("+no" + ext for ext, flag in _ARM_EXTS if flag not in feats)
+    return ["-mcpu=" + _ARM_PARTS[part] + off]
 
 
 def _stale(path):
@@ -76,9 +94,13 @@ def build(force=False, verbose=False):
 
 
 def build_timing(force=False, verbose=False):
-    """Compile the timing flavour (same source, host-tuned target flags)."""
-    return _compile(TIMING_LIB_PATH, CXXFLAGS + timing_target_flags(), force,
-                    verbose)
+    """Compile the timing flavour (same source, host-tuned target flags;
+    without them if the compiler refuses the flags)."""
+    try:
+        return _compile(TIMING_LIB_PATH, CXXFLAGS + timing_target_flags(),
+                        force, verbose)
+    except subprocess.CalledProcessError:
+        return _compile(TIMING_LIB_PATH, CXXFLAGS, True, verbose)
 
 
 def timing_build_string():

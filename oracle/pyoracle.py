@@ -47,12 +47,65 @@ def lib():
     return _lib
 
 
+TIMING_FALLBACK = None  # why the checker build stands in for the timing one
+
+
+def _timing_build_runs(path):
+    """Runs a small staged request through the timing build in a child
+    process: a build whose target flags the host cannot execute traps
+    there, not in the caller."""
+    import subprocess
+    import sys
+    code = ("import numpy as np, ctypes\n"
+            "from oracle import pyoracle as o\n"
+            "lb = o._load(%r)\n"
+            "d = 64\n"
+            "p = o.make_params(coeff_bits=64, log_degree=6, log_modulus=52,"
+            " log_modulus1_after_switch=24, log_modulus2_after_switch=18,"
+            " pack_log_digit=19, pack_num_digits=2, eval_log_digit=19,"
+            " eval_num_digits=3, num_entries=256, interpolation_degree=2,"
+            " entry_size_multiple=1)\n"
+            "r = np.random.default_rng(1)\n"
+            "u = lambda *s: r.integers(0, 1 << 52, size=s, dtype=np.uint64)\n"
+            "db = r.integers(0, 65535, size=(2 * d, 128), dtype=np.uint16)\n"
+            "pk = r.integers(-1000, 1000, size=(2 * d, 2 * d), dtype=np.int32)\n"
+            "for c in (0, 1):\n"
+            "    o.process_response_staged(p, db, pk, u(2, d), u(4, d),"
+            " u(6, d), u(128), u(6, d), u(4, d), threads=2, condensed_db=c,"
+            " library=lb)\n"
+            "p.coeff_bits, p.log_modulus = 32, 32\n"
+            "w = lambda *s: u(*s).astype(np.uint32)\n"
+            "o.process_response_staged(p, db, pk, w(2, d), w(4, d), w(6, d),"
+            " w(128), w(6, d), w(4, d), threads=2, library=lb)\n" % path)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], cwd=root,
+                       capture_output=True, text=True, timeout=300)
+    return r.returncode == 0, (r.stderr.strip().splitlines() or [""])[-1]
+
+
 def timing_lib():
-    """The timing build (same source, host-tuned flags): the CPU baseline."""
-    global _timing_lib
+    """The timing build (same source, host-tuned flags): the CPU baseline.
+    If that build cannot run on this host, the checker build is timed
+    instead and TIMING_FALLBACK says why."""
+    global _timing_lib, TIMING_FALLBACK
     if _timing_lib is None:
-        _timing_lib = _load(build_oracle.build_timing())
+        path = build_oracle.build_timing()
+        ok, why = _timing_build_runs(path)
+        if ok:
+            _timing_lib = _load(path)
+        else:
+            TIMING_FALLBACK = "timing build failed its self-check (%s)" % why
+            _timing_lib = lib()
     return _timing_lib
+
+
+def timing_build_string():
+    """The compiler flags of the library timing_lib() returns."""
+    timing_lib()
+    if TIMING_FALLBACK:
+        return ("g++ -O3 -ffp-contract=off (no target flags: %s)"
+                % TIMING_FALLBACK)
+    return build_oracle.timing_build_string()
 
 
 def _load(path):

@@ -187,6 +187,25 @@ int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,
                                 char* err, size_t err_len);
 
 /*
+ * Stage 1 of a device-resident batch on the tensor engine in a given form
+ * (no reference counterpart: the forms are this build's two layouts of the
+ * same product). form INSPIRE_FORM_PLANES reads the DB as resident fp16
+ * digit planes, INSPIRE_FORM_RAW reads the DB as stored (u16) and splits it
+ * into digits in shared memory; split > 0 forces that split-K factor (0:
+ * the tuned or heuristic one). Same buffers and result as
+ * inspire_pir_products_device with INSPIRE_ENGINE_TENSOR.
+ * FAILED_PRECONDITION when the server has no such form.
+ */
+#define INSPIRE_FORM_PLANES 0
+#define INSPIRE_FORM_RAW 1
+int inspire_pir_tensor_products_device(inspire_pir_server* server,
+                                       int32_t batch, const void* first_dim,
+                                       const void* packing_key, void* out,
+                                       int32_t form, int32_t split,
+                                       void* stream, char* err,
+                                       size_t err_len);
+
+/*
  * The packing step of a device-resident batch, as the packing benchmark's
  * server loop runs it (crypto/pir/benchmarking/pir_packing_metrics_tool.cc:
  * 226-283): DB * q1 + P * y_g, then FinalizeMatrixPack

@@ -93,6 +93,18 @@ constexpr int kBSlots = 3;
 constexpr int kBHalves = kStagesPerUnit / 2;               // request slots per unit
 constexpr int kRingBytes = kRowBlocks * kARingBytes + kBSlots * kBSlotBytes;  // 224 KB
 constexpr int kThreads = 384;
+// The converting form (a u16 DB read as it is stored): a fourth warpgroup
+// (warps 12-15) turns each raw 128-row x 32-column u16 tile, loaded by TMA
+// into the first half of its A box, into the box's two fp16 digit planes.
+constexpr int kConvThreads = 128;
+constexpr int kThreadsConv = kThreads + kConvThreads;
+constexpr int kRawTileBytes = kBlockRows * kStageK * 2;    // 8 KB
+// Register split of the converting form, per warpgroup (128 threads each):
+// producer / MMA / allocator, two epilogue groups, converter. The launch
+// holds 512 threads x 128 registers = 65536; the split sums to the same.
+constexpr int kRegsCtl = 56, kRegsEpi = 176, kRegsConv = 104;
+static_assert(kRegsCtl + 2 * kRegsEpi + kRegsConv == 4 * 128,
+              "register split of the converting form");
 constexpr int kTmemCols = 512;     // one 256-column accumulator per row block
 constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr size_t kSmemBytes = kRingBytes + 1024 + 256;
@@ -225,6 +237,50 @@ __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// Generic-proxy shared-memory writes become visible to the async proxy (the
+// tensor core's operand reads).
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Barrier 1 among the converter warpgroup only.
+__device__ __forceinline__ void conv_bar() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kConvThreads) : "memory");
+}
+
+__device__ __forceinline__ uint4 lds128(uint32_t addr) {
+  uint4 v;
+  asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "r"(addr)
+               : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void sts128(uint32_t addr, uint4 v) {
+  asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x),
+               "r"(v.y), "r"(v.z), "r"(v.w)
+               : "memory");
+}
+
+// Two u16 DB entries x (one per 16-bit half of w) -> their balanced digits
+// x - 2^15 = x0 + 2^8 x1 as half2 pairs. With b0, b1 the bytes of x:
+// x0 + 128 = b0 ^ 0x80 in [0, 255] and x1 + 128 = b1 + (b0 >> 7) in
+// [0, 256]; 0x6400 | v is the fp16 encoding of 1024 + v for v < 1024, so
+// one fp16 subtraction of 1152 = 1024 + 128 gives each digit exactly.
+__device__ __forceinline__ void u16_digits(uint32_t w, uint32_t& d0,
+                                           uint32_t& d1) {
+  const uint32_t h0 = (w & 0x00FF00FFu) ^ 0x64806480u;
+  const uint32_t h1 = __byte_perm(w, 0u, 0x4341) + ((w >> 7) & 0x00010001u) +
+                      0x64006400u;
+  const __half2 off = __halves2half2(__ushort_as_half(0x6480),
+                                     __ushort_as_half(0x6480));
+  const __half2 x0 = __hsub2(*reinterpret_cast<const __half2*>(&h0), off);
+  const __half2 x1 = __hsub2(*reinterpret_cast<const __half2*>(&h1), off);
+  d0 = *reinterpret_cast<const uint32_t*>(&x0);
+  d1 = *reinterpret_cast<const uint32_t*>(&x1);
+}
+
 // Instruction descriptor of kind::f16: fp16 A/B, fp32 D, both K-major.
 __host__ __device__ constexpr uint32_t instr_desc(int n, int m) {
   return (1u << 4) | (static_cast<uint32_t>(n >> 3) << 17) |
@@ -277,6 +333,8 @@ struct UnitSrc {
   const CUtensorMap* am;
   const CUtensorMap* bm;
   int ax, a_step, bx, nb;
+  int kind;  // 0: DB unit, 1 / 2: low / high pack planes
+  int rx;    // DB column of step 0 (raw u16 tiles of the converting form)
 };
 
 template <int NQ>
@@ -294,12 +352,19 @@ __device__ __forceinline__ UnitSrc unit_src(int u, int n_db_units,
   r.ax = kb * kStagesPerUnit * r.a_step + (kind == 2 ? 2 * kStageK : 0);
   r.bx = kb * kUnitK;
   r.nb = kind == 2 ? NQ - 2 : NQ;
+  r.kind = kind;
+  r.rx = kb * kUnitK;
   return r;
 }
 
-template <int NQ>
-__global__ void __launch_bounds__(kThreads, 1)
+// CONV = false: the DB comes as resident fp16 digit planes (tm_db). CONV =
+// true: the DB comes as stored, u16 (tm_raw), and the converter warpgroup
+// writes each A box's digit planes from its raw tile (pack units keep
+// their planes in both forms).
+template <int NQ, bool CONV>
+__global__ void __launch_bounds__(CONV ? kThreadsConv : kThreads, 1)
 limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
+                 const __grid_constant__ CUtensorMap tm_raw,
                  const __grid_constant__ CUtensorMap tm_pk,
                  const __grid_constant__ CUtensorMap tm_q,
                  const __grid_constant__ CUtensorMap tm_y, LimbArgs a,
@@ -318,7 +383,9 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   uint64_t* acc_full = b_empty + kBSlots;
   uint64_t* acc_empty = acc_full + kRowBlocks;
   uint64_t* mma_done = acc_empty + kRowBlocks;
-  uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
+  uint64_t* raw_full = mma_done + 1;                                     // [rb][pair]
+  uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(raw_full + kRowBlocks * kAPairs);
+  volatile int* conv_go = reinterpret_cast<volatile int*>(tmem_base_slot + 1);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -352,6 +419,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       mbar_init(&acc_empty[b], 4);
     }
     mbar_init(mma_done, 1);
+    for (int s = 0; s < kRowBlocks * kAPairs; ++s) mbar_init(&raw_full[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 2) tmem_alloc(tmem_base_slot, kTmemCols);
@@ -365,26 +433,49 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   // row-block pass before it is read again; request half n of unit i (steps
   // 2n, 2n+1) lives in slot (kBHalves * i + n) % kBSlots, refilled after
   // row block 1 has read its previous half.
+  // In the converting form registers move from the control and converter
+  // warpgroups to the two epilogue groups (kRegsCtl / kRegsEpi /
+  // kRegsConv), each warpgroup at the top of its role.
+  if (warp < 4) {
+  if constexpr (CONV) {
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kRegsCtl));
+  }
   if (warp == 0 && lane == 0) {
     // ---------------------------------------------------- TMA producer --
     // Loads go out in the order the MMA pipe frees their buffers: the row
     // block 0 boxes of the unit, then per pair its request half and its row
     // block 1 boxes.
     int a_last[kRowBlocks * kAPairs];
+    bool a_raw[kRowBlocks * kAPairs];
     int b_last[kBSlots];
-    for (int s = 0; s < kRowBlocks * kAPairs; ++s) a_last[s] = -1;
+    for (int s = 0; s < kRowBlocks * kAPairs; ++s) {
+      a_last[s] = -1;
+      a_raw[s] = false;
+    }
     for (int s = 0; s < kBSlots; ++s) b_last[s] = -1;
     bool ok = true;
     auto load_pair = [&](int rb, int p, const UnitSrc& src, int i) {
       const int s = rb * kAPairs + p;
       if (!mbar_wait(&a_empty[s], (i & 1) ^ 1, err)) return false;
-      mbar_expect_tx(&a_full[s], 2 * kABoxBytes);
-      for (int hh = 0; hh < 2; ++hh) {
-        const int h = 2 * p + hh;
-        tma_load_2d(src.am, &a_full[s], smem + rb * kARingBytes + h * kABoxBytes,
-                    src.ax + h * src.a_step, row0 + rb * kBlockRows);
+      const bool raw = CONV && src.kind == 0;
+      if (raw) {
+        // Raw u16 tiles into the first half of each box, for the converter.
+        mbar_expect_tx(&raw_full[s], 2 * kRawTileBytes);
+        for (int hh = 0; hh < 2; ++hh) {
+          const int h = 2 * p + hh;
+          tma_load_2d(&tm_raw, &raw_full[s], smem + rb * kARingBytes + h * kABoxBytes,
+                      src.rx + h * kStageK, row0 + rb * kBlockRows);
+        }
+      } else {
+        mbar_expect_tx(&a_full[s], 2 * kABoxBytes);
+        for (int hh = 0; hh < 2; ++hh) {
+          const int h = 2 * p + hh;
+          tma_load_2d(src.am, &a_full[s], smem + rb * kARingBytes + h * kABoxBytes,
+                      src.ax + h * src.a_step, row0 + rb * kBlockRows);
+        }
       }
       a_last[s] = i;
+      a_raw[s] = raw;
       return true;
     };
     for (int i = 0; i < nu && ok; ++i) {
@@ -409,7 +500,9 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     }
     // Drain: every copy this thread issued has landed before the CTA exits.
     for (int s = 0; s < kRowBlocks * kAPairs; ++s) {
-      if (a_last[s] >= 0) mbar_wait(&a_full[s], a_last[s] & 1, nullptr);
+      if (a_last[s] >= 0) {
+        mbar_wait(a_raw[s] ? &raw_full[s] : &a_full[s], a_last[s] & 1, nullptr);
+      }
     }
     for (int s = 0; s < kBSlots; ++s) {
       if (b_last[s] >= 0) mbar_wait(&b_full[s], (b_last[s] / kBSlots) & 1, nullptr);
@@ -481,7 +574,77 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     }
     mma_commit(mma_done);
     mbar_wait(mma_done, 0, nullptr);
-  } else if (warp >= 4) {
+  }
+  } else if (CONV && warp >= 12) {
+    if constexpr (CONV) {
+      asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kRegsConv));
+    }
+    // ------------------------------------------------------- converter --
+    // Per box pair of a DB unit, in the order the MMA pipe reads them: one
+    // thread waits for the raw tiles (bounded) and shares the outcome; all
+    // 128 threads load the two raw tiles (16 bytes per thread per access,
+    // four accesses per tile), meet, then write both boxes' digit planes
+    // over them (in place, hence the barrier between reads and writes),
+    // fence them for the tensor core and meet again before one thread
+    // marks the pair full. Thread t takes the 16-byte units
+    // g = 128 k + t: row r = (g & 7) | (g >> 5) << 3, unit u = (g >> 3) & 3
+    // (eight K values). Eight consecutive lanes cover eight consecutive rows
+    // of one unit, so both the raw reads (64-byte rows, 64-byte swizzle:
+    // unit u at u ^ ((r >> 1) & 3)) and the plane writes (128-byte rows,
+    // 128-byte swizzle: unit v at v ^ (r & 7); x0 in units 0-3, x1 in 4-7)
+    // hit eight different bank groups.
+    const int t = threadIdx.x - kThreads;
+    const uint32_t ring = smem_addr(smem);
+    bool ok = true;
+    for (int i = 0; i < nu && ok; ++i) {
+      if (unit_kind(u0 + i, a.n_db_units) != 0) break;  // DB units come first
+      for (int rb = 0; rb < kRowBlocks && ok; ++rb) {
+        for (int p = 0; p < kAPairs; ++p) {
+          const int s = rb * kAPairs + p;
+          if (t == 0) *conv_go = mbar_wait(&raw_full[s], i & 1, err) ? 1 : 0;
+          conv_bar();
+          if (*conv_go == 0) {
+            ok = false;
+            break;
+          }
+          uint4 raw[2][4];
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            const uint32_t box = ring + rb * kARingBytes + (2 * p + hh) * kABoxBytes;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const int g = 128 * k + t;
+              const int r = (g & 7) | ((g >> 5) << 3), u = (g >> 3) & 3;
+              raw[hh][k] = lds128(box + r * 64 + ((u ^ ((r >> 1) & 3)) << 4));
+            }
+          }
+          conv_bar();
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            const uint32_t box = ring + rb * kARingBytes + (2 * p + hh) * kABoxBytes;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const int g = 128 * k + t;
+              const int r = (g & 7) | ((g >> 5) << 3), u = (g >> 3) & 3;
+              uint4 x0, x1;
+              u16_digits(raw[hh][k].x, x0.x, x1.x);
+              u16_digits(raw[hh][k].y, x0.y, x1.y);
+              u16_digits(raw[hh][k].z, x0.z, x1.z);
+              u16_digits(raw[hh][k].w, x0.w, x1.w);
+              sts128(box + r * 128 + ((u ^ (r & 7)) << 4), x0);
+              sts128(box + r * 128 + (((4 + u) ^ (r & 7)) << 4), x1);
+            }
+          }
+          fence_proxy_async_smem();
+          conv_bar();
+          if (t == 0) mbar_arrive(&a_full[s]);
+        }
+      }
+    }
+  } else {
+    if constexpr (CONV) {
+      asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kRegsEpi));
+    }
     // -------------------------------------------------------- epilogue --
     const int e = (warp - 4) / 4;   // row block
     const int ew = (warp - 4) % 4;  // TMEM lanes 32*ew .. 32*ew+31
@@ -747,6 +910,26 @@ bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols,
   return r == CUDA_SUCCESS;
 }
 
+// The u16 DB as stored, [rows][cols]: boxes of 128 rows x 32 columns
+// (64-byte rows, 64-byte swizzle), zero fill past the last column. Needs
+// rows of a multiple of 16 bytes (cols % 8 == 0).
+bool make_raw_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols) {
+  auto fn = encode_fn();
+  if (fn == nullptr || cols % 8 != 0 ||
+      (reinterpret_cast<uintptr_t>(base) & 15) != 0) {
+    return false;
+  }
+  cuuint64_t dims[2] = {cols, rows};
+  cuuint64_t strides[1] = {cols * 2};
+  cuuint32_t box[2] = {static_cast<cuuint32_t>(kStageK), static_cast<cuuint32_t>(kBlockRows)};
+  cuuint32_t elem[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void*>(base), dims,
+                  strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
 class LimbScratchImpl : public LimbScratch {
@@ -771,8 +954,11 @@ class LimbGemmImpl : public LimbGemm {
     if (err_) cudaFree(err_);
   }
 
+  // planes: also keep the DB's fp16 digit planes resident (2x the DB's
+  // bytes), so that both forms of the kernel can run and the autotuner
+  // picks per batch size. Without them the DB is read as stored.
   bool Init(int nq, const void* db, int64_t rows, int64_t db_cols, int mat_kind,
-            const void* pack, int64_t pack_cols) {
+            const void* pack, int64_t pack_cols, bool planes) {
     nq_ = nq;
     tq_ = kBRows / nq;
     word_ = nq == 4 ? 4 : 8;
@@ -781,29 +967,41 @@ class LimbGemmImpl : public LimbGemm {
     pk_cols_ = pack_cols;
     cpad_ = round_up(db_cols, kUnitK);
     kpad_ = round_up(pack_cols, kUnitK);
+    conv_ = make_raw_map(&tm_raw_, db, rows, db_cols);
+    if (!conv_) planes = true;  // rows not 16-byte multiples: planes only
     if (cudaMalloc(&err_, sizeof(int)) != cudaSuccess) return false;
     if (cudaMemset(err_, 0, sizeof(int)) != cudaSuccess) return false;
-    if (cudaMalloc(&db_planes_, 2ull * rows * cpad_ * 2) != cudaSuccess) return false;
+    if (planes) {
+      if (cudaMalloc(&db_planes_, 2ull * rows * cpad_ * 2) != cudaSuccess) return false;
+      split_u16_kernel<<<152 * 16, 256>>>(static_cast<const uint16_t*>(db), rows,
+                                          db_cols, cpad_, db_planes_);
+    }
     if (cudaMalloc(&pk_planes_, 4ull * rows * kpad_ * 2) != cudaSuccess) return false;
-    split_u16_kernel<<<152 * 16, 256>>>(static_cast<const uint16_t*>(db), rows,
-                                        db_cols, cpad_, db_planes_);
     split_u32_kernel<<<152 * 16, 256>>>(pack, mat_kind, rows, pack_cols, pack_cols,
                                         rows, rows, kpad_, pk_planes_, 1, nq == 8 ? 1 : 0);
     if (cudaDeviceSynchronize() != cudaSuccess) return false;
-    if (!make_map(&tm_db_, db_planes_, rows, 2ull * cpad_, kBlockRows, 2 * kStageK)) return false;
+    if (planes &&
+        !make_map(&tm_db_, db_planes_, rows, 2ull * cpad_, kBlockRows, 2 * kStageK)) {
+      return false;
+    }
     if (!make_map(&tm_pk_, pk_planes_, rows, 4ull * kpad_, kBlockRows, 2 * kStageK)) return false;
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev);
-    const cudaError_t fe =
-        nq == 4 ? cudaFuncSetAttribute(limb_gemm_kernel<4>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(kSmemBytes))
-                : cudaFuncSetAttribute(limb_gemm_kernel<8>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(kSmemBytes));
-    if (fe != cudaSuccess) return false;
-    return true;
+    const int smem = static_cast<int>(kSmemBytes);
+    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t fe = nq == 4 ? cudaFuncSetAttribute(limb_gemm_kernel<4, false>, attr, smem)
+                             : cudaFuncSetAttribute(limb_gemm_kernel<8, false>, attr, smem);
+    if (fe == cudaSuccess && conv_) {
+      fe = nq == 4 ? cudaFuncSetAttribute(limb_gemm_kernel<4, true>, attr, smem)
+                   : cudaFuncSetAttribute(limb_gemm_kernel<8, true>, attr, smem);
+    }
+    return fe == cudaSuccess;
+  }
+
+  // Resident device bytes of the engine (digit planes).
+  int64_t ResidentBytes() const override {
+    return (db_planes_ ? 2 * rows_ * cpad_ * 2 : 0) + 4 * rows_ * kpad_ * 2;
   }
 
   std::unique_ptr<LimbScratch> NewScratch() override {
@@ -847,7 +1045,15 @@ class LimbGemmImpl : public LimbGemm {
   cudaError_t Run(int batch, const void* q1, int64_t q1_stride, const void* yg,
                   int64_t yg_stride, void* out, LimbScratch* scratch,
                   cudaStream_t st) override {
-    return Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, 0);
+    return Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, 0, -1);
+  }
+
+  cudaError_t RunForm(int batch, const void* q1, int64_t q1_stride, const void* yg,
+                      int64_t yg_stride, void* out, LimbScratch* scratch,
+                      cudaStream_t st, int form, int split) override {
+    if (form == kFormRaw && !conv_) return cudaErrorNotSupported;
+    if (form == kFormPlanes && !db_planes_) return cudaErrorNotSupported;
+    return Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, split, form);
   }
 
   // Times every split-K factor that keeps at least 8 K units per CTA and at
@@ -856,7 +1062,8 @@ class LimbGemmImpl : public LimbGemm {
   // batch size. Synchronises `st`.
   cudaError_t Tune(int batch, const void* q1, int64_t q1_stride, const void* yg,
                    int64_t yg_stride, void* out, LimbScratch* scratch,
-                   cudaStream_t st, int* chosen, float* best_ms) override {
+                   cudaStream_t st, int* chosen, int* chosen_form,
+                   float* best_ms) override {
     if (batch <= 0) return cudaErrorInvalidValue;
     const int64_t bpad = round_up(batch, tq_);
     const int64_t tiles = (rows_ / kTileRows) * (bpad / tq_);
@@ -871,26 +1078,30 @@ class LimbGemmImpl : public LimbGemm {
       cudaEventDestroy(e0);
       return e;
     }
-    int best = heuristic;
+    int best = heuristic, best_form = DefaultForm();
     float best_t = 0;
-    for (int k = 1; k <= 16 && e == cudaSuccess; ++k) {
-      if (n_units / k < 8) break;
-      const int64_t items = tiles * k;
-      const int64_t waves = (items + sms - 1) / sms;
-      const double eff = static_cast<double>(items) / (waves * sms);
-      if (k != heuristic && eff < 0.8) continue;
-      e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, k);
-      if (e == cudaSuccess) e = cudaEventRecord(e0, st);
-      for (int r = 0; r < 2 && e == cudaSuccess; ++r) {
-        e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, k);
-      }
-      if (e == cudaSuccess) e = cudaEventRecord(e1, st);
-      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-      float ms = 0;
-      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-      if (e == cudaSuccess && (best_t == 0 || ms < best_t)) {
-        best_t = ms;
-        best = k;
+    for (int form = kFormPlanes; form <= kFormRaw && e == cudaSuccess; ++form) {
+      if ((form == kFormRaw && !conv_) || (form == kFormPlanes && !db_planes_)) continue;
+      for (int k = 1; k <= 16 && e == cudaSuccess; ++k) {
+        if (n_units / k < 8) break;
+        const int64_t items = tiles * k;
+        const int64_t waves = (items + sms - 1) / sms;
+        const double eff = static_cast<double>(items) / (waves * sms);
+        if (k != heuristic && eff < 0.8) continue;
+        e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, k, form);
+        if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+        for (int r = 0; r < 2 && e == cudaSuccess; ++r) {
+          e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, k, form);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess && (best_t == 0 || ms < best_t)) {
+          best_t = ms;
+          best = k;
+          best_form = form;
+        }
       }
     }
     cudaEventDestroy(e0);
@@ -898,16 +1109,22 @@ class LimbGemmImpl : public LimbGemm {
     if (e != cudaSuccess) return e;
     {
       std::lock_guard<std::mutex> lk(tune_mu_);
-      tuned_[bpad] = best;
+      tuned_[bpad] = {best, best_form};
     }
     if (chosen) *chosen = best;
+    if (chosen_form) *chosen_form = best_form;
     if (best_ms) *best_ms = best_t / 2;
     return cudaSuccess;
   }
 
+  // Without a tuned choice: the resident planes when there are some (the
+  // form measured at the tensor peak for large batches), else the raw DB.
+  int DefaultForm() const { return db_planes_ ? kFormPlanes : kFormRaw; }
+
+  // force_split > 0 / form >= 0 override the tuned (or default) choice.
   cudaError_t Launch(int batch, const void* q1, int64_t q1_stride, const void* yg,
                      int64_t yg_stride, void* out, LimbScratch* scratch,
-                     cudaStream_t st, int force_split) {
+                     cudaStream_t st, int force_split, int form) {
     if (batch <= 0) return cudaSuccess;
     LimbScratchImpl* sc = static_cast<LimbScratchImpl*>(scratch);
     cudaError_t e = EnsureQueries(sc, batch);
@@ -942,35 +1159,51 @@ class LimbGemmImpl : public LimbGemm {
     a.out_stride = rows_;
     const int nqt = static_cast<int>(bpad / tq_);
     const int64_t tiles = (rows_ / kTileRows) * nqt;
-    a.ksplit = force_split > 0 ? force_split
-                               : Split(bpad, tiles, a.n_db_units + 2 * a.n_pk_blocks);
+    const Choice c = Chosen(bpad, tiles, a.n_db_units + 2 * a.n_pk_blocks);
+    a.ksplit = force_split > 0 ? force_split : c.split;
+    const int f = form >= 0 ? form : c.form;
+    if ((f == kFormRaw && !conv_) || (f == kFormPlanes && !db_planes_)) {
+      return cudaErrorNotSupported;
+    }
     if (a.ksplit > 1) {
       e = cudaMemsetAsync(out, 0, static_cast<size_t>(batch) * rows_ * word_, st);
       if (e != cudaSuccess) return e;
     }
     const unsigned grid = static_cast<unsigned>(tiles * a.ksplit);
-    if (nq_ == 4) {
-      limb_gemm_kernel<4><<<grid, kThreads, kSmemBytes, st>>>(
-          tm_db_, tm_pk_, sc->tm_q, sc->tm_y, a, static_cast<const uint32_t*>(sc->qsum),
-          static_cast<uint32_t*>(out), err_);
+    using U = unsigned long long;
+    if (nq_ == 4 && f == kFormPlanes) {
+      limb_gemm_kernel<4, false><<<grid, kThreads, kSmemBytes, st>>>(
+          tm_db_, tm_raw_, tm_pk_, sc->tm_q, sc->tm_y, a,
+          static_cast<const uint32_t*>(sc->qsum), static_cast<uint32_t*>(out), err_);
+    } else if (nq_ == 4) {
+      limb_gemm_kernel<4, true><<<grid, kThreadsConv, kSmemBytes, st>>>(
+          tm_db_, tm_raw_, tm_pk_, sc->tm_q, sc->tm_y, a,
+          static_cast<const uint32_t*>(sc->qsum), static_cast<uint32_t*>(out), err_);
+    } else if (f == kFormPlanes) {
+      limb_gemm_kernel<8, false><<<grid, kThreads, kSmemBytes, st>>>(
+          tm_db_, tm_raw_, tm_pk_, sc->tm_q, sc->tm_y, a, static_cast<const U*>(sc->qsum),
+          static_cast<U*>(out), err_);
     } else {
-      using U = unsigned long long;
-      limb_gemm_kernel<8><<<grid, kThreads, kSmemBytes, st>>>(
-          tm_db_, tm_pk_, sc->tm_q, sc->tm_y, a, static_cast<const U*>(sc->qsum),
+      limb_gemm_kernel<8, true><<<grid, kThreadsConv, kSmemBytes, st>>>(
+          tm_db_, tm_raw_, tm_pk_, sc->tm_q, sc->tm_y, a, static_cast<const U*>(sc->qsum),
           static_cast<U*>(out), err_);
     }
     return cudaGetLastError();
   }
 
-  // The tuned split-K factor for this padded batch size, else the
-  // heuristic one.
-  int Split(int64_t bpad, int64_t tiles, int n_units) {
+  struct Choice {
+    int split, form;
+  };
+
+  // The tuned split-K factor and form for this padded batch size, else the
+  // heuristic factor and the default form.
+  Choice Chosen(int64_t bpad, int64_t tiles, int n_units) {
     {
       std::lock_guard<std::mutex> lk(tune_mu_);
       auto it = tuned_.find(bpad);
       if (it != tuned_.end()) return it->second;
     }
-    return ChooseSplit(tiles, n_units);
+    return {ChooseSplit(tiles, n_units), DefaultForm()};
   }
 
   // Split-K factor that fills the SMs in whole waves (one CTA per SM), with
@@ -1006,17 +1239,18 @@ class LimbGemmImpl : public LimbGemm {
   int sms_ = 0;
   int nq_ = 4, tq_ = 64, word_ = 4;  // request digit planes, requests per tile, word bytes
   __half *db_planes_ = nullptr, *pk_planes_ = nullptr;
+  bool conv_ = false;  // the raw-DB (converting) form can run
   int* err_ = nullptr;
-  CUtensorMap tm_db_{}, tm_pk_{};
+  CUtensorMap tm_db_{}, tm_raw_{}, tm_pk_{};
   std::mutex tune_mu_;
-  std::map<int64_t, int> tuned_;  // padded batch size -> split-K factor
+  std::map<int64_t, Choice> tuned_;  // padded batch size -> split-K and form
 };
 
 }  // namespace
 
 void LimbGemm::Create(int coeff_bits, int db_kind, const void* db, int64_t rows,
                       int64_t db_cols, int mat_kind, const void* pack,
-                      int64_t pack_cols, std::unique_ptr<LimbGemm>* out) {
+                      int64_t pack_cols, bool db_planes, std::unique_ptr<LimbGemm>* out) {
   out->reset();
   // A u16 DB over Z_{2^32} (4 request digit planes; int16, int32 or u32
   // pack matrices) or Z_{2^64} (8 planes; int16 or int32 pack matrices,
@@ -1036,7 +1270,8 @@ void LimbGemm::Create(int coeff_bits, int db_kind, const void* db, int64_t rows,
   cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
   if (major != 10) return;
   std::unique_ptr<LimbGemmImpl> impl(new LimbGemmImpl());
-  if (!impl->Init(coeff_bits == 32 ? 4 : 8, db, rows, db_cols, mat_kind, pack, pack_cols)) {
+  if (!impl->Init(coeff_bits == 32 ? 4 : 8, db, rows, db_cols, mat_kind, pack, pack_cols,
+                  db_planes)) {
     cudaGetLastError();
     return;
   }

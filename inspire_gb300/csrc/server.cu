@@ -1254,7 +1254,7 @@ Status CreateServer(const inspire_pir_params* prm, const void* db,
   RETURN_IF_ERROR(InitWorkspace(s->ws0.get()));
   // The tensor-core engine when the shapes allow it.
   LimbGemm::Create(cb, prm->db_kind, s->db.get(), db_rows, db_cols,
-                   prm->mat_kind, s->pack.get(), pack_cols, &s->limb);
+                   prm->mat_kind, s->pack.get(), pack_cols, true, &s->limb);
   *out = std::move(s);
   return Status{};
 }
@@ -2567,13 +2567,13 @@ int inspire_pir_autotune(inspire_pir_server* server, int32_t batch,
     // work does not depend on the operand values.
     st = Cuda(cudaMemsetAsync(ws->q1.get(), 0, ws->q1.bytes(), ws->stream), "memset");
   }
-  int chosen = 0;
+  int chosen = 0, form = 0;
   float best = 0;
   if (st.ok()) {
     st = Cuda(server->limb->Tune(batch, ws->q1.get(), server->db_cols, ws->pkey.get(),
                                  static_cast<int64_t>(2 * server->k) * server->d,
                                  ws->gemv.get(), ws->limb.get(), ws->stream, &chosen,
-                                 &best),
+                                 &form, &best),
               "autotune");
   }
   if (st.ok()) {
@@ -2673,6 +2673,36 @@ int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,
   Status st = Products(server, server->ws0.get(), batch, first_dim, packing_key,
                        out, engine, static_cast<cudaStream_t>(stream));
   return Report(st, err, err_len);
+}
+
+int inspire_pir_tensor_products_device(inspire_pir_server* server, int32_t batch,
+                                       const void* first_dim, const void* packing_key,
+                                       void* out, int32_t form, int32_t split,
+                                       void* stream, char* err, size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr || batch <= 0 || (form != kFormPlanes && form != kFormRaw)) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT,
+                      "server is null, batch <= 0 or unknown form."),
+                  err, err_len);
+  }
+  if (!server->limb) {
+    return Report(Err(INSPIRE_FAILED_PRECONDITION,
+                      "tensor engine unavailable for these parameters"),
+                  err, err_len);
+  }
+  std::lock_guard<std::mutex> lock(server->mu);
+  Workspace* ws = server->ws0.get();
+  if (!ws->limb) ws->limb = server->limb->NewScratch();
+  const cudaError_t e = server->limb->RunForm(
+      batch, first_dim, server->db_cols, packing_key,
+      static_cast<int64_t>(2 * server->k) * server->d, out, ws->limb.get(),
+      static_cast<cudaStream_t>(stream), form, split);
+  if (e == cudaErrorNotSupported) {
+    return Report(Err(INSPIRE_FAILED_PRECONDITION,
+                      "this form of the tensor engine is not available on this server"),
+                  err, err_len);
+  }
+  return Report(Cuda(e, "limb gemm"), err, err_len);
 }
 
 int64_t inspire_pir_workspace_bytes(const inspire_pir_server* server,

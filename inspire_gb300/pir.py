@@ -27,6 +27,9 @@ INTERNAL = 13
 
 ENGINE_PLAIN = 0
 ENGINE_TENSOR = 1
+# Layouts of the tensor engine's DB operand (inspire_pir_tensor_products_device).
+FORM_PLANES = 0   # resident fp16 digit planes
+FORM_RAW = 1      # the u16 DB as stored, split into digits in shared memory
 
 KINDS = {np.dtype(np.uint8): 0, np.dtype(np.uint16): 1,
          np.dtype(np.uint32): 2, np.dtype(np.uint64): 3,
@@ -460,6 +463,17 @@ class PirServer:
             self._h, batch, ctypes.c_void_p(ct_ptr), ctypes.c_void_p(rgsw_ptr),
             ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream), err, len(err))
         _check(rc, err)
+
+    def tensor_products_device(self, batch, first_dim_ptr, packing_key_ptr,
+                               out_ptr, form, split=0, stream=0):
+        """Stage 1 (DB * q1 + P * y_g) of a device batch on the tensor engine
+        in a given form (FORM_PLANES / FORM_RAW); split > 0 forces the
+        split-K factor. first_dim holds db_cols words per request."""
+        err = _errbuf()
+        _check(_lib.load().inspire_pir_tensor_products_device(
+            self._h, batch, ctypes.c_void_p(first_dim_ptr),
+            ctypes.c_void_p(packing_key_ptr), ctypes.c_void_p(out_ptr), form,
+            split, ctypes.c_void_p(stream), err, len(err)), err)
 
     def autotune(self, batch):
         """Tunes the tensor engine's split-K factor for this batch size;

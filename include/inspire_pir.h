@@ -49,6 +49,7 @@ extern "C" {
 /* Answer engines for the batched entry points. */
 #define INSPIRE_ENGINE_PLAIN 0  /* fused CUDA-core GEMV, HBM-bound        */
 #define INSPIRE_ENGINE_TENSOR 1 /* 8-bit limbs on the tcgen05 tensor cores */
+#define INSPIRE_ENGINE_AUTO 2   /* per batch size: the server's tuned choice */
 /* (u16 DB; i16/i32/u32 pack matrices over Z_2^32, i16/i32 over Z_2^64;
  * l*t*d a multiple of 256. Other servers return FAILED_PRECONDITION.) */
 
@@ -257,6 +258,19 @@ int inspire_pir_external_product_device(inspire_pir_server* server,
  */
 int inspire_pir_autotune(inspire_pir_server* server, int32_t batch,
                          int32_t* split, float* ms, char* err, size_t err_len);
+
+/*
+ * Engine autotuner (no reference counterpart): times the plain engine and
+ * the tensor engine (every form and split-K factor, as inspire_pir_autotune)
+ * on this server's matrices at batch sizes 1..8, the powers of two up to
+ * max_batch and max_batch itself, and keeps as the server's crossover the
+ * smallest tested size from which the tensor engine is faster at every
+ * larger tested size (0x7fffffff: never, or no tensor engine). Calls with
+ * INSPIRE_ENGINE_AUTO then use the tensor engine for batches of at least
+ * the crossover (5 until this has run). Synchronous.
+ */
+int inspire_pir_tune_engines(inspire_pir_server* server, int32_t max_batch,
+                             int32_t* crossover, char* err, size_t err_len);
 
 typedef struct inspire_graph inspire_graph;
 int inspire_graph_begin(void* stream, char* err, size_t err_len);

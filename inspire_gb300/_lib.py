@@ -51,6 +51,7 @@ SIGNATURES = {
     "inspire_pir_external_product_device": (
         [_vp, _i32, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),
     "inspire_pir_autotune": ([_vp, _i32, _vp, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_tune_engines": ([_vp, _i32, _vp, _cp, _sz], ctypes.c_int),
     "inspire_pir_tensor_products_device": (
         [_vp, _i32, _vp, _vp, _vp, _i32, _i32, _vp, _cp, _sz], ctypes.c_int),
     "inspire_graph_begin": ([_vp, _cp, _sz], ctypes.c_int),

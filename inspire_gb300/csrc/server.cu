@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdint>
@@ -436,6 +437,9 @@ struct inspire_pir_server {
   std::unique_ptr<inspire::Workspace> ws0;  // for the synchronous calls
   std::mutex mu;                           // guards ws0 and the timers
   double t_db = 0, t_pack = 0, t_eval = 0;
+  // INSPIRE_ENGINE_AUTO: batches of at least `crossover` requests go to the
+  // tensor engine (set by inspire_pir_tune_engines; until then a default).
+  std::atomic<int32_t> crossover{-1};
 };
 
 struct inspire_graph {
@@ -784,6 +788,24 @@ Status ValidateRequest(const inspire_pir_server* s, int64_t first_dim_len,
   }
   return s->deferred;
 }
+
+// Batches from this size on use the tensor engine under INSPIRE_ENGINE_AUTO
+// until inspire_pir_tune_engines has measured the crossover: the plain
+// engine streams the matrices once per group of up to 4 requests, the
+// tensor engine once per batch.
+constexpr int32_t kDefaultCrossover = 5;
+
+}  // namespace
+
+int ResolveEngine(const inspire_pir_server* s, int engine, int batch) {
+  if (engine != INSPIRE_ENGINE_AUTO) return engine;
+  if (!s->limb) return INSPIRE_ENGINE_PLAIN;
+  const int32_t c = s->crossover.load();
+  return batch >= (c >= 0 ? c : kDefaultCrossover) ? INSPIRE_ENGINE_TENSOR
+                                                   : INSPIRE_ENGINE_PLAIN;
+}
+
+namespace {
 
 // Stage 1: out[q] = DB * q1[q] + P * y_g[q] for the whole batch.
 Status Products(inspire_pir_server* s, Workspace* ws, int batch,
@@ -2093,6 +2115,7 @@ int LaunchBatch(inspire_pir_server* s, Workspace* w, const RequestSegment* segs,
   if (status.ok() && (batch <= 0 || batch > w->cap)) {
     status = Err(INSPIRE_INVALID_ARGUMENT, "batch exceeds the workspace capacity.");
   }
+  engine = ResolveEngine(s, engine, batch);
   if (status.ok()) {
     status = AnswerOnDevice(s, w, batch, w->q1.get(), w->pkey.get(), w->sdim.get(),
                             w->resp.get(), engine, st, false);
@@ -2117,7 +2140,7 @@ int QueryBatch(Workspace* w) {
 
 int FinishBatch(inspire_pir_server* s, Workspace* w, int engine, std::string* err) {
   Status st = Cuda(cudaEventSynchronize(w->done), "answer");
-  if (st.ok() && engine == INSPIRE_ENGINE_TENSOR && s->limb &&
+  if (st.ok() && engine != INSPIRE_ENGINE_PLAIN && s->limb &&
       s->limb->CheckError() != 0) {
     st = Err(INSPIRE_INTERNAL, "tensor engine pipeline timed out");
   }
@@ -2411,6 +2434,7 @@ int inspire_pir_process_batch(inspire_pir_server* server, int32_t batch,
   if (server == nullptr) {
     return Report(Err(INSPIRE_INVALID_ARGUMENT, "server is null."), err, err_len);
   }
+  engine = inspire::ResolveEngine(server, engine, batch);
   return Report(inspire::ProcessHostBatch(server, batch, first_dim,
                                           first_dim_len, second_dim,
                                           second_dim_count, packing_key,
@@ -2434,6 +2458,7 @@ int inspire_pir_process_batch_device(inspire_pir_server* server,
     return Report(Err(INSPIRE_INVALID_ARGUMENT, "batch must be positive."), err,
                   err_len);
   }
+  engine = inspire::ResolveEngine(server, engine, batch);
   Status st = inspire::ValidateRequest(server, first_dim_len, second_dim_count,
                                        packing_key_count);
   if (!st.ok()) return Report(st, err, err_len);
@@ -2461,6 +2486,7 @@ int inspire_pir_pack_batch_device(inspire_pir_server* server, int32_t batch,
     return Report(Err(INSPIRE_INVALID_ARGUMENT, "server is null or batch <= 0."),
                   err, err_len);
   }
+  engine = ResolveEngine(server, engine, batch);
   Status st = ValidateRequest(server, first_dim_len, 2 * server->ne,
                               packing_key_count);
   if (!st.ok()) return Report(st, err, err_len);
@@ -2583,6 +2609,81 @@ int inspire_pir_autotune(inspire_pir_server* server, int32_t batch,
   return Report(st, err, err_len);
 }
 
+int inspire_pir_tune_engines(inspire_pir_server* server, int32_t max_batch,
+                             int32_t* crossover, char* err, size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr || max_batch <= 0) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server is null or max_batch <= 0."),
+                  err, err_len);
+  }
+  constexpr int32_t kNever = 0x7fffffff;
+  if (!server->limb) {
+    server->crossover.store(kNever);
+    if (crossover) *crossover = kNever;
+    return INSPIRE_OK;
+  }
+  std::lock_guard<std::mutex> lock(server->mu);
+  Workspace* ws = server->ws0.get();
+  Status st = EnsureWorkspace(server, ws, max_batch);
+  if (st.ok() && !ws->limb) ws->limb = server->limb->NewScratch();
+  if (st.ok()) {
+    st = Cuda(cudaMemsetAsync(ws->q1.get(), 0, ws->q1.bytes(), ws->stream), "memset");
+  }
+  // Every size up to 8 (the plain engine's cost steps every 4 requests),
+  // then powers of two, then max_batch.
+  std::vector<int> sizes;
+  for (int b = 1; b <= std::min(8, max_batch); ++b) sizes.push_back(b);
+  for (int b = 16; b < max_batch; b *= 2) sizes.push_back(b);
+  if (max_batch > 8) sizes.push_back(max_batch);
+  std::vector<float> plain_ms(sizes.size()), tensor_ms(sizes.size());
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (st.ok()) st = Cuda(cudaEventCreate(&e0), "event");
+  if (st.ok()) st = Cuda(cudaEventCreate(&e1), "event");
+  const int64_t pk_stride = static_cast<int64_t>(2 * server->k) * server->d;
+  for (size_t i = 0; i < sizes.size() && st.ok(); ++i) {
+    const int b = sizes[i];
+    // The plain engine: one launch to warm up, the mean of three.
+    st = Products(server, ws, b, ws->q1.get(), ws->pkey.get(), ws->gemv.get(),
+                  INSPIRE_ENGINE_PLAIN, ws->stream);
+    if (st.ok()) st = Cuda(cudaEventRecord(e0, ws->stream), "event");
+    for (int r = 0; r < 3 && st.ok(); ++r) {
+      st = Products(server, ws, b, ws->q1.get(), ws->pkey.get(), ws->gemv.get(),
+                    INSPIRE_ENGINE_PLAIN, ws->stream);
+    }
+    if (st.ok()) st = Cuda(cudaEventRecord(e1, ws->stream), "event");
+    if (st.ok()) st = Cuda(cudaEventSynchronize(e1), "event");
+    float ms = 0;
+    if (st.ok()) st = Cuda(cudaEventElapsedTime(&ms, e0, e1), "event");
+    plain_ms[i] = ms / 3;
+    // The tensor engine at its tuned form and split-K factor.
+    int split = 0, form = 0;
+    float best = 0;
+    if (st.ok()) {
+      st = Cuda(server->limb->Tune(b, ws->q1.get(), server->db_cols, ws->pkey.get(),
+                                   pk_stride, ws->gemv.get(), ws->limb.get(),
+                                   ws->stream, &split, &form, &best),
+                "autotune");
+    }
+    tensor_ms[i] = best;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (!st.ok()) return Report(st, err, err_len);
+  // The smallest tested size from which the tensor engine wins at every
+  // larger tested size.
+  int32_t c = kNever;
+  for (size_t i = sizes.size(); i-- > 0;) {
+    if (tensor_ms[i] < plain_ms[i]) {
+      c = sizes[i];
+    } else {
+      break;
+    }
+  }
+  server->crossover.store(c);
+  if (crossover) *crossover = c;
+  return INSPIRE_OK;
+}
+
 int inspire_pir_server_check(inspire_pir_server* server, char* err,
                              size_t err_len) {
   using namespace inspire;
@@ -2607,6 +2708,7 @@ int inspire_vpir_process_batch(inspire_pir_server* server, int32_t batch,
                   err, err_len);
   }
   inspire_pir_server* s = server;
+  engine = ResolveEngine(s, engine, batch);
   const int expected = local_finalize ? s->k : 2 * s->k;
   if (packing_key_count != expected) {
     return Report(Err(INSPIRE_INVALID_ARGUMENT,
@@ -2669,6 +2771,7 @@ int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,
     return Report(Err(INSPIRE_INVALID_ARGUMENT, "server is null or batch <= 0."),
                   err, err_len);
   }
+  engine = ResolveEngine(server, engine, batch);
   std::lock_guard<std::mutex> lock(server->mu);
   Status st = Products(server, server->ws0.get(), batch, first_dim, packing_key,
                        out, engine, static_cast<cudaStream_t>(stream));
@@ -2769,6 +2872,7 @@ int inspire_pir_workspace_submit(inspire_pir_workspace* ws, int32_t batch,
                       "batch must be between 1 and the workspace capacity."),
                   err, err_len);
   }
+  engine = ResolveEngine(s, engine, batch);
   Status st = s->deferred;
   const size_t cw = Words(s->prm.coeff_bits);
   const size_t d = s->d;

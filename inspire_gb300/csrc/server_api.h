@@ -32,6 +32,9 @@ struct ServerGeometry {
 };
 
 ServerGeometry GetGeometry(const inspire_pir_server* s);
+// INSPIRE_ENGINE_AUTO -> the engine the server's tuned crossover picks for
+// `batch` requests; other engines unchanged.
+int ResolveEngine(const inspire_pir_server* s, int engine, int batch);
 int64_t BatchWorkspaceBytes(const inspire_pir_server* s, int max_batch);
 // A workspace for up to max_batch requests: device buffers, a stream, a
 // completion event and, when available, the tensor engine's request planes.

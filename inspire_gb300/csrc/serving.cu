@@ -59,6 +59,9 @@ class Backend {
   virtual int WordBytes(int q) const = 0;
   virtual int Validate(int q, int64_t first_dim_len, std::string* err) = 0;
   virtual bool TensorOk(int q) const = 0;
+  // The engine the queue's server picks for a batch of n (its tuned
+  // crossover).
+  virtual int ChooseEngine(int q, int n) const = 0;
   virtual int Workspaces(int q) const = 0;
   virtual int64_t WorkspaceBytes(int q) const = 0;
   virtual bool Pinned() const = 0;
@@ -110,6 +113,9 @@ class PirBackend : public Backend {
     return ValidateFirstDim(servers_[q], len, err);
   }
   bool TensorOk(int q) const override { return geo_[q].tensor; }
+  int ChooseEngine(int q, int n) const override {
+    return ResolveEngine(servers_[q], INSPIRE_ENGINE_AUTO, n);
+  }
   int Workspaces(int q) const override { return static_cast<int>(ws_[q].size()); }
   int64_t WorkspaceBytes(int q) const override { return bytes_[q]; }
   bool Pinned() const override { return true; }
@@ -158,6 +164,10 @@ class LoopbackBackend : public Backend {
     return INSPIRE_OK;
   }
   bool TensorOk(int) const override { return true; }
+  // The loopback device's crossover is fixed: batches of 5 or more.
+  int ChooseEngine(int, int n) const override {
+    return n >= 5 ? INSPIRE_ENGINE_TENSOR : INSPIRE_ENGINE_PLAIN;
+  }
   int Workspaces(int q) const override { return static_cast<int>(q_[q].slots.size()); }
   int64_t WorkspaceBytes(int) const override { return 0; }
   bool Pinned() const override { return false; }
@@ -529,8 +539,13 @@ class Engine {
             for (int k = 0; k < n; ++k) r.state[(b.first + k) % r.cap] = kInflight;
             r.next_launch += n;
           }
-          b.engine = (b.n > plain_max_ && be_->TensorOk(q)) ? INSPIRE_ENGINE_TENSOR
-                                                            : INSPIRE_ENGINE_PLAIN;
+          // plain_max < 0: each server's tuned crossover decides.
+          if (plain_max_ < 0) {
+            b.engine = be_->ChooseEngine(q, b.n);
+          } else {
+            b.engine = (b.n > plain_max_ && be_->TensorOk(q)) ? INSPIRE_ENGINE_TENSOR
+                                                              : INSPIRE_ENGINE_PLAIN;
+          }
           // At most two contiguous runs of slots (the ring wraps once).
           Ring& r = qq.ring;
           RequestSegment segs[2];

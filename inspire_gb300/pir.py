@@ -27,6 +27,7 @@ INTERNAL = 13
 
 ENGINE_PLAIN = 0
 ENGINE_TENSOR = 1
+ENGINE_AUTO = 2   # per batch size, the server's tuned crossover
 # Layouts of the tensor engine's DB operand (inspire_pir_tensor_products_device).
 FORM_PLANES = 0   # resident fp16 digit planes
 FORM_RAW = 1      # the u16 DB as stored, split into digits in shared memory
@@ -474,6 +475,16 @@ class PirServer:
             self._h, batch, ctypes.c_void_p(first_dim_ptr),
             ctypes.c_void_p(packing_key_ptr), ctypes.c_void_p(out_ptr), form,
             split, ctypes.c_void_p(stream), err, len(err)), err)
+
+    def tune_engines(self, max_batch):
+        """Times both engines at batch sizes up to max_batch and keeps the
+        crossover for ENGINE_AUTO; returns it (0x7fffffff: never)."""
+        err = _errbuf()
+        c = ctypes.c_int32()
+        _check(_lib.load().inspire_pir_tune_engines(self._h, max_batch,
+                                                    ctypes.byref(c), err,
+                                                    len(err)), err)
+        return c.value
 
     def autotune(self, batch):
         """Tunes the tensor engine's split-K factor for this batch size;

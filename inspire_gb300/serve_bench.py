@@ -105,8 +105,9 @@ def main(argv=None):
     ap.add_argument("--hbm-budget-gb", type=float, default=48.0)
     ap.add_argument("--max-wait-us", type=int, default=0,
                     help="batching window of the serving loop")
-    ap.add_argument("--plain-max-batch", type=int, default=8,
-                    help="largest batch answered by the plain engine")
+    ap.add_argument("--plain-max-batch", type=int, default=None,
+                    help="largest batch answered by the plain engine "
+                         "(default: each server's tuned crossover)")
     ap.add_argument("--small", action="store_true",
                     help="shrunk shapes (n / 16) for a quick functional run")
     args = ap.parse_args(argv)
@@ -159,6 +160,7 @@ def main(argv=None):
                 "submit_s": t_sub,
                 "mismatches": mismatches})
         ws = {nm: eng.queue_info(nm) for nm in names}
+        crossovers = dict(eng.crossovers)
     line = {
         "metric": "serving p50/p99 latency and queries/s, open-loop Poisson "
                   "arrivals over two device-resident DBs, bit-exact",
@@ -170,6 +172,7 @@ def main(argv=None):
                    "max_batch": args.max_batch,
                    "max_wait_us": args.max_wait_us,
                    "plain_max_batch": args.plain_max_batch,
+                   "tuned_crossovers": crossovers,
                    "hbm_budget_gb": args.hbm_budget_gb,
                    "workspaces": ws},
         "peak_qps": peak,

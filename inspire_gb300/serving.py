@@ -58,18 +58,27 @@ class ServingEngine:
     servers: {name: PirServer}. max_batch: requests per batch. hbm_budget:
     device bytes the workspaces of all servers may take (split evenly);
     each server gets between 1 and max_workspaces of them. plain_max_batch:
-    batches up to this size use the plain engine, larger ones the tensor
-    engine when the server has it. max_wait_us: batching window (a partial
+    None (default) lets each server's engine autotuner pick the engine per
+    batch size (inspire_pir_tune_engines runs once per server here, up to
+    max_batch); a number instead sends batches up to that size to the plain
+    engine and larger ones to the tensor engine when the server has it.
+    max_wait_us: batching window (a partial
     batch waits until its oldest request has waited this long; 0 launches as
     soon as a workspace is free). ring_slots: request slots per server
     (default 4 * max_batch).
     """
 
     def __init__(self, servers, max_batch=256, hbm_budget=8 << 30,
-                 max_workspaces=3, plain_max_batch=4, max_wait_us=0,
+                 max_workspaces=3, plain_max_batch=None, max_wait_us=0,
                  ring_slots=None, _loopback=None):
         self._lib = _lib.load()
         self.max_batch = max_batch
+        self.crossovers = {}
+        if plain_max_batch is None:
+            if _loopback is None:
+                for n, srv in servers.items():
+                    self.crossovers[n] = srv.tune_engines(max_batch)
+            plain_max_batch = -1
         ring_slots = ring_slots or 4 * max_batch
         err = pir._errbuf()
         h = ctypes.c_void_p()

@@ -104,6 +104,20 @@ def test_small_batches_use_plain_engine_large_tensor():
         assert eng.stats()["tensor_batches"] >= 1
 
 
+def test_default_engine_choice_is_the_servers_crossover():
+    # plain_max_batch=None: each queue's device picks the engine per batch
+    # size (the loopback device's crossover is 5 requests).
+    with serving.ServingEngine.loopback({"A": (4, 0, 2, 2)}, workspaces=1,
+                                        delay_us=3000, max_batch=32) as eng:
+        for i in range(3):
+            eng.submit("A", *_req(eng, "A", i)).result(timeout=30)
+        assert eng.stats()["tensor_batches"] == 0
+        futs = [eng.submit("A", *_req(eng, "A", i)) for i in range(40)]
+        for i, f in enumerate(futs):
+            assert np.array_equal(f.result(timeout=30), _want(eng, "A", i))
+        assert eng.stats()["tensor_batches"] >= 1
+
+
 def test_failed_batch_sets_exceptions_and_loop_survives():
     with serving.ServingEngine.loopback({"A": (4, 0, 2, 2)}, workspaces=1,
                                         delay_us=100, max_batch=4) as eng:

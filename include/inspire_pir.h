@@ -189,16 +189,19 @@ int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,
 
 /*
  * Stage 1 of a device-resident batch on the tensor engine in a given form
- * (no reference counterpart: the forms are this build's two layouts of the
- * same product). form INSPIRE_FORM_PLANES reads the DB as resident fp16
- * digit planes, INSPIRE_FORM_RAW reads the DB as stored (u16) and splits it
- * into digits in shared memory; split > 0 forces that split-K factor (0:
- * the tuned or heuristic one). Same buffers and result as
- * inspire_pir_products_device with INSPIRE_ENGINE_TENSOR.
- * FAILED_PRECONDITION when the server has no such form.
+ * (no reference counterpart: the forms are this build's layouts and tile
+ * shapes of the same product). form INSPIRE_FORM_PLANES reads the DB as
+ * resident fp16 digit planes, INSPIRE_FORM_RAW reads the DB as stored (u16)
+ * and splits it into digits in shared memory; or-ed with
+ * INSPIRE_FORM_NARROW the kernel takes 16 requests per tile instead of 64
+ * (32 over Z_2^64). split > 0 forces that split-K factor (0: the tuned or
+ * heuristic one). Same buffers and result as inspire_pir_products_device
+ * with INSPIRE_ENGINE_TENSOR. FAILED_PRECONDITION when the server has no
+ * such form.
  */
 #define INSPIRE_FORM_PLANES 0
 #define INSPIRE_FORM_RAW 1
+#define INSPIRE_FORM_NARROW 2
 int inspire_pir_tensor_products_device(inspire_pir_server* server,
                                        int32_t batch, const void* first_dim,
                                        const void* packing_key, void* out,

@@ -111,16 +111,20 @@ constexpr size_t kSmemBytes = kRingBytes + 1024 + 256;
 static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
 
 // Request words split into NQ balanced base-256 digit planes: NQ = 4 for
-// Z_2^32 words, 8 for Z_2^64. A request tile holds TQ = 256 / NQ requests,
-// so its B operand always has 256 rows (NQ planes x TQ requests), the DB /
-// low-pack MMA has N = 256 and the accumulator of a row block NQ weight
-// blocks of TQ columns (256 TMEM columns).
+// Z_2^32 words, 8 for Z_2^64. A full request tile holds TQ = 256 / NQ
+// requests, so its B operand has 256 rows (NQ planes x TQ requests), the DB
+// / low-pack MMA has N = 256 and the accumulator of a row block NQ weight
+// blocks of TQ columns (256 TMEM columns). The narrow tile (kNarrowTQ = 16
+// requests) cuts the MMA work of small batches by 256 / (16 NQ): the DB is
+// then streamed once per 16 requests instead of once per 64 (or 32) padded
+// ones, with N = 16 NQ, ..., 16 (NQ - 3), all multiples of 16 as M = 128
+// needs.
 template <int NQ>
 struct LimbShape {
   static constexpr int kTQ = kBRows / NQ;
-  static constexpr int kBPlaneBytes = kTQ * kBSlotK * 2;  // 8 or 4 KB
   using Acc = typename std::conditional<NQ == 4, uint32_t, unsigned long long>::type;
 };
+constexpr int kNarrowTQ = 16;
 
 // ------------------------------------------------------------------ PTX --
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -232,6 +236,32 @@ __device__ __forceinline__ void tmem_ld_x32(uint32_t taddr, uint32_t (&v)[32]) {
       : "r"(taddr));
 }
 #undef INSPIRE_R32
+
+#define INSPIRE_R16(i) "=r"(v[i])
+__device__ __forceinline__ void tmem_ld_x16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+      "[%16];"
+      : INSPIRE_R16(0), INSPIRE_R16(1), INSPIRE_R16(2), INSPIRE_R16(3),
+        INSPIRE_R16(4), INSPIRE_R16(5), INSPIRE_R16(6), INSPIRE_R16(7),
+        INSPIRE_R16(8), INSPIRE_R16(9), INSPIRE_R16(10), INSPIRE_R16(11),
+        INSPIRE_R16(12), INSPIRE_R16(13), INSPIRE_R16(14), INSPIRE_R16(15)
+      : "r"(taddr));
+}
+#undef INSPIRE_R16
+
+// tcgen05.ld of N consecutive 32-bit columns (N = 16 or 32) of the warp's
+// 32 TMEM lanes.
+template <int N>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&v)[N]) {
+  if constexpr (N == 32) {
+    tmem_ld_x32(taddr, v);
+  } else {
+    static_assert(N == 16, "tcgen05.ld width");
+    tmem_ld_x16(taddr, v);
+  }
+}
 
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -361,7 +391,7 @@ __device__ __forceinline__ UnitSrc unit_src(int u, int n_db_units,
 // true: the DB comes as stored, u16 (tm_raw), and the converter warpgroup
 // writes each A box's digit planes from its raw tile (pack units keep
 // their planes in both forms).
-template <int NQ, bool CONV>
+template <int NQ, bool CONV, int TQ>
 __global__ void __launch_bounds__(CONV ? kThreadsConv : kThreads, 1)
 limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
                  const __grid_constant__ CUtensorMap tm_raw,
@@ -371,8 +401,10 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
                  const typename LimbShape<NQ>::Acc* __restrict__ qsum,
                  typename LimbShape<NQ>::Acc* __restrict__ out, int* __restrict__ err) {
   using Acc = typename LimbShape<NQ>::Acc;
-  constexpr int kTileQ = LimbShape<NQ>::kTQ;
-  constexpr int kBPlaneBytes = LimbShape<NQ>::kBPlaneBytes;
+  constexpr int kTileQ = TQ;
+  constexpr int kBPlaneBytes = TQ * kBSlotK * 2;  // rows of 128 bytes
+  static_assert(NQ * TQ <= kBRows && ((NQ - 3) * TQ) % 16 == 0 && TQ % 16 == 0,
+                "request tile: N of every MMA a multiple of 16, at most 256");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -668,15 +700,18 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
 #pragma unroll
       for (int sblk = 0; sblk < NQ; ++sblk) {
         if (kind == 2 && sblk < 2) continue;
-        uint32_t v[kTileQ / 32][32];
+        constexpr int kLd = kTileQ < 32 ? kTileQ : 32;  // columns per load
+        uint32_t v[kTileQ / kLd][kLd];
 #pragma unroll
-        for (int c = 0; c < kTileQ / 32; ++c) tmem_ld_x32(base + sblk * kTileQ + 32 * c, v[c]);
+        for (int c = 0; c < kTileQ / kLd; ++c) {
+          tmem_ld<kLd>(base + sblk * kTileQ + kLd * c, v[c]);
+        }
         tmem_wait_ld();
 #pragma unroll
-        for (int c = 0; c < kTileQ / 32; ++c) {
+        for (int c = 0; c < kTileQ / kLd; ++c) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            acc[32 * c + j] +=
+          for (int j = 0; j < kLd; ++j) {
+            acc[kLd * c + j] +=
                 static_cast<Acc>(__float_as_uint(__uint_as_float(v[c][j]) + 12582912.0f))
                 << (8 * sblk);
           }
@@ -943,7 +978,8 @@ class LimbScratchImpl : public LimbScratch {
   __half* q_planes = nullptr;
   __half* y_planes = nullptr;
   void* qsum = nullptr;  // sum_c q1[q][c] per request (coefficient words)
-  CUtensorMap tm_q{}, tm_y{};
+  CUtensorMap tm_q{}, tm_y{};      // boxes of a full request tile
+  CUtensorMap tm_qn{}, tm_yn{};    // boxes of a narrow tile
 };
 
 class LimbGemmImpl : public LimbGemm {
@@ -990,11 +1026,24 @@ class LimbGemmImpl : public LimbGemm {
     cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev);
     const int smem = static_cast<int>(kSmemBytes);
     const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t fe = nq == 4 ? cudaFuncSetAttribute(limb_gemm_kernel<4, false>, attr, smem)
-                             : cudaFuncSetAttribute(limb_gemm_kernel<8, false>, attr, smem);
-    if (fe == cudaSuccess && conv_) {
-      fe = nq == 4 ? cudaFuncSetAttribute(limb_gemm_kernel<4, true>, attr, smem)
-                   : cudaFuncSetAttribute(limb_gemm_kernel<8, true>, attr, smem);
+    cudaError_t fe = cudaSuccess;
+    auto allow = [&](const void* fn) {
+      if (fe == cudaSuccess) fe = cudaFuncSetAttribute(fn, attr, smem);
+    };
+    if (nq == 4) {
+      allow(reinterpret_cast<const void*>(limb_gemm_kernel<4, false, 64>));
+      allow(reinterpret_cast<const void*>(limb_gemm_kernel<4, false, kNarrowTQ>));
+      if (conv_) {
+        allow(reinterpret_cast<const void*>(limb_gemm_kernel<4, true, 64>));
+        allow(reinterpret_cast<const void*>(limb_gemm_kernel<4, true, kNarrowTQ>));
+      }
+    } else {
+      allow(reinterpret_cast<const void*>(limb_gemm_kernel<8, false, 32>));
+      allow(reinterpret_cast<const void*>(limb_gemm_kernel<8, false, kNarrowTQ>));
+      if (conv_) {
+        allow(reinterpret_cast<const void*>(limb_gemm_kernel<8, true, 32>));
+        allow(reinterpret_cast<const void*>(limb_gemm_kernel<8, true, kNarrowTQ>));
+      }
     }
     return fe == cudaSuccess;
   }
@@ -1035,7 +1084,11 @@ class LimbGemmImpl : public LimbGemm {
     if (!make_map(&sc->tm_q, sc->q_planes, static_cast<uint64_t>(nq_) * need, cpad_, tq_,
                   kBSlotK) ||
         !make_map(&sc->tm_y, sc->y_planes, static_cast<uint64_t>(nq_) * need, kpad_, tq_,
-                  kBSlotK)) {
+                  kBSlotK) ||
+        !make_map(&sc->tm_qn, sc->q_planes, static_cast<uint64_t>(nq_) * need, cpad_,
+                  kNarrowTQ, kBSlotK) ||
+        !make_map(&sc->tm_yn, sc->y_planes, static_cast<uint64_t>(nq_) * need, kpad_,
+                  kNarrowTQ, kBSlotK)) {
       return cudaErrorInvalidValue;
     }
     sc->qcap = need;
@@ -1045,31 +1098,46 @@ class LimbGemmImpl : public LimbGemm {
   cudaError_t Run(int batch, const void* q1, int64_t q1_stride, const void* yg,
                   int64_t yg_stride, void* out, LimbScratch* scratch,
                   cudaStream_t st) override {
-    return Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, 0, -1);
+    return Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st,
+                  Chosen(batch));
   }
 
   cudaError_t RunForm(int batch, const void* q1, int64_t q1_stride, const void* yg,
                       int64_t yg_stride, void* out, LimbScratch* scratch,
                       cudaStream_t st, int form, int split) override {
-    if (form == kFormRaw && !conv_) return cudaErrorNotSupported;
-    if (form == kFormPlanes && !db_planes_) return cudaErrorNotSupported;
-    return Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, split, form);
+    Choice c = Chosen(batch);
+    c.form = form & 1;
+    c.narrow = (form >> 1) & 1;
+    if (split > 0) c.split = split;
+    if (!Available(c)) return cudaErrorNotSupported;
+    return Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, c);
   }
 
-  // Times every split-K factor that keeps at least 8 K units per CTA and at
-  // least 80 % of the last wave busy (plus the heuristic choice) on this
-  // batch size and keeps the fastest for later launches of the same padded
-  // batch size. Synchronises `st`.
+  // One configuration of the product: split-K factor, DB form and request
+  // tile (1: the narrow 16-request tile).
+  struct Choice {
+    int split, form, narrow;
+  };
+
+  bool Available(const Choice& c) const {
+    return (c.form == kFormRaw && conv_) || (c.form == kFormPlanes && db_planes_);
+  }
+
+  // Tuned choices are kept per batch size rounded up to the narrow tile.
+  static int64_t TuneKey(int batch) { return round_up(batch, kNarrowTQ); }
+
+  // Autotuner: times every available (form, request tile, split-K factor)
+  // with at least 8 K units per CTA and 80 % of the last wave busy (plus the
+  // heuristic factor) on this batch size, and keeps the fastest for later
+  // launches of the same size. The narrow tile is tried up to 64 requests.
+  // Synchronises `st`.
   cudaError_t Tune(int batch, const void* q1, int64_t q1_stride, const void* yg,
                    int64_t yg_stride, void* out, LimbScratch* scratch,
                    cudaStream_t st, int* chosen, int* chosen_form,
                    float* best_ms) override {
     if (batch <= 0) return cudaErrorInvalidValue;
-    const int64_t bpad = round_up(batch, tq_);
-    const int64_t tiles = (rows_ / kTileRows) * (bpad / tq_);
     const int n_units = static_cast<int>((cpad_ + 2 * kpad_) / kUnitK);
     const int sms = sms_ > 0 ? sms_ : 148;
-    const int heuristic = ChooseSplit(tiles, n_units);
     cudaEvent_t e0, e1;
     cudaError_t e = cudaEventCreate(&e0);
     if (e != cudaSuccess) return e;
@@ -1078,29 +1146,34 @@ class LimbGemmImpl : public LimbGemm {
       cudaEventDestroy(e0);
       return e;
     }
-    int best = heuristic, best_form = DefaultForm();
+    Choice best = Heuristic(batch);
     float best_t = 0;
-    for (int form = kFormPlanes; form <= kFormRaw && e == cudaSuccess; ++form) {
-      if ((form == kFormRaw && !conv_) || (form == kFormPlanes && !db_planes_)) continue;
-      for (int k = 1; k <= 16 && e == cudaSuccess; ++k) {
-        if (n_units / k < 8) break;
-        const int64_t items = tiles * k;
-        const int64_t waves = (items + sms - 1) / sms;
-        const double eff = static_cast<double>(items) / (waves * sms);
-        if (k != heuristic && eff < 0.8) continue;
-        e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, k, form);
-        if (e == cudaSuccess) e = cudaEventRecord(e0, st);
-        for (int r = 0; r < 2 && e == cudaSuccess; ++r) {
-          e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, k, form);
-        }
-        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
-        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-        float ms = 0;
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-        if (e == cudaSuccess && (best_t == 0 || ms < best_t)) {
-          best_t = ms;
-          best = k;
-          best_form = form;
+    for (int narrow = 0; narrow <= (batch <= 64 ? 1 : 0) && e == cudaSuccess; ++narrow) {
+      const int tq = narrow ? kNarrowTQ : tq_;
+      const int64_t tiles = (rows_ / kTileRows) * ((batch + tq - 1) / tq);
+      const int heuristic = ChooseSplit(tiles, n_units);
+      for (int form = kFormPlanes; form <= kFormRaw && e == cudaSuccess; ++form) {
+        for (int k = 1; k <= 16 && e == cudaSuccess; ++k) {
+          const Choice c{k, form, narrow};
+          if (!Available(c)) break;
+          if (n_units / k < 8) break;
+          const int64_t items = tiles * k;
+          const int64_t waves = (items + sms - 1) / sms;
+          const double eff = static_cast<double>(items) / (waves * sms);
+          if (k != heuristic && eff < 0.8) continue;
+          e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, c);
+          if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+          for (int r = 0; r < 2 && e == cudaSuccess; ++r) {
+            e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, c);
+          }
+          if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+          if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+          float ms = 0;
+          if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+          if (e == cudaSuccess && (best_t == 0 || ms < best_t)) {
+            best_t = ms;
+            best = c;
+          }
         }
       }
     }
@@ -1109,23 +1182,37 @@ class LimbGemmImpl : public LimbGemm {
     if (e != cudaSuccess) return e;
     {
       std::lock_guard<std::mutex> lk(tune_mu_);
-      tuned_[bpad] = {best, best_form};
+      tuned_[TuneKey(batch)] = best;
     }
-    if (chosen) *chosen = best;
-    if (chosen_form) *chosen_form = best_form;
+    if (chosen) *chosen = best.split;
+    if (chosen_form) *chosen_form = best.form + 2 * best.narrow;
     if (best_ms) *best_ms = best_t / 2;
     return cudaSuccess;
   }
 
-  // Without a tuned choice: the resident planes when there are some (the
-  // form measured at the tensor peak for large batches), else the raw DB.
-  int DefaultForm() const { return db_planes_ ? kFormPlanes : kFormRaw; }
+  // Without a tuned choice: the full tile, the resident planes when there
+  // are some (the form measured fastest for large batches), else the DB as
+  // stored, and the split-K factor that fills the SMs.
+  Choice Heuristic(int batch) const {
+    const int64_t tiles = (rows_ / kTileRows) * ((batch + tq_ - 1) / tq_);
+    return {ChooseSplit(tiles, static_cast<int>((cpad_ + 2 * kpad_) / kUnitK)),
+            db_planes_ ? kFormPlanes : kFormRaw, 0};
+  }
 
-  // force_split > 0 / form >= 0 override the tuned (or default) choice.
+  Choice Chosen(int batch) {
+    {
+      std::lock_guard<std::mutex> lk(tune_mu_);
+      auto it = tuned_.find(TuneKey(batch));
+      if (it != tuned_.end()) return it->second;
+    }
+    return Heuristic(batch);
+  }
+
   cudaError_t Launch(int batch, const void* q1, int64_t q1_stride, const void* yg,
                      int64_t yg_stride, void* out, LimbScratch* scratch,
-                     cudaStream_t st, int force_split, int form) {
+                     cudaStream_t st, const Choice& c) {
     if (batch <= 0) return cudaSuccess;
+    if (!Available(c)) return cudaErrorNotSupported;
     LimbScratchImpl* sc = static_cast<LimbScratchImpl*>(scratch);
     cudaError_t e = EnsureQueries(sc, batch);
     if (e != cudaSuccess) return e;
@@ -1157,53 +1244,39 @@ class LimbGemmImpl : public LimbGemm {
     a.qcap = static_cast<int>(sc->qcap);
     a.batch = batch;
     a.out_stride = rows_;
-    const int nqt = static_cast<int>(bpad / tq_);
-    const int64_t tiles = (rows_ / kTileRows) * nqt;
-    const Choice c = Chosen(bpad, tiles, a.n_db_units + 2 * a.n_pk_blocks);
-    a.ksplit = force_split > 0 ? force_split : c.split;
-    const int f = form >= 0 ? form : c.form;
-    if ((f == kFormRaw && !conv_) || (f == kFormPlanes && !db_planes_)) {
-      return cudaErrorNotSupported;
-    }
+    a.ksplit = c.split;
+    const int tq = c.narrow ? kNarrowTQ : tq_;
+    const int64_t tiles = (rows_ / kTileRows) * ((batch + tq - 1) / tq);
     if (a.ksplit > 1) {
       e = cudaMemsetAsync(out, 0, static_cast<size_t>(batch) * rows_ * word_, st);
       if (e != cudaSuccess) return e;
     }
     const unsigned grid = static_cast<unsigned>(tiles * a.ksplit);
+    const CUtensorMap& mq = c.narrow ? sc->tm_qn : sc->tm_q;
+    const CUtensorMap& my = c.narrow ? sc->tm_yn : sc->tm_y;
     using U = unsigned long long;
-    if (nq_ == 4 && f == kFormPlanes) {
-      limb_gemm_kernel<4, false><<<grid, kThreads, kSmemBytes, st>>>(
-          tm_db_, tm_raw_, tm_pk_, sc->tm_q, sc->tm_y, a,
-          static_cast<const uint32_t*>(sc->qsum), static_cast<uint32_t*>(out), err_);
-    } else if (nq_ == 4) {
-      limb_gemm_kernel<4, true><<<grid, kThreadsConv, kSmemBytes, st>>>(
-          tm_db_, tm_raw_, tm_pk_, sc->tm_q, sc->tm_y, a,
-          static_cast<const uint32_t*>(sc->qsum), static_cast<uint32_t*>(out), err_);
-    } else if (f == kFormPlanes) {
-      limb_gemm_kernel<8, false><<<grid, kThreads, kSmemBytes, st>>>(
-          tm_db_, tm_raw_, tm_pk_, sc->tm_q, sc->tm_y, a, static_cast<const U*>(sc->qsum),
-          static_cast<U*>(out), err_);
+    const uint32_t* qs4 = static_cast<const uint32_t*>(sc->qsum);
+    const U* qs8 = static_cast<const U*>(sc->qsum);
+    uint32_t* o4 = static_cast<uint32_t*>(out);
+    U* o8 = static_cast<U*>(out);
+    const bool raw = c.form == kFormRaw;
+    const int nt = raw ? kThreadsConv : kThreads;
+#define INSPIRE_LIMB_LAUNCH(NQ, CONV, TQ, QS, OUT)                                  \
+  limb_gemm_kernel<NQ, CONV, TQ><<<grid, nt, kSmemBytes, st>>>(                     \
+      tm_db_, tm_raw_, tm_pk_, mq, my, a, QS, OUT, err_)
+    if (nq_ == 4) {
+      if (!raw && !c.narrow) INSPIRE_LIMB_LAUNCH(4, false, 64, qs4, o4);
+      if (!raw && c.narrow) INSPIRE_LIMB_LAUNCH(4, false, kNarrowTQ, qs4, o4);
+      if (raw && !c.narrow) INSPIRE_LIMB_LAUNCH(4, true, 64, qs4, o4);
+      if (raw && c.narrow) INSPIRE_LIMB_LAUNCH(4, true, kNarrowTQ, qs4, o4);
     } else {
-      limb_gemm_kernel<8, true><<<grid, kThreadsConv, kSmemBytes, st>>>(
-          tm_db_, tm_raw_, tm_pk_, sc->tm_q, sc->tm_y, a, static_cast<const U*>(sc->qsum),
-          static_cast<U*>(out), err_);
+      if (!raw && !c.narrow) INSPIRE_LIMB_LAUNCH(8, false, 32, qs8, o8);
+      if (!raw && c.narrow) INSPIRE_LIMB_LAUNCH(8, false, kNarrowTQ, qs8, o8);
+      if (raw && !c.narrow) INSPIRE_LIMB_LAUNCH(8, true, 32, qs8, o8);
+      if (raw && c.narrow) INSPIRE_LIMB_LAUNCH(8, true, kNarrowTQ, qs8, o8);
     }
+#undef INSPIRE_LIMB_LAUNCH
     return cudaGetLastError();
-  }
-
-  struct Choice {
-    int split, form;
-  };
-
-  // The tuned split-K factor and form for this padded batch size, else the
-  // heuristic factor and the default form.
-  Choice Chosen(int64_t bpad, int64_t tiles, int n_units) {
-    {
-      std::lock_guard<std::mutex> lk(tune_mu_);
-      auto it = tuned_.find(bpad);
-      if (it != tuned_.end()) return it->second;
-    }
-    return {ChooseSplit(tiles, n_units), DefaultForm()};
   }
 
   // Split-K factor that fills the SMs in whole waves (one CTA per SM), with
@@ -1243,7 +1316,7 @@ class LimbGemmImpl : public LimbGemm {
   int* err_ = nullptr;
   CUtensorMap tm_db_{}, tm_raw_{}, tm_pk_{};
   std::mutex tune_mu_;
-  std::map<int64_t, Choice> tuned_;  // padded batch size -> split-K and form
+  std::map<int64_t, Choice> tuned_;  // TuneKey(batch) -> tuned configuration
 };
 
 }  // namespace

@@ -19,6 +19,8 @@ class LimbScratch {
 // the DB read as stored (u16) and split into digits in shared memory.
 constexpr int kFormPlanes = 0;
 constexpr int kFormRaw = 1;
+// Or-ed into a form: the narrow (16-request) request tile.
+constexpr int kFormNarrow = 2;
 
 class LimbGemm {
  public:
@@ -40,8 +42,9 @@ class LimbGemm {
   virtual cudaError_t Run(int batch, const void* q1, int64_t q1_stride,
                           const void* yg, int64_t yg_stride, void* out,
                           LimbScratch* scratch, cudaStream_t stream) = 0;
-  // Run with a given form and split-K factor (split <= 0: the tuned or
-  // heuristic one); cudaErrorNotSupported when the form is unavailable.
+  // Run with a given form (kFormPlanes or kFormRaw, | kFormNarrow for the
+  // 16-request tile) and split-K factor (split <= 0: the tuned or heuristic
+  // one); cudaErrorNotSupported when the form is unavailable.
   virtual cudaError_t RunForm(int batch, const void* q1, int64_t q1_stride,
                               const void* yg, int64_t yg_stride, void* out,
                               LimbScratch* scratch, cudaStream_t stream, int form,

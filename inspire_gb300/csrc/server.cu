@@ -2783,7 +2783,7 @@ int inspire_pir_tensor_products_device(inspire_pir_server* server, int32_t batch
                                        void* out, int32_t form, int32_t split,
                                        void* stream, char* err, size_t err_len) {
   using namespace inspire;
-  if (server == nullptr || batch <= 0 || (form != kFormPlanes && form != kFormRaw)) {
+  if (server == nullptr || batch <= 0 || form < 0 || form > (kFormRaw | kFormNarrow)) {
     return Report(Err(INSPIRE_INVALID_ARGUMENT,
                       "server is null, batch <= 0 or unknown form."),
                   err, err_len);

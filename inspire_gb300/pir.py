@@ -31,6 +31,7 @@ ENGINE_AUTO = 2   # per batch size, the server's tuned crossover
 # Layouts of the tensor engine's DB operand (inspire_pir_tensor_products_device).
 FORM_PLANES = 0   # resident fp16 digit planes
 FORM_RAW = 1      # the u16 DB as stored, split into digits in shared memory
+FORM_NARROW = 2   # or-ed in: 16 requests per tile instead of 64 (32 at u64)
 
 KINDS = {np.dtype(np.uint8): 0, np.dtype(np.uint16): 1,
          np.dtype(np.uint32): 2, np.dtype(np.uint64): 3,

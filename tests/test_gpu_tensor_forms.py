@@ -1,7 +1,8 @@
-"""The two forms of the tensor engine's product: the DB as resident fp16
-digit planes, and the DB read as stored (u16) and split into digits in
-shared memory by the kernel's converter warpgroup. Both must give the plain
-engine's stage-1 words (b' + b_agg_partial, pir_server.cc:215-254) bit for
+"""The forms of the tensor engine's product: the DB as resident fp16 digit
+planes, or read as stored (u16) and split into digits in shared memory by
+the kernel's converter warpgroup, each with full (64-request; 32 over
+Z_2^64) or narrow (16-request) tiles. All must give the plain engine's
+stage-1 words (b' + b_agg_partial, pir_server.cc:215-254) bit for
 bit, for every split-K factor, ragged batches, column counts that are not a
 multiple of the 128-column accumulation unit, both word sizes, and DB
 entries at the ends of their range (0 and 0xFFFF, whose digits are the
@@ -73,9 +74,14 @@ def test_raw_form_equals_planes_and_plain(cb, d, n, t, batch):
     raw = _products(srv, params, fd, pk, form=pir.FORM_RAW)
     assert np.array_equal(planes, plain)
     assert np.array_equal(raw, plain)
+    for form in (pir.FORM_PLANES | pir.FORM_NARROW,
+                 pir.FORM_RAW | pir.FORM_NARROW):
+        got = _products(srv, params, fd, pk, form=form)
+        assert np.array_equal(got, plain), form
     for split in (1, 2, 3):
-        got = _products(srv, params, fd, pk, form=pir.FORM_RAW, split=split)
-        assert np.array_equal(got, plain), split
+        for form in (pir.FORM_RAW, pir.FORM_RAW | pir.FORM_NARROW):
+            got = _products(srv, params, fd, pk, form=form, split=split)
+            assert np.array_equal(got, plain), (form, split)
     # Exact integer products mod 2^w on a few requests.
     m = np.uint64((1 << cb) - 1) if cb == 32 else None
     db = mat.db.astype(np.uint64)
@@ -103,6 +109,9 @@ def test_raw_form_extreme_entries(db_value):
     plain = _products(srv, params, fd, pk, engine=pir.ENGINE_PLAIN)
     raw = _products(srv, params, fd, pk, form=pir.FORM_RAW)
     assert np.array_equal(raw, plain)
+    narrow = _products(srv, params, fd, pk,
+                       form=pir.FORM_RAW | pir.FORM_NARROW)
+    assert np.array_equal(narrow, plain)
 
 
 def test_raw_form_unavailable_when_rows_are_not_16_byte_multiples():

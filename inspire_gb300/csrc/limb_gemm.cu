@@ -273,11 +273,6 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// Barrier 1 among the converter warpgroup only.
-__device__ __forceinline__ void conv_bar() {
-  asm volatile("bar.sync 1, %0;" ::"n"(kConvThreads) : "memory");
-}
-
 __device__ __forceinline__ uint4 lds128(uint32_t addr) {
   uint4 v;
   asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
@@ -417,7 +412,6 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   uint64_t* mma_done = acc_empty + kRowBlocks;
   uint64_t* raw_full = mma_done + 1;                                     // [rb][pair]
   uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(raw_full + kRowBlocks * kAPairs);
-  volatile int* conv_go = reinterpret_cast<volatile int*>(tmem_base_slot + 1);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -439,7 +433,9 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kRowBlocks * kAPairs; ++s) {
-      mbar_init(&a_full[s], 1);
+      // The converting form fills a DB box pair from two converter warps
+      // (one arrival each); the producer's pack-unit loads arrive twice.
+      mbar_init(&a_full[s], CONV ? 2 : 1);
       mbar_init(&a_empty[s], 1);
     }
     for (int s = 0; s < kBSlots; ++s) {
@@ -499,6 +495,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
                       src.rx + h * kStageK, row0 + rb * kBlockRows);
         }
       } else {
+        if (CONV) mbar_arrive(&a_full[s]);
         mbar_expect_tx(&a_full[s], 2 * kABoxBytes);
         for (int hh = 0; hh < 2; ++hh) {
           const int h = 2 * p + hh;
@@ -612,65 +609,58 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(kRegsConv));
     }
     // ------------------------------------------------------- converter --
-    // Per box pair of a DB unit, in the order the MMA pipe reads them: one
-    // thread waits for the raw tiles (bounded) and shares the outcome; all
-    // 128 threads load the two raw tiles (16 bytes per thread per access,
-    // four accesses per tile), meet, then write both boxes' digit planes
-    // over them (in place, hence the barrier between reads and writes),
-    // fence them for the tensor core and meet again before one thread
-    // marks the pair full. Thread t takes the 16-byte units
-    // g = 128 k + t: row r = (g & 7) | (g >> 5) << 3, unit u = (g >> 3) & 3
-    // (eight K values). Eight consecutive lanes cover eight consecutive rows
-    // of one unit, so both the raw reads (64-byte rows, 64-byte swizzle:
-    // unit u at u ^ ((r >> 1) & 3)) and the plane writes (128-byte rows,
-    // 128-byte swizzle: unit v at v ^ (r & 7); x0 in units 0-3, x1 in 4-7)
-    // hit eight different bank groups.
-    const int t = threadIdx.x - kThreads;
+    // Converter warp w (0..3) owns box w of every DB unit's step ring, in
+    // the order the MMA pipe reads the boxes: row block 0, then row block
+    // 1. Warps 0 and 1 fill box pair 0, warps 2 and 3 pair 1, so four boxes
+    // are converted at once and each pair's a_full completes on its two
+    // warps' arrivals. Per box: lane 0 waits for the pair's raw tiles
+    // (bounded) and the warp shares the outcome; every lane loads its 16
+    // raw units (16 bytes, eight K values each) of the tile, the warp meets
+    // (the digit planes overwrite the raw tile in place), then writes the
+    // units' x0 and x1 digits, fences them for the tensor core, meets again
+    // and lane 0 arrives. Lane l takes the units g = 32 k + l: row
+    // r = (l & 7) | k << 3, unit u = (l >> 3) & 3. Eight consecutive lanes
+    // cover eight consecutive rows of one unit, so the raw reads (64-byte
+    // rows, 64-byte swizzle: unit u at u ^ ((r >> 1) & 3)) and the plane
+    // writes (128-byte rows, 128-byte swizzle: unit v at v ^ (r & 7); x0 in
+    // units 0-3, x1 in 4-7) hit eight different bank groups.
+    const int cw = warp - 12;
+    const int p = cw >> 1;
     const uint32_t ring = smem_addr(smem);
+    const int u = (lane >> 3) & 3;
     bool ok = true;
     for (int i = 0; i < nu && ok; ++i) {
       if (unit_kind(u0 + i, a.n_db_units) != 0) break;  // DB units come first
-      for (int rb = 0; rb < kRowBlocks && ok; ++rb) {
-        for (int p = 0; p < kAPairs; ++p) {
-          const int s = rb * kAPairs + p;
-          if (t == 0) *conv_go = mbar_wait(&raw_full[s], i & 1, err) ? 1 : 0;
-          conv_bar();
-          if (*conv_go == 0) {
-            ok = false;
-            break;
-          }
-          uint4 raw[2][4];
-#pragma unroll
-          for (int hh = 0; hh < 2; ++hh) {
-            const uint32_t box = ring + rb * kARingBytes + (2 * p + hh) * kABoxBytes;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              const int g = 128 * k + t;
-              const int r = (g & 7) | ((g >> 5) << 3), u = (g >> 3) & 3;
-              raw[hh][k] = lds128(box + r * 64 + ((u ^ ((r >> 1) & 3)) << 4));
-            }
-          }
-          conv_bar();
-#pragma unroll
-          for (int hh = 0; hh < 2; ++hh) {
-            const uint32_t box = ring + rb * kARingBytes + (2 * p + hh) * kABoxBytes;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              const int g = 128 * k + t;
-              const int r = (g & 7) | ((g >> 5) << 3), u = (g >> 3) & 3;
-              uint4 x0, x1;
-              u16_digits(raw[hh][k].x, x0.x, x1.x);
-              u16_digits(raw[hh][k].y, x0.y, x1.y);
-              u16_digits(raw[hh][k].z, x0.z, x1.z);
-              u16_digits(raw[hh][k].w, x0.w, x1.w);
-              sts128(box + r * 128 + ((u ^ (r & 7)) << 4), x0);
-              sts128(box + r * 128 + (((4 + u) ^ (r & 7)) << 4), x1);
-            }
-          }
-          fence_proxy_async_smem();
-          conv_bar();
-          if (t == 0) mbar_arrive(&a_full[s]);
+      for (int rb = 0; rb < kRowBlocks; ++rb) {
+        const int s = rb * kAPairs + p;
+        bool ready = false;
+        if (lane == 0) ready = mbar_wait(&raw_full[s], i & 1, err);
+        if (__shfl_sync(0xffffffffu, ready ? 1 : 0, 0) == 0) {
+          ok = false;
+          break;
         }
+        const uint32_t box = ring + rb * kARingBytes + cw * kABoxBytes;
+        uint4 raw[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const int r = (lane & 7) | (k << 3);
+          raw[k] = lds128(box + r * 64 + ((u ^ ((r >> 1) & 3)) << 4));
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+          const int r = (lane & 7) | (k << 3);
+          uint4 x0, x1;
+          u16_digits(raw[k].x, x0.x, x1.x);
+          u16_digits(raw[k].y, x0.y, x1.y);
+          u16_digits(raw[k].z, x0.z, x1.z);
+          u16_digits(raw[k].w, x0.w, x1.w);
+          sts128(box + r * 128 + ((u ^ (r & 7)) << 4), x0);
+          sts128(box + r * 128 + (((4 + u) ^ (r & 7)) << 4), x1);
+        }
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&a_full[s]);
       }
     }
   } else {

@@ -2,6 +2,7 @@
 
   python -m inspire_gb300.profile_case --n 262144 --d 4096 --t 8 \
       --engine plain --batch 1 --reps 3 [--stage products|answer]
+      [--form planes|raw|planes-narrow|raw-narrow --split K]
 
 The server material is seeded synthetic data of the given shape; the chosen
 stage runs `reps` times on one stream and the process exits 0 on success.
@@ -27,6 +28,13 @@ def main():
     ap.add_argument("--engine", default="plain", choices=["plain", "tensor"])
     ap.add_argument("--stage", default="products",
                     choices=["products", "answer"])
+    ap.add_argument("--form", default="tuned",
+                    choices=["tuned", "planes", "raw", "planes-narrow",
+                             "raw-narrow"],
+                    help="tensor engine products: the DB form and request "
+                         "tile (tuned: the engine's own choice)")
+    ap.add_argument("--split", type=int, default=0,
+                    help="split-K factor of a forced form (0: heuristic)")
     args = ap.parse_args()
 
     import ctypes
@@ -63,7 +71,15 @@ def main():
     err = ctypes.create_string_buffer(256)
     t0 = time.perf_counter()
     for _ in range(args.reps):
-        if args.stage == "products":
+        if args.stage == "products" and args.engine == "tensor" and \
+                args.form != "tuned":
+            form = {"planes": pir.FORM_PLANES, "raw": pir.FORM_RAW,
+                    "planes-narrow": pir.FORM_PLANES | pir.FORM_NARROW,
+                    "raw-narrow": pir.FORM_RAW | pir.FORM_NARROW}[args.form]
+            srv.tensor_products_device(args.batch, t_fd.data_ptr(),
+                                       t_pk.data_ptr(), t_out.data_ptr(), form,
+                                       args.split, stream.cuda_stream)
+        elif args.stage == "products":
             rc = lib.inspire_pir_products_device(
                 srv._h, args.batch, t_fd.data_ptr(), t_pk.data_ptr(),
                 t_out.data_ptr(), eng, stream.cuda_stream, err, len(err))

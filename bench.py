@@ -849,11 +849,17 @@ def main():
     except pir.InspireError:
         engine = pir.ENGINE_PLAIN
 
-    # The tensor engine's split-K factor for this batch size, by timing.
+    # The engine autotuner: plain vs tensor (every DB form, request tile
+    # and split-K factor) at batch sizes up to B; the timed step then runs
+    # the tensor engine in the configuration tuned for B.
     tuned = None
     if engine == pir.ENGINE_TENSOR:
-        split, tune_ms = srv.autotune(B)
-        tuned = {"split_k": split, "product_ms": tune_ms}
+        crossover = srv.tune_engines(B)
+        table = srv.engine_table()
+        row = [r for r in table if r["batch"] == B][0]
+        tuned = {"form": row["form"], "split_k": row["split"],
+                 "product_ms": row["tensor_ms"], "crossover": crossover,
+                 "engine_table": table}
 
     # Parity of the two engines on the first requests.
     check = min(B, 8)

@@ -275,6 +275,19 @@ int inspire_pir_autotune(inspire_pir_server* server, int32_t batch,
 int inspire_pir_tune_engines(inspire_pir_server* server, int32_t max_batch,
                              int32_t* crossover, char* err, size_t err_len);
 
+/*
+ * The measurements of the last inspire_pir_tune_engines call (no reference
+ * counterpart): per tested batch size, the plain and the tensor engine's
+ * product time (ms), and the tensor engine's chosen form (INSPIRE_FORM_*,
+ * with INSPIRE_FORM_NARROW) and split-K factor. Fills up to `cap` rows of
+ * the non-null arrays and returns the number of rows (0 before any tuning,
+ * -1 for a null server).
+ */
+int32_t inspire_pir_engine_table(inspire_pir_server* server, int32_t cap,
+                                 int32_t* batch, float* plain_ms,
+                                 float* tensor_ms, int32_t* form,
+                                 int32_t* split);
+
 typedef struct inspire_graph inspire_graph;
 int inspire_graph_begin(void* stream, char* err, size_t err_len);
 int inspire_graph_end(void* stream, inspire_graph** out, char* err,

@@ -52,6 +52,7 @@ SIGNATURES = {
         [_vp, _i32, _vp, _vp, _vp, _vp, _cp, _sz], ctypes.c_int),
     "inspire_pir_autotune": ([_vp, _i32, _vp, _vp, _cp, _sz], ctypes.c_int),
     "inspire_pir_tune_engines": ([_vp, _i32, _vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_engine_table": ([_vp, _i32, _vp, _vp, _vp, _vp, _vp], _i32),
     "inspire_pir_tensor_products_device": (
         [_vp, _i32, _vp, _vp, _vp, _i32, _i32, _vp, _cp, _sz], ctypes.c_int),
     "inspire_graph_begin": ([_vp, _cp, _sz], ctypes.c_int),

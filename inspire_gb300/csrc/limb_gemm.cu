@@ -95,7 +95,7 @@ constexpr int kRingBytes = kRowBlocks * kARingBytes + kBSlots * kBSlotBytes;  //
 constexpr int kThreads = 384;
 // The converting form (a u16 DB read as it is stored): a fourth warpgroup
 // (warps 12-15) turns each raw 128-row x 32-column u16 tile, loaded by TMA
-// into the first half of its A box, into the box's two fp16 digit planes.
+// into a staging ring, into its A box's two fp16 digit planes.
 constexpr int kConvThreads = 128;
 constexpr int kThreadsConv = kThreads + kConvThreads;
 constexpr int kRawTileBytes = kBlockRows * kStageK * 2;    // 8 KB
@@ -107,8 +107,27 @@ static_assert(kRegsCtl + 2 * kRegsEpi + kRegsConv == 4 * 128,
               "register split of the converting form");
 constexpr int kTmemCols = 512;     // one 256-column accumulator per row block
 constexpr uint32_t kSpinLimit = 1u << 22;
-constexpr size_t kSmemBytes = kRingBytes + 1024 + 256;
+constexpr int kBarrierBytes = 512;
+constexpr size_t kSmemBytes = kRingBytes + 1024 + kBarrierBytes;
 static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
+
+// Shared-memory plan of one kernel form within the kRingBytes budget: the
+// two A rings, the request slots (NQ planes x TQ requests x 64 K of fp16;
+// three, or two for full tiles in the converting form) and, in the
+// converting form, a staging ring of raw u16 tiles (8 KB each, up to 8) that
+// the producer fills ahead of the converter, so that a raw tile is already
+// on chip when its box frees up.
+template <int NQ, bool CONV, int TQ>
+struct RingPlan {
+  static constexpr int kBSlotB = NQ * TQ * kBSlotK * 2;
+  static constexpr int kBS = (CONV && NQ * TQ == kBRows) ? 2 : kBSlots;
+  static constexpr int kBBase = kRowBlocks * kARingBytes;
+  static constexpr int kStageBase = kBBase + kBS * kBSlotB;
+  static constexpr int kFree = (kRingBytes - kStageBase) / kRawTileBytes;
+  static constexpr int kStages = CONV ? (kFree < 8 ? kFree : 8) : 0;
+  static_assert(!CONV || kStages >= 4, "raw staging ring");
+  static_assert(kStageBase + kStages * kRawTileBytes <= kRingBytes, "ring budget");
+};
 
 // Request words split into NQ balanced base-256 digit planes: NQ = 4 for
 // Z_2^32 words, 8 for Z_2^64. A full request tile holds TQ = 256 / NQ
@@ -400,6 +419,10 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   constexpr int kBPlaneBytes = TQ * kBSlotK * 2;  // rows of 128 bytes
   static_assert(NQ * TQ <= kBRows && ((NQ - 3) * TQ) % 16 == 0 && TQ % 16 == 0,
                 "request tile: N of every MMA a multiple of 16, at most 256");
+  using Plan = RingPlan<NQ, CONV, TQ>;
+  constexpr int kBS = Plan::kBS;            // request slots
+  constexpr int kBSlotB = Plan::kBSlotB;    // bytes per request slot
+  constexpr int kNS = Plan::kStages;        // raw staging slots (converting form)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -410,8 +433,11 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   uint64_t* acc_full = b_empty + kBSlots;
   uint64_t* acc_empty = acc_full + kRowBlocks;
   uint64_t* mma_done = acc_empty + kRowBlocks;
-  uint64_t* raw_full = mma_done + 1;                                     // [rb][pair]
-  uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(raw_full + kRowBlocks * kAPairs);
+  uint64_t* st_full = mma_done + 1;                                      // [staging slot]
+  uint64_t* st_empty = st_full + 8;
+  uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(st_empty + 8);
+  static_assert((3 * kRowBlocks * 2 + 2 * kBSlots + 1 + 16) * 8 + 4 <= kBarrierBytes,
+                "barrier region");
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -438,7 +464,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       mbar_init(&a_full[s], CONV ? 2 : 1);
       mbar_init(&a_empty[s], 1);
     }
-    for (int s = 0; s < kBSlots; ++s) {
+    for (int s = 0; s < kBS; ++s) {
       mbar_init(&b_full[s], 1);
       mbar_init(&b_empty[s], 1);
     }
@@ -447,7 +473,10 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       mbar_init(&acc_empty[b], 4);
     }
     mbar_init(mma_done, 1);
-    for (int s = 0; s < kRowBlocks * kAPairs; ++s) mbar_init(&raw_full[s], 1);
+    for (int s = 0; s < kNS; ++s) {
+      mbar_init(&st_full[s], 1);
+      mbar_init(&st_empty[s], 1);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 2) tmem_alloc(tmem_base_slot, kTmemCols);
@@ -474,37 +503,39 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     // block 0 boxes of the unit, then per pair its request half and its row
     // block 1 boxes.
     int a_last[kRowBlocks * kAPairs];
-    bool a_raw[kRowBlocks * kAPairs];
     int b_last[kBSlots];
-    for (int s = 0; s < kRowBlocks * kAPairs; ++s) {
-      a_last[s] = -1;
-      a_raw[s] = false;
-    }
+    int st_last[8];
+    for (int s = 0; s < kRowBlocks * kAPairs; ++s) a_last[s] = -1;
     for (int s = 0; s < kBSlots; ++s) b_last[s] = -1;
+    for (int s = 0; s < 8; ++s) st_last[s] = -1;
     bool ok = true;
+    int seq = 0;  // raw tiles issued (converting form), in the MMA's box order
     auto load_pair = [&](int rb, int p, const UnitSrc& src, int i) {
-      const int s = rb * kAPairs + p;
-      if (!mbar_wait(&a_empty[s], (i & 1) ^ 1, err)) return false;
-      const bool raw = CONV && src.kind == 0;
-      if (raw) {
-        // Raw u16 tiles into the first half of each box, for the converter.
-        mbar_expect_tx(&raw_full[s], 2 * kRawTileBytes);
-        for (int hh = 0; hh < 2; ++hh) {
-          const int h = 2 * p + hh;
-          tma_load_2d(&tm_raw, &raw_full[s], smem + rb * kARingBytes + h * kABoxBytes,
-                      src.rx + h * kStageK, row0 + rb * kBlockRows);
-        }
-      } else {
-        if (CONV) mbar_arrive(&a_full[s]);
-        mbar_expect_tx(&a_full[s], 2 * kABoxBytes);
-        for (int hh = 0; hh < 2; ++hh) {
-          const int h = 2 * p + hh;
-          tma_load_2d(src.am, &a_full[s], smem + rb * kARingBytes + h * kABoxBytes,
-                      src.ax + h * src.a_step, row0 + rb * kBlockRows);
+      if constexpr (CONV) {
+        if (src.kind == 0) {
+          // Raw u16 tiles into the staging ring; the converter writes the
+          // boxes once the MMA pipe has freed them.
+          for (int hh = 0; hh < 2; ++hh, ++seq) {
+            const int j = seq % kNS;
+            if (!mbar_wait(&st_empty[j], ((seq / kNS) & 1) ^ 1, err)) return false;
+            mbar_expect_tx(&st_full[j], kRawTileBytes);
+            tma_load_2d(&tm_raw, &st_full[j], smem + Plan::kStageBase + j * kRawTileBytes,
+                        src.rx + (2 * p + hh) * kStageK, row0 + rb * kBlockRows);
+            st_last[j] = seq;
+          }
+          return true;
         }
       }
+      const int s = rb * kAPairs + p;
+      if (!mbar_wait(&a_empty[s], (i & 1) ^ 1, err)) return false;
+      if (CONV) mbar_arrive(&a_full[s]);
+      mbar_expect_tx(&a_full[s], 2 * kABoxBytes);
+      for (int hh = 0; hh < 2; ++hh) {
+        const int h = 2 * p + hh;
+        tma_load_2d(src.am, &a_full[s], smem + rb * kARingBytes + h * kABoxBytes,
+                    src.ax + h * src.a_step, row0 + rb * kBlockRows);
+      }
       a_last[s] = i;
-      a_raw[s] = raw;
       return true;
     };
     for (int i = 0; i < nu && ok; ++i) {
@@ -512,13 +543,13 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       for (int p = 0; p < kAPairs && ok; ++p) ok = load_pair(0, p, src, i);
       for (int p = 0; p < kAPairs && ok; ++p) {
         const int n = kBHalves * i + p;
-        const int slot = n % kBSlots;
-        if (!mbar_wait(&b_empty[slot], ((n / kBSlots) & 1) ^ 1, err)) {
+        const int slot = n % kBS;
+        if (!mbar_wait(&b_empty[slot], ((n / kBS) & 1) ^ 1, err)) {
           ok = false;
           break;
         }
         mbar_expect_tx(&b_full[slot], src.nb * kBPlaneBytes);
-        unsigned char* bs = smem + kRowBlocks * kARingBytes + slot * kBSlotBytes;
+        unsigned char* bs = smem + Plan::kBBase + slot * kBSlotB;
         for (int j = 0; j < src.nb; ++j) {
           tma_load_2d(src.bm, &b_full[slot], bs + j * kBPlaneBytes, src.bx + p * kBSlotK,
                       j * a.qcap + q0);
@@ -529,12 +560,13 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     }
     // Drain: every copy this thread issued has landed before the CTA exits.
     for (int s = 0; s < kRowBlocks * kAPairs; ++s) {
-      if (a_last[s] >= 0) {
-        mbar_wait(a_raw[s] ? &raw_full[s] : &a_full[s], a_last[s] & 1, nullptr);
-      }
+      if (a_last[s] >= 0) mbar_wait(&a_full[s], a_last[s] & 1, nullptr);
     }
-    for (int s = 0; s < kBSlots; ++s) {
-      if (b_last[s] >= 0) mbar_wait(&b_full[s], (b_last[s] / kBSlots) & 1, nullptr);
+    for (int s = 0; s < kBS; ++s) {
+      if (b_last[s] >= 0) mbar_wait(&b_full[s], (b_last[s] / kBS) & 1, nullptr);
+    }
+    for (int s = 0; s < kNS; ++s) {
+      if (st_last[s] >= 0) mbar_wait(&st_full[s], (st_last[s] / kNS) & 1, nullptr);
     }
   } else if (warp == 1 && lane == 0) {
     // ------------------------------------------------------ MMA issuer --
@@ -562,8 +594,8 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       uint32_t b_lo[kBHalves];
 #pragma unroll
       for (int p = 0; p < kBHalves; ++p) {
-        slot[p] = (kBHalves * i + p) % kBSlots;
-        b_lo[p] = lo0 + ((kRowBlocks * kARingBytes + slot[p] * kBSlotBytes) >> 4);
+        slot[p] = (kBHalves * i + p) % kBS;
+        b_lo[p] = lo0 + ((Plan::kBBase + slot[p] * kBSlotB) >> 4);
       }
 #pragma unroll
       for (int rb = 0; rb < kRowBlocks; ++rb) {
@@ -574,7 +606,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
         for (int p = 0; p < kAPairs; ++p) {
           if (rb == 0) {
             const int n = kBHalves * i + p;
-            ok = ok && mbar_wait(&b_full[slot[p]], (n / kBSlots) & 1, err);
+            ok = ok && mbar_wait(&b_full[slot[p]], (n / kBS) & 1, err);
           }
           ok = ok && mbar_wait(&a_full[rb * kAPairs + p], i & 1, err);
           if (ok) {
@@ -613,17 +645,20 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     // the order the MMA pipe reads the boxes: row block 0, then row block
     // 1. Warps 0 and 1 fill box pair 0, warps 2 and 3 pair 1, so four boxes
     // are converted at once and each pair's a_full completes on its two
-    // warps' arrivals. Per box: lane 0 waits for the pair's raw tiles
-    // (bounded) and the warp shares the outcome; every lane loads its 16
-    // raw units (16 bytes, eight K values each) of the tile, the warp meets
-    // (the digit planes overwrite the raw tile in place), then writes the
-    // units' x0 and x1 digits, fences them for the tensor core, meets again
+    // warps' arrivals. The box's raw tile is staging slot seq % kNS, where
+    // seq = 8 i + 4 rb + w counts the DB boxes in the producer's order. Per
+    // box: lane 0 waits (bounded) for the raw tile and for the MMA pipe to
+    // have freed the box, and the warp shares the outcome; every lane loads
+    // its 16 raw units (16 bytes, eight K values each), the warp meets and
+    // lane 0 frees the staging slot; then the lanes write the units' x0 and
+    // x1 digits into the box, fence them for the tensor core, meet again
     // and lane 0 arrives. Lane l takes the units g = 32 k + l: row
     // r = (l & 7) | k << 3, unit u = (l >> 3) & 3. Eight consecutive lanes
     // cover eight consecutive rows of one unit, so the raw reads (64-byte
     // rows, 64-byte swizzle: unit u at u ^ ((r >> 1) & 3)) and the plane
     // writes (128-byte rows, 128-byte swizzle: unit v at v ^ (r & 7); x0 in
     // units 0-3, x1 in 4-7) hit eight different bank groups.
+    if constexpr (CONV) {
     const int cw = warp - 12;
     const int p = cw >> 1;
     const uint32_t ring = smem_addr(smem);
@@ -633,20 +668,27 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       if (unit_kind(u0 + i, a.n_db_units) != 0) break;  // DB units come first
       for (int rb = 0; rb < kRowBlocks; ++rb) {
         const int s = rb * kAPairs + p;
+        const int sq = 8 * i + 4 * rb + cw;
+        const int j = sq % kNS;
         bool ready = false;
-        if (lane == 0) ready = mbar_wait(&raw_full[s], i & 1, err);
+        if (lane == 0) {
+          ready = mbar_wait(&st_full[j], (sq / kNS) & 1, err) &&
+                  mbar_wait(&a_empty[s], (i & 1) ^ 1, err);
+        }
         if (__shfl_sync(0xffffffffu, ready ? 1 : 0, 0) == 0) {
           ok = false;
           break;
         }
-        const uint32_t box = ring + rb * kARingBytes + cw * kABoxBytes;
+        const uint32_t stage = ring + Plan::kStageBase + j * kRawTileBytes;
         uint4 raw[16];
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
           const int r = (lane & 7) | (k << 3);
-          raw[k] = lds128(box + r * 64 + ((u ^ ((r >> 1) & 3)) << 4));
+          raw[k] = lds128(stage + r * 64 + ((u ^ ((r >> 1) & 3)) << 4));
         }
         __syncwarp();
+        if (lane == 0) mbar_arrive(&st_empty[j]);
+        const uint32_t box = ring + rb * kARingBytes + cw * kABoxBytes;
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
           const int r = (lane & 7) | (k << 3);
@@ -662,6 +704,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
         __syncwarp();
         if (lane == 0) mbar_arrive(&a_full[s]);
       }
+    }
     }
   } else {
     if constexpr (CONV) {

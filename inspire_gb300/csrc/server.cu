@@ -394,6 +394,9 @@ struct Workspace {
   // dimension (read only by the polynomial stage) overlaps the products.
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t copy_go = nullptr, sdim_ready = nullptr;
+  // The answer forks the request polynomials' transforms onto copy_stream
+  // (fork) and joins them back before the polynomial stage (side_done).
+  cudaEvent_t fork = nullptr, side_done = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   cudaEvent_t done = nullptr;
   void* host[4] = {nullptr, nullptr, nullptr, nullptr};  // fd, sd, pk, resp
@@ -404,6 +407,8 @@ struct Workspace {
     if (done) cudaEventDestroy(done);
     if (copy_go) cudaEventDestroy(copy_go);
     if (sdim_ready) cudaEventDestroy(sdim_ready);
+    if (fork) cudaEventDestroy(fork);
+    if (side_done) cudaEventDestroy(side_done);
     if (stream) cudaStreamDestroy(stream);
     if (copy_stream) cudaStreamDestroy(copy_stream);
     for (auto& h : host)
@@ -440,6 +445,13 @@ struct inspire_pir_server {
   // INSPIRE_ENGINE_AUTO: batches of at least `crossover` requests go to the
   // tensor engine (set by inspire_pir_tune_engines; until then a default).
   std::atomic<int32_t> crossover{-1};
+  // The last engine tuning: per tested batch size the plain and tensor
+  // product times and the tensor engine's chosen form and split-K factor.
+  struct TuneRow {
+    int32_t batch, form, split;
+    float plain_ms, tensor_ms;
+  };
+  std::vector<TuneRow> tune_table;
 };
 
 struct inspire_graph {
@@ -592,16 +604,36 @@ inline int64_t Ext16Min(const inspire_pir_server* s, int d) {
 
 // FinalizeMatrixPack for every shard of every request of a batch
 // (lwes_to_rlwe.cc:448-479): w->packed[q][shard] = b_agg.
+// y_h = packing_key[k..2k): forward NTT over the finalize primes.
+template <typename T>
+Status YhTransform(inspire_pir_server* s, Workspace* w, int batch, const T* pkey,
+                   cudaStream_t st) {
+  const int d = s->d, k = s->k;
+  return NttCoeffs<T>(s, pkey, static_cast<int64_t>(2 * k) * d,
+                      static_cast<int64_t>(k) * d, k, static_cast<T>(s->vmask_f),
+                      w->yh.get<uint32_t>(), d, s->ctx_f, batch, st);
+}
+
+// The RGSW b parts of the second dimension: forward NTT over the eval
+// primes.
+template <typename T>
+Status RgswTransform(inspire_pir_server* s, Workspace* w, int batch, const T* sdim,
+                     cudaStream_t st) {
+  const int d = s->d, ne = s->ne;
+  return NttCoeffs<T>(s, sdim, static_cast<int64_t>(2 * ne) * d, 0, 2 * ne,
+                      static_cast<T>(s->vmask_e), w->rgswb.get<uint32_t>(), d, s->ctx_e,
+                      batch, st);
+}
+
+// yh_done: the y_h transform is already in w->yh (enqueued on another
+// stream that `st` has joined).
 template <typename T>
 Status FinalizeStage(inspire_pir_server* s, Workspace* w, int batch,
-                     const T* pkey, const T* gemv, cudaStream_t st) {
+                     const T* pkey, const T* gemv, cudaStream_t st,
+                     bool yh_done = false) {
   const int d = s->d, t = s->t, l = s->l, k = s->k;
   const int log_q = s->prm.log_modulus;
-  // y_h = packing_key[k..2k): forward NTT over the finalize primes.
-  RETURN_IF_ERROR(NttCoeffs<T>(s, pkey, static_cast<int64_t>(2 * k) * d,
-                               static_cast<int64_t>(k) * d, k,
-                               static_cast<T>(s->vmask_f), w->yh.get<uint32_t>(), d,
-                               s->ctx_f, batch, st));
+  if (!yh_done) RETURN_IF_ERROR(YhTransform<T>(s, w, batch, pkey, st));
   if (s->ctx_f.tables16 != nullptr && static_cast<int64_t>(l) * t * batch >= s->sms) {
     const NttCtx& c = s->ctx_f;
     const size_t smem = static_cast<size_t>(c.r + 1) * d * 4;
@@ -637,14 +669,16 @@ Status FinalizeStage(inspire_pir_server* s, Workspace* w, int batch,
   return Status{};
 }
 
+// transforms_done: YhTransform and RgswTransform are already enqueued on a
+// stream that `st` has joined.
 template <typename T>
 Status RunPolyStage(inspire_pir_server* s, Workspace* w, int batch,
                     const T* pkey, const T* sdim, const T* gemv, T* resp,
-                    cudaStream_t st, bool timed) {
+                    cudaStream_t st, bool timed, bool transforms_done = false) {
   const int d = s->d, t = s->t, l = s->l, ne = s->ne;
   const int log_q = s->prm.log_modulus;
   const int nt = PolyThreads(d);
-  RETURN_IF_ERROR(FinalizeStage<T>(s, w, batch, pkey, gemv, st));
+  RETURN_IF_ERROR(FinalizeStage<T>(s, w, batch, pkey, gemv, st, transforms_done));
   if (timed) cudaEventRecord(w->ev[2], st);
   const T* a_tilde = s->a_tilde.get<T>();
   const T* packed = w->packed.get<T>();
@@ -653,9 +687,7 @@ Status RunPolyStage(inspire_pir_server* s, Workspace* w, int batch,
   uint32_t* resid[2] = {w->resid0.get<uint32_t>(), w->resid1.get<uint32_t>()};
   if (t > 1) {
     const NttCtx& c = s->ctx_e;
-    RETURN_IF_ERROR(NttCoeffs<T>(s, sdim, static_cast<int64_t>(2 * ne) * d, 0, 2 * ne,
-                                 static_cast<T>(s->vmask_e), w->rgswb.get<uint32_t>(),
-                                 d, c, batch, st));
+    if (!transforms_done) RETURN_IF_ERROR(RgswTransform<T>(s, w, batch, sdim, st));
     ExtArgs e{log_q, s->prm.eval_log_digit, ne,
               LiveDigits(log_q, s->prm.eval_log_digit, ne), s->umask_e};
     const size_t smem = static_cast<size_t>(d) * 4 + 2ull * d * sizeof(T);
@@ -759,6 +791,10 @@ Status InitWorkspace(Workspace* ws) {
   RETURN_IF_ERROR(Cuda(cudaEventCreateWithFlags(&ws->copy_go, cudaEventDisableTiming),
                        "cudaEventCreate"));
   RETURN_IF_ERROR(Cuda(cudaEventCreateWithFlags(&ws->sdim_ready, cudaEventDisableTiming),
+                       "cudaEventCreate"));
+  RETURN_IF_ERROR(Cuda(cudaEventCreateWithFlags(&ws->fork, cudaEventDisableTiming),
+                       "cudaEventCreate"));
+  RETURN_IF_ERROR(Cuda(cudaEventCreateWithFlags(&ws->side_done, cudaEventDisableTiming),
                        "cudaEventCreate"));
   return Cuda(cudaEventCreateWithFlags(&ws->done, cudaEventDisableTiming),
               "cudaEventCreate");
@@ -878,22 +914,47 @@ Status AnswerOnDevice(inspire_pir_server* s, Workspace* w, int batch,
                       void* resp, int engine, cudaStream_t st, bool timed,
                       cudaEvent_t sdim_ready = nullptr) {
   const int cb = s->prm.coeff_bits;
+  // The request polynomials' transforms (y_h for FinalizeMatrixPack, the
+  // RGSW b parts for EvalPoly) do not depend on the products: they run on
+  // the workspace's second stream while the products stream the matrices,
+  // after the copies already queued there (the host-buffer call copies the
+  // second dimension on it), and join back before the polynomial stage.
+  RETURN_IF_ERROR(Cuda(cudaEventRecord(w->fork, st), "record fork"));
+  RETURN_IF_ERROR(Cuda(cudaStreamWaitEvent(w->copy_stream, w->fork, 0), "wait fork"));
+  if (sdim_ready != nullptr) {
+    RETURN_IF_ERROR(
+        Cuda(cudaStreamWaitEvent(w->copy_stream, sdim_ready, 0), "wait second_dim"));
+  }
+  if (cb == 32) {
+    RETURN_IF_ERROR(YhTransform<uint32_t>(s, w, batch, static_cast<const uint32_t*>(pkey),
+                                          w->copy_stream));
+    if (s->t > 1) {
+      RETURN_IF_ERROR(RgswTransform<uint32_t>(
+          s, w, batch, static_cast<const uint32_t*>(sdim), w->copy_stream));
+    }
+  } else {
+    RETURN_IF_ERROR(YhTransform<uint64_t>(s, w, batch, static_cast<const uint64_t*>(pkey),
+                                          w->copy_stream));
+    if (s->t > 1) {
+      RETURN_IF_ERROR(RgswTransform<uint64_t>(
+          s, w, batch, static_cast<const uint64_t*>(sdim), w->copy_stream));
+    }
+  }
+  RETURN_IF_ERROR(Cuda(cudaEventRecord(w->side_done, w->copy_stream), "record join"));
   if (timed) cudaEventRecord(w->ev[0], st);
   RETURN_IF_ERROR(Products(s, w, batch, q1, pkey, w->gemv.get(), engine, st));
   if (timed) cudaEventRecord(w->ev[1], st);
-  if (sdim_ready != nullptr) {
-    RETURN_IF_ERROR(Cuda(cudaStreamWaitEvent(st, sdim_ready, 0), "wait second_dim"));
-  }
+  RETURN_IF_ERROR(Cuda(cudaStreamWaitEvent(st, w->side_done, 0), "wait join"));
   if (cb == 32) {
     RETURN_IF_ERROR(RunPolyStage<uint32_t>(
         s, w, batch, static_cast<const uint32_t*>(pkey),
         static_cast<const uint32_t*>(sdim), w->gemv.get<uint32_t>(),
-        static_cast<uint32_t*>(resp), st, timed));
+        static_cast<uint32_t*>(resp), st, timed, true));
   } else {
     RETURN_IF_ERROR(RunPolyStage<uint64_t>(
         s, w, batch, static_cast<const uint64_t*>(pkey),
         static_cast<const uint64_t*>(sdim), w->gemv.get<uint64_t>(),
-        static_cast<uint64_t*>(resp), st, timed));
+        static_cast<uint64_t*>(resp), st, timed, true));
   }
   if (timed) cudaEventRecord(w->ev[3], st);
   return Status{};
@@ -2636,6 +2697,7 @@ int inspire_pir_tune_engines(inspire_pir_server* server, int32_t max_batch,
   for (int b = 16; b < max_batch; b *= 2) sizes.push_back(b);
   if (max_batch > 8) sizes.push_back(max_batch);
   std::vector<float> plain_ms(sizes.size()), tensor_ms(sizes.size());
+  std::vector<int> forms(sizes.size()), splits(sizes.size());
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (st.ok()) st = Cuda(cudaEventCreate(&e0), "event");
   if (st.ok()) st = Cuda(cudaEventCreate(&e1), "event");
@@ -2665,6 +2727,8 @@ int inspire_pir_tune_engines(inspire_pir_server* server, int32_t max_batch,
                 "autotune");
     }
     tensor_ms[i] = best;
+    forms[i] = form;
+    splits[i] = split;
   }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
@@ -2680,8 +2744,30 @@ int inspire_pir_tune_engines(inspire_pir_server* server, int32_t max_batch,
     }
   }
   server->crossover.store(c);
+  server->tune_table.clear();
+  for (size_t i = 0; i < sizes.size(); ++i) {
+    server->tune_table.push_back(
+        {sizes[i], forms[i], splits[i], plain_ms[i], tensor_ms[i]});
+  }
   if (crossover) *crossover = c;
   return INSPIRE_OK;
+}
+
+int32_t inspire_pir_engine_table(inspire_pir_server* server, int32_t cap,
+                                 int32_t* batch, float* plain_ms, float* tensor_ms,
+                                 int32_t* form, int32_t* split) {
+  if (server == nullptr) return -1;
+  std::lock_guard<std::mutex> lock(server->mu);
+  const int32_t n = static_cast<int32_t>(server->tune_table.size());
+  for (int32_t i = 0; i < n && i < cap; ++i) {
+    const auto& r = server->tune_table[i];
+    if (batch) batch[i] = r.batch;
+    if (plain_ms) plain_ms[i] = r.plain_ms;
+    if (tensor_ms) tensor_ms[i] = r.tensor_ms;
+    if (form) form[i] = r.form;
+    if (split) split[i] = r.split;
+  }
+  return n;
 }
 
 int inspire_pir_server_check(inspire_pir_server* server, char* err,

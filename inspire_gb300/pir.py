@@ -487,6 +487,26 @@ class PirServer:
                                                     len(err)), err)
         return c.value
 
+    def engine_table(self):
+        """The last tune_engines measurements: a list of dicts (batch,
+        plain_ms, tensor_ms, form, split)."""
+        lib = _lib.load()
+        n = lib.inspire_pir_engine_table(self._h, 0, None, None, None, None,
+                                         None)
+        if n <= 0:
+            return []
+        b = (ctypes.c_int32 * n)()
+        pm = (ctypes.c_float * n)()
+        tm = (ctypes.c_float * n)()
+        f = (ctypes.c_int32 * n)()
+        sp = (ctypes.c_int32 * n)()
+        lib.inspire_pir_engine_table(self._h, n, b, pm, tm, f, sp)
+        names = {FORM_PLANES: "planes", FORM_RAW: "raw"}
+        return [{"batch": b[i], "plain_ms": pm[i], "tensor_ms": tm[i],
+                 "form": names[f[i] & 1] + ("+narrow" if f[i] & FORM_NARROW
+                                            else ""),
+                 "split": sp[i]} for i in range(n)]
+
     def autotune(self, batch):
         """Tunes the tensor engine's split-K factor for this batch size;
         returns (factor, product ms)."""

@@ -299,6 +299,29 @@ int inspire_pir_server_check(inspire_pir_server* server, char* err,
                              size_t err_len);
 
 /*
+ * Resident layout of the tensor engine (no reference counterpart). With
+ * keep != 0 (the default after create / load) the server keeps the DB's
+ * fp16 digit planes resident beside the DB (twice the DB's bytes): the
+ * fastest form for large batches. With keep == 0 it drops them and the
+ * tensor engine reads the u16 DB as stored, splitting it into digits in
+ * shared memory (the DB then takes its own bytes only; large batches run
+ * slower, small ones as fast or faster). Re-creates the engine and clears
+ * the tuned choices; synchronises the device. Call it between batches,
+ * never while a call on this server is in flight. INTERNAL if the engine
+ * cannot be re-created (the server then answers with the plain engine).
+ */
+int inspire_pir_server_set_tensor_planes(inspire_pir_server* server,
+                                         int32_t keep, char* err,
+                                         size_t err_len);
+
+/*
+ * Device bytes the server holds resident: the DB and pack matrices plus the
+ * tensor engine's digit planes (workspaces not included). -1 for a null
+ * server. No reference counterpart.
+ */
+int64_t inspire_pir_server_device_bytes(const inspire_pir_server* server);
+
+/*
  * VpirServer::ProcessResponse (crypto/vpir/server/vpir_server.cc:102-195)
  * for `batch` requests in host memory, on a server created with
  * interpolation_degree 1 and entry_size_multiple = ell (DB: ell*d rows x N

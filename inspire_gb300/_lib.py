@@ -60,6 +60,8 @@ SIGNATURES = {
     "inspire_graph_launch": ([_vp, _vp, _cp, _sz], ctypes.c_int),
     "inspire_graph_destroy": ([_vp], None),
     "inspire_pir_server_check": ([_vp, _cp, _sz], ctypes.c_int),
+    "inspire_pir_server_set_tensor_planes": ([_vp, _i32, _cp, _sz], ctypes.c_int),
+    "inspire_pir_server_device_bytes": ([_vp], _i64),
     "inspire_serving_create": (
         [_vp, _i32, _i32, _i32, _i32, _i32, _i64, _i32, _vp, _cp, _sz],
         ctypes.c_int),

@@ -38,6 +38,7 @@ struct InterpArgs {
   int l;
   int64_t groups;           // n / t
   uint32_t p, tinv;
+  uint32_t lazy_off;        // multiple of p >= t * max record value (LAZY)
   int G, R;                 // tile: groups x classes
   int64_t out_cols;
 };
@@ -205,7 +206,14 @@ __device__ __forceinline__ uint32_t scale_p(uint32_t x, uint32_t tinv, uint32_t 
   }
 }
 
-template <typename V, int T, bool SMALL>
+// LAZY: the transform runs on signed 32-bit integers without any reduction:
+// every butterfly is an addition and a subtraction of values whose rotation
+// by a power of w only permutes and negates them, so after log2(t) stages
+// |x| <= t * max(V) (< 2^20 for 8- and 16-bit records). One reduction at the
+// end, (x + lazy_off) * t^-1 mod p with lazy_off a multiple of p at least
+// that bound (Shoup, valid for any 32-bit operand), gives the same residue
+// as reducing after every step. Used when 2 * lazy_off < 2^32 and p < 2^31.
+template <typename V, int T, bool SMALL, bool LAZY = false>
 __global__ void __launch_bounds__(kFastR * FastShape<V>::kGW)
 interpolate_fast_kernel(const V* __restrict__ raw, InterpArgs a, ModConsts mc,
                         V* __restrict__ out) {
@@ -240,8 +248,52 @@ interpolate_fast_kernel(const V* __restrict__ raw, InterpArgs a, ModConsts mc,
                      c_start + c0;
 #pragma unroll
       for (int m = 0; m < H; ++m) {
-        x[rb][m] = reduce_p(static_cast<uint32_t>(src[m * a.s]), p, mc.barrett);
+        const uint32_t v = static_cast<uint32_t>(src[m * a.s]);
+        x[rb][m] = LAZY ? v : reduce_p(v, p, mc.barrett);
       }
+    }
+    if constexpr (LAZY) {
+      // Butterflies on signed integers: (u, b) -> (u + v, u - v) with
+      // v = +-b, the rotation's permutation and sign fixed at compile time.
+#pragma unroll
+      for (int len = 2; len <= T; len <<= 1) {
+        const int h = len / 2;
+#pragma unroll
+        for (int i = 0; i < T; i += len) {
+#pragma unroll
+          for (int j = 0; j < h; ++j) {
+            const int wu = (j * (T - T / len)) % T;
+            const bool neg_all = wu >= H;
+            const int q = neg_all ? wu - H : wu;
+            int32_t v[H];
+#pragma unroll
+            for (int m = 0; m < H; ++m) {
+              const bool wrap = m < q;
+              const int src = wrap ? m - q + H : m - q;
+              const int32_t b = static_cast<int32_t>(x[i + j + h][src]);
+              v[m] = (wrap != neg_all) ? -b : b;
+            }
+#pragma unroll
+            for (int m = 0; m < H; ++m) {
+              const int32_t u = static_cast<int32_t>(x[i + j][m]);
+              x[i + j][m] = static_cast<uint32_t>(u + v[m]);
+              x[i + j + h][m] = static_cast<uint32_t>(u - v[m]);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < T; ++r) {
+#pragma unroll
+        for (int m = 0; m < H; ++m) {
+          const uint32_t y = x[r][m] + a.lazy_off;  // in [0, 2 lazy_off)
+          const uint32_t qq = __umulhi(y, mc.tinv_s32);
+          uint32_t rr = y * a.tinv - qq * p;
+          rr = rr >= p ? rr - p : rr;
+          tile[((r * H + m) * kFastR + c0) * kRow + gi] = static_cast<V>(rr);
+        }
+      }
+      continue;
     }
     // Butterflies: len = 2 .. T; pair (i + j, i + j + h) with w^j.
 #pragma unroll
@@ -395,7 +447,7 @@ int Run(const V* raw, int64_t n, int d, int t, int l, uint32_t p, V* out,
     transpose_kernel<V><<<grid, dim3(32, 8), 0, st>>>(raw, d, l, groups, out_cols, out);
     e = cudaGetLastError();
   } else if (e == cudaSuccess && groups > 0) {
-    InterpArgs a;
+    InterpArgs a{};
     a.d = d;
     a.t = t;
     a.logt = 0;
@@ -418,6 +470,12 @@ int Run(const V* raw, int64_t n, int d, int t, int l, uint32_t p, V* out,
       mc.tinv_s64 = static_cast<uint64_t>((static_cast<unsigned __int128>(a.tinv) << 64) / p);
       mc.tinv_s32 = static_cast<uint32_t>((static_cast<uint64_t>(a.tinv) << 32) / p);
       const bool small = p < (1u << 31);
+      // The lazy transform: t * max(record value) bounds every intermediate.
+      const uint64_t vmax = sizeof(V) >= 4 ? 0xffffffffull : (1ull << (8 * sizeof(V))) - 1;
+      const uint64_t bound = static_cast<uint64_t>(t) * std::max<uint64_t>(vmax, p);
+      const uint64_t off = (bound + p - 1) / p * p;
+      const bool lazy = sizeof(V) <= 2 && small && 2 * off < (1ull << 31);
+      a.lazy_off = static_cast<uint32_t>(lazy ? off : 0);
       constexpr int kFastG = FastShape<V>::kG;
       dim3 grid(static_cast<unsigned>(a.s / kFastR),
                 static_cast<unsigned>((groups + kFastG - 1) / kFastG), static_cast<unsigned>(l));
@@ -434,14 +492,17 @@ int Run(const V* raw, int64_t n, int d, int t, int l, uint32_t p, V* out,
         return r;
       };
       if (t == 2) {
-        e = small ? launch(interpolate_fast_kernel<V, 2, true>)
-                  : launch(interpolate_fast_kernel<V, 2, false>);
+        e = lazy    ? launch(interpolate_fast_kernel<V, 2, true, true>)
+            : small ? launch(interpolate_fast_kernel<V, 2, true>)
+                    : launch(interpolate_fast_kernel<V, 2, false>);
       } else if (t == 4) {
-        e = small ? launch(interpolate_fast_kernel<V, 4, true>)
-                  : launch(interpolate_fast_kernel<V, 4, false>);
+        e = lazy    ? launch(interpolate_fast_kernel<V, 4, true, true>)
+            : small ? launch(interpolate_fast_kernel<V, 4, true>)
+                    : launch(interpolate_fast_kernel<V, 4, false>);
       } else {
-        e = small ? launch(interpolate_fast_kernel<V, 8, true>)
-                  : launch(interpolate_fast_kernel<V, 8, false>);
+        e = lazy    ? launch(interpolate_fast_kernel<V, 8, true, true>)
+            : small ? launch(interpolate_fast_kernel<V, 8, true>)
+                    : launch(interpolate_fast_kernel<V, 8, false>);
       }
       if (e != cudaSuccess) {
         return Fail(err, err_len, INSPIRE_INTERNAL,

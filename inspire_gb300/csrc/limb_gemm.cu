@@ -117,15 +117,19 @@ static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
 // converting form, a staging ring of raw u16 tiles (8 KB each, up to 8) that
 // the producer fills ahead of the converter, so that a raw tile is already
 // on chip when its box frees up.
+// Full request tiles leave no room for staging: their converting form loads
+// each raw tile into the first half of its own box (once the MMA pipe has
+// freed it) and the converter expands it in place.
 template <int NQ, bool CONV, int TQ>
 struct RingPlan {
   static constexpr int kBSlotB = NQ * TQ * kBSlotK * 2;
-  static constexpr int kBS = (CONV && NQ * TQ == kBRows) ? 2 : kBSlots;
+  static constexpr bool kStaged = CONV && NQ * TQ < kBRows;
+  static constexpr int kBS = kBSlots;
   static constexpr int kBBase = kRowBlocks * kARingBytes;
   static constexpr int kStageBase = kBBase + kBS * kBSlotB;
   static constexpr int kFree = (kRingBytes - kStageBase) / kRawTileBytes;
-  static constexpr int kStages = CONV ? (kFree < 8 ? kFree : 8) : 0;
-  static_assert(!CONV || kStages >= 4, "raw staging ring");
+  static constexpr int kStages = kStaged ? (kFree < 8 ? kFree : 8) : 0;
+  static_assert(!kStaged || kStages >= 4, "raw staging ring");
   static_assert(kStageBase + kStages * kRawTileBytes <= kRingBytes, "ring budget");
 };
 
@@ -140,7 +144,6 @@ struct RingPlan {
 // needs.
 template <int NQ>
 struct LimbShape {
-  static constexpr int kTQ = kBRows / NQ;
   using Acc = typename std::conditional<NQ == 4, uint32_t, unsigned long long>::type;
 };
 constexpr int kNarrowTQ = 16;
@@ -423,6 +426,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   constexpr int kBS = Plan::kBS;            // request slots
   constexpr int kBSlotB = Plan::kBSlotB;    // bytes per request slot
   constexpr int kNS = Plan::kStages;        // raw staging slots (converting form)
+  constexpr bool kStaged = Plan::kStaged;   // else raw tiles convert in place
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -433,7 +437,9 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   uint64_t* acc_full = b_empty + kBSlots;
   uint64_t* acc_empty = acc_full + kRowBlocks;
   uint64_t* mma_done = acc_empty + kRowBlocks;
-  uint64_t* st_full = mma_done + 1;                                      // [staging slot]
+  // Staged: st_full / st_empty per staging slot. In place: st_full[pair]
+  // is the pair's raw-tiles-landed barrier.
+  uint64_t* st_full = mma_done + 1;
   uint64_t* st_empty = st_full + 8;
   uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(st_empty + 8);
   static_assert((3 * kRowBlocks * 2 + 2 * kBSlots + 1 + 16) * 8 + 4 <= kBarrierBytes,
@@ -473,7 +479,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       mbar_init(&acc_empty[b], 4);
     }
     mbar_init(mma_done, 1);
-    for (int s = 0; s < kNS; ++s) {
+    for (int s = 0; s < (kStaged ? kNS : kRowBlocks * kAPairs); ++s) {
       mbar_init(&st_full[s], 1);
       mbar_init(&st_empty[s], 1);
     }
@@ -503,15 +509,19 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     // block 0 boxes of the unit, then per pair its request half and its row
     // block 1 boxes.
     int a_last[kRowBlocks * kAPairs];
+    bool a_raw[kRowBlocks * kAPairs];  // in place: last load was raw tiles
     int b_last[kBSlots];
     int st_last[8];
-    for (int s = 0; s < kRowBlocks * kAPairs; ++s) a_last[s] = -1;
+    for (int s = 0; s < kRowBlocks * kAPairs; ++s) {
+      a_last[s] = -1;
+      a_raw[s] = false;
+    }
     for (int s = 0; s < kBSlots; ++s) b_last[s] = -1;
     for (int s = 0; s < 8; ++s) st_last[s] = -1;
     bool ok = true;
     int seq = 0;  // raw tiles issued (converting form), in the MMA's box order
     auto load_pair = [&](int rb, int p, const UnitSrc& src, int i) {
-      if constexpr (CONV) {
+      if constexpr (kStaged) {
         if (src.kind == 0) {
           // Raw u16 tiles into the staging ring; the converter writes the
           // boxes once the MMA pipe has freed them.
@@ -528,6 +538,20 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       }
       const int s = rb * kAPairs + p;
       if (!mbar_wait(&a_empty[s], (i & 1) ^ 1, err)) return false;
+      if constexpr (CONV && !kStaged) {
+        if (src.kind == 0) {
+          // Raw u16 tiles into the first half of each box of the pair.
+          mbar_expect_tx(&st_full[s], 2 * kRawTileBytes);
+          for (int hh = 0; hh < 2; ++hh) {
+            const int h = 2 * p + hh;
+            tma_load_2d(&tm_raw, &st_full[s], smem + rb * kARingBytes + h * kABoxBytes,
+                        src.rx + h * kStageK, row0 + rb * kBlockRows);
+          }
+          a_last[s] = i;
+          a_raw[s] = true;
+          return true;
+        }
+      }
       if (CONV) mbar_arrive(&a_full[s]);
       mbar_expect_tx(&a_full[s], 2 * kABoxBytes);
       for (int hh = 0; hh < 2; ++hh) {
@@ -536,6 +560,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
                     src.ax + h * src.a_step, row0 + rb * kBlockRows);
       }
       a_last[s] = i;
+      a_raw[s] = false;
       return true;
     };
     for (int i = 0; i < nu && ok; ++i) {
@@ -560,13 +585,17 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     }
     // Drain: every copy this thread issued has landed before the CTA exits.
     for (int s = 0; s < kRowBlocks * kAPairs; ++s) {
-      if (a_last[s] >= 0) mbar_wait(&a_full[s], a_last[s] & 1, nullptr);
+      if (a_last[s] >= 0) {
+        mbar_wait(a_raw[s] ? &st_full[s] : &a_full[s], a_last[s] & 1, nullptr);
+      }
     }
     for (int s = 0; s < kBS; ++s) {
       if (b_last[s] >= 0) mbar_wait(&b_full[s], (b_last[s] / kBS) & 1, nullptr);
     }
     for (int s = 0; s < kNS; ++s) {
-      if (st_last[s] >= 0) mbar_wait(&st_full[s], (st_last[s] / kNS) & 1, nullptr);
+      if (st_last[s] >= 0) {
+        mbar_wait(&st_full[s], (st_last[s] / (kNS > 0 ? kNS : 1)) & 1, nullptr);
+      }
     }
   } else if (warp == 1 && lane == 0) {
     // ------------------------------------------------------ MMA issuer --
@@ -645,12 +674,14 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     // the order the MMA pipe reads the boxes: row block 0, then row block
     // 1. Warps 0 and 1 fill box pair 0, warps 2 and 3 pair 1, so four boxes
     // are converted at once and each pair's a_full completes on its two
-    // warps' arrivals. The box's raw tile is staging slot seq % kNS, where
-    // seq = 8 i + 4 rb + w counts the DB boxes in the producer's order. Per
-    // box: lane 0 waits (bounded) for the raw tile and for the MMA pipe to
-    // have freed the box, and the warp shares the outcome; every lane loads
-    // its 16 raw units (16 bytes, eight K values each), the warp meets and
-    // lane 0 frees the staging slot; then the lanes write the units' x0 and
+    // warps' arrivals. Staged (narrow tiles): the box's raw tile is staging
+    // slot seq % kNS, where seq = 8 i + 4 rb + w counts the DB boxes in the
+    // producer's order; in place (full tiles): the first half of the box.
+    // Per box: lane 0 waits (bounded) for the raw tile (and, staged, for
+    // the MMA pipe to have freed the box) and the warp shares the outcome;
+    // every lane loads its 16 raw units (16 bytes, eight K values each), the
+    // warp meets (and lane 0 frees the staging slot); then the lanes write
+    // the units' x0 and
     // x1 digits into the box, fence them for the tensor core, meet again
     // and lane 0 arrives. Lane l takes the units g = 32 k + l: row
     // r = (l & 7) | k << 3, unit u = (l >> 3) & 3. Eight consecutive lanes
@@ -669,17 +700,24 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       for (int rb = 0; rb < kRowBlocks; ++rb) {
         const int s = rb * kAPairs + p;
         const int sq = 8 * i + 4 * rb + cw;
-        const int j = sq % kNS;
+        const int j = kStaged ? sq % kNS : 0;
+        const uint32_t box = ring + rb * kARingBytes + cw * kABoxBytes;
         bool ready = false;
         if (lane == 0) {
-          ready = mbar_wait(&st_full[j], (sq / kNS) & 1, err) &&
-                  mbar_wait(&a_empty[s], (i & 1) ^ 1, err);
+          if constexpr (kStaged) {
+            ready = mbar_wait(&st_full[j], (sq / kNS) & 1, err) &&
+                    mbar_wait(&a_empty[s], (i & 1) ^ 1, err);
+          } else {
+            ready = mbar_wait(&st_full[s], i & 1, err);
+          }
         }
         if (__shfl_sync(0xffffffffu, ready ? 1 : 0, 0) == 0) {
           ok = false;
           break;
         }
-        const uint32_t stage = ring + Plan::kStageBase + j * kRawTileBytes;
+        // Staged: the slot's tile; in place: the first half of the box.
+        const uint32_t stage =
+            kStaged ? ring + Plan::kStageBase + j * kRawTileBytes : box;
         uint4 raw[16];
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
@@ -687,8 +725,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
           raw[k] = lds128(stage + r * 64 + ((u ^ ((r >> 1) & 3)) << 4));
         }
         __syncwarp();
-        if (lane == 0) mbar_arrive(&st_empty[j]);
-        const uint32_t box = ring + rb * kARingBytes + cw * kABoxBytes;
+        if (kStaged && lane == 0) mbar_arrive(&st_empty[j]);
 #pragma unroll
         for (int k = 0; k < 16; ++k) {
           const int r = (lane & 7) | (k << 3);

@@ -2770,6 +2770,36 @@ int32_t inspire_pir_engine_table(inspire_pir_server* server, int32_t cap,
   return n;
 }
 
+int inspire_pir_server_set_tensor_planes(inspire_pir_server* server, int32_t keep,
+                                         char* err, size_t err_len) {
+  using namespace inspire;
+  if (server == nullptr) {
+    return Report(Err(INSPIRE_INVALID_ARGUMENT, "server is null."), err, err_len);
+  }
+  std::lock_guard<std::mutex> lock(server->mu);
+  Status st = Cuda(cudaDeviceSynchronize(), "synchronize");
+  if (!st.ok()) return Report(st, err, err_len);
+  const bool had = server->limb != nullptr;
+  if (server->ws0) server->ws0->limb.reset();
+  server->limb.reset();
+  server->crossover.store(-1);
+  server->tune_table.clear();
+  LimbGemm::Create(server->prm.coeff_bits, server->prm.db_kind, server->db.get(),
+                   server->rows, server->db_cols, server->prm.mat_kind, server->pack.get(),
+                   server->pack_cols, keep != 0, &server->limb);
+  if (had && !server->limb) {
+    return Report(Err(INSPIRE_INTERNAL, "tensor engine could not be re-created"), err,
+                  err_len);
+  }
+  return INSPIRE_OK;
+}
+
+int64_t inspire_pir_server_device_bytes(const inspire_pir_server* server) {
+  if (server == nullptr) return -1;
+  return static_cast<int64_t>(server->db.bytes() + server->pack.bytes()) +
+         (server->limb ? server->limb->ResidentBytes() : 0);
+}
+
 int inspire_pir_server_check(inspire_pir_server* server, char* err,
                              size_t err_len) {
   using namespace inspire;

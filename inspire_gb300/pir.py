@@ -477,6 +477,18 @@ class PirServer:
             ctypes.c_void_p(packing_key_ptr), ctypes.c_void_p(out_ptr), form,
             split, ctypes.c_void_p(stream), err, len(err)), err)
 
+    def set_tensor_planes(self, keep):
+        """Keep (True, the default) or drop the DB's resident fp16 digit
+        planes of the tensor engine; without them the engine reads the u16
+        DB as stored. Clears the tuned choices."""
+        err = _errbuf()
+        _check(_lib.load().inspire_pir_server_set_tensor_planes(
+            self._h, 1 if keep else 0, err, len(err)), err)
+
+    def device_bytes(self):
+        """Resident device bytes: DB, pack matrix and digit planes."""
+        return _lib.load().inspire_pir_server_device_bytes(self._h)
+
     def tune_engines(self, max_batch):
         """Times both engines at batch sizes up to max_batch and keeps the
         crossover for ENGINE_AUTO; returns it (0x7fffffff: never)."""

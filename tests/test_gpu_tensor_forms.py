@@ -127,3 +127,29 @@ def test_raw_form_unavailable_when_rows_are_not_16_byte_multiples():
     with pytest.raises(pir.InspireError) as e:
         _products(srv, params, fd, pk, form=pir.FORM_RAW)
     assert e.value.code == pir.FAILED_PRECONDITION
+
+
+def test_dropping_resident_planes_keeps_answers_and_frees_memory():
+    params = synthetic.make_params(d=256, n=2 * 16384, t=2, coeff_bits=32)
+    mat = synthetic.make_material(params, seed=9)
+    srv = _server(params, mat)
+    fd, sd, pk = synthetic.make_requests(params, 20, seed=10, full_range=True)
+    want = srv.process_arrays(fd, sd, pk, pir.ENGINE_PLAIN)
+    with_planes = srv.device_bytes()
+    srv.set_tensor_planes(False)
+    # The DB planes were 2 x the u16 DB.
+    assert with_planes - srv.device_bytes() == 2 * mat.db.nbytes
+    assert np.array_equal(srv.process_arrays(fd, sd, pk, pir.ENGINE_TENSOR),
+                          want)
+    srv.tune_engines(32)
+    assert np.array_equal(srv.process_arrays(fd, sd, pk, pir.ENGINE_AUTO),
+                          want)
+    assert all(r["form"].startswith("raw") for r in srv.engine_table())
+    with pytest.raises(pir.InspireError) as e:
+        _products(srv, params, fd, pk, form=pir.FORM_PLANES)
+    assert e.value.code == pir.FAILED_PRECONDITION
+    srv.set_tensor_planes(True)
+    assert srv.device_bytes() == with_planes
+    assert np.array_equal(_products(srv, params, fd, pk, form=pir.FORM_PLANES),
+                          _products(srv, params, fd, pk,
+                                    engine=pir.ENGINE_PLAIN))

@@ -254,9 +254,11 @@ int inspire_pir_external_product_device(inspire_pir_server* server,
  */
 /*
  * Autotuner of the tensor engine (no reference counterpart): times the
- * split-K factors of the batched product for `batch` requests on this
- * server's matrices and keeps the fastest for later batches of the same
- * size (rounded up to 64 requests). Reports the factor and the product's
+ * batched product for `batch` requests on this server's matrices in every
+ * available form (resident digit planes or the DB as stored), request tile
+ * (64 requests, 32 over Z_2^64; or 16, tried up to 64 requests) and split-K
+ * factor, and keeps the fastest for later batches of the same size
+ * (rounded up to 16 requests). Reports the split-K factor and the product's
  * time in ms. Synchronous; FAILED_PRECONDITION without the tensor engine.
  */
 int inspire_pir_autotune(inspire_pir_server* server, int32_t batch,

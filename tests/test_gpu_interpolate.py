@@ -99,6 +99,21 @@ def test_interpolate_db_matches_oracle(dtype, n, d, t, l, pad):
     assert np.array_equal(got, oracle_db(raw, n, d, t, l, p, cols))
 
 
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint16])
+def test_interpolate_db_streaming_many_tiles_per_block(dtype):
+    # 8197 groups x 2 class blocks: more tiles than SMs, so every block of
+    # the streaming kernel walks several tiles through its double-buffered
+    # input stage; the last tile holds 5 groups.
+    n, d, t, l = 8 * 8197, 256, 8, 1
+    p = 255 if dtype == np.uint8 else 65535
+    hi = 256 if dtype == np.uint8 else 65536
+    raw = np.random.default_rng(17).integers(0, hi, size=n * l * d).astype(dtype)
+    params = synthetic.make_params(d=d, n=n, t=t, l=l, coeff_bits=64,
+                                   log_q=52, plaintext_modulus=p)
+    got = pir.interpolate_db(raw, params, out_cols=n // t)
+    assert np.array_equal(got, oracle_db(raw, n, d, t, l, p, n // t))
+
+
 def test_interpolate_db_device_call_and_size_check():
     import ctypes
     import torch

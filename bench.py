@@ -625,7 +625,7 @@ def run_single_workload(args):
         if rc:
             raise SystemExit(err.value)
 
-    def per_step(fn, steps, warm):
+    def per_step(fn, steps, warm, label="timed_request"):
         for i in range(warm):
             fn(i % nreq)
         stream.synchronize()
@@ -635,9 +635,12 @@ def run_single_workload(args):
                 flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
+            # NVTX range: a profiler's launch list can keep only the request.
+            torch.cuda.nvtx.range_push(label)
             e0.record(stream)
             fn(i % nreq)
             e1.record(stream)
+            torch.cuda.nvtx.range_pop()
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
         return times
@@ -665,7 +668,7 @@ def run_single_workload(args):
     hbm, _, peak_kind = peaks()
     with ClockSampler(0) as clk:
         t_ans = per_step(answer, args.steps, args.warmup)
-    t_prod_ms = per_step(products, args.steps, args.warmup)
+    t_prod_ms = per_step(products, args.steps, args.warmup, "timed_products")
 
     # The same answer replayed from a CUDA graph (one launch per request).
     graphs = []
@@ -673,7 +676,8 @@ def run_single_workload(args):
         with pir.Graph(sptr) as g:
             answer(i)
         graphs.append(g)
-    t_graph = per_step(lambda i: graphs[i].launch(sptr), args.steps, args.warmup)
+    t_graph = per_step(lambda i: graphs[i].launch(sptr), args.steps, args.warmup,
+                       "timed_graph")
 
     # End to end through the host-buffer C ABI (pinned host memory).
     h_fd = torch.from_numpy(fd.view(iv)).pin_memory().numpy().view(params.coeff_dtype)

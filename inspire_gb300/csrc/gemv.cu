@@ -205,10 +205,12 @@ cudaError_t launch_typed(const void* db, int64_t db_cols, const void* q1,
                          const void* yg, int64_t yg_stride, void* out,
                          int64_t out_stride, int64_t rows,
                          cudaStream_t stream) {
-  if (NQ == 1 && rows < 16384) {
+  if (NQ == 1 && rows < 16384 && rows > 4 * 1216) {
     // Smaller matrices (e.g. 8192 rows: 2048 blocks of 4 rows are 1.7 waves)
     // take 2 rows per block, which evens out the last wave: 0.84 instead of
-    // 0.78 of the copy peak at 8192 x 16384 u16 + 8192 x 4096 i32.
+    // 0.78 of the copy peak at 8192 x 16384 u16 + 8192 x 4096 i32. Up to
+    // 4 x 1216 rows (1216 blocks of 256 threads: one wave at eight blocks
+    // per SM) the 4-row blocks below all run in one wave.
     fused_gemv_kernel<T, DbT, MatT, 2, NQ, kThreads>
         <<<static_cast<unsigned>((rows + 1) / 2), kThreads, 0, stream>>>(
             static_cast<const DbT*>(db), db_cols, static_cast<const T*>(q1),

@@ -206,6 +206,92 @@ __device__ __forceinline__ uint32_t scale_p(uint32_t x, uint32_t tinv, uint32_t 
   }
 }
 
+// r with its low `bits` bits reversed (bits <= 3), a constant expression for
+// a constant r, so that register arrays indexed by it stay in registers.
+__host__ __device__ constexpr int bit_reverse(int r, int bits) {
+  return bits == 1 ? r
+         : bits == 2 ? ((r & 1) << 1) | ((r >> 1) & 1)
+                     : ((r & 1) << 2) | (r & 2) | ((r >> 2) & 1);
+}
+
+// The t x t/2 values of subproblem (group grp, class c) in bit-reversed
+// record order, as they are stored (no reduction).
+template <typename V, int T>
+__device__ __forceinline__ void lazy_load(uint32_t (&x)[T][T / 2], const V* __restrict__ raw,
+                                          int64_t grp, int64_t rec_stride, int k, int c,
+                                          const InterpArgs& a) {
+  constexpr int LOGT = T == 2 ? 1 : (T == 4 ? 2 : 3);
+#pragma unroll
+  for (int r = 0; r < T; ++r) {
+    const V* src = raw + (grp * T + r) * rec_stride + static_cast<int64_t>(k) * a.d + c;
+#pragma unroll
+    for (int m = 0; m < T / 2; ++m) {
+      x[bit_reverse(r, LOGT)][m] = static_cast<uint32_t>(src[m * a.s]);
+    }
+  }
+}
+
+// One butterfly stage (pairs LEN/2 apart within blocks of LEN) of the lazy
+// transform, then the next: every bound is a template constant, so the
+// subproblem's registers are indexed by constants only.
+template <int T, int LEN>
+__device__ __forceinline__ void lazy_stage(uint32_t (&x)[T][T / 2]) {
+  constexpr int H = T / 2;
+  constexpr int h = LEN / 2;
+#pragma unroll
+  for (int i = 0; i < T; i += LEN) {
+#pragma unroll
+    for (int j = 0; j < h; ++j) {
+      // w^j = X^(j (2d - 2d/LEN)): in units of s a rotation by wu classes
+      // mod T, negating all when it reaches d (H units).
+      const int wu = (j * (T - T / LEN)) % T;
+      const bool neg_all = wu >= H;
+      const int q = neg_all ? wu - H : wu;
+      int32_t v[H];
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        const bool wrap = m < q;
+        const int32_t b = static_cast<int32_t>(x[i + j + h][wrap ? m - q + H : m - q]);
+        v[m] = (wrap != neg_all) ? -b : b;
+      }
+#pragma unroll
+      for (int m = 0; m < H; ++m) {
+        const int32_t u = static_cast<int32_t>(x[i + j][m]);
+        x[i + j][m] = static_cast<uint32_t>(u + v[m]);
+        x[i + j + h][m] = static_cast<uint32_t>(u - v[m]);
+      }
+    }
+  }
+  if constexpr (2 * LEN <= T) lazy_stage<T, 2 * LEN>(x);
+}
+
+// The lazy transform of one (group, class) subproblem x (t x t/2 values
+// of at most max(V) each, bit-reversed record order): butterflies on signed
+// integers, (u, b) -> (u + v, u - v) with v = +-b, the rotation's
+// permutation and sign fixed at compile time; |x| <= t * max(V) after
+// log2(t) stages. One reduction at the end, (x + lazy_off) * t^-1 mod p
+// (Shoup, valid for any 32-bit operand), written to the block's tile at
+// column gi.
+template <typename V, int T>
+__device__ __forceinline__ void lazy_transform_store(uint32_t (&x)[T][T / 2], int gi, int c0,
+                                                     const InterpArgs& a, const ModConsts& mc,
+                                                     V* tile) {
+  constexpr int H = T / 2;
+  constexpr int kRow = FastShape<V>::kRow;
+  lazy_stage<T, 2>(x);
+#pragma unroll
+  for (int r = 0; r < T; ++r) {
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      const uint32_t y = x[r][m] + a.lazy_off;  // in [0, 2 lazy_off)
+      const uint32_t qq = __umulhi(y, mc.tinv_s32);
+      uint32_t rr = y * a.tinv - qq * a.p;
+      rr = rr >= a.p ? rr - a.p : rr;
+      tile[((r * H + m) * kFastR + c0) * kRow + gi] = static_cast<V>(rr);
+    }
+  }
+}
+
 // LAZY: the transform runs on signed 32-bit integers without any reduction:
 // every butterfly is an addition and a subtraction of values whose rotation
 // by a power of w only permutes and negates them, so after log2(t) stages
@@ -234,6 +320,20 @@ interpolate_fast_kernel(const V* __restrict__ raw, InterpArgs a, ModConsts mc,
   const int k = blockIdx.z;
   const int64_t rec_stride = static_cast<int64_t>(a.l) * a.d;
   const uint32_t p = a.p;
+  if constexpr (LAZY) {
+    // Two groups per pass: both groups' 2 t (t/2) loads are issued before
+    // either is transformed, twice the bytes in flight per warp.
+    for (int gi = gw; gi < kFastG; gi += 2 * kFastGW) {
+      const int gj = gi + kFastGW;
+      const bool ha = g_base + gi < a.groups;
+      const bool hb = gj < kFastG && g_base + gj < a.groups;
+      uint32_t xa[T][H], xb[T][H];
+      if (ha) lazy_load<V, T>(xa, raw, g_base + gi, rec_stride, k, c_start + c0, a);
+      if (hb) lazy_load<V, T>(xb, raw, g_base + gj, rec_stride, k, c_start + c0, a);
+      if (ha) lazy_transform_store<V, T>(xa, gi, c0, a, mc, tile);
+      if (hb) lazy_transform_store<V, T>(xb, gj, c0, a, mc, tile);
+    }
+  } else {
   for (int gi = gw; gi < kFastG; gi += kFastGW) {
     const int64_t grp = g_base + gi;
     if (grp >= a.groups) break;
@@ -248,53 +348,10 @@ interpolate_fast_kernel(const V* __restrict__ raw, InterpArgs a, ModConsts mc,
                      c_start + c0;
 #pragma unroll
       for (int m = 0; m < H; ++m) {
-        const uint32_t v = static_cast<uint32_t>(src[m * a.s]);
-        x[rb][m] = LAZY ? v : reduce_p(v, p, mc.barrett);
+        x[rb][m] = reduce_p(static_cast<uint32_t>(src[m * a.s]), p, mc.barrett);
       }
     }
-    if constexpr (LAZY) {
-      // Butterflies on signed integers: (u, b) -> (u + v, u - v) with
-      // v = +-b, the rotation's permutation and sign fixed at compile time.
-#pragma unroll
-      for (int len = 2; len <= T; len <<= 1) {
-        const int h = len / 2;
-#pragma unroll
-        for (int i = 0; i < T; i += len) {
-#pragma unroll
-          for (int j = 0; j < h; ++j) {
-            const int wu = (j * (T - T / len)) % T;
-            const bool neg_all = wu >= H;
-            const int q = neg_all ? wu - H : wu;
-            int32_t v[H];
-#pragma unroll
-            for (int m = 0; m < H; ++m) {
-              const bool wrap = m < q;
-              const int src = wrap ? m - q + H : m - q;
-              const int32_t b = static_cast<int32_t>(x[i + j + h][src]);
-              v[m] = (wrap != neg_all) ? -b : b;
-            }
-#pragma unroll
-            for (int m = 0; m < H; ++m) {
-              const int32_t u = static_cast<int32_t>(x[i + j][m]);
-              x[i + j][m] = static_cast<uint32_t>(u + v[m]);
-              x[i + j + h][m] = static_cast<uint32_t>(u - v[m]);
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int r = 0; r < T; ++r) {
-#pragma unroll
-        for (int m = 0; m < H; ++m) {
-          const uint32_t y = x[r][m] + a.lazy_off;  // in [0, 2 lazy_off)
-          const uint32_t qq = __umulhi(y, mc.tinv_s32);
-          uint32_t rr = y * a.tinv - qq * p;
-          rr = rr >= p ? rr - p : rr;
-          tile[((r * H + m) * kFastR + c0) * kRow + gi] = static_cast<V>(rr);
-        }
-      }
-      continue;
-    }
+
     // Butterflies: len = 2 .. T; pair (i + j, i + j + h) with w^j.
 #pragma unroll
     for (int len = 2; len <= T; len <<= 1) {
@@ -336,6 +393,7 @@ interpolate_fast_kernel(const V* __restrict__ raw, InterpArgs a, ModConsts mc,
       }
     }
   }
+  }
   __syncthreads();
   // Stores: kFastG consecutive columns of each DB row.
   const int64_t left = a.groups - g_base;
@@ -371,189 +429,6 @@ interpolate_fast_kernel(const V* __restrict__ raw, InterpArgs a, ModConsts mc,
                         c_start + c + static_cast<int64_t>(m) * a.s;
     out[row * a.out_cols + g_base + g] = tile[(rm * kFastR + c) * kRow + g];
   }
-}
-
-// Streaming form of the lazy kernel for 8- and 16-bit records: persistent
-// blocks (one per SM: 198 KB of shared memory at t = 8, 16-bit) walk the
-// (class block, group block) tiles, and while one tile is transformed and
-// stored the next tile's records are already on their way into the other
-// half of a double-buffered input stage with cp.async (16-byte copies, no
-// registers held), so every SM keeps a whole tile (64 KB at t = 8) of reads
-// in flight. Tile = kStreamG groups x 32 classes, the transform and the
-// transposed stores as in interpolate_fast_kernel (LAZY). Input stage:
-// [group][record (bit-reversed order)][m][class].
-constexpr int kStreamG = 32;   // groups per tile
-constexpr int kStreamThreads = 256;
-
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
-  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst));
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gmem_src)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;" ::: "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all_but_one() {
-  asm volatile("cp.async.wait_group 1;" ::: "memory");
-}
-
-template <typename V, int T>
-struct StreamShape {
-  static constexpr int H = T / 2;
-  static constexpr int kSeg = kFastR * static_cast<int>(sizeof(V));   // bytes of 32 classes
-  static constexpr int kChunks = kSeg / 16;                           // 16-byte copies per segment
-  static constexpr int kStageValues = kStreamG * T * H * kFastR;      // one tile's inputs
-  static constexpr int kRow = kStreamG + (sizeof(V) == 2 ? 2 : 1);    // output tile pitch
-  static constexpr int kOutValues = T * H * kFastR * kRow;
-  static constexpr size_t kSmem =
-      (2 * static_cast<size_t>(kStageValues) + kOutValues) * sizeof(V);
-};
-
-template <typename V, int T>
-__global__ void __launch_bounds__(kStreamThreads, 1)
-interpolate_stream_kernel(const V* __restrict__ raw, InterpArgs a, ModConsts mc,
-                          V* __restrict__ out) {
-  using S = StreamShape<V, T>;
-  constexpr int H = S::H;
-  constexpr int LOGT = T == 2 ? 1 : (T == 4 ? 2 : 3);
-  constexpr int kRow = S::kRow;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  V* stage = reinterpret_cast<V*>(smem_raw);            // [2][kStageValues]
-  V* tile = stage + 2 * S::kStageValues;                // [T*H][32][kRow]
-  const int c0 = threadIdx.x % kFastR;
-  const int gw = threadIdx.x / kFastR;
-  constexpr int kWarps = kStreamThreads / kFastR;
-  const int n_cb = a.s / kFastR;
-  const int64_t n_gb = (a.groups + kStreamG - 1) / kStreamG;
-  const int64_t n_tiles = n_cb * n_gb * a.l;
-  const int64_t rec_stride = static_cast<int64_t>(a.l) * a.d;
-  const uint32_t p = a.p;
-
-  // Copies of one tile's records into stage buffer `buf`: segment
-  // (g, r, m) = 32 classes of record g*T + r at position c_start + m*s.
-  auto fetch = [&](int64_t tl, int buf) {
-    const int cb = static_cast<int>(tl % n_cb);
-    const int64_t rest = tl / n_cb;
-    const int64_t gb = rest % n_gb;
-    const int k = static_cast<int>(rest / n_gb);
-    const int64_t g0 = gb * kStreamG;
-    const int G = static_cast<int>(min(static_cast<int64_t>(kStreamG), a.groups - g0));
-    const int n = G * T * H * S::kChunks;
-    V* dst0 = stage + buf * S::kStageValues;
-    for (int q = threadIdx.x; q < n; q += kStreamThreads) {
-      const int piece = q % S::kChunks;
-      const int seg = q / S::kChunks;      // (g * T + r) * H + m
-      const int m = seg % H;
-      const int gr = seg / H;              // g * T + r
-      const int r = gr % T, g = gr / T;
-      int rb = 0;
-#pragma unroll
-      for (int b = 0; b < LOGT; ++b) rb |= ((r >> b) & 1) << (LOGT - 1 - b);
-      const V* src = raw + ((g0 + g) * T + r) * rec_stride + static_cast<int64_t>(k) * a.d +
-                     cb * kFastR + static_cast<int64_t>(m) * a.s +
-                     piece * (16 / static_cast<int>(sizeof(V)));
-      V* dst = dst0 + ((g * T + rb) * H + m) * kFastR + piece * (16 / static_cast<int>(sizeof(V)));
-      cp_async16(dst, src);
-    }
-  };
-
-  int64_t tl = blockIdx.x;
-  int buf = 0;
-  if (tl < n_tiles) fetch(tl, 0);
-  cp_async_commit();
-  for (; tl < n_tiles; tl += gridDim.x, buf ^= 1) {
-    if (tl + gridDim.x < n_tiles) fetch(tl + gridDim.x, buf ^ 1);
-    cp_async_commit();
-    cp_async_wait_all_but_one();
-    __syncthreads();  // the tile's records are in; the last stores are done
-    const int cb = static_cast<int>(tl % n_cb);
-    const int64_t rest = tl / n_cb;
-    const int64_t gb = rest % n_gb;
-    const int k = static_cast<int>(rest / n_gb);
-    const int64_t g_base = gb * kStreamG;
-    const int G = static_cast<int>(min(static_cast<int64_t>(kStreamG), a.groups - g_base));
-    const V* in = stage + buf * S::kStageValues;
-    for (int gi = gw; gi < G; gi += kWarps) {
-      uint32_t x[T][H];
-#pragma unroll
-      for (int r = 0; r < T; ++r)
-#pragma unroll
-        for (int m = 0; m < H; ++m) x[r][m] = in[((gi * T + r) * H + m) * kFastR + c0];
-#pragma unroll
-      for (int len = 2; len <= T; len <<= 1) {
-        const int h = len / 2;
-#pragma unroll
-        for (int i = 0; i < T; i += len) {
-#pragma unroll
-          for (int j = 0; j < h; ++j) {
-            const int wu = (j * (T - T / len)) % T;
-            const bool neg_all = wu >= H;
-            const int q = neg_all ? wu - H : wu;
-            int32_t v[H];
-#pragma unroll
-            for (int m = 0; m < H; ++m) {
-              const bool wrap = m < q;
-              const int src = wrap ? m - q + H : m - q;
-              const int32_t b = static_cast<int32_t>(x[i + j + h][src]);
-              v[m] = (wrap != neg_all) ? -b : b;
-            }
-#pragma unroll
-            for (int m = 0; m < H; ++m) {
-              const int32_t u = static_cast<int32_t>(x[i + j][m]);
-              x[i + j][m] = static_cast<uint32_t>(u + v[m]);
-              x[i + j + h][m] = static_cast<uint32_t>(u - v[m]);
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int r = 0; r < T; ++r) {
-#pragma unroll
-        for (int m = 0; m < H; ++m) {
-          const uint32_t y = x[r][m] + a.lazy_off;
-          const uint32_t qq = __umulhi(y, mc.tinv_s32);
-          uint32_t rr = y * a.tinv - qq * p;
-          rr = rr >= p ? rr - p : rr;
-          tile[((r * H + m) * kFastR + c0) * kRow + gi] = static_cast<V>(rr);
-        }
-      }
-    }
-    __syncthreads();
-    // Stores: G consecutive columns of each of the tile's DB rows.
-    const int c_start = cb * kFastR;
-    bool paired = false;
-    if constexpr (sizeof(V) == 2) {
-      paired = (a.out_cols & 1) == 0 && G == kStreamG &&
-               (reinterpret_cast<uintptr_t>(out) & 3) == 0;
-    }
-    if (paired) {
-      constexpr int kPairs = kStreamG / 2;
-      for (int idx = threadIdx.x; idx < T * H * kFastR * kPairs; idx += kStreamThreads) {
-        const int gp = idx % kPairs;
-        const int c = (idx / kPairs) % kFastR;
-        const int rm = idx / (kPairs * kFastR);
-        const int r = rm / H, m = rm % H;
-        const int64_t row = static_cast<int64_t>(k) * T * a.d + static_cast<int64_t>(r) * a.d +
-                            c_start + c + static_cast<int64_t>(m) * a.s;
-        const uint32_t v =
-            *reinterpret_cast<const uint32_t*>(tile + (rm * kFastR + c) * kRow + 2 * gp);
-        *reinterpret_cast<uint32_t*>(out + row * a.out_cols + g_base + 2 * gp) = v;
-      }
-    } else {
-      for (int idx = threadIdx.x; idx < T * H * kFastR * kStreamG; idx += kStreamThreads) {
-        const int g = idx % kStreamG;
-        const int c = (idx / kStreamG) % kFastR;
-        const int rm = idx / (kStreamG * kFastR);
-        if (g >= G) continue;
-        const int r = rm / H, m = rm % H;
-        const int64_t row = static_cast<int64_t>(k) * T * a.d + static_cast<int64_t>(r) * a.d +
-                            c_start + c + static_cast<int64_t>(m) * a.s;
-        out[row * a.out_cols + g_base + g] = tile[(rm * kFastR + c) * kRow + g];
-      }
-    }
-  }
-  cp_async_wait_all_but_one();
-  asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 // t == 1: the transposition alone (Interpolate returns the row unchanged).
@@ -659,41 +534,6 @@ int Run(const V* raw, int64_t n, int d, int t, int l, uint32_t p, V* out,
       const uint64_t off = (bound + p - 1) / p * p;
       const bool lazy = sizeof(V) <= 2 && small && 2 * off < (1ull << 31);
       a.lazy_off = static_cast<uint32_t>(lazy ? off : 0);
-      // The streaming kernel when the records are 16-byte addressable.
-      const bool stream_ok =
-          lazy && (reinterpret_cast<uintptr_t>(raw) & 15) == 0 &&
-          (static_cast<int64_t>(a.s) * sizeof(V)) % 16 == 0 &&
-          (static_cast<int64_t>(d) * sizeof(V)) % 16 == 0;
-      if (stream_ok) {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const int64_t tiles = static_cast<int64_t>(a.s / kFastR) *
-                              ((groups + kStreamG - 1) / kStreamG) * l;
-        const unsigned blocks =
-            static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(tiles, sms)));
-        auto launch_s = [&](auto kernel, size_t smem) {
-          cudaError_t r = cudaFuncSetAttribute(
-              kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-          if (r == cudaSuccess) {
-            kernel<<<blocks, kStreamThreads, smem, st>>>(raw, a, mc, out);
-            r = cudaGetLastError();
-          }
-          return r;
-        };
-        if (t == 2) {
-          e = launch_s(interpolate_stream_kernel<V, 2>, StreamShape<V, 2>::kSmem);
-        } else if (t == 4) {
-          e = launch_s(interpolate_stream_kernel<V, 4>, StreamShape<V, 4>::kSmem);
-        } else {
-          e = launch_s(interpolate_stream_kernel<V, 8>, StreamShape<V, 8>::kSmem);
-        }
-        if (e != cudaSuccess) {
-          return Fail(err, err_len, INSPIRE_INTERNAL,
-                      std::string("interpolate: ") + cudaGetErrorString(e));
-        }
-        return INSPIRE_OK;
-      }
       constexpr int kFastG = FastShape<V>::kG;
       dim3 grid(static_cast<unsigned>(a.s / kFastR),
                 static_cast<unsigned>((groups + kFastG - 1) / kFastG), static_cast<unsigned>(l));

@@ -103,6 +103,8 @@ def main(argv=None):
     ap.add_argument("--pool", type=int, default=64)
     ap.add_argument("--max-batch", type=int, default=256)
     ap.add_argument("--hbm-budget-gb", type=float, default=48.0)
+    ap.add_argument("--max-workspaces", type=int, default=1,
+                    help="batches in flight per server at most")
     ap.add_argument("--max-wait-us", type=int, default=0,
                     help="batching window of the serving loop")
     ap.add_argument("--plain-max-batch", type=int, default=None,
@@ -138,7 +140,7 @@ def main(argv=None):
     loads = []
     with serving.ServingEngine(servers, max_batch=args.max_batch,
                                hbm_budget=int(args.hbm_budget_gb * (1 << 30)),
-                               max_workspaces=3,
+                               max_workspaces=args.max_workspaces,
                                plain_max_batch=args.plain_max_batch,
                                max_wait_us=args.max_wait_us) as eng:
         for frac in [float(x) for x in args.loads.split(",")]:
@@ -174,6 +176,7 @@ def main(argv=None):
                    "plain_max_batch": args.plain_max_batch,
                    "tuned_crossovers": crossovers,
                    "hbm_budget_gb": args.hbm_budget_gb,
+                   "max_workspaces": args.max_workspaces,
                    "workspaces": ws},
         "peak_qps": peak,
         "per_server_peak_qps": per_rate,

@@ -193,8 +193,9 @@ int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,
  * shapes of the same product). form INSPIRE_FORM_PLANES reads the DB as
  * resident fp16 digit planes, INSPIRE_FORM_RAW reads the DB as stored (u16)
  * and splits it into digits in shared memory; or-ed with
- * INSPIRE_FORM_NARROW the kernel takes 16 requests per tile instead of 64
- * (32 over Z_2^64). split > 0 forces that split-K factor (0: the tuned or
+ * INSPIRE_FORM_NARROW the kernel takes 16 requests per tile instead of 64.
+ * The raw form and the narrow tiles serve Z_2^32 servers; a Z_2^64 server
+ * runs the planes with 32-request tiles. split > 0 forces that split-K factor (0: the tuned or
  * heuristic one). Same buffers and result as inspire_pir_products_device
  * with INSPIRE_ENGINE_TENSOR. FAILED_PRECONDITION when the server has no
  * such form.

@@ -1073,7 +1073,10 @@ class LimbGemmImpl : public LimbGemm {
     pk_cols_ = pack_cols;
     cpad_ = round_up(db_cols, kUnitK);
     kpad_ = round_up(pack_cols, kUnitK);
-    conv_ = make_raw_map(&tm_raw_, db, rows, db_cols);
+    // The converting form and the narrow tiles serve Z_2^32 words; over
+    // Z_2^64 the engine keeps the resident planes and full tiles (the form
+    // the 64-bit tests and benchmarks were validated with).
+    conv_ = nq == 4 && make_raw_map(&tm_raw_, db, rows, db_cols);
     if (!conv_) planes = true;  // rows not 16-byte multiples: planes only
     if (cudaMalloc(&err_, sizeof(int)) != cudaSuccess) return false;
     if (cudaMemset(err_, 0, sizeof(int)) != cudaSuccess) return false;
@@ -1109,11 +1112,6 @@ class LimbGemmImpl : public LimbGemm {
       }
     } else {
       allow(reinterpret_cast<const void*>(limb_gemm_kernel<8, false, 32>));
-      allow(reinterpret_cast<const void*>(limb_gemm_kernel<8, false, kNarrowTQ>));
-      if (conv_) {
-        allow(reinterpret_cast<const void*>(limb_gemm_kernel<8, true, 32>));
-        allow(reinterpret_cast<const void*>(limb_gemm_kernel<8, true, kNarrowTQ>));
-      }
     }
     return fe == cudaSuccess;
   }
@@ -1190,6 +1188,7 @@ class LimbGemmImpl : public LimbGemm {
   };
 
   bool Available(const Choice& c) const {
+    if (c.narrow && nq_ != 4) return false;
     return (c.form == kFormRaw && conv_) || (c.form == kFormPlanes && db_planes_);
   }
 
@@ -1218,7 +1217,8 @@ class LimbGemmImpl : public LimbGemm {
     }
     Choice best = Heuristic(batch);
     float best_t = 0;
-    for (int narrow = 0; narrow <= (batch <= 64 ? 1 : 0) && e == cudaSuccess; ++narrow) {
+    for (int narrow = 0; narrow <= (batch <= 64 && nq_ == 4 ? 1 : 0) && e == cudaSuccess;
+         ++narrow) {
       const int tq = narrow ? kNarrowTQ : tq_;
       const int64_t tiles = (rows_ / kTileRows) * ((batch + tq - 1) / tq);
       const int heuristic = ChooseSplit(tiles, n_units);
@@ -1340,10 +1340,7 @@ class LimbGemmImpl : public LimbGemm {
       if (raw && !c.narrow) INSPIRE_LIMB_LAUNCH(4, true, 64, qs4, o4);
       if (raw && c.narrow) INSPIRE_LIMB_LAUNCH(4, true, kNarrowTQ, qs4, o4);
     } else {
-      if (!raw && !c.narrow) INSPIRE_LIMB_LAUNCH(8, false, 32, qs8, o8);
-      if (!raw && c.narrow) INSPIRE_LIMB_LAUNCH(8, false, kNarrowTQ, qs8, o8);
-      if (raw && !c.narrow) INSPIRE_LIMB_LAUNCH(8, true, 32, qs8, o8);
-      if (raw && c.narrow) INSPIRE_LIMB_LAUNCH(8, true, kNarrowTQ, qs8, o8);
+      INSPIRE_LIMB_LAUNCH(8, false, 32, qs8, o8);  // Available(): planes, full tiles
     }
 #undef INSPIRE_LIMB_LAUNCH
     return cudaGetLastError();

@@ -1,7 +1,8 @@
 """The forms of the tensor engine's product: the DB as resident fp16 digit
 planes, or read as stored (u16) and split into digits in shared memory by
-the kernel's converter warpgroup, each with full (64-request; 32 over
-Z_2^64) or narrow (16-request) tiles. All must give the plain engine's
+the kernel's converter warpgroup, each with full (64-request) or narrow
+(16-request) tiles; over Z_2^64 the planes with 32-request tiles only. All
+must give the plain engine's
 stage-1 words (b' + b_agg_partial, pir_server.cc:215-254) bit for
 bit, for every split-K factor, ragged batches, column counts that are not a
 multiple of the 128-column accumulation unit, both word sizes, and DB
@@ -59,7 +60,6 @@ def _products(srv, params, fd, pk, engine=None, form=None, split=0):
     (32, 128, 8192, 2, 65),      # a ragged second request tile
     (32, 256, 16000, 4, 7),      # C = 4000: the last unit reads past the end
     (32, 1024, 32768, 4, 130),   # three request tiles
-    (64, 256, 8192, 2, 33),      # Z_2^64: 32 requests per tile
 ])
 def test_raw_form_equals_planes_and_plain(cb, d, n, t, batch):
     params = synthetic.make_params(d=d, n=n, t=t, coeff_bits=cb,
@@ -112,6 +112,30 @@ def test_raw_form_extreme_entries(db_value):
     narrow = _products(srv, params, fd, pk,
                        form=pir.FORM_RAW | pir.FORM_NARROW)
     assert np.array_equal(narrow, plain)
+
+
+def test_z64_engine_keeps_planes_and_full_tiles():
+    # Over Z_2^64 the tensor engine runs its resident planes with 32-request
+    # tiles only; the other forms are refused, and AUTO / TENSOR answer as
+    # the plain engine does.
+    params = synthetic.make_params(d=256, n=8192, t=2, coeff_bits=64,
+                                   log_q=56)
+    mat = synthetic.make_material(params, seed=33)
+    srv = _server(params, mat)
+    fd, sd, pk = synthetic.make_requests(params, 33, seed=34, full_range=True)
+    plain = _products(srv, params, fd, pk, engine=pir.ENGINE_PLAIN)
+    assert np.array_equal(_products(srv, params, fd, pk,
+                                    form=pir.FORM_PLANES), plain)
+    for form in (pir.FORM_RAW, pir.FORM_PLANES | pir.FORM_NARROW,
+                 pir.FORM_RAW | pir.FORM_NARROW):
+        with pytest.raises(pir.InspireError) as e:
+            _products(srv, params, fd, pk, form=form)
+        assert e.value.code == pir.FAILED_PRECONDITION
+    srv.tune_engines(64)
+    assert all(r["form"] == "planes" for r in srv.engine_table())
+    want = srv.process_arrays(fd, sd, pk, pir.ENGINE_PLAIN)
+    assert np.array_equal(srv.process_arrays(fd, sd, pk, pir.ENGINE_AUTO),
+                          want)
 
 
 def test_raw_form_unavailable_when_rows_are_not_16_byte_multiples():

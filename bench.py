@@ -450,16 +450,35 @@ def run_interpolate_workload(args):
     moved = 2 * raw.nbytes
     hbm, _, peak_kind = peaks()
     gbs = moved / (ms / 1000.0) / 1e9
+
+    # Bit-exact check of the timed output: the first, middle and last DB
+    # columns (one group of t records each) against the oracle's Interpolate.
+    from oracle import pyoracle as orc
+    groups = raw.reshape(n // t, t * d)
+    picks = sorted({0, (n // t) // 2, n // t - 1})
+    t0 = time.perf_counter()
+    bad = [i for i in picks
+           if not np.array_equal(t_out[:, i].cpu().numpy().view(np.uint16),
+                                 orc.interpolate(groups[i], d, t, p))]
+    if bad:
+        raise SystemExit("interpolated DB columns %s differ from the oracle"
+                         % bad)
+    ocheck = {"columns": picks, "mismatches": bad,
+              "oracle": "Interpolate restated on the host",
+              "seconds": round(time.perf_counter() - t0, 2)}
+    n_txt = ("2^%d" % (n.bit_length() - 1)) if n & (n - 1) == 0 else str(n)
     line = {
-        "metric": "DB interpolation + transposition GB/s (n=2^20, d=4096, "
-                  "t=8, u16 records), bit-exact",
+        "metric": "DB interpolation + transposition GB/s (n=%s, d=%d, "
+                  "t=%d, u16 records), bit-exact" % (n_txt, d, t),
         "value": gbs, "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u16",
         "data": "synthetic (seeded uniform records in [0, p))",
-        "config": {"workload": "interpolate_n%d_d4096_t8_l1_u16" % n,
+        "config": {"workload": "interpolate_n%d_d%d_t%d_l1_u16" % (n, d, t),
                    "records_per_s": n / (ms / 1000.0),
-                   "l2": "inputs larger than L2 (8 GiB)"},
+                   "l2": "inputs larger than L2 (%.0f GiB)"
+                         % (raw.nbytes / 2**30)},
+        "oracle_check": ocheck,
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm,
                      "unit": "GB/s", "frac": gbs / hbm, "traffic": None,
                      "peak_kind": peak_kind},
@@ -531,9 +550,29 @@ def run_hint_workload(args):
         for _ in range(args.steps):
             step()
     ms = (time.perf_counter() - t0) * 1000 / args.steps
+
+    # Exact check of the timed output: the first, middle and last hint rows
+    # against the oracle's exact negacyclic inner product of the DB row's n
+    # polynomials with the reversed-negated a-components.
+    from oracle import pyoracle as orc
+    vinv = np.concatenate([a[:, :1], (0 - a[:, :0:-1].astype(np.uint64))
+                           .astype(np.uint32)], axis=1)
+    chunk = min(20, int((53.0 - np.log2(n) - np.log2(d)) / 2.0))
+    picks = sorted({0, rows // 2, rows - 1})
+    t0 = time.perf_counter()
+    bad = [i for i in picks
+           if not np.array_equal(
+               t_out[i].cpu().numpy().view(np.uint32),
+               orc.inner_product(db[i].reshape(n, d).astype(np.uint32), vinv,
+                                 32, 16, 32, chunk))]
+    if bad:
+        raise SystemExit("hint rows %s differ from the oracle" % bad)
+    ocheck = {"rows": picks, "mismatches": bad,
+              "oracle": "exact inner product restated on the host",
+              "seconds": round(time.perf_counter() - t0, 2)}
     line = {
-        "metric": "hint matrix rows/s (ComputeHintMatrix, 32768 x 131072 "
-                  "u16 DB, 32 a-components, d=4096, Z_2^32), exact",
+        "metric": "hint matrix rows/s (ComputeHintMatrix, %d x %d u16 DB, "
+                  "%d a-components, d=%d, Z_2^32), exact" % (rows, cols, n, d),
         "value": rows / (ms / 1000.0), "unit": "rows/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -544,13 +583,10 @@ def run_hint_workload(args):
                    "cols": cols, "a_components": n,
                    "ntts_per_step": rows * (n + 1) * 3,
                    "timing": "host clock around synchronous calls"},
+        "oracle_check": ocheck,
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:
-        from oracle import pyoracle as orc
-        vinv = np.concatenate([a[:, :1], (0 - a[:, :0:-1].astype(np.uint64))
-                               .astype(np.uint32)], axis=1)
-        chunk = min(20, int((53.0 - np.log2(n) - np.log2(d)) / 2.0))
         t0 = time.perf_counter()
         done = 0
         while time.perf_counter() - t0 < 10.0:

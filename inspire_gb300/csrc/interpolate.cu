@@ -148,16 +148,18 @@ interpolate_kernel(const V* __restrict__ raw, InterpArgs a, V* __restrict__ out)
 // stores run over kFastG consecutive groups (DB columns).
 constexpr int kFastR = 32;   // classes per block (one warp's lanes)
 // Groups per block (kG: the stores run over kG consecutive columns) and
-// groups in flight (kGW warps per block). 16-bit values take 32 groups
-// (64-byte stores, a 68 KB tile at t = 8, three blocks per SM); wider values
-// 16, which keeps the tile within a block's limit.
+// groups in flight (kGW warps per block). 8- and 16-bit values take 32
+// groups (64-byte row pieces; an 80 KB tile of 16-bit values at t = 8, two
+// blocks per SM, as the registers of the t = 8 transform allow); wider
+// values 16, which keeps the tile within a block's limit.
 template <typename V>
 struct FastShape {
   static constexpr int kG = sizeof(V) <= 2 ? 32 : 16;
   static constexpr int kGW = 8;
-  // Tile row pitch in values: padded against bank conflicts, and even for
-  // 16-bit values so that two neighbouring groups read as one 32-bit word.
-  static constexpr int kRow = kG + (sizeof(V) == 2 ? 2 : 1);
+  // Tile row pitch in values: padded against bank conflicts; for 16-bit
+  // values 40 (80-byte rows), so that eight neighbouring groups read as one
+  // 16-byte vector.
+  static constexpr int kRow = kG + (sizeof(V) == 2 ? 8 : 1);
 };
 
 // Modular helpers; SMALL: p < 2^31, so sums and Shoup remainders fit in 32
@@ -270,24 +272,47 @@ __device__ __forceinline__ void lazy_stage(uint32_t (&x)[T][T / 2]) {
 // integers, (u, b) -> (u + v, u - v) with v = +-b, the rotation's
 // permutation and sign fixed at compile time; |x| <= t * max(V) after
 // log2(t) stages. One reduction at the end, (x + lazy_off) * t^-1 mod p
-// (Shoup, valid for any 32-bit operand), written to the block's tile at
-// column gi.
-template <typename V, int T>
-__device__ __forceinline__ void lazy_transform_store(uint32_t (&x)[T][T / 2], int gi, int c0,
-                                                     const InterpArgs& a, const ModConsts& mc,
-                                                     V* tile) {
-  constexpr int H = T / 2;
-  constexpr int kRow = FastShape<V>::kRow;
+// (Shoup, valid for any 32-bit operand), left in x.
+template <int T>
+__device__ __forceinline__ void lazy_transform(uint32_t (&x)[T][T / 2], const InterpArgs& a,
+                                               const ModConsts& mc) {
   lazy_stage<T, 2>(x);
 #pragma unroll
   for (int r = 0; r < T; ++r) {
 #pragma unroll
-    for (int m = 0; m < H; ++m) {
+    for (int m = 0; m < T / 2; ++m) {
       const uint32_t y = x[r][m] + a.lazy_off;  // in [0, 2 lazy_off)
       const uint32_t qq = __umulhi(y, mc.tinv_s32);
       uint32_t rr = y * a.tinv - qq * a.p;
-      rr = rr >= a.p ? rr - a.p : rr;
-      tile[((r * H + m) * kFastR + c0) * kRow + gi] = static_cast<V>(rr);
+      x[r][m] = rr >= a.p ? rr - a.p : rr;
+    }
+  }
+}
+
+// Writes the transformed subproblems of groups gi (xa) and gi + 1 (xb, when
+// hb) of class c0 to the block's tile; 16-bit values of the two groups go as
+// one 32-bit word (gi even, even row pitch).
+template <typename V, int T>
+__device__ __forceinline__ void lazy_tile_store(const uint32_t (&xa)[T][T / 2],
+                                                const uint32_t (&xb)[T][T / 2], bool hb,
+                                                int gi, int c0, V* tile) {
+  constexpr int H = T / 2;
+  constexpr int kRow = FastShape<V>::kRow;
+#pragma unroll
+  for (int r = 0; r < T; ++r) {
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      V* dst = tile + ((r * H + m) * kFastR + c0) * kRow + gi;
+      if constexpr (sizeof(V) == 2) {
+        if (hb) {
+          *reinterpret_cast<uint32_t*>(dst) = xa[r][m] | (xb[r][m] << 16);
+        } else {
+          dst[0] = static_cast<V>(xa[r][m]);
+        }
+      } else {
+        dst[0] = static_cast<V>(xa[r][m]);
+        if (hb) dst[1] = static_cast<V>(xb[r][m]);
+      }
     }
   }
 }
@@ -321,17 +346,19 @@ interpolate_fast_kernel(const V* __restrict__ raw, InterpArgs a, ModConsts mc,
   const int64_t rec_stride = static_cast<int64_t>(a.l) * a.d;
   const uint32_t p = a.p;
   if constexpr (LAZY) {
-    // Two groups per pass: both groups' 2 t (t/2) loads are issued before
-    // either is transformed, twice the bytes in flight per warp.
-    for (int gi = gw; gi < kFastG; gi += 2 * kFastGW) {
-      const int gj = gi + kFastGW;
+    // Two neighbouring groups per pass: both groups' 2 t (t/2) loads are
+    // issued before either is transformed (twice the bytes in flight per
+    // warp), and their results share 32-bit tile words.
+    for (int gi = 2 * gw; gi < kFastG; gi += 2 * kFastGW) {
       const bool ha = g_base + gi < a.groups;
-      const bool hb = gj < kFastG && g_base + gj < a.groups;
+      const bool hb = g_base + gi + 1 < a.groups;
+      if (!ha) break;
       uint32_t xa[T][H], xb[T][H];
-      if (ha) lazy_load<V, T>(xa, raw, g_base + gi, rec_stride, k, c_start + c0, a);
-      if (hb) lazy_load<V, T>(xb, raw, g_base + gj, rec_stride, k, c_start + c0, a);
-      if (ha) lazy_transform_store<V, T>(xa, gi, c0, a, mc, tile);
-      if (hb) lazy_transform_store<V, T>(xb, gj, c0, a, mc, tile);
+      lazy_load<V, T>(xa, raw, g_base + gi, rec_stride, k, c_start + c0, a);
+      if (hb) lazy_load<V, T>(xb, raw, g_base + gi + 1, rec_stride, k, c_start + c0, a);
+      lazy_transform<T>(xa, a, mc);
+      if (hb) lazy_transform<T>(xb, a, mc);
+      lazy_tile_store<V, T>(xa, xb, hb, gi, c0, tile);
     }
   } else {
   for (int gi = gw; gi < kFastG; gi += kFastGW) {
@@ -399,6 +426,35 @@ interpolate_fast_kernel(const V* __restrict__ raw, InterpArgs a, ModConsts mc,
   const int64_t left = a.groups - g_base;
   const int G = left < kFastG ? static_cast<int>(left) : kFastG;
   if constexpr (sizeof(V) == 2) {
+    if ((a.out_cols & 7) == 0 && G == kFastG &&
+        (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
+      // Eight neighbouring groups per 16-byte store: four lanes write one
+      // DB row's 64 bytes, a warp eight rows per instruction (row pitch a
+      // multiple of 8 values, g_base a multiple of 32). Thread i writes
+      // chunk i % 4 of class (i / 4) % 32, tile rows i / 128 + 2 j.
+      constexpr int kChunks = kFastG / 8;
+      constexpr int kThreads = kFastR * kFastGW;
+      constexpr int kRmStep = kThreads / (kChunks * kFastR);
+      constexpr int kIters = T * H / kRmStep;
+      static_assert(kThreads % (kChunks * kFastR) == 0 && (T * H) % kRmStep == 0,
+                    "16-byte store mapping");
+      const int q = threadIdx.x % kChunks;
+      const int c = (threadIdx.x / kChunks) % kFastR;
+      const int rm0 = threadIdx.x / (kChunks * kFastR);
+      const int64_t ds = static_cast<int64_t>(a.d) * a.out_cols;
+      const int64_t ss = static_cast<int64_t>(a.s) * a.out_cols;
+      V* dst = out + (static_cast<int64_t>(k) * T * a.d + c_start + c) * a.out_cols + g_base +
+               8 * q;
+      const V* src = tile + c * kRow + 8 * q;
+#pragma unroll
+      for (int j = 0; j < kIters; ++j) {
+        const int rm = rm0 + kRmStep * j;
+        const int r = rm / H, m = rm % H;
+        const uint4 v = *reinterpret_cast<const uint4*>(src + rm * kFastR * kRow);
+        *reinterpret_cast<uint4*>(dst + r * ds + m * ss) = v;
+      }
+      return;
+    }
     if ((a.out_cols & 1) == 0 && G == kFastG &&
         (reinterpret_cast<uintptr_t>(out) & 3) == 0) {
       // Two neighbouring groups per 32-bit store (even row pitch, g_base a

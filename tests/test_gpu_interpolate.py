@@ -86,6 +86,9 @@ def oracle_db(raw, n, d, t, l, p, cols):
     (256, 512, 2, 2, 0),      # register form (s = 2d/t >= 32)
     (640, 128, 4, 2, 32),     # register form, padded columns
     (560, 256, 8, 1, 0),      # register form, 70 groups: a ragged last tile
+    (1600, 256, 8, 1, 8),     # 16-byte row stores, 8 groups in the last tile
+    (1608, 256, 8, 2, 7),     # 16-byte row stores, odd last tile (9 groups)
+    (1024, 128, 2, 1, 8),     # t = 2, 16-byte row stores
 ])
 def test_interpolate_db_matches_oracle(dtype, n, d, t, l, pad):
     p = 255 if dtype == np.uint8 else 65535

@@ -57,11 +57,23 @@ __device__ __forceinline__ uint32_t mont_mul(uint32_t a, uint32_t b,
                : static_cast<uint32_t>(r);
 }
 
+// min(a, b) of unsigned words: with b = a - k (mod 2^32) it is a - k when
+// a >= k and a otherwise (the wrapped difference is the larger), the
+// conditional subtraction in two instructions.
+__device__ __forceinline__ uint32_t umin32(uint32_t a, uint32_t b) { return min(a, b); }
+
 __device__ __forceinline__ uint32_t reduce_u32(uint32_t x, uint32_t p) {
   // x < 2^32 < 3p for p > 2^31 / 1.5
   if (x >= p) x -= p;
   if (x >= p) x -= p;
   return x;
+}
+
+// Shoup without the final correction: a * w mod p in [0, 2p) for any
+// 32-bit a and a constant w < p with ws = floor(w * 2^32 / p).
+__device__ __forceinline__ uint32_t shoup_mul_lazy(uint32_t a, uint32_t w,
+                                                   uint32_t ws, uint32_t p) {
+  return a * w - __umulhi(a, ws) * p;
 }
 
 __device__ __forceinline__ uint32_t reduce_u64(uint64_t x, uint32_t p) {

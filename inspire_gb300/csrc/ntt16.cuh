@@ -111,6 +111,14 @@ __device__ __forceinline__ uint32_t ntt16_tw(const uint32_t* t, int i) {
 // Tukey, stages skip .. 3) or inverse (Gentleman-Sande, 3 .. skip). With a
 // compile-time window every index folds; the compact transforms pass a
 // run-time one and the same instructions serve every window.
+//
+// Values stay in [0, 2p) between butterflies (2p < 2^32 for the 31-bit
+// primes): each butterfly brings its two inputs to [0, p) with one unsigned
+// min each, forms u + v and u - v + p in [0, 2p) without a compare, and the
+// twiddle product is Shoup's without its correction (Harvey, "Faster
+// arithmetic for number-theoretic transforms", 2014, with the reductions
+// moved to the inputs since 4p does not fit 32 bits). ntt16_forward and
+// ntt16_inverse_tw reduce to [0, p) at the end unless asked not to.
 template <int LOGD, bool kSmem, bool kInverse>
 __device__ __forceinline__ void ntt16_window(uint32_t (&x)[16],
                                              const uint32_t* __restrict__ tw,
@@ -137,13 +145,16 @@ __device__ __forceinline__ void ntt16_window(uint32_t (&x)[16],
       for (int i = 0; i < half; ++i) {
         const int k = b * 2 * half + i;
         if (kInverse) {
-          const uint32_t u = x[k], v = x[k + half];
-          x[k] = add_mod(u, v, p);
-          x[k + half] = shoup_mul(sub_mod(u, v, p), wv[b], wsv[b], p);
+          const uint32_t u = umin32(x[k], x[k] - p);
+          const uint32_t v = umin32(x[k + half], x[k + half] - p);
+          x[k] = u + v;
+          x[k + half] = shoup_mul_lazy(u + p - v, wv[b], wsv[b], p);
         } else {
-          const uint32_t v = shoup_mul(x[k + half], wv[b], wsv[b], p);
-          x[k + half] = sub_mod(x[k], v, p);
-          x[k] = add_mod(x[k], v, p);
+          const uint32_t u = umin32(x[k], x[k] - p);
+          uint32_t v = shoup_mul_lazy(x[k + half], wv[b], wsv[b], p);
+          v = umin32(v, v - p);
+          x[k] = u + v;
+          x[k + half] = u + p - v;
         }
       }
     }
@@ -168,15 +179,18 @@ __device__ __forceinline__ void ntt16_load(uint32_t (&x)[16], const uint32_t* xs
   for (int k = 0; k < 16; ++k) x[k] = xs[ntt16_pos<LOGD>(base + stride * k)];
 }
 
-// Forward transform. In: x[k] = coefficient tid + (d / 16) k. Out: x[k] =
-// NTT slot 16 tid + k (the bit-reversed output array of ntt_forward). `xs`
+// Forward transform. In: x[k] = coefficient tid + (d / 16) k, any value
+// below 2p. Out: x[k] = NTT slot 16 tid + k in [0, p) (the bit-reversed
+// output array of ntt_forward). `xs`
 // is a d-word shared buffer, free again when this returns. tab16 = the
 // prime's permuted tables [W | W shoup | IW | IW shoup], d words each. tid
 // in [0, d / 16) within the group that synchronises on `bar`. kSmem: the
 // tables were copied to shared memory (tab16 points there). kCompact: one
 // window body for all windows (a third of the code, for launches whose
 // blocks each run once per SM, where fetching unrolled code sets the time).
-template <int LOGD, bool kSmem = false, bool kCompact = false>
+// kLazyOut: the slots are left in [0, 2p), for a caller that only passes
+// them to mont_mul with a reduced second operand (a b < 2 p^2 < 2^32 p).
+template <int LOGD, bool kSmem = false, bool kCompact = false, bool kLazyOut = false>
 __device__ __forceinline__ void ntt16_forward(uint32_t (&x)[16], uint32_t* xs,
                                               const uint32_t* __restrict__ tab16,
                                               uint32_t p, int tid, int bar = 0) {
@@ -205,10 +219,16 @@ __device__ __forceinline__ void ntt16_forward(uint32_t (&x)[16], uint32_t* xs,
       ntt16_sync<LOGD>(bar);
     }
   }
+  if constexpr (!kLazyOut) {
+    // [0, 2p) -> [0, p).
+#pragma unroll
+    for (int k = 0; k < 16; ++k) x[k] = umin32(x[k], x[k] - p);
+  }
 }
 
-// Inverse transform without the 1/d scaling. In: x[k] = slot 16 tid + k.
-// Out: x[k] = coefficient tid + (d / 16) k. itw / itws: the permuted
+// Inverse transform without the 1/d scaling. In: x[k] = slot 16 tid + k,
+// any value below 2p. Out: x[k] = coefficient tid + (d / 16) k in [0, p).
+// itw / itws: the permuted
 // inverse twiddles and their Shoup constants.
 template <int LOGD, bool kSmem = false, bool kCompact = false>
 __device__ __forceinline__ void ntt16_inverse_tw(uint32_t (&x)[16], uint32_t* xs,
@@ -237,6 +257,9 @@ __device__ __forceinline__ void ntt16_inverse_tw(uint32_t (&x)[16], uint32_t* xs
       ntt16_sync<LOGD>(bar);
     }
   }
+  // [0, 2p) -> [0, p).
+#pragma unroll
+  for (int k = 0; k < 16; ++k) x[k] = umin32(x[k], x[k] - p);
 }
 
 // The inverse with the prime's whole table block [W | W shoup | IW | IW shoup].

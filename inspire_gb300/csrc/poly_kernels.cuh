@@ -641,7 +641,7 @@ ext_step16_kernel(bool first, const uint32_t* __restrict__ resid_in,
                                       e.num_digits, dg);
         x[k] = to_residue<T>(dig & static_cast<T>(e.umask), p);
       }
-      ntt16_forward<LOGD, false, LOGD != 12>(x, xs, tab16, p, tid);
+      ntt16_forward<LOGD, false, LOGD != 12, true>(x, xs, tab16, p, tid);
       const uint4* wa = reinterpret_cast<const uint4*>(
           RGSWa + q * rgswa_qstride + (static_cast<int64_t>(g) * c.r + pi) * d + 16 * tid);
       const uint4* wb = reinterpret_cast<const uint4*>(
@@ -739,7 +739,7 @@ ext_step16_pair_kernel(bool first, const uint32_t* __restrict__ resid_in,
                                     e.num_digits, dg);
       x[k] = to_residue<T>(dig & static_cast<T>(e.umask), p);
     }
-    ntt16_forward<LOGD, false, true>(x, region, tab16, p, lt, bar);
+    ntt16_forward<LOGD, false, true, true>(x, region, tab16, p, lt, bar);
     const uint4* wa = reinterpret_cast<const uint4*>(
         RGSWa + q * rgswa_qstride + (static_cast<int64_t>(g) * c.r + pi) * d + 16 * lt);
     const uint4* wb = reinterpret_cast<const uint4*>(

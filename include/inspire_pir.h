@@ -176,11 +176,15 @@ int inspire_pir_process_batch_device(inspire_pir_server* server,
 
 /*
  * Stage 1 alone for a device-resident batch: out[q][r] = (DB * q1_q)[r] +
- * (P * y_g,q)[r] mod 2^w, the b' + b_agg_partial vector that
- * FinalizeMatrixPack consumes (pir_server.cc:215-254). first_dim holds
- * db_cols words per request, packing_key 2*pack_num_digits polynomials per
- * request (its first half is y_vec_g); out holds rows words per request.
- * Enqueued on `stream` without synchronising.
+ * (P * y_g,q)[r], the b' + b_agg_partial vector that FinalizeMatrixPack
+ * consumes (pir_server.cc:215-254), exact in the bits the answer reads:
+ * mod 2^w with the plain engine and for Z_2^32; a Z_2^64 server with
+ * log_modulus <= 56 on the tensor engine computes the words mod 2^56 only
+ * (the top digit position's products reach no lower bit, and
+ * FinalizeMatrixPack keeps LowBits(., log_modulus), lwes_to_rlwe.cc:464-469).
+ * first_dim holds db_cols words per request, packing_key 2*pack_num_digits
+ * polynomials per request (its first half is y_vec_g); out holds rows words
+ * per request. Enqueued on `stream` without synchronising.
  */
 int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,
                                 const void* first_dim, const void* packing_key,
@@ -196,8 +200,9 @@ int inspire_pir_products_device(inspire_pir_server* server, int32_t batch,
  * INSPIRE_FORM_NARROW the kernel takes 16 requests per tile instead of 64.
  * The raw form and the narrow tiles serve Z_2^32 servers; a Z_2^64 server
  * runs the planes with 32-request tiles. split > 0 forces that split-K factor (0: the tuned or
- * heuristic one). Same buffers and result as inspire_pir_products_device
- * with INSPIRE_ENGINE_TENSOR. FAILED_PRECONDITION when the server has no
+ * heuristic one). Same buffers as inspire_pir_products_device with
+ * INSPIRE_ENGINE_TENSOR; the words are exact mod 2^w in every case (all
+ * digit positions computed). FAILED_PRECONDITION when the server has no
  * such form.
  */
 #define INSPIRE_FORM_PLANES 0

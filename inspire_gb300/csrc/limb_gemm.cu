@@ -384,7 +384,7 @@ struct UnitSrc {
   int rx;    // DB column of step 0 (raw u16 tiles of the converting form)
 };
 
-template <int NQ>
+template <int NW>
 __device__ __forceinline__ UnitSrc unit_src(int u, int n_db_units,
                                             const CUtensorMap* tm_db,
                                             const CUtensorMap* tm_pk,
@@ -398,7 +398,7 @@ __device__ __forceinline__ UnitSrc unit_src(int u, int n_db_units,
   r.a_step = kind == 0 ? 2 * kStageK : 4 * kStageK;
   r.ax = kb * kStagesPerUnit * r.a_step + (kind == 2 ? 2 * kStageK : 0);
   r.bx = kb * kUnitK;
-  r.nb = kind == 2 ? NQ - 2 : NQ;
+  r.nb = kind == 2 ? NW - 2 : NW;
   r.kind = kind;
   r.rx = kb * kUnitK;
   return r;
@@ -407,8 +407,10 @@ __device__ __forceinline__ UnitSrc unit_src(int u, int n_db_units,
 // CONV = false: the DB comes as resident fp16 digit planes (tm_db). CONV =
 // true: the DB comes as stored, u16 (tm_raw), and the converter warpgroup
 // writes each A box's digit planes from its raw tile (pack units keep
-// their planes in both forms).
-template <int NQ, bool CONV, int TQ>
+// their planes in both forms). NW <= NQ: the weight blocks computed, so the
+// products are exact mod 2^(8 NW) (NW = 7 when the caller reads only the
+// low 56 bits of a Z_2^64 word: q <= 2^56, LowBits after the product).
+template <int NQ, bool CONV, int TQ, int NW = NQ>
 __global__ void __launch_bounds__(CONV ? kThreadsConv : kThreads, 1)
 limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
                  const __grid_constant__ CUtensorMap tm_raw,
@@ -422,6 +424,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   constexpr int kBPlaneBytes = TQ * kBSlotK * 2;  // rows of 128 bytes
   static_assert(NQ * TQ <= kBRows && ((NQ - 3) * TQ) % 16 == 0 && TQ % 16 == 0,
                 "request tile: N of every MMA a multiple of 16, at most 256");
+  static_assert(NW <= NQ && NW >= 4 && ((NW - 3) * TQ) % 16 == 0, "weight blocks");
   using Plan = RingPlan<NQ, CONV, TQ>;
   constexpr int kBS = Plan::kBS;            // request slots
   constexpr int kBSlotB = Plan::kBSlotB;    // bytes per request slot
@@ -564,7 +567,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       return true;
     };
     for (int i = 0; i < nu && ok; ++i) {
-      const UnitSrc src = unit_src<NQ>(u0 + i, a.n_db_units, &tm_db, &tm_pk, &tm_q, &tm_y);
+      const UnitSrc src = unit_src<NW>(u0 + i, a.n_db_units, &tm_db, &tm_pk, &tm_q, &tm_y);
       for (int p = 0; p < kAPairs && ok; ++p) ok = load_pair(0, p, src, i);
       for (int p = 0; p < kAPairs && ok; ++p) {
         const int n = kBHalves * i + p;
@@ -604,18 +607,19 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     // which keep the one issuing thread ahead of the tensor pipe. The ring
     // waits need no tcgen05 fence (the copies and the MMAs are both in the
     // async proxy, ordered by the mbarrier); the accumulator hand-off does.
-    // N of the four MMA shapes: all NQ request planes (DB x0, pack p0),
-    // one fewer (x1, p1), and for the high pack planes NQ-2 (p2), NQ-3 (p3).
-    constexpr uint32_t id_n0 = instr_desc(NQ * kTileQ, kBlockRows);
-    constexpr uint32_t id_n1 = instr_desc((NQ - 1) * kTileQ, kBlockRows);
-    constexpr uint32_t id_n2 = instr_desc((NQ - 2) * kTileQ, kBlockRows);
-    constexpr uint32_t id_n3 = instr_desc((NQ - 3) * kTileQ, kBlockRows);
+    // N of the four MMA shapes: the NW request planes that reach a
+    // computed weight block (DB x0, pack p0), one fewer (x1, p1), and for
+    // the high pack planes NW-2 (p2), NW-3 (p3).
+    constexpr uint32_t id_n0 = instr_desc(NW * kTileQ, kBlockRows);
+    constexpr uint32_t id_n1 = instr_desc((NW - 1) * kTileQ, kBlockRows);
+    constexpr uint32_t id_n2 = instr_desc((NW - 2) * kTileQ, kBlockRows);
+    constexpr uint32_t id_n3 = instr_desc((NW - 3) * kTileQ, kBlockRows);
     const uint32_t lo0 = (smem_addr(smem) >> 4) | (1u << 16);
     bool ok = true;
     for (int i = 0; i < nu && ok; ++i) {
-      // DB and low pack units: x0 * [y0..y_{NQ-1}] -> weight blocks
-      // 0..NQ-1, then x1 * [y0..y_{NQ-2}] -> blocks 1..NQ-1; high pack
-      // units: p2 * [y0..y_{NQ-3}] -> blocks 2.., then p3 -> blocks 3..
+      // DB and low pack units: x0 * [y0..y_{NW-1}] -> weight blocks
+      // 0..NW-1, then x1 * [y0..y_{NW-2}] -> blocks 1..NW-1; high pack
+      // units: p2 * [y0..y_{NW-3}] -> blocks 2.., then p3 -> blocks 3..
       const bool high = unit_kind(u0 + i, a.n_db_units) == 2;
       const uint32_t id_0 = high ? id_n2 : id_n0, id_1 = high ? id_n3 : id_n1;
       const uint32_t c_0 = high ? 2u * kTileQ : 0u, c_1 = high ? 3u * kTileQ : 1u * kTileQ;
@@ -768,7 +772,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       const uint32_t base =
           tmem + (static_cast<uint32_t>(ew * 32) << 16) + e * 256;
 #pragma unroll
-      for (int sblk = 0; sblk < NQ; ++sblk) {
+      for (int sblk = 0; sblk < NW; ++sblk) {
         if (kind == 2 && sblk < 2) continue;
         constexpr int kLd = kTileQ < 32 ? kTileQ : 32;  // columns per load
         uint32_t v[kTileQ / kLd][kLd];
@@ -797,7 +801,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       const Acc m = 0x4B400000u;
       Acc corr = 0;
 #pragma unroll
-      for (int sblk = 0; sblk < NQ; ++sblk) {
+      for (int sblk = 0; sblk < NW; ++sblk) {
         corr += static_cast<Acc>(sblk < 2 ? n01 : n23) * (m << (8 * sblk));
       }
       const int row = row0 + e * kBlockRows + ew * 32 + lane;
@@ -1112,6 +1116,7 @@ class LimbGemmImpl : public LimbGemm {
       }
     } else {
       allow(reinterpret_cast<const void*>(limb_gemm_kernel<8, false, 32>));
+      allow(reinterpret_cast<const void*>(limb_gemm_kernel<8, false, 32, 7>));
     }
     return fe == cudaSuccess;
   }
@@ -1165,20 +1170,28 @@ class LimbGemmImpl : public LimbGemm {
 
   cudaError_t Run(int batch, const void* q1, int64_t q1_stride, const void* yg,
                   int64_t yg_stride, void* out, LimbScratch* scratch,
-                  cudaStream_t st) override {
+                  cudaStream_t st, int out_bits) override {
     return Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st,
-                  Chosen(batch));
+                  Chosen(batch), WeightBlocks(out_bits));
   }
 
   cudaError_t RunForm(int batch, const void* q1, int64_t q1_stride, const void* yg,
                       int64_t yg_stride, void* out, LimbScratch* scratch,
-                      cudaStream_t st, int form, int split) override {
+                      cudaStream_t st, int form, int split, int out_bits) override {
     Choice c = Chosen(batch);
     c.form = form & 1;
     c.narrow = (form >> 1) & 1;
     if (split > 0) c.split = split;
     if (!Available(c)) return cudaErrorNotSupported;
-    return Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, c);
+    return Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, c,
+                  WeightBlocks(out_bits));
+  }
+
+  // Weight blocks (base-256 digit positions) of the product words the
+  // caller reads: all of them, or for Z_2^64 words read mod 2^b with
+  // b <= 56 only the seven below 2^56.
+  int WeightBlocks(int out_bits) const {
+    return nq_ == 8 && out_bits > 0 && out_bits <= 56 ? 7 : nq_;
   }
 
   // One configuration of the product: split-K factor, DB form and request
@@ -1202,9 +1215,10 @@ class LimbGemmImpl : public LimbGemm {
   // Synchronises `st`.
   cudaError_t Tune(int batch, const void* q1, int64_t q1_stride, const void* yg,
                    int64_t yg_stride, void* out, LimbScratch* scratch,
-                   cudaStream_t st, int* chosen, int* chosen_form,
+                   cudaStream_t st, int out_bits, int* chosen, int* chosen_form,
                    float* best_ms) override {
     if (batch <= 0) return cudaErrorInvalidValue;
+    const int nw = WeightBlocks(out_bits);
     const int n_units = static_cast<int>((cpad_ + 2 * kpad_) / kUnitK);
     const int sms = sms_ > 0 ? sms_ : 148;
     cudaEvent_t e0, e1;
@@ -1231,10 +1245,10 @@ class LimbGemmImpl : public LimbGemm {
           const int64_t waves = (items + sms - 1) / sms;
           const double eff = static_cast<double>(items) / (waves * sms);
           if (k != heuristic && eff < 0.8) continue;
-          e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, c);
+          e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, c, nw);
           if (e == cudaSuccess) e = cudaEventRecord(e0, st);
           for (int r = 0; r < 2 && e == cudaSuccess; ++r) {
-            e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, c);
+            e = Launch(batch, q1, q1_stride, yg, yg_stride, out, scratch, st, c, nw);
           }
           if (e == cudaSuccess) e = cudaEventRecord(e1, st);
           if (e == cudaSuccess) e = cudaEventSynchronize(e1);
@@ -1280,7 +1294,7 @@ class LimbGemmImpl : public LimbGemm {
 
   cudaError_t Launch(int batch, const void* q1, int64_t q1_stride, const void* yg,
                      int64_t yg_stride, void* out, LimbScratch* scratch,
-                     cudaStream_t st, const Choice& c) {
+                     cudaStream_t st, const Choice& c, int nw) {
     if (batch <= 0) return cudaSuccess;
     if (!Available(c)) return cudaErrorNotSupported;
     LimbScratchImpl* sc = static_cast<LimbScratchImpl*>(scratch);
@@ -1331,16 +1345,19 @@ class LimbGemmImpl : public LimbGemm {
     U* o8 = static_cast<U*>(out);
     const bool raw = c.form == kFormRaw;
     const int nt = raw ? kThreadsConv : kThreads;
-#define INSPIRE_LIMB_LAUNCH(NQ, CONV, TQ, QS, OUT)                                  \
-  limb_gemm_kernel<NQ, CONV, TQ><<<grid, nt, kSmemBytes, st>>>(                     \
+#define INSPIRE_LIMB_LAUNCH(NQ, CONV, TQ, NW, QS, OUT)                              \
+  limb_gemm_kernel<NQ, CONV, TQ, NW><<<grid, nt, kSmemBytes, st>>>(                 \
       tm_db_, tm_raw_, tm_pk_, mq, my, a, QS, OUT, err_)
     if (nq_ == 4) {
-      if (!raw && !c.narrow) INSPIRE_LIMB_LAUNCH(4, false, 64, qs4, o4);
-      if (!raw && c.narrow) INSPIRE_LIMB_LAUNCH(4, false, kNarrowTQ, qs4, o4);
-      if (raw && !c.narrow) INSPIRE_LIMB_LAUNCH(4, true, 64, qs4, o4);
-      if (raw && c.narrow) INSPIRE_LIMB_LAUNCH(4, true, kNarrowTQ, qs4, o4);
+      if (!raw && !c.narrow) INSPIRE_LIMB_LAUNCH(4, false, 64, 4, qs4, o4);
+      if (!raw && c.narrow) INSPIRE_LIMB_LAUNCH(4, false, kNarrowTQ, 4, qs4, o4);
+      if (raw && !c.narrow) INSPIRE_LIMB_LAUNCH(4, true, 64, 4, qs4, o4);
+      if (raw && c.narrow) INSPIRE_LIMB_LAUNCH(4, true, kNarrowTQ, 4, qs4, o4);
+    } else if (nw == 7) {
+      // Available(): planes, full tiles; products read mod 2^56.
+      INSPIRE_LIMB_LAUNCH(8, false, 32, 7, qs8, o8);
     } else {
-      INSPIRE_LIMB_LAUNCH(8, false, 32, qs8, o8);  // Available(): planes, full tiles
+      INSPIRE_LIMB_LAUNCH(8, false, 32, 8, qs8, o8);
     }
 #undef INSPIRE_LIMB_LAUNCH
     return cudaGetLastError();

@@ -39,23 +39,26 @@ class LimbGemm {
   // first use otherwise).
   virtual cudaError_t Reserve(LimbScratch* scratch, int batch) = 0;
   // out[q][r] = db[r] . q1[q] + pack[r] . yg[q]  (mod 2^w), q < batch.
+  // out_bits: the low bits of each word the caller reads (0: all w); the
+  // words are exact mod 2^out_bits at least, and a Z_2^64 product read mod
+  // 2^56 or less skips its top digit position.
   virtual cudaError_t Run(int batch, const void* q1, int64_t q1_stride,
                           const void* yg, int64_t yg_stride, void* out,
-                          LimbScratch* scratch, cudaStream_t stream) = 0;
+                          LimbScratch* scratch, cudaStream_t stream, int out_bits) = 0;
   // Run with a given form (kFormPlanes or kFormRaw, | kFormNarrow for the
   // 16-request tile) and split-K factor (split <= 0: the tuned or heuristic
   // one); cudaErrorNotSupported when the form is unavailable.
   virtual cudaError_t RunForm(int batch, const void* q1, int64_t q1_stride,
                               const void* yg, int64_t yg_stride, void* out,
                               LimbScratch* scratch, cudaStream_t stream, int form,
-                              int split) = 0;
+                              int split, int out_bits) = 0;
   // Autotuner: times the split-K factors of every available form for this
   // batch size on these operands, keeps the fastest (factor, form) for
   // later Runs of the same padded batch size and reports it. Synchronises
   // the stream.
   virtual cudaError_t Tune(int batch, const void* q1, int64_t q1_stride,
                            const void* yg, int64_t yg_stride, void* out,
-                           LimbScratch* scratch, cudaStream_t stream,
+                           LimbScratch* scratch, cudaStream_t stream, int out_bits,
                            int* chosen, int* chosen_form, float* best_ms) = 0;
   // Device bytes the engine keeps resident (digit planes).
   virtual int64_t ResidentBytes() const = 0;

@@ -843,7 +843,11 @@ int ResolveEngine(const inspire_pir_server* s, int engine, int batch) {
 
 namespace {
 
-// Stage 1: out[q] = DB * q1[q] + P * y_g[q] for the whole batch.
+// Stage 1: out[q] = DB * q1[q] + P * y_g[q] for the whole batch, exact in
+// the bits the answer reads: every caller takes the words mod 2^log_q
+// (FinalizeMatrixPack and vPIR's local finalize apply LowBits first,
+// lwes_to_rlwe.cc:464-469), so the tensor engine may skip digit positions
+// at or above log_q.
 Status Products(inspire_pir_server* s, Workspace* ws, int batch,
                 const void* q1, const void* pkey, void* out, int engine,
                 cudaStream_t st, int64_t pk_stride = -1) {
@@ -857,7 +861,7 @@ Status Products(inspire_pir_server* s, Workspace* ws, int batch,
     }
     if (!ws->limb) ws->limb = s->limb->NewScratch();
     return Cuda(s->limb->Run(batch, q1, s->db_cols, pkey, pk_stride, out,
-                             ws->limb.get(), st),
+                             ws->limb.get(), st, s->prm.log_modulus),
                 "limb gemm");
   }
   if (engine != INSPIRE_ENGINE_PLAIN) {
@@ -2659,8 +2663,8 @@ int inspire_pir_autotune(inspire_pir_server* server, int32_t batch,
   if (st.ok()) {
     st = Cuda(server->limb->Tune(batch, ws->q1.get(), server->db_cols, ws->pkey.get(),
                                  static_cast<int64_t>(2 * server->k) * server->d,
-                                 ws->gemv.get(), ws->limb.get(), ws->stream, &chosen,
-                                 &form, &best),
+                                 ws->gemv.get(), ws->limb.get(), ws->stream,
+                                 server->prm.log_modulus, &chosen, &form, &best),
               "autotune");
   }
   if (st.ok()) {
@@ -2723,7 +2727,8 @@ int inspire_pir_tune_engines(inspire_pir_server* server, int32_t max_batch,
     if (st.ok()) {
       st = Cuda(server->limb->Tune(b, ws->q1.get(), server->db_cols, ws->pkey.get(),
                                    pk_stride, ws->gemv.get(), ws->limb.get(),
-                                   ws->stream, &split, &form, &best),
+                                   ws->stream, server->prm.log_modulus, &split, &form,
+                                   &best),
                 "autotune");
     }
     tensor_ms[i] = best;
@@ -2915,7 +2920,7 @@ int inspire_pir_tensor_products_device(inspire_pir_server* server, int32_t batch
   const cudaError_t e = server->limb->RunForm(
       batch, first_dim, server->db_cols, packing_key,
       static_cast<int64_t>(2 * server->k) * server->d, out, ws->limb.get(),
-      static_cast<cudaStream_t>(stream), form, split);
+      static_cast<cudaStream_t>(stream), form, split, /*out_bits=*/0);
   if (e == cudaErrorNotSupported) {
     return Report(Err(INSPIRE_FAILED_PRECONDITION,
                       "this form of the tensor engine is not available on this server"),

@@ -38,8 +38,16 @@ def plain_bytes(rows, db_cols, pack_cols, db_elem=2, pack_elem=4, word=4):
             (db_cols + pack_cols) * word + rows * word)
 
 
-def limb_ops(rows, db_cols, pack_cols, batch, coeff_bits=32):
-    db_pairs, pk_pairs = (7, 10) if coeff_bits == 32 else (15, 26)
+def limb_ops(rows, db_cols, pack_cols, batch, coeff_bits=32, log_q=None):
+    """Digit products of the exact limb plan: base-256 digit pairs whose
+    weight falls below the bits the answer reads (2^32; 2^64, or 2^56 when
+    log_q <= 56, over Z_2^64), times 2 R C B (DB) and 2 R K B (pack)."""
+    if coeff_bits == 32:
+        db_pairs, pk_pairs = 7, 10
+    elif log_q is not None and log_q <= 56:
+        db_pairs, pk_pairs = 13, 22
+    else:
+        db_pairs, pk_pairs = 15, 26
     return 2.0 * (db_pairs * rows * db_cols + pk_pairs * rows * pack_cols) * batch
 
 
@@ -108,7 +116,8 @@ def kernel_times(srv, engine, batch, t_fd, t_sd, t_pk, t_out, stream, n1,
                                  "frac_hbm": plain_gbs / hbm}}
     if engine == pir.ENGINE_TENSOR:
         ms_t = time_it(batch, engine)
-        ops = limb_ops(rows, srv.db_cols, srv.pack_cols, batch, cb)
+        ops = limb_ops(rows, srv.db_cols, srv.pack_cols, batch, cb,
+                       srv.params.rlwe.log_modulus)
         ach = ops / (ms_t / 1e3) / 1e12
         kernels["limb_gemm_b%d" % batch] = {"ms": ms_t, "limb_ops": ops,
                                             "tflops": ach,

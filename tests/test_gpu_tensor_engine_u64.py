@@ -83,9 +83,13 @@ def _from_digits(digits):
     return sum(int(d) << (8 * i) for i, d in enumerate(digits)) % (1 << 64)
 
 
+@pytest.mark.parametrize("log_q", [64, 56])
 @pytest.mark.parametrize("pattern", ["alternating", "random_extremes"])
-def test_u64_tensor_extreme_digits(pattern):
-    params = synthetic.make_params(d=128, n=2 * 16384, t=2, coeff_bits=64)
+def test_u64_tensor_extreme_digits(pattern, log_q):
+    # log_q = 56: the engine computes seven weight blocks (the products
+    # mod 2^56 that FinalizeMatrixPack reads), with the same extremes.
+    params = synthetic.make_params(d=128, n=2 * 16384, t=2, coeff_bits=64,
+                                   log_q=log_q)
     mat = synthetic.make_material(params, seed=13, mat_dtype=np.int32)
     rng = np.random.default_rng(14)
     fd, sd, pk = synthetic.make_requests(params, 32, seed=15, full_range=True)
@@ -153,4 +157,44 @@ def test_u64_split_k_and_buffer_reuse():
                                              full_range=True)
         assert np.array_equal(srv.process_arrays(fd, sd, pk, pir.ENGINE_TENSOR),
                               srv.process_arrays(fd, sd, pk, pir.ENGINE_PLAIN))
+    srv.check()
+
+
+@pytest.mark.parametrize("log_q", [56, 52])
+def test_u64_tensor_products_mod_2_56_when_q_is_at_most_2_56(log_q):
+    # With q <= 2^56 the answer reads the stage-1 words mod 2^56 only, and
+    # the tensor engine skips the digit position of weight 2^56: its words
+    # equal the plain engine's mod 2^56; the forms API still computes all
+    # eight positions (exact mod 2^64).
+    import torch
+    params = synthetic.make_params(d=128, n=2 * 4096, t=2, coeff_bits=64,
+                                   log_q=log_q)
+    mat = synthetic.make_material(params, seed=19, mat_dtype=np.int32)
+    batch = 40
+    fd, sd, pk = synthetic.make_requests(params, batch, seed=20, full_range=True)
+    srv = _server(params, mat)
+    rows = mat.db.shape[0]
+    dev = torch.device("cuda", 0)
+    t_fd = torch.from_numpy(fd.view(np.int64)).to(dev)
+    t_pk = torch.from_numpy(pk.view(np.int64)).to(dev)
+    lib = pir._lib.load()
+    err = pir._errbuf()
+
+    def products(engine):
+        out = torch.zeros((batch, rows), dtype=torch.int64, device=dev)
+        rc = lib.inspire_pir_products_device(
+            srv._h, batch, t_fd.data_ptr(), t_pk.data_ptr(), out.data_ptr(),
+            engine, None, err, len(err))
+        assert rc == 0, err.value
+        torch.cuda.synchronize()
+        return out.cpu().numpy().view(np.uint64)
+    plain = products(pir.ENGINE_PLAIN)
+    tensor = products(pir.ENGINE_TENSOR)
+    low = np.uint64((1 << 56) - 1)
+    assert np.array_equal(tensor & low, plain & low)
+    out = torch.zeros((batch, rows), dtype=torch.int64, device=dev)
+    srv.tensor_products_device(batch, t_fd.data_ptr(), t_pk.data_ptr(),
+                               out.data_ptr(), pir.FORM_PLANES)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), plain)
     srv.check()

@@ -601,6 +601,91 @@ def run_hint_workload(args):
     print(json.dumps(line))
 
 
+def run_preprocess_workload(args):
+    """Offline PreprocessMatrixPack (crypto/lwes_to_rlwe.cc:163-446, per
+    slice as PreprocessingServer calls it, preprocessing_server.h:248-271)
+    for the n = 2^20, d = 4096, t = 8 packing material: 8 slices of d LWE
+    a-vectors (the hint rows) against a k = 2 pack key -> a_tilde_agg, the
+    32768 x 8192 int32 pack matrix and t_vec_h. `value`: the device-pointer
+    call (inputs and outputs in HBM; its scratch allocations included),
+    CUDA events; `e2e`: the host-buffer call (hint in, matrix out).
+    Exactness is checked against the oracle by the tests at d = 64 / 256 /
+    2048 and by decryption at 4096; here the timing only."""
+    import torch
+    from inspire_gb300 import _lib, build, pir
+    build.build()
+    d, slices, k, log_q, log_digit = DEGREE, INTERP, 2, 32, 19
+    rng = np.random.default_rng(61)
+    hint = rng.integers(0, 1 << 32, size=(slices * d, d), dtype=np.uint64
+                        ).astype(np.uint32)
+    pack_a = rng.integers(0, 1 << 32, size=(2 * k, d), dtype=np.uint64
+                          ).astype(np.uint32)
+    dev = torch.device("cuda", 0)
+    t_hint = torch.from_numpy(hint.view(np.int32)).to(dev)
+    t_pa = torch.from_numpy(pack_a.view(np.int32)).to(dev)
+    t_a = torch.empty((slices, d), dtype=torch.int32, device=dev)
+    t_m = torch.empty((slices * d, k * d), dtype=torch.int32, device=dev)
+    t_th = torch.empty((slices, k, d), dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    lib = _lib.load()
+    err = ctypes.create_string_buffer(256)
+
+    def step():
+        rc = lib.inspire_preprocess_matrix_pack(
+            32, 5, log_q, log_digit, k, d, slices,
+            ctypes.c_void_p(t_hint.data_ptr()), d,
+            ctypes.c_void_p(t_pa.data_ptr()), 2 * k,
+            ctypes.c_void_p(t_a.data_ptr()), ctypes.c_void_p(t_m.data_ptr()),
+            ctypes.c_void_p(t_th.data_ptr()), 1,
+            ctypes.c_void_p(stream.cuda_stream), err, len(err))
+        if rc:
+            raise SystemExit(err.value)
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    # The same through the host-buffer call.
+    pir.PreprocessMatrixPack(hint, pack_a, log_q, log_digit, k,
+                             mat_dtype=np.int32)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        a_h, m_h, th_h = pir.PreprocessMatrixPack(hint, pack_a, log_q,
+                                                  log_digit, k,
+                                                  mat_dtype=np.int32)
+    ms_e2e = (time.perf_counter() - t0) * 1000 / args.steps
+    same = (np.array_equal(a_h, t_a.cpu().numpy().view(np.uint32)) and
+            np.array_equal(m_h, t_m.cpu().numpy()) and
+            np.array_equal(th_h, t_th.cpu().numpy().view(np.uint32)))
+    if not same:
+        raise SystemExit("device and host-buffer PreprocessMatrixPack differ")
+    line = {
+        "metric": "PreprocessMatrixPack slices/s (d=%d, k=%d, Z_2^32, int32 "
+                  "matrix)" % (d, k),
+        "value": slices / (ms / 1000.0), "unit": "slices/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic (seeded uniform hint rows and "
+                                "pack key)",
+        "config": {"workload": "preprocess_d%d_slices%d_k%d_u32"
+                               % (d, slices, k),
+                   "matrix": [slices * d, k * d]},
+        "e2e": {"value": slices / (ms_e2e / 1000.0), "unit": "slices/s",
+                "h2d_bytes_per_step": int(hint.nbytes + pack_a.nbytes),
+                "d2h_bytes_per_step": int(m_h.nbytes + a_h.nbytes +
+                                          th_h.nbytes)},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 SINGLE_CONFIGS = {
     # The reference metrics tool's shapes for a single request.
     "c2": dict(n=65536, d=2048, t=4, l=1, coeff_bits=32, log_q=32),
@@ -815,11 +900,14 @@ def main():
     ap.add_argument("--entries", type=int, default=N_ENTRIES,
                     help="records of the interpolate / hint workloads")
     ap.add_argument("--workload", default="answer",
-                    choices=["answer", "pack", "interpolate", "hint", "single"],
+                    choices=["answer", "pack", "interpolate", "hint", "single",
+                             "preprocess"],
                     help="answer: the online answer (default); pack: the "
                          "packing micro-workload; interpolate: the offline "
-                         "DB interpolation; single: one request at a time on "
-                         "the small shapes (--config c2 or c1)")
+                         "DB interpolation; hint: the offline hint matrix; "
+                         "preprocess: the offline PreprocessMatrixPack; "
+                         "single: one request at a time on the small shapes "
+                         "(--config c2 or c1)")
     ap.add_argument("--config", default="c2", choices=sorted(SINGLE_CONFIGS),
                     help="shape of the single workload")
     ap.add_argument("--coeff-bits", type=int, default=32, choices=[32, 64],
@@ -837,6 +925,9 @@ def main():
         return
     if args.workload == "hint" and args.impl == "ours":
         run_hint_workload(args)
+        return
+    if args.workload == "preprocess" and args.impl == "ours":
+        run_preprocess_workload(args)
         return
     if args.workload == "single" and args.impl == "ours":
         run_single_workload(args)

@@ -19,6 +19,7 @@
 #include <type_traits>
 
 #include "ntt.cuh"
+#include "ntt16.cuh"
 
 namespace inspire {
 
@@ -319,6 +320,150 @@ pp_tail_kernel(const T* __restrict__ fin, ChainArgs a, NttCtx c, T* __restrict__
   __syncthreads();
   pp_link<T, ITERS>(cur, scratch, acc, a, c, 1, a.Wh,
                     t_vec_h + static_cast<int64_t>(s) * a.k * d, tgf);
+  for (int r = threadIdx.x; r < d; r += blockDim.x) {
+    a_tilde[static_cast<int64_t>(s) * d + r] = pp_low<T>(cur[r], a.log_q);
+  }
+}
+
+// pp_link with the radix-16 register transforms of ntt16.cuh (d = 2^LOGD,
+// LOGD = 11..13), for a block of G groups of d/16 threads: group g takes
+// primes g, g + G, ..., each group's transforms synchronising on named
+// barrier g + 1, so the k forward transforms and the inverse of G primes run
+// side by side; the residues meet in shared memory (res, natural
+// coefficient order) for the CRT. xs: G exchange buffers of d words; dig:
+// the k digit planes of `cur` (k d words of T). The link is a chain of
+// dependent steps, so the digit planes go to shared memory for the
+// transforms (and out to `digits` for the matrix, not read back), and
+// `add` is loaded while other groups finish. Signed digits are below p in
+// magnitude, so their residues need no division. Same words as pp_link.
+template <typename T, int LOGD, int G>
+__device__ __forceinline__ void pp_link16(T* cur, uint32_t* res, uint32_t* xs, T* dig,
+                                          const ChainArgs& a, const NttCtx& c, int power,
+                                          const uint32_t* W, T* digits, const T* add) {
+  using S = typename std::make_signed<T>::type;
+  constexpr int d = 1 << LOGD;
+  constexpr int NT = Ntt16<LOGD>::kThreads;
+  constexpr int kPerThread = (d + G * NT - 1) / (G * NT);
+  // The compact transforms (one pass body: fewer registers beside the
+  // digit and accumulator arrays, less code for a block that runs alone).
+  constexpr bool kCompact = true;
+  const int g = threadIdx.x / NT;
+  const int lt = threadIdx.x % NT;
+  // The digit planes, in shared memory and out for the matrix.
+  for (int r = threadIdx.x; r < d; r += G * NT) {
+    pp_signed_digits<T>(cur[r], a.log_q, a.log_digit, a.k, dig + r, d);
+    for (int l = 0; l < a.k; ++l) digits[static_cast<int64_t>(l) * d + r] = dig[l * d + r];
+  }
+  __syncthreads();
+  uint32_t* x_buf = xs + g * d;
+  for (int pi = g; pi < c.r; pi += G) {
+    const uint32_t p = c.p[pi];
+    const uint32_t pinv = c.pinv[pi];
+    const uint32_t* tab16 = c.tables16 + static_cast<size_t>(pi) * 4 * d;
+    uint32_t acc[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q] = 0;
+    for (int l = 0; l < a.k; ++l) {
+      uint32_t x[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        // Digit l of coefficient lt + NT q; |digit| <= 2^(log_digit - 1) < p.
+        const S v = static_cast<S>(dig[l * d + lt + NT * q]);
+        x[q] = v < 0 ? static_cast<uint32_t>(static_cast<int64_t>(v) + p)
+                     : static_cast<uint32_t>(v);
+      }
+      ntt16_forward<LOGD, false, kCompact, true>(x, x_buf, tab16, p, lt, g + 1);
+      // Slot 16 lt + q times the key part read through X -> X^power
+      // (pp_link's permutation).
+      const uint32_t* w = W + (static_cast<int64_t>(l) * c.r + pi) * d;
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        const int sl = 16 * lt + q;
+        const int e = static_cast<int>(
+            (static_cast<int64_t>(power) * (2 * pp_bitrev(sl, LOGD) + 1)) & (2 * d - 1));
+        const int src = pp_bitrev((e - 1) >> 1, LOGD);
+        acc[q] = add_mod(acc[q], mont_mul(x[q], __ldg(w + src), p, pinv), p);
+      }
+    }
+    ntt16_inverse<LOGD, false, kCompact>(acc, x_buf, tab16, p, lt, g + 1);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      res[static_cast<int64_t>(pi) * d + lt + NT * q] =
+          shoup_mul(acc[q], c.scale[pi], c.scale_s[pi], p);
+    }
+  }
+  T add_r[kPerThread];
+#pragma unroll
+  for (int j = 0; j < kPerThread; ++j) {
+    const int r = threadIdx.x + j * G * NT;
+    add_r[j] = r < d ? add[r] : T{0};
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kPerThread; ++j) {
+    const int r = threadIdx.x + j * G * NT;
+    if (r < d) {
+      uint32_t x[kMaxPrimes] = {0, 0, 0, 0, 0};
+#pragma unroll
+      for (int pi = 0; pi < kMaxPrimes; ++pi) {
+        if (pi < c.r) x[pi] = res[static_cast<int64_t>(pi) * d + r];
+      }
+      cur[r] = static_cast<T>(add_r[j] + crt_reconstruct<T>(x, c));
+    }
+  }
+  __syncthreads();
+}
+
+// pp_chain_kernel with pp_link16: grid = (2, slices), block = G d/16
+// threads, shared memory (1 + k) d words of T + (r + G) d words (needs
+// c.tables16).
+template <typename T, int LOGD, int G>
+__global__ void __launch_bounds__(G * Ntt16<LOGD>::kThreads, 1)
+pp_chain16_kernel(const T* __restrict__ ev, ChainArgs a, NttCtx c, T* __restrict__ tg,
+                  T* __restrict__ tgh, T* __restrict__ fin) {
+  extern __shared__ __align__(16) unsigned char pp_smem[];
+  constexpr int d = 1 << LOGD;
+  T* cur = reinterpret_cast<T*>(pp_smem);
+  uint32_t* res = reinterpret_cast<uint32_t*>(cur + d);
+  uint32_t* xs = res + static_cast<int64_t>(c.r) * d;
+  T* dig = reinterpret_cast<T*>(xs + G * d);
+  const int chain = blockIdx.x, s = blockIdx.y;
+  const T* evs = ev + static_cast<int64_t>(s) * d * d;
+  const T* start = evs + static_cast<int64_t>(__ldg(a.hat_row + (chain == 0 ? d / 2 - 1 : d - 1))) * d;
+  for (int r = threadIdx.x; r < d; r += blockDim.x) cur[r] = start[r];
+  __syncthreads();
+  T* out = (chain == 0 ? tg : tgh) + s * a.chain_stride;
+  for (int i = d / 2 - 2; i >= 0; --i) {
+    const int p5 = __ldg(a.pow5 + i);
+    const int power = chain == 0
+                          ? p5
+                          : static_cast<int>((static_cast<int64_t>(p5) * (2 * d - 1)) % (2 * d));
+    const T* add = evs + static_cast<int64_t>(__ldg(a.hat_row + (chain == 0 ? i : d / 2 + i))) * d;
+    pp_link16<T, LOGD, G>(cur, res, xs, dig, a, c, power, a.Wg,
+                          out + static_cast<int64_t>(i) * a.k * d, add);
+  }
+  T* f = fin + (static_cast<int64_t>(s) * 2 + chain) * d;
+  for (int r = threadIdx.x; r < d; r += blockDim.x) f[r] = cur[r];
+}
+
+// pp_tail_kernel with pp_link16. grid = slices, block = G d/16 threads.
+template <typename T, int LOGD, int G>
+__global__ void __launch_bounds__(G * Ntt16<LOGD>::kThreads, 1)
+pp_tail16_kernel(const T* __restrict__ fin, ChainArgs a, NttCtx c, T* __restrict__ t_vec_h,
+                 T* __restrict__ a_tilde) {
+  extern __shared__ __align__(16) unsigned char pp_smem[];
+  constexpr int d = 1 << LOGD;
+  T* cur = reinterpret_cast<T*>(pp_smem);
+  uint32_t* res = reinterpret_cast<uint32_t*>(cur + d);
+  uint32_t* xs = res + static_cast<int64_t>(c.r) * d;
+  T* dig = reinterpret_cast<T*>(xs + G * d);
+  const int s = blockIdx.x;
+  const T* tgf = fin + static_cast<int64_t>(s) * 2 * d;
+  const T* tghf = tgf + d;
+  for (int r = threadIdx.x; r < d; r += blockDim.x) cur[r] = tghf[r];
+  __syncthreads();
+  pp_link16<T, LOGD, G>(cur, res, xs, dig, a, c, 1, a.Wh,
+                        t_vec_h + static_cast<int64_t>(s) * a.k * d, tgf);
   for (int r = threadIdx.x; r < d; r += blockDim.x) {
     a_tilde[static_cast<int64_t>(s) * d + r] = pp_low<T>(cur[r], a.log_q);
   }

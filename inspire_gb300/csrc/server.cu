@@ -3554,7 +3554,42 @@ int inspire_preprocess_matrix_pack(int32_t coeff_bits, int32_t mat_kind,
           dfin.get<T>(), ca, c, static_cast<T*>(th_out), static_cast<T*>(a_out));
       return Cuda(cudaGetLastError(), "a_tilde_agg");
     };
-    if (iters == 2) {
+    // The radix-16 register transforms (d = 2048..8192): G groups of d/16
+    // threads, one prime each at a time, at most 768 threads (85 registers
+    // a thread).
+    auto chains16 = [&](auto ltag, auto gtag) -> Status {
+      constexpr int LG = decltype(ltag)::value;
+      constexpr int GR = decltype(gtag)::value;
+      const size_t smem16 = (1 + k) * d * w + static_cast<size_t>(d) * 4 * (r + GR);
+      RETURN_IF_ERROR(SetSmem(pp_chain16_kernel<T, LG, GR>, smem16));
+      RETURN_IF_ERROR(SetSmem(pp_tail16_kernel<T, LG, GR>, smem16));
+      constexpr int nt = GR * Ntt16<LG>::kThreads;
+      pp_chain16_kernel<T, LG, GR><<<dim3(2, slices), nt, smem16, cs>>>(
+          ev->get<T>(), ca, c, dtg.get<T>(), dtgh.get<T>(), dfin.get<T>());
+      RETURN_IF_ERROR(Cuda(cudaGetLastError(), "reduction chains"));
+      pp_tail16_kernel<T, LG, GR><<<slices, nt, smem16, cs>>>(
+          dfin.get<T>(), ca, c, static_cast<T*>(th_out), static_cast<T*>(a_out));
+      return Cuda(cudaGetLastError(), "a_tilde_agg");
+    };
+    using I1 = std::integral_constant<int, 1>;
+    using I2 = std::integral_constant<int, 2>;
+    using I3 = std::integral_constant<int, 3>;
+    using I4 = std::integral_constant<int, 4>;
+    using I5 = std::integral_constant<int, 5>;
+    const int groups16 = logd == 11 ? std::min(r, 5) : logd == 12 ? std::min(r, 3) : 1;
+    const bool fits16 =
+        (1 + k) * d * w + static_cast<size_t>(d) * 4 * (r + groups16) <= 227 * 1024;
+    if (c.tables16 != nullptr && fits16 && logd == 11) {
+      if (groups16 == 2) RETURN_IF_ERROR(chains16(std::integral_constant<int, 11>{}, I2{}));
+      if (groups16 == 3) RETURN_IF_ERROR(chains16(std::integral_constant<int, 11>{}, I3{}));
+      if (groups16 == 4) RETURN_IF_ERROR(chains16(std::integral_constant<int, 11>{}, I4{}));
+      if (groups16 == 5) RETURN_IF_ERROR(chains16(std::integral_constant<int, 11>{}, I5{}));
+    } else if (c.tables16 != nullptr && fits16 && logd == 12) {
+      if (groups16 == 2) RETURN_IF_ERROR(chains16(std::integral_constant<int, 12>{}, I2{}));
+      if (groups16 == 3) RETURN_IF_ERROR(chains16(std::integral_constant<int, 12>{}, I3{}));
+    } else if (c.tables16 != nullptr && fits16 && logd == 13) {
+      RETURN_IF_ERROR(chains16(std::integral_constant<int, 13>{}, I1{}));
+    } else if (iters == 2) {
       RETURN_IF_ERROR(chains(std::integral_constant<int, 2>{}));
     } else {
       RETURN_IF_ERROR(chains(std::integral_constant<int, 1>{}));

@@ -3,7 +3,8 @@ full ring degree.
 
 * Parity: a_tilde_agg, t_vec_h and the matrix (every element type the
   reference instantiates, crypto/lwes_to_rlwe.cc:533-575) equal the oracle's
-  exact restatement for several slices at once, d = 64 and 256.
+  exact restatement for several slices at once, d = 64 and 256, and for one
+  slice at d = 2048 (the radix-16 reduction chains).
 * d = 2048 / 4096 (the C2 / C3 ring degrees): LWE ciphertexts extracted
   from one RLWE encryption, the GPU's matrix and t_vec_h, then
   FinalizeMatrixPack(b + P y_g) decrypts to the messages
@@ -51,6 +52,22 @@ def test_matches_oracle(d, bits, log_q, log_digit, k):
         assert np.array_equal(th_gpu[s], ref["t_vec_h"]), s
         want = ref["matrix"].astype(dtype_of(bits))
         assert np.array_equal(m_gpu[s * d:(s + 1) * d], want), s
+
+
+@pytest.mark.parametrize("bits,log_q", [(32, 32), (64, 52)])
+def test_radix16_chains_match_oracle_at_d2048(bits, log_q):
+    # d = 2048: the reduction chains run on the radix-16 register
+    # transforms, one thread group per prime (the oracle's chain is O(d^3)
+    # and takes seconds here; 4096 is left to the decryption tests below).
+    d, k, log_digit = 2048, 2, 19
+    hint, pack_a = _random_case(d, bits, log_q, k, 1, 2048 + log_q)
+    a_gpu, m_gpu, th_gpu = pir.PreprocessMatrixPack(hint, pack_a, log_q,
+                                                    log_digit, k)
+    ref = orc.preprocess_matrix_pack(hint[:, :d], pack_a[:k], pack_a[k:], bits,
+                                     log_q, log_digit, k)
+    assert np.array_equal(a_gpu[0], ref["a_tilde_agg"])
+    assert np.array_equal(th_gpu[0], ref["t_vec_h"])
+    assert np.array_equal(m_gpu, ref["matrix"].astype(dtype_of(bits)))
 
 
 @pytest.mark.parametrize("mat", [np.int16, np.int32])

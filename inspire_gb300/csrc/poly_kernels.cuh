@@ -442,6 +442,56 @@ hint_rows_kernel(const S* __restrict__ db, int64_t cols, int n,
   }
 }
 
+// hint_rows_kernel for d = 2^LOGD with the radix-16 register transforms of
+// ntt16.cuh: one block per (prime, DB row), d / 16 threads; a thread reads
+// coefficients tid + (d/16) q of each row block (coalesced), the forward
+// transform leaves it slots 16 tid + q (in [0, 2p), straight into the
+// Montgomery products with 16-byte loads of V), and the inverse starts from
+// the accumulators. Same residues as hint_rows_kernel. grid = (r, rows),
+// d words of shared memory, needs c.tables16.
+template <typename S, int LOGD>
+__global__ void __launch_bounds__(Ntt16<LOGD>::kThreads, 512 / Ntt16<LOGD>::kThreads)
+hint_rows16_kernel(const S* __restrict__ db, int64_t cols, int n,
+                   const uint32_t* __restrict__ V, uint32_t* __restrict__ out,
+                   NttCtx c) {
+  extern __shared__ uint32_t smem[];
+  constexpr int d = Ntt16<LOGD>::kD;
+  constexpr int NT = Ntt16<LOGD>::kThreads;
+  constexpr bool kCompact = true;  // the unrolled form spills at d = 4096
+  const int pi = blockIdx.x;
+  const int64_t row = blockIdx.y;
+  const int tid = threadIdx.x;
+  const uint32_t p = c.p[pi];
+  const uint32_t pinv = c.pinv[pi];
+  const uint32_t* tab16 = c.tables16 + static_cast<size_t>(pi) * 4 * d;
+  uint32_t acc[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) acc[q] = 0;
+  const S* src = db + row * cols;
+  for (int k = 0; k < n; ++k) {
+    uint32_t x[16];
+    const S* rk = src + static_cast<int64_t>(k) * d + tid;  // + NT q: immediates
+#pragma unroll
+    for (int q = 0; q < 16; ++q) x[q] = reduce_u32(static_cast<uint32_t>(rk[NT * q]), p);
+    ntt16_forward<LOGD, false, kCompact, true>(x, smem, tab16, p, tid);
+    const uint4* vk = reinterpret_cast<const uint4*>(
+        V + (static_cast<int64_t>(k) * c.r + pi) * d + 16 * tid);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const uint4 w = __ldg(vk + v);
+      const uint32_t wv[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        acc[4 * v + i] = add_mod(acc[4 * v + i], mont_mul(x[4 * v + i], wv[i], p, pinv), p);
+      }
+    }
+  }
+  ntt16_inverse<LOGD, false, kCompact>(acc, smem, tab16, p, tid);
+  uint32_t* o = out + (row * c.r + pi) * d + tid;
+#pragma unroll
+  for (int q = 0; q < 16; ++q) o[NT * q] = shoup_mul(acc[q], c.scale[pi], c.scale_s[pi], p);
+}
+
 // CRT of the hint residues: out[row][j] = the integer mod 2^w.
 template <typename T>
 __global__ void hint_crt_kernel(const uint32_t* __restrict__ res, int64_t rows, int d,

@@ -3283,13 +3283,22 @@ int inspire_compute_hint_matrix(int32_t db_kind, int32_t coeff_bits, const void*
       ntt_coeffs_kernel<T><<<dim3(n * r, 1), PolyThreads(d), d * 4, cs>>>(
           dv.get<T>(), 0, 0, n, static_cast<T>(~0ull), dV.get<uint32_t>(), d, c);
       RETURN_IF_ERROR(Cuda(cudaGetLastError(), "a-component transforms"));
-      const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(r) * rows, sms);
       const dim3 grid(r, static_cast<unsigned>(rows));
-      INSPIRE_ITERS_DISPATCH(
-          pl.iters, RETURN_IF_ERROR(SetSmem(hint_rows_kernel<S, IT>, d * 4));
-          hint_rows_kernel<S, IT><<<grid, pl.nt, d * 4, cs>>>(
-              static_cast<const S*>(db_dev), cols, n, dV.get<uint32_t>(),
-              dres.get<uint32_t>(), c));
+      if (c.tables16 != nullptr) {
+        // d = 2048..8192: the radix-16 register transforms.
+        INSPIRE_NTT16_DISPATCH(
+            c.logd, RETURN_IF_ERROR(SetSmem(hint_rows16_kernel<S, LG>, d * 4));
+            hint_rows16_kernel<S, LG><<<grid, Ntt16<LG>::kThreads, d * 4, cs>>>(
+                static_cast<const S*>(db_dev), cols, n, dV.get<uint32_t>(),
+                dres.get<uint32_t>(), c));
+      } else {
+        const PolyLaunch pl = PolyShapeFor(d, static_cast<int64_t>(r) * rows, sms);
+        INSPIRE_ITERS_DISPATCH(
+            pl.iters, RETURN_IF_ERROR(SetSmem(hint_rows_kernel<S, IT>, d * 4));
+            hint_rows_kernel<S, IT><<<grid, pl.nt, d * 4, cs>>>(
+                static_cast<const S*>(db_dev), cols, n, dV.get<uint32_t>(),
+                dres.get<uint32_t>(), c));
+      }
       RETURN_IF_ERROR(Cuda(cudaGetLastError(), "hint rows"));
       const int64_t total = rows * static_cast<int64_t>(d);
       const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 152 * 8));

@@ -82,7 +82,7 @@ def test_narrow_matrix_types(mat):
 
 @pytest.mark.parametrize("d,bits,log_q,log_digit,k,noise", [
     (2048, 32, 32, 19, 2, 0), (4096, 32, 32, 19, 2, 0), (4096, 32, 32, 8, 4, 2),
-    (2048, 64, 52, 19, 2, 2)])
+    (2048, 64, 52, 19, 2, 2), (4096, 64, 52, 19, 2, 2), (8192, 32, 32, 19, 2, 0)])
 def test_packed_ciphertext_decrypts_at_full_degree(d, bits, log_q, log_digit,
                                                    k, noise):
     t = 16

@@ -1576,7 +1576,6 @@ Status LoadImage(const inspire_pir_params* prm, const uint8_t* buf, size_t size,
 struct ImageWriter {
   uint8_t* dst;
   size_t cap, off = 0;
-  bool fits() const { return dst != nullptr && off <= cap; }
   void put(const void* p, size_t n) {
     if (dst != nullptr && off + n <= cap) std::memcpy(dst + off, p, n);
     off += n;

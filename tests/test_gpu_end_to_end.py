@@ -129,3 +129,33 @@ def test_client_rejects_bad_index():
     c = pir.PirClient.Create(params, a, clients=1)
     with pytest.raises(pir.InspireError, match="Index out of bounds"):
         c.CreateRequests([2048])
+
+
+def test_headline_shape_decrypts_over_z64():
+    """The benchmarked shape, n = 2^20 records of d = 4096 coefficients,
+    t = 8, over Z_2^64 with q = 2^56 (the real-parameter set; over Z_2^32
+    the first-dimension noise of 2^17 columns exceeds the message scale):
+    the 8 GiB raw DB preprocessed on the GPU (interpolation, the 32768 x
+    4096 hint, PreprocessMatrixPack of its 8 slices), answered by both
+    engines, and the first, last and six random records decrypt exactly."""
+    import gc
+
+    from inspire_gb300 import synthetic
+    d, t, n = 4096, 8, 1 << 20
+    params = _params(d, t, n)
+    db_raw = synthetic.parallel_integers((n, d), 0, P, np.uint16, 2048)
+    a = _a_components(params, seed=17)
+    pre = pir.PreprocessingServer.Create(params, a).Preprocess(db_raw)
+    server = pir.PirServer.Create(params, pre)
+    del pre
+    gc.collect()
+    batch = 8
+    client = pir.PirClient.Create(params, a, clients=batch, seed=9, variance=6)
+    idx = np.random.default_rng(19).integers(0, n, batch)
+    idx[0], idx[1] = 0, n - 1
+    fd, sd, pk = client.CreateRequests(idx)
+    for engine in (pir.ENGINE_PLAIN, pir.ENGINE_TENSOR):
+        got = client.ProcessResponses(server.process_arrays(fd, sd, pk, engine))
+        for b in range(batch):
+            assert np.array_equal(got[b].astype(np.int64),
+                                  db_raw[idx[b]].astype(np.int64)), (engine, b, idx[b])

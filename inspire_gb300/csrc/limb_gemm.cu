@@ -114,12 +114,14 @@ static_assert(kSmemBytes <= 227 * 1024, "shared memory per CTA");
 // Shared-memory plan of one kernel form within the kRingBytes budget: the
 // two A rings, the request slots (NQ planes x TQ requests x 64 K of fp16;
 // three, or two for full tiles in the converting form) and, in the
-// converting form, a staging ring of raw u16 tiles (8 KB each, up to 8) that
+// converting form, a staging ring of raw u16 tiles (8 KB each, as many as
+// fit: 9 with narrow request tiles) that
 // the producer fills ahead of the converter, so that a raw tile is already
 // on chip when its box frees up.
 // Full request tiles leave no room for staging: their converting form loads
 // each raw tile into the first half of its own box (once the MMA pipe has
 // freed it) and the converter expands it in place.
+constexpr int kMaxStages = 16;  // staging slots the barrier region provides for
 template <int NQ, bool CONV, int TQ>
 struct RingPlan {
   static constexpr int kBSlotB = NQ * TQ * kBSlotK * 2;
@@ -128,7 +130,7 @@ struct RingPlan {
   static constexpr int kBBase = kRowBlocks * kARingBytes;
   static constexpr int kStageBase = kBBase + kBS * kBSlotB;
   static constexpr int kFree = (kRingBytes - kStageBase) / kRawTileBytes;
-  static constexpr int kStages = kStaged ? (kFree < 8 ? kFree : 8) : 0;
+  static constexpr int kStages = kStaged ? (kFree < kMaxStages ? kFree : kMaxStages) : 0;
   static_assert(!kStaged || kStages >= 4, "raw staging ring");
   static_assert(kStageBase + kStages * kRawTileBytes <= kRingBytes, "ring budget");
 };
@@ -443,9 +445,9 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   // Staged: st_full / st_empty per staging slot. In place: st_full[pair]
   // is the pair's raw-tiles-landed barrier.
   uint64_t* st_full = mma_done + 1;
-  uint64_t* st_empty = st_full + 8;
-  uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(st_empty + 8);
-  static_assert((3 * kRowBlocks * 2 + 2 * kBSlots + 1 + 16) * 8 + 4 <= kBarrierBytes,
+  uint64_t* st_empty = st_full + kMaxStages;
+  uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(st_empty + kMaxStages);
+  static_assert((3 * kRowBlocks * 2 + 2 * kBSlots + 1 + 2 * kMaxStages) * 8 + 4 <= kBarrierBytes,
                 "barrier region");
 
   const int warp = threadIdx.x >> 5;
@@ -514,13 +516,13 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     int a_last[kRowBlocks * kAPairs];
     bool a_raw[kRowBlocks * kAPairs];  // in place: last load was raw tiles
     int b_last[kBSlots];
-    int st_last[8];
+    int st_last[kMaxStages];
     for (int s = 0; s < kRowBlocks * kAPairs; ++s) {
       a_last[s] = -1;
       a_raw[s] = false;
     }
     for (int s = 0; s < kBSlots; ++s) b_last[s] = -1;
-    for (int s = 0; s < 8; ++s) st_last[s] = -1;
+    for (int s = 0; s < kMaxStages; ++s) st_last[s] = -1;
     bool ok = true;
     int seq = 0;  // raw tiles issued (converting form), in the MMA's box order
     auto load_pair = [&](int rb, int p, const UnitSrc& src, int i) {

@@ -446,8 +446,11 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
   // is the pair's raw-tiles-landed barrier.
   uint64_t* st_full = mma_done + 1;
   uint64_t* st_empty = st_full + kMaxStages;
-  uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(st_empty + kMaxStages);
-  static_assert((3 * kRowBlocks * 2 + 2 * kBSlots + 1 + 2 * kMaxStages) * 8 + 4 <= kBarrierBytes,
+  // Staged: the converter warps are done with the DB units (one arrival
+  // each).
+  uint64_t* conv_done = st_empty + kMaxStages;
+  uint32_t* tmem_base_slot = reinterpret_cast<uint32_t*>(conv_done + 1);
+  static_assert((3 * kRowBlocks * 2 + 2 * kBSlots + 2 + 2 * kMaxStages) * 8 + 4 <= kBarrierBytes,
                 "barrier region");
 
   const int warp = threadIdx.x >> 5;
@@ -484,6 +487,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
       mbar_init(&acc_empty[b], 4);
     }
     mbar_init(mma_done, 1);
+    mbar_init(conv_done, kConvThreads / 32);
     for (int s = 0; s < (kStaged ? kNS : kRowBlocks * kAPairs); ++s) {
       mbar_init(&st_full[s], 1);
       mbar_init(&st_empty[s], 1);
@@ -524,6 +528,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     for (int s = 0; s < kBSlots; ++s) b_last[s] = -1;
     for (int s = 0; s < kMaxStages; ++s) st_last[s] = -1;
     bool ok = true;
+    bool conv_seen = false;  // staged: conv_done observed
     int seq = 0;  // raw tiles issued (converting form), in the MMA's box order
     auto load_pair = [&](int rb, int p, const UnitSrc& src, int i) {
       if constexpr (kStaged) {
@@ -539,6 +544,15 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
             st_last[j] = seq;
           }
           return true;
+        }
+        // A pack unit's boxes: this thread waited on no A barrier during
+        // the DB units, and a parity wait cannot tell phases two apart, so
+        // it first waits until the converter warps are done with the DB
+        // units (the MMA pipe has then freed all but the last DB unit's
+        // boxes, and the wait below is for the next phase).
+        if (!conv_seen) {
+          if (!mbar_wait(conv_done, 0, err)) return false;
+          conv_seen = true;
         }
       }
       const int s = rb * kAPairs + p;
@@ -748,6 +762,7 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
         if (lane == 0) mbar_arrive(&a_full[s]);
       }
     }
+    if (lane == 0) mbar_arrive(conv_done);
     }
   } else {
     if constexpr (CONV) {

@@ -18,6 +18,7 @@
 // sums. Arithmetic wraps mod 2^w exactly like the reference's CoeffType.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <type_traits>
 
@@ -38,6 +39,8 @@ int elem_size(int kind) {
 }
 
 namespace {
+
+constexpr int kGemvDevices = 64;
 
 struct NoMat {};
 
@@ -92,22 +95,29 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// One matrix segment: rows x cols of E, query rows of T.
-template <typename T, typename E, int RB, int NQ, int NT>
+// The RB row vectors at column c.
+template <typename E, int RB>
+__device__ __forceinline__ void load_rows(uint4 (&w)[RB], const E* m, int64_t cols,
+                                          int64_t row0, int64_t rows, int64_t c) {
+#pragma unroll
+  for (int r = 0; r < RB; ++r) {
+    const int64_t row = row0 + r;
+    w[r] = row < rows ? ld_stream(m + row * cols + c) : make_uint4(0, 0, 0, 0);
+  }
+}
+
+// One matrix segment: rows x cols of E, query rows of T. PF (a launch of one
+// wave, a few iterations per thread): the next iteration's matrix vectors
+// are loaded before this one's products, so a thread keeps two iterations'
+// loads in flight instead of waiting out one round trip per iteration.
+template <typename T, typename E, int RB, int NQ, int NT, bool PF>
 __device__ __forceinline__ void segment(T (&acc)[RB][NQ], const E* m,
                                         int64_t cols, const T* q,
                                         int64_t q_stride, int64_t row0,
                                         int64_t rows) {
   constexpr int EPV = 16 / sizeof(E);  // matrix elements per 16-byte vector
   const int64_t nvec = cols / EPV;
-  for (int64_t v = threadIdx.x; v < nvec; v += NT) {
-    const int64_t c = v * EPV;
-    uint4 w[RB];
-#pragma unroll
-    for (int r = 0; r < RB; ++r) {
-      const int64_t row = row0 + r;
-      w[r] = row < rows ? ld_stream(m + row * cols + c) : make_uint4(0, 0, 0, 0);
-    }
+  auto products = [&](const uint4 (&w)[RB], int64_t c) {
 #pragma unroll
     for (int qi = 0; qi < NQ; ++qi) {
       alignas(16) T qv[EPV];
@@ -115,11 +125,38 @@ __device__ __forceinline__ void segment(T (&acc)[RB][NQ], const E* m,
 #pragma unroll
       for (int r = 0; r < RB; ++r) acc[r][qi] = mac_vec<T, E>(acc[r][qi], w[r], qv);
     }
+  };
+  if constexpr (PF) {
+    int64_t v = threadIdx.x;
+    if (v >= nvec) return;
+    uint4 w[RB];
+    load_rows<E, RB>(w, m, cols, row0, rows, v * EPV);
+    for (;;) {
+      uint4 cur[RB];
+#pragma unroll
+      for (int r = 0; r < RB; ++r) cur[r] = w[r];
+      const int64_t c = v * EPV;
+      v += NT;
+      const bool more = v < nvec;
+      if (more) load_rows<E, RB>(w, m, cols, row0, rows, v * EPV);
+      products(cur, c);
+      if (!more) break;
+    }
+  } else {
+    for (int64_t v = threadIdx.x; v < nvec; v += NT) {
+      uint4 w[RB];
+      load_rows<E, RB>(w, m, cols, row0, rows, v * EPV);
+      products(w, v * EPV);
+    }
   }
 }
 
-template <typename T, typename DbT, typename MatT, int RB, int NQ, int NT>
-__global__ void __launch_bounds__(NT)
+// PF kernels (128 threads) are built for at least seven resident blocks per
+// SM (72 registers a thread at most), so that a launch of up to 7 x 152
+// blocks runs in one wave.
+template <typename T, typename DbT, typename MatT, int RB, int NQ, int NT,
+          bool PF = false>
+__global__ void __launch_bounds__(NT, PF ? 896 / NT : 1)
 fused_gemv_kernel(const DbT* __restrict__ db, int64_t db_cols,
                   const T* __restrict__ q1, int64_t q1_stride,
                   const MatT* __restrict__ pk, int64_t pk_cols,
@@ -132,9 +169,11 @@ fused_gemv_kernel(const DbT* __restrict__ db, int64_t db_cols,
     for (int q = 0; q < NQ; ++q) acc[r][q] = 0;
   const int64_t row0 = static_cast<int64_t>(blockIdx.x) * RB;
 
-  if (db_cols > 0) segment<T, DbT, RB, NQ, NT>(acc, db, db_cols, q1, q1_stride, row0, rows);
+  if (db_cols > 0)
+    segment<T, DbT, RB, NQ, NT, PF>(acc, db, db_cols, q1, q1_stride, row0, rows);
   if constexpr (!std::is_same<MatT, NoMat>::value) {
-    if (pk_cols > 0) segment<T, MatT, RB, NQ, NT>(acc, pk, pk_cols, yg, yg_stride, row0, rows);
+    if (pk_cols > 0)
+      segment<T, MatT, RB, NQ, NT, PF>(acc, pk, pk_cols, yg, yg_stride, row0, rows);
   }
 
   __shared__ T partial[NT / 32][RB * NQ];
@@ -199,35 +238,91 @@ __global__ void generic_gemv_kernel(int db_kind, const void* db,
 
 constexpr int kThreads = 256;
 
+// Blocks of `kernel` (nt threads, no dynamic shared memory) that the current
+// device holds at once; 0 if the runtime cannot say.
+template <typename K>
+int64_t resident_blocks(K kernel, int nt) {
+  int dev = 0, per_sm = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, nt, 0) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    return 0;
+  }
+  return static_cast<int64_t>(per_sm) * sms;
+}
+
+// resident_blocks, computed once per device and call site (`cache`).
+template <typename K>
+int64_t resident_cached(std::atomic<int64_t> (&cache)[kGemvDevices], K kernel, int nt) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kGemvDevices) {
+    return resident_blocks(kernel, nt);
+  }
+  int64_t v = cache[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    v = resident_blocks(kernel, nt);
+    cache[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
+
+template <typename T, typename DbT, typename MatT, int RB, int NQ, int NT, bool PF>
+cudaError_t launch_rows(int64_t blocks, const void* db, int64_t db_cols, const void* q1,
+                        int64_t q1_stride, const void* pk, int64_t pk_cols,
+                        const void* yg, int64_t yg_stride, void* out,
+                        int64_t out_stride, int64_t rows, cudaStream_t stream) {
+  fused_gemv_kernel<T, DbT, MatT, RB, NQ, NT, PF>
+      <<<static_cast<unsigned>(blocks), NT, 0, stream>>>(
+          static_cast<const DbT*>(db), db_cols, static_cast<const T*>(q1),
+          q1_stride, static_cast<const MatT*>(pk), pk_cols,
+          static_cast<const T*>(yg), yg_stride, static_cast<T*>(out),
+          out_stride, rows);
+  return cudaGetLastError();
+}
+
 template <typename T, typename DbT, typename MatT, int NQ>
 cudaError_t launch_typed(const void* db, int64_t db_cols, const void* q1,
                          int64_t q1_stride, const void* pk, int64_t pk_cols,
                          const void* yg, int64_t yg_stride, void* out,
                          int64_t out_stride, int64_t rows,
                          cudaStream_t stream) {
-  if (NQ == 1 && rows < 16384 && rows > 4 * 1216) {
-    // Smaller matrices (e.g. 8192 rows: 2048 blocks of 4 rows are 1.7 waves)
-    // take 2 rows per block, which evens out the last wave: 0.84 instead of
-    // 0.78 of the copy peak at 8192 x 16384 u16 + 8192 x 4096 i32. Up to
-    // 4 x 1216 rows (1216 blocks of 256 threads: one wave at eight blocks
-    // per SM) the 4-row blocks below all run in one wave.
-    fused_gemv_kernel<T, DbT, MatT, 2, NQ, kThreads>
-        <<<static_cast<unsigned>((rows + 1) / 2), kThreads, 0, stream>>>(
-            static_cast<const DbT*>(db), db_cols, static_cast<const T*>(q1),
-            q1_stride, static_cast<const MatT*>(pk), pk_cols,
-            static_cast<const T*>(yg), yg_stride, static_cast<T*>(out),
-            out_stride, rows);
-    return cudaGetLastError();
+  if constexpr (NQ == 1) {
+    if (rows < 16384 && rows > 4 * 1216) {
+      // Mid-size matrices (e.g. 8192 rows) take 2 rows per block, which
+      // evens out the last of their waves: 0.84 instead of 0.78 of the copy
+      // peak at 8192 x 16384 u16 + 8192 x 4096 i32.
+      return launch_rows<T, DbT, MatT, 2, 1, kThreads, false>(
+          (rows + 1) / 2, db, db_cols, q1, q1_stride, pk, pk_cols, yg, yg_stride, out,
+          out_stride, rows, stream);
+    }
+    const int64_t blocks = (rows + 3) / 4;
+    if (rows <= 4 * 1216) {
+      // Small matrices: 4-row blocks. When 256-thread blocks would not all
+      // fit on the device at once (at 64 registers a thread, four per SM)
+      // but 128-thread ones would, the launch takes 128-thread blocks with
+      // prefetching segments: one wave instead of a second, partly filled
+      // one (4096 x 2048 u16 + 4096 x 4096 i32 over Z_2^64: 1.68 waves of
+      // 256-thread blocks).
+      static std::atomic<int64_t> fit256[kGemvDevices];
+      static std::atomic<int64_t> fit128[kGemvDevices];
+      if (blocks > resident_cached(fit256, fused_gemv_kernel<T, DbT, MatT, 4, 1, kThreads>,
+                                   kThreads) &&
+          blocks <= resident_cached(fit128, fused_gemv_kernel<T, DbT, MatT, 4, 1, 128, true>,
+                                    128)) {
+        return launch_rows<T, DbT, MatT, 4, 1, 128, true>(
+            blocks, db, db_cols, q1, q1_stride, pk, pk_cols, yg, yg_stride, out, out_stride,
+            rows, stream);
+      }
+    }
+    return launch_rows<T, DbT, MatT, 4, 1, kThreads, false>(
+        blocks, db, db_cols, q1, q1_stride, pk, pk_cols, yg, yg_stride, out, out_stride, rows,
+        stream);
+  } else {
+    constexpr int RB = NQ >= 4 ? 2 : 4;
+    return launch_rows<T, DbT, MatT, RB, NQ, kThreads, false>(
+        (rows + RB - 1) / RB, db, db_cols, q1, q1_stride, pk, pk_cols, yg, yg_stride, out,
+        out_stride, rows, stream);
   }
-  constexpr int RB = NQ >= 4 ? 2 : 4;
-  const int64_t blocks = (rows + RB - 1) / RB;
-  fused_gemv_kernel<T, DbT, MatT, RB, NQ, kThreads>
-      <<<static_cast<unsigned>(blocks), kThreads, 0, stream>>>(
-          static_cast<const DbT*>(db), db_cols, static_cast<const T*>(q1),
-          q1_stride, static_cast<const MatT*>(pk), pk_cols,
-          static_cast<const T*>(yg), yg_stride, static_cast<T*>(out),
-          out_stride, rows);
-  return cudaGetLastError();
 }
 
 template <typename T, typename DbT, typename MatT>

@@ -302,15 +302,15 @@ finalize16_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ 
   }
 }
 
-// finalize16_kernel for launches with fewer blocks than SMs: d / 8 threads
-// in two groups of d / 16, group g taking primes g, g + 2, ... side by side, each
+// finalize16_kernel for launches with fewer blocks than SMs: NGR groups of
+// d / 16 threads, group g taking primes g, g + NGR, ... side by side, each
 // with its prime's inverse tables copied to shared memory and the compact
 // inverse (a block runs once per SM: global twiddle reads would each wait on
 // L2 and the unrolled code on instruction fetch); then the whole block does
-// the CRT. grid = (l * t, batch), shared memory (2 + 4 + r) * d words, needs
+// the CRT. grid = (l * t, batch), shared memory (3 NGR + r) * d words, needs
 // c.tables16.
-template <typename T, int LOGD>
-__global__ void __launch_bounds__(2 * Ntt16<LOGD>::kThreads, 1)
+template <typename T, int LOGD, int NGR = 2>
+__global__ void __launch_bounds__(NGR * Ntt16<LOGD>::kThreads, 1)
 finalize16_pair_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restrict__ Yh,
                        int k, const T* __restrict__ gemv, const T* __restrict__ gemv2,
                        int64_t gemv_qstride, T* __restrict__ packed_b, int log_q,
@@ -323,11 +323,11 @@ finalize16_pair_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restri
   const int lt = tid & (NT - 1);
   const int bar = 1 + grp;
   uint32_t* xs = smem + grp * d;
-  uint32_t* itab = smem + 2 * d + grp * 2 * d;  // IW | IW shoup of the prime
-  uint32_t* res = smem + 6 * d;                 // [r][d] scaled residues
+  uint32_t* itab = smem + NGR * d + grp * 2 * d;  // IW | IW shoup of the prime
+  uint32_t* res = smem + 3 * NGR * d;             // [r][d] scaled residues
   const int s = blockIdx.x;
   const int q = blockIdx.y;
-  for (int pi = grp; pi < c.r; pi += 2) {
+  for (int pi = grp; pi < c.r; pi += NGR) {
     const uint32_t p = c.p[pi];
     const uint32_t pinv = c.pinv[pi];
     const uint4* g16 = reinterpret_cast<const uint4*>(
@@ -365,7 +365,7 @@ finalize16_pair_kernel(const uint32_t* __restrict__ Th, const uint32_t* __restri
   const int64_t base = q * gemv_qstride + static_cast<int64_t>(s) * d;
   T* outp = packed_b + (static_cast<int64_t>(q) * gridDim.x + s) * d;
 #pragma unroll 4
-  for (int j = tid; j < d; j += 2 * NT) {
+  for (int j = tid; j < d; j += NGR * NT) {
     uint32_t x[kMaxPrimes] = {0, 0, 0, 0, 0};
 #pragma unroll
     for (int pi = 0; pi < kMaxPrimes; ++pi) {

@@ -594,6 +594,31 @@ Status LaunchPairExt(int64_t blocks, int sms, dim3 grid, cudaStream_t st, A... a
   return Cuda(cudaGetLastError(), "external product");
 }
 
+// Launches finalize16_pair_kernel with three transform groups at d = 2048
+// when there are three primes or more (each group inverts one of the first
+// three primes; at most 114 KB of shared memory), else with two groups,
+// which take the primes in turns.
+template <typename T, int LG>
+Status LaunchPairFinalize(const NttCtx& c, dim3 grid, cudaStream_t st, const uint32_t* th,
+                          const uint32_t* yh, int k, const T* gemv, int64_t rows,
+                          T* packed, int log_q) {
+  constexpr int d = Ntt16<LG>::kD;
+  if constexpr (LG <= 11) {
+    if (c.r >= 3) {
+      const size_t smem = static_cast<size_t>(9 + c.r) * d * 4;
+      RETURN_IF_ERROR(SetSmem(finalize16_pair_kernel<T, LG, 3>, smem));
+      finalize16_pair_kernel<T, LG, 3><<<grid, 3 * Ntt16<LG>::kThreads, smem, st>>>(
+          th, yh, k, gemv, nullptr, rows, packed, log_q, c);
+      return Cuda(cudaGetLastError(), "finalize");
+    }
+  }
+  const size_t smem = static_cast<size_t>(6 + c.r) * d * 4;
+  RETURN_IF_ERROR(SetSmem(finalize16_pair_kernel<T, LG, 2>, smem));
+  finalize16_pair_kernel<T, LG, 2><<<grid, 2 * Ntt16<LG>::kThreads, smem, st>>>(
+      th, yh, k, gemv, nullptr, rows, packed, log_q, c);
+  return Cuda(cudaGetLastError(), "finalize");
+}
+
 // Blocks (one per shard and request) from which the external product takes
 // one block per request over all primes rather than one per prime: a block
 // per SM at d >= 4096; at d = 2048 (128-thread blocks) two per SM, below
@@ -644,16 +669,12 @@ Status FinalizeStage(inspire_pir_server* s, Workspace* w, int batch,
             w->packed.get<T>(), log_q, c));
     RETURN_IF_ERROR(Cuda(cudaGetLastError(), "finalize"));
   } else if (s->ctx_f.tables16 != nullptr && d <= 4096) {
-    // Two transform groups per block: d / 8 threads.
+    // Several transform groups per block.
     const NttCtx& c = s->ctx_f;
-    const size_t smem = static_cast<size_t>(6 + c.r) * d * 4;
     INSPIRE_NTT16_PAIR_DISPATCH(
-        c.logd, RETURN_IF_ERROR(SetSmem(finalize16_pair_kernel<T, LG>, smem));
-        finalize16_pair_kernel<T, LG><<<dim3(l * t, batch), 2 * Ntt16<LG>::kThreads, smem,
-                                        st>>>(s->th_ntt.get<uint32_t>(), w->yh.get<uint32_t>(),
-                                              k, gemv, nullptr, s->rows, w->packed.get<T>(),
-                                              log_q, c));
-    RETURN_IF_ERROR(Cuda(cudaGetLastError(), "finalize"));
+        c.logd, RETURN_IF_ERROR((LaunchPairFinalize<T, LG>(
+                    c, dim3(l * t, batch), st, s->th_ntt.get<uint32_t>(),
+                    w->yh.get<uint32_t>(), k, gemv, s->rows, w->packed.get<T>(), log_q))));
   } else {
     const NttCtx& c = s->ctx_f;
     const size_t smem = static_cast<size_t>(c.r) * d * 4;

@@ -549,7 +549,10 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
         // the DB units, and a parity wait cannot tell phases two apart, so
         // it first waits until the converter warps are done with the DB
         // units (the MMA pipe has then freed all but the last DB unit's
-        // boxes, and the wait below is for the next phase).
+        // boxes, and the wait below is for the next phase). With three
+        // request slots the request-slot waits already keep this thread
+        // within one unit of the MMA pipe; this wait does not depend on
+        // that depth.
         if (!conv_seen) {
           if (!mbar_wait(conv_done, 0, err)) return false;
           conv_seen = true;
@@ -697,8 +700,9 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
     // warps' arrivals. Staged (narrow tiles): the box's raw tile is staging
     // slot seq % kNS, where seq = 8 i + 4 rb + w counts the DB boxes in the
     // producer's order; in place (full tiles): the first half of the box.
-    // Per box: lane 0 waits (bounded) for the raw tile (and, staged, for
-    // the MMA pipe to have freed the box) and the warp shares the outcome;
+    // Per box: lane 0 waits (bounded) for the raw tile (staged: first for
+    // the MMA pipe to have freed the box, then for the tile) and the warp
+    // shares the outcome;
     // every lane loads its 16 raw units (16 bytes, eight K values each), the
     // warp meets (and lane 0 frees the staging slot); then the lanes write
     // the units' x0 and
@@ -725,8 +729,13 @@ limb_gemm_kernel(const __grid_constant__ CUtensorMap tm_db,
         bool ready = false;
         if (lane == 0) {
           if constexpr (kStaged) {
-            ready = mbar_wait(&st_full[j], (sq / kNS) & 1, err) &&
-                    mbar_wait(&a_empty[s], (i & 1) ^ 1, err);
+            // The box first: once the MMA pipe has freed unit i - 1's box,
+            // the staging slot's previous tile (sq - kNS, another warp's
+            // when kNS is not a multiple of 4) has been read, so the parity
+            // wait on the slot is for the right phase even when copies land
+            // out of order.
+            ready = mbar_wait(&a_empty[s], (i & 1) ^ 1, err) &&
+                    mbar_wait(&st_full[j], (sq / kNS) & 1, err);
           } else {
             ready = mbar_wait(&st_full[s], i & 1, err);
           }

@@ -132,6 +132,10 @@ struct RingPlan {
   static constexpr int kFree = (kRingBytes - kStageBase) / kRawTileBytes;
   static constexpr int kStages = kStaged ? (kFree < kMaxStages ? kFree : kMaxStages) : 0;
   static_assert(!kStaged || kStages >= 4, "raw staging ring");
+  // The converter warps' parity waits on the staging slots are exact when
+  // each warp owns its slots (a multiple of 4) or, waiting for the freed box
+  // first, when the ring holds at least two row blocks' tiles (8).
+  static_assert(!kStaged || kStages % 4 == 0 || kStages >= 8, "staging ring size");
   static_assert(kStageBase + kStages * kRawTileBytes <= kRingBytes, "ring budget");
 };
 

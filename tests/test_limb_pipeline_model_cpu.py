@@ -355,6 +355,19 @@ def test_staged_converter_waits_for_the_box_before_the_tile():
     assert violations(make(8, False), 800) == []
 
 
+@pytest.mark.parametrize("stages", [4, 5, 6, 7, 8, 10, 12, 16])
+def test_staged_ring_sizes(stages):
+    """The staging ring sizes the kernel admits (a multiple of 4, or 8 and
+    more) keep the converter's waits exact; 5 to 7 slots would not, in
+    either wait order."""
+    found = violations(lambda rng: Kernel("staged", rng.choice([2, 3, 4]),
+                                          rng.choice([0, 1, 2]), stages=stages), 500)
+    if stages % 4 == 0 or stages >= 8:
+        assert found == []
+    else:
+        assert found and all("converter read staging slot" in f for f in found)
+
+
 def test_staged_producer_waits_for_the_converters_before_pack_boxes():
     """The producer waits on no box during the DB units. With three request
     slots its request-slot waits keep it within a unit of the MMA pipe, so

@@ -15,7 +15,8 @@ two apart.
 Every box, staging slot, request slot and accumulator records what was last
 written to it and what its reader last finished with, and the model checks
 that nothing is read before it is written or overwritten before it is
-freed, and that every role runs to its end. Two orderings of the staged
+freed, that every role runs to its end, and that the producer's drain
+leaves no copy in flight when it exits. Two orderings of the staged
 form are checked both ways: its converter warps wait for the freed box
 before the raw tile (the other order reads stale tiles once copies land out
 of order), and its producer waits on the converter warps before the first
@@ -125,6 +126,10 @@ class Kernel:
     def producer(self):
         seq = 0
         conv_seen = False
+        nslot = ROW_BLOCKS * PAIRS
+        a_last, a_raw = [-1] * nslot, [False] * nslot
+        b_last = [-1] * self.nb
+        st_last = [-1] * self.ns
 
         def load_pair(rb, p, i):
             nonlocal seq, conv_seen
@@ -140,6 +145,7 @@ class Kernel:
                                         % (j, seq, seq - self.ns))
                     self.st_full[j].expect_tx(1)
                     self.tma.append(("stage", j, seq))
+                    st_last[j] = seq
                     seq += 1
                 return
             if self.staged and self.use_conv_done and not conv_seen:
@@ -151,12 +157,14 @@ class Kernel:
                 self.st_full[s].expect_tx(2)
                 for h in (0, 1):
                     self.tma.append(("raw", s, h, i))
+                a_last[s], a_raw[s] = i, True
                 return
             if self.conv:
                 self.a_full[s].arrive()
             self.a_full[s].expect_tx(2)
             for h in (0, 1):
                 self.tma.append(("box", s, h, i))
+            a_last[s], a_raw[s] = i, False
 
         for i in range(self.nu):
             for p in range(PAIRS):
@@ -169,7 +177,20 @@ class Kernel:
                     raise Violation("request slot %d overwritten by %d" % (slot, n))
                 self.b_full[slot].expect_tx(1)
                 self.tma.append(("b", slot, n))
+                b_last[slot] = n
                 yield from load_pair(1, p, i)
+        # Drain: every copy this thread issued has landed before it exits.
+        for s in range(nslot):
+            if a_last[s] >= 0:
+                yield ((self.st_full if a_raw[s] else self.a_full)[s], a_last[s] & 1)
+        for slot in range(self.nb):
+            if b_last[slot] >= 0:
+                yield (self.b_full[slot], (b_last[slot] // self.nb) & 1)
+        for j in range(self.ns if self.staged else 0):
+            if st_last[j] >= 0:
+                yield (self.st_full[j], (st_last[j] // self.ns) & 1)
+        if self.tma:
+            raise Violation("producer exits with %d copies in flight" % len(self.tma))
 
     def converter(self, cw):
         p, h = cw >> 1, cw & 1

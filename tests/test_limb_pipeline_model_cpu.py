@@ -77,8 +77,11 @@ class Kernel:
     """
 
     def __init__(self, form, n_db, n_pk, stages=9, conv_done=True, b_slots=3,
-                 box_first=True):
+                 box_first=True, lenient=False):
         self.form, self.n_db, self.nu = form, n_db, n_db + n_pk
+        # lenient: record stale reads and early overwrites in `log` and go
+        # on, to see where they lead.
+        self.lenient, self.log = lenient, []
         self.conv = form != "planes"
         self.staged = form == "staged"
         self.use_conv_done = conv_done
@@ -111,16 +114,21 @@ class Kernel:
         self.commits = []  # tcgen05 commits: land in issue order
 
     # ---- checks ------------------------------------------------------
+    def fail(self, msg):
+        if not self.lenient:
+            raise Violation(msg)
+        self.log.append(msg)
+
     def box_free(self, s, i):
         if self.freed[s] < i - 1:
-            raise Violation("box pair %d overwritten for unit %d while unit %d "
-                            "is not freed" % (s, i, self.freed[s] + 1))
+            self.fail("box pair %d overwritten for unit %d while unit %d "
+                      "is not freed" % (s, i, self.freed[s] + 1))
 
     def box_ready(self, s, i):
         for h in (0, 1):
             if self.box.get((s, h)) != ("A", i):
-                raise Violation("MMA read box (%d, %d) for unit %d holding %r"
-                                % (s, h, i, self.box.get((s, h))))
+                self.fail("MMA read box (%d, %d) for unit %d holding %r"
+                          % (s, h, i, self.box.get((s, h))))
 
     # ---- roles -------------------------------------------------------
     def producer(self):
@@ -140,9 +148,8 @@ class Kernel:
                     j = seq % self.ns
                     yield (self.st_empty[j], ((seq // self.ns) & 1) ^ 1)
                     if self.stage_read[j] != seq - self.ns and seq >= self.ns:
-                        raise Violation("staging slot %d overwritten by tile %d "
-                                        "before tile %d was read"
-                                        % (j, seq, seq - self.ns))
+                        self.fail("staging slot %d overwritten by tile %d "
+                                  "before tile %d was read" % (j, seq, seq - self.ns))
                     self.st_full[j].expect_tx(1)
                     self.tma.append(("stage", j, seq))
                     st_last[j] = seq
@@ -209,16 +216,16 @@ class Kernel:
                         yield (self.st_full[j], (sq // self.ns) & 1)
                         yield (self.a_empty[s], (i & 1) ^ 1)
                     if self.stage[j] != sq:
-                        raise Violation("converter read staging slot %d for tile "
-                                        "%d holding %r" % (j, sq, self.stage[j]))
+                        self.fail("converter read staging slot %d for tile "
+                                  "%d holding %r" % (j, sq, self.stage[j]))
                     self.stage_read[j] = sq
                     self.st_empty[j].arrive()
                     self.box_free(s, i)
                 else:
                     yield (self.st_full[s], i & 1)
                     if self.box.get((s, h)) != ("raw", i):
-                        raise Violation("converter read box (%d, %d) for unit %d "
-                                        "holding %r" % (s, h, i, self.box.get((s, h))))
+                        self.fail("converter read box (%d, %d) for unit %d "
+                                  "holding %r" % (s, h, i, self.box.get((s, h))))
                 yield None
                 self.box[(s, h)] = ("A", i)
                 self.a_full[s].arrive()
@@ -402,3 +409,37 @@ def test_staged_producer_waits_for_the_converters_before_pack_boxes():
     found = violations(make(6, False), 600)
     assert found and all("overwritten" in f for f in found)
     assert violations(make(6, True), 600) == []
+
+
+def outcomes(make, seeds):
+    """Counts of how lenient runs end: clean, with stale reads or early
+    overwrites logged, with a broken barrier (an arrival beyond a phase's
+    count) or stalled (every role blocked, which the kernel's bounded waits
+    report as a pipeline timeout)."""
+    out = {"clean": 0, "logged": 0, "broken": 0, "stalled": 0}
+    for seed in range(seeds):
+        k = make(random.Random(10_000 + seed))
+        try:
+            simulate(k, seed)
+            out["logged" if k.log else "clean"] += 1
+        except Deadlock:
+            out["stalled"] += 1
+        except Violation:
+            out["broken"] += 1
+    return out
+
+
+def test_inexact_staging_waits_can_stall_the_pipe():
+    """A six-slot staging ring (what the shared memory left for narrow
+    request tiles over Z_2^64, eight digit planes a request) lets converter
+    warps pass their staging waits a phase early in either wait order; the
+    stale reads free slots early, and some schedules end with every role
+    blocked, i.e. a pipeline timeout. Nine slots with the box waited first
+    run clean."""
+    def make(stages, box_first):
+        return lambda rng: Kernel("staged", rng.choice([2, 3, 4, 6]), rng.choice([0, 1, 2]),
+                                  stages=stages, box_first=box_first, lenient=True)
+    for box_first in (False, True):
+        assert outcomes(make(6, box_first), 600)["stalled"] > 0
+    assert outcomes(make(9, True), 600) == {"clean": 600, "logged": 0, "broken": 0,
+                                            "stalled": 0}

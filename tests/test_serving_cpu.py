@@ -205,3 +205,131 @@ def test_bad_ticket_and_arguments(lib):
         assert lib.inspire_serving_release(h, t.value) == 0
     finally:
         lib.inspire_serving_destroy(h)
+
+
+def _loopback(lib, words, workspaces=2, delay_us=0, max_batch=4,
+              plain_max_batch=1, max_wait_us=0, ring_slots=8):
+    import ctypes
+    err = pir._errbuf()
+    h = ctypes.c_void_p()
+    w = (ctypes.c_int64 * len(words))(*words)
+    rc = lib.inspire_serving_create_loopback(
+        len(words) // 4, w, workspaces, delay_us, max_batch, plain_max_batch,
+        max_wait_us, ring_slots, ctypes.byref(h), err, len(err))
+    assert rc == 0, err.value
+    return h
+
+
+def _acquire(lib, h, q, timeout_ms):
+    """(status, ticket, [first_dim, second_dim, packing_key, response])."""
+    import ctypes
+    err = pir._errbuf()
+    t = ctypes.c_int64()
+    p = [ctypes.c_void_p() for _ in range(4)]
+    rc = lib.inspire_serving_acquire(h, q, timeout_ms, ctypes.byref(t),
+                                     *[ctypes.byref(x) for x in p], err, len(err))
+    return rc, t.value, [x.value for x in p]
+
+
+def _submit(lib, h, ticket, fd_ptr, word0, n_words):
+    import ctypes
+    fd = (ctypes.c_uint32 * n_words).from_address(fd_ptr)
+    fd[0] = word0
+    err = pir._errbuf()
+    return lib.inspire_serving_submit(h, ticket, 1, err, len(err))
+
+
+def test_full_ring_refuses_acquire_after_its_timeout(lib):
+    """inspire_serving_acquire blocks up to its timeout for a free slot and
+    then answers RESOURCE_EXHAUSTED; releasing the oldest slot frees one."""
+    import time
+    h = _loopback(lib, [4, 0, 2, 2], max_batch=4, ring_slots=4)
+    try:
+        tickets = []
+        for _ in range(4):
+            rc, t, _ = _acquire(lib, h, 0, 100)
+            assert rc == 0
+            tickets.append(t)
+        t0 = time.monotonic()
+        rc, _, _ = _acquire(lib, h, 0, 50)
+        assert rc == pir.RESOURCE_EXHAUSTED
+        assert time.monotonic() - t0 >= 0.04
+        assert lib.inspire_serving_release(h, tickets[0]) == 0
+        rc, t, _ = _acquire(lib, h, 0, 100)
+        assert rc == 0
+        for t in tickets[1:] + [t]:
+            assert lib.inspire_serving_release(h, t) == 0
+    finally:
+        lib.inspire_serving_destroy(h)
+
+
+def test_wait_reports_a_request_still_in_flight(lib):
+    """inspire_serving_wait answers DEADLINE_EXCEEDED while the batch runs
+    and the response once it is done; a running request cannot be
+    released."""
+    import ctypes
+    err = pir._errbuf()
+    h = _loopback(lib, [4, 0, 2, 3], delay_us=300_000)
+    try:
+        rc, t, p = _acquire(lib, h, 0, 100)
+        assert rc == 0
+        assert _submit(lib, h, t, p[0], 11, 4) == 0
+        assert lib.inspire_serving_wait(h, t, 1, err, len(err)) == pir.DEADLINE_EXCEEDED
+        assert b"in flight" in err.value
+        assert lib.inspire_serving_release(h, t) == pir.FAILED_PRECONDITION
+        assert lib.inspire_serving_wait(h, t, 5000, err, len(err)) == 0
+        resp = (ctypes.c_uint32 * 3).from_address(p[3])
+        assert list(resp) == [11 * 7 + k for k in range(3)]
+        assert lib.inspire_serving_release(h, t) == 0
+    finally:
+        lib.inspire_serving_destroy(h)
+
+
+def test_stats_count_completed_and_failed_requests_and_reset(lib):
+    """get_stats: completed and failed requests, batches, mean batch size,
+    latency percentiles in order, the largest number of batches in flight;
+    reset_stats clears them."""
+    import ctypes
+    err = pir._errbuf()
+    h = _loopback(lib, [4, 0, 2, 2], workspaces=2, delay_us=2000, max_batch=4,
+                  ring_slots=16)
+    try:
+        tickets = []
+        for i in range(10):
+            rc, t, p = _acquire(lib, h, 0, 1000)
+            assert rc == 0
+            assert _submit(lib, h, t, p[0], 0xDEAD if i == 9 else i + 1, 4) == 0
+            tickets.append(t)
+        codes = [lib.inspire_serving_wait(h, t, 5000, err, len(err)) for t in tickets]
+        for t in tickets:
+            assert lib.inspire_serving_release(h, t) == 0
+        st = serving._Stats()
+        assert lib.inspire_serving_get_stats(h, ctypes.byref(st)) == 0
+        n_failed = sum(c != 0 for c in codes)
+        assert codes[9] == pir.INVALID_ARGUMENT and n_failed >= 1
+        assert st.failed == n_failed
+        assert st.requests == 10 - n_failed
+        assert st.batches >= 3 and st.mean_batch == pytest.approx(10 / st.batches)
+        assert 0 < st.p50_ms <= st.p99_ms <= st.max_ms
+        assert 1 <= st.max_inflight <= 2
+        assert lib.inspire_serving_reset_stats(h) == 0
+        assert lib.inspire_serving_get_stats(h, ctypes.byref(st)) == 0
+        assert (st.requests, st.failed, st.batches, st.max_inflight) == (0, 0, 0, 0)
+        assert st.p50_ms == st.max_ms == 0.0
+    finally:
+        lib.inspire_serving_destroy(h)
+
+
+def test_queue_info(lib):
+    import ctypes
+    h = _loopback(lib, [4, 0, 2, 2, 8, 2, 2, 4], workspaces=3, ring_slots=12)
+    try:
+        ws, nbytes, slots = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int32()
+        for q in (0, 1):
+            assert lib.inspire_serving_queue_info(h, q, ctypes.byref(ws), ctypes.byref(nbytes),
+                                                  ctypes.byref(slots)) == 0
+            assert (ws.value, slots.value) == (3, 12)
+        assert lib.inspire_serving_queue_info(h, 2, ctypes.byref(ws), ctypes.byref(nbytes),
+                                              ctypes.byref(slots)) == pir.INVALID_ARGUMENT
+    finally:
+        lib.inspire_serving_destroy(h)

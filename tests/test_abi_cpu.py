@@ -61,3 +61,24 @@ def test_inner_product_rejects_empty_without_gpu(lib):
                                    err, len(err))
     assert rc == 3
     assert b"cannot be empty" in err.value
+
+
+@pytest.mark.parametrize("coeff_bits,n,d,u_bits,v_bits,chunk_bits,message", [
+    (16, 1, 64, 8, 8, 8, b"coeff_bits must be 32 or 64."),
+    (32, 1, 48, 8, 8, 8, b"Polynomial lengths or context mismatch."),
+    (32, 1, 1, 8, 8, 8, b"Polynomial lengths or context mismatch."),
+    (32, 1, 64, 0, 8, 8, b"Invalid bits or chunk_bits."),
+    (32, 1, 64, 8, -1, 8, b"Invalid bits or chunk_bits."),
+    (64, 1, 64, 8, 8, 64, b"Invalid bits or chunk_bits."),
+    # log2(n) + log2(d) + 2 chunk_bits > 53 (polynomial_fft.cc:93-96).
+    (32, 8, 4096, 19, 32, 20, b"Potential precision overflow in accumulation."),
+])
+def test_inner_product_argument_checks_without_gpu(lib, coeff_bits, n, d, u_bits,
+                                                   v_bits, chunk_bits, message):
+    """InnerProductFft's checks (crypto/polynomial_fft.cc:68-96) come before
+    any device work, with the reference's messages."""
+    err = ctypes.create_string_buffer(256)
+    rc = lib.inspire_inner_product(coeff_bits, None, None, n, d, u_bits, v_bits,
+                                   chunk_bits, 0, None, err, len(err))
+    assert rc == 3
+    assert message in err.value

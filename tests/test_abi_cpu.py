@@ -82,3 +82,20 @@ def test_inner_product_argument_checks_without_gpu(lib, coeff_bits, n, d, u_bits
                                    chunk_bits, 0, None, err, len(err))
     assert rc == 3
     assert message in err.value
+
+
+@pytest.mark.parametrize("n,d,t,p,message", [
+    (64 * 4 - 1, 64, 4, 65537, b"Length of evals must be ring_degree * interpolation_degree."),
+    (48 * 4, 48, 4, 65537, b"ring_degree must be a power of two."),
+    (64 * 3, 64, 3, 65537, b"interpolation_degree must be a power of two."),
+    (16 * 64, 16, 64, 65537,
+     b"interpolation_degree must be less than or equal to 2 * ring_degree."),
+    (64 * 4, 64, 4, 65536, b"plaintext_modulus must be odd."),
+])
+def test_interpolate_argument_checks_without_gpu(lib, n, d, t, p, message):
+    """Interpolate's checks (crypto/db_row_interpolation.cc:115-143) come
+    before any device work, with the reference's messages."""
+    err = ctypes.create_string_buffer(256)
+    rc = lib.inspire_interpolate(16, None, n, d, t, p, None, err, len(err))
+    assert rc == 3
+    assert message in err.value

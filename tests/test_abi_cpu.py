@@ -99,3 +99,19 @@ def test_interpolate_argument_checks_without_gpu(lib, n, d, t, p, message):
     rc = lib.inspire_interpolate(16, None, n, d, t, p, None, err, len(err))
     assert rc == 3
     assert message in err.value
+
+
+@pytest.mark.parametrize("rows,cols,n,d,message", [
+    (0, 128, 2, 64, b"Database matrix cannot be empty."),
+    (4, 128, 0, 64, b"a_components cannot be empty."),
+    (4, 100, 2, 64, b"Database columns must match d * n where d is the polynomial "
+                    b"length and n is the number of polynomials."),
+])
+def test_hint_matrix_argument_checks_without_gpu(lib, rows, cols, n, d, message):
+    """ComputeHintMatrix's checks, in the reference's order
+    (crypto/hint_computation.cc:81-97), before any device work."""
+    err = ctypes.create_string_buffer(256)
+    rc = lib.inspire_compute_hint_matrix(1, 32, None, rows, cols, None, n, d, None,  # u16 DB
+                                         0, None, err, len(err))
+    assert rc == 3
+    assert message in err.value

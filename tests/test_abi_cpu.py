@@ -115,3 +115,23 @@ def test_hint_matrix_argument_checks_without_gpu(lib, rows, cols, n, d, message)
                                          0, None, err, len(err))
     assert rc == 3
     assert message in err.value
+
+
+@pytest.mark.parametrize("coeff_bits,mat_kind,log_q,log_digit,digits,d,slices,a_count,message", [
+    # PreprocessMatrixPack's inner product of the gadget vector
+    # (crypto/lwes_to_rlwe.cc:62-68): 2 * num_digits a-polynomials.
+    (32, 5, 32, 8, 4, 64, 1, 7, b"InnerProduct: size mismatch or empty"),
+    (48, 5, 32, 8, 4, 64, 1, 8, b"coeff_bits must be 32 or 64."),
+    (32, 5, 32, 0, 4, 64, 1, 8, b"log_digit and num_digits must be positive."),
+    (32, 5, 40, 8, 4, 64, 1, 8, b"log_modulus must be in (0, coeff_bits]."),
+    (32, 5, 32, 8, 4, 48, 1, 8, b"polynomial length must be a power of two"),
+    (32, 5, 32, 8, 4, 64, 0, 8, b"slices must be positive."),
+])
+def test_preprocess_matrix_pack_argument_checks_without_gpu(
+        lib, coeff_bits, mat_kind, log_q, log_digit, digits, d, slices, a_count, message):
+    err = ctypes.create_string_buffer(256)
+    rc = lib.inspire_preprocess_matrix_pack(coeff_bits, mat_kind, log_q, log_digit, digits,
+                                            d, slices, None, d, None, a_count, None, None,
+                                            None, 0, None, err, len(err))
+    assert rc == 3
+    assert message in err.value
